@@ -1,0 +1,1053 @@
+"""Minimal interpreter for the Fortran 90 subset used by the FWI solver files.
+
+Used only to generate the golden vectors under tests/golden/ from the
+reference's own source (no Fortran compiler exists in the build container).
+It executes the reference subroutines as written, with default REAL as IEEE
+single precision (numpy float32, one rounding per operation, no fused
+multiply-add, no reassociation: what gfortran emits for x86-64 without
+-march flags), default INTEGER as Python int, ``x**2`` as ``x*x`` and
+``exp``/``log`` through the C library's ``expf``/``logf``.
+
+Supported: subroutines and functions, type declarations (explicit-shape,
+allocatable), allocate/deallocate, scalar/array/section/vector-subscript
+assignment, DO / DO WHILE / IF blocks, one-line IF, CALL with
+pass-by-reference (dummies alias the actual argument; explicit-shape dummies
+are reshaped views, i.e. sequence association), EXIT/CYCLE/RETURN, and the
+intrinsics the solver files use.  I/O statements (write/print/open/close) are
+skipped; READ is rejected.
+"""
+from __future__ import annotations
+
+import ctypes
+import ctypes.util
+import math
+import re
+
+import numpy as np
+
+_libm = ctypes.CDLL(ctypes.util.find_library("m"))
+_libm.expf.restype = ctypes.c_float
+_libm.expf.argtypes = [ctypes.c_float]
+_libm.logf.restype = ctypes.c_float
+_libm.logf.argtypes = [ctypes.c_float]
+
+F32 = np.float32
+
+
+def _vec(fn, x):
+    if isinstance(x, np.ndarray):
+        out = np.empty(x.shape, dtype=np.float32, order="F")
+        flat_in = x.reshape(-1, order="F")
+        flat_out = out.reshape(-1, order="F")
+        for i in range(flat_in.size):
+            flat_out[i] = fn(float(flat_in[i]))
+        return out
+    return F32(fn(float(x)))
+
+
+class Return(Exception):
+    pass
+
+
+class Exit(Exception):
+    pass
+
+
+class Cycle(Exception):
+    pass
+
+
+class Var:
+    """A mutable box so that dummies can alias actual arguments."""
+
+    __slots__ = ("value", "ftype", "alloc")
+
+    def __init__(self, value=None, ftype="real", alloc=False):
+        self.value = value
+        self.ftype = ftype
+        self.alloc = alloc
+
+
+# ----------------------------------------------------------------------------
+# lexing
+# ----------------------------------------------------------------------------
+
+def _strip_comment(line: str) -> str:
+    out, q = [], None
+    for ch in line:
+        if q:
+            out.append(ch)
+            if ch == q:
+                q = None
+            continue
+        if ch in "'\"":
+            q = ch
+            out.append(ch)
+            continue
+        if ch == "!":
+            break
+        out.append(ch)
+    return "".join(out)
+
+
+def _split_semis(line: str):
+    parts, depth, q, cur = [], 0, None, []
+    for ch in line:
+        if q:
+            cur.append(ch)
+            if ch == q:
+                q = None
+            continue
+        if ch in "'\"":
+            q = ch
+        elif ch == "(":
+            depth += 1
+        elif ch == ")":
+            depth -= 1
+        elif ch == ";" and depth == 0:
+            parts.append("".join(cur))
+            cur = []
+            continue
+        cur.append(ch)
+    parts.append("".join(cur))
+    return [p.strip() for p in parts if p.strip()]
+
+
+def logical_lines(text: str):
+    """Yield (lineno, statement) pairs with comments, continuations and
+    statement labels removed, lower-cased."""
+    raw = text.split("\n")
+    buf, start = "", None
+    for no, line in enumerate(raw, 1):
+        s = _strip_comment(line).rstrip()
+        if not s.strip():
+            if buf:
+                continue
+            continue
+        st = s.strip()
+        if buf:
+            if st.startswith("&"):
+                st = st[1:]
+            buf += " " + st
+        else:
+            buf, start = st, no
+        if buf.endswith("&"):
+            buf = buf[:-1]
+            continue
+        full = buf
+        buf = ""
+        full = re.sub(r"^\d+\s+", "", full)  # statement label
+        for stmt in _split_semis(full):
+            yield start, stmt.lower()
+
+
+_TOKEN = re.compile(
+    r"""
+    (?P<ws>\s+)
+  | (?P<str>'[^']*'|"[^"]*")
+  | (?P<real>(\d+\.(?!(eq|ne|lt|le|gt|ge|and|or|not|true|false)\.)\d*([ed][+-]?\d+)?)|(\.\d+([ed][+-]?\d+)?)|(\d+[ed][+-]?\d+))
+  | (?P<int>\d+)
+  | (?P<dotop>\.(eq|ne|lt|le|gt|ge|and|or|not|true|false|eqv|neqv)\.)
+  | (?P<name>[a-z_][a-z0-9_]*)
+  | (?P<op>\*\*|//|==|/=|<=|>=|=>|[-+*/(),:<>=%])
+    """,
+    re.X,
+)
+
+
+def tokenize(s: str):
+    pos, out = 0, []
+    while pos < len(s):
+        m = _TOKEN.match(s, pos)
+        if not m:
+            raise SyntaxError(f"cannot tokenize {s[pos:]!r} in {s!r}")
+        pos = m.end()
+        kind = m.lastgroup
+        if kind == "ws":
+            continue
+        val = m.group(kind)
+        if kind == "dotop":
+            val = val.strip(".")
+            mp = {"eq": "==", "ne": "/=", "lt": "<", "le": "<=", "gt": ">", "ge": ">="}
+            if val in mp:
+                out.append(("op", mp[val]))
+            elif val in ("true", "false"):
+                out.append(("bool", val == "true"))
+            else:
+                out.append(("op", "." + val + "."))
+            continue
+        out.append((kind, val))
+    out.append(("end", None))
+    return out
+
+
+# ----------------------------------------------------------------------------
+# expression parsing (Pratt)
+# ----------------------------------------------------------------------------
+
+_BIN = {
+    ".or.": (1, "l"), ".and.": (2, "l"), ".eqv.": (0, "l"), ".neqv.": (0, "l"),
+    "==": (4, "l"), "/=": (4, "l"), "<": (4, "l"), "<=": (4, "l"), ">": (4, "l"), ">=": (4, "l"),
+    "//": (4.5, "l"),
+    "+": (5, "l"), "-": (5, "l"),
+    "*": (6, "l"), "/": (6, "l"),
+    "**": (8, "r"),
+}
+
+
+class Parser:
+    def __init__(self, toks):
+        self.t = toks
+        self.i = 0
+
+    def peek(self):
+        return self.t[self.i]
+
+    def next(self):
+        tok = self.t[self.i]
+        self.i += 1
+        return tok
+
+    def expect(self, kind, val=None):
+        tok = self.next()
+        if tok[0] != kind or (val is not None and tok[1] != val):
+            raise SyntaxError(f"expected {kind} {val}, got {tok}")
+        return tok
+
+    def expr(self, rbp=0):
+        tok = self.next()
+        left = self.nud(tok)
+        while True:
+            tok = self.peek()
+            if tok[0] != "op" or tok[1] not in _BIN:
+                break
+            lbp, assoc = _BIN[tok[1]]
+            if lbp <= rbp:
+                break
+            self.next()
+            right = self.expr(lbp - 0.1 if assoc == "r" else lbp)
+            left = ("bin", tok[1], left, right)
+        return left
+
+    def nud(self, tok):
+        kind, val = tok
+        if kind == "int":
+            return ("int", int(val))
+        if kind == "real":
+            return ("real", F32(float(val.replace("d", "e"))))
+        if kind == "bool":
+            return ("bool", val)
+        if kind == "str":
+            return ("str", val[1:-1])
+        if kind == "op" and val in ("-", "+"):
+            # unary sign applies to a multiplication-level operand
+            operand = self.expr(5)
+            return ("neg", operand) if val == "-" else operand
+        if kind == "op" and val == ".not.":
+            return ("not", self.expr(3))
+        if kind == "op" and val == "(":
+            e = self.expr(0)
+            self.expect("op", ")")
+            return ("paren", e)
+        if kind == "name":
+            if self.peek() == ("op", "("):
+                self.next()
+                args = []
+                if self.peek() != ("op", ")"):
+                    while True:
+                        args.append(self.subscript())
+                        if self.peek() == ("op", ","):
+                            self.next()
+                            continue
+                        break
+                self.expect("op", ")")
+                return ("ref", val, args)
+            return ("name", val)
+        raise SyntaxError(f"unexpected token {tok}")
+
+    def subscript(self):
+        # range a:b, :, a:, :b, or expression; also keyword arg name=expr
+        if self.peek() == ("op", ":"):
+            self.next()
+            hi = None
+            if self.peek() not in (("op", ","), ("op", ")")):
+                hi = self.expr(0)
+            return ("range", None, hi)
+        if self.peek()[0] == "name" and self.t[self.i + 1] == ("op", "="):
+            name = self.next()[1]
+            self.next()
+            return ("kw", name, self.expr(0))
+        e = self.expr(0)
+        if self.peek() == ("op", ":"):
+            self.next()
+            hi = None
+            if self.peek() not in (("op", ","), ("op", ")")):
+                hi = self.expr(0)
+            return ("range", e, hi)
+        return e
+
+
+def parse_expr(s: str):
+    p = Parser(tokenize(s))
+    e = p.expr(0)
+    if p.peek()[0] != "end":
+        raise SyntaxError(f"trailing tokens in {s!r}: {p.t[p.i:]}")
+    return e
+
+
+# ----------------------------------------------------------------------------
+# statements
+# ----------------------------------------------------------------------------
+
+def _top_level_eq(s: str):
+    depth, q = 0, None
+    for i, ch in enumerate(s):
+        if q:
+            if ch == q:
+                q = None
+            continue
+        if ch in "'\"":
+            q = ch
+        elif ch == "(":
+            depth += 1
+        elif ch == ")":
+            depth -= 1
+        elif ch == "=" and depth == 0:
+            prev = s[i - 1] if i else ""
+            nxt = s[i + 1] if i + 1 < len(s) else ""
+            if prev in "=/<>" or nxt in "=>":
+                continue
+            return i
+    return -1
+
+
+def _match_paren(s: str, start: int) -> int:
+    depth = 0
+    for i in range(start, len(s)):
+        if s[i] == "(":
+            depth += 1
+        elif s[i] == ")":
+            depth -= 1
+            if depth == 0:
+                return i
+    raise SyntaxError(f"unbalanced parentheses in {s!r}")
+
+
+_DECL = re.compile(r"^(integer(\*\d+)?|real(\*\d+)?|logical|character(\s*\([^)]*\))?(\*\d+)?|double\s+precision)\b(.*)$")
+_SKIP = re.compile(r"^(write|print|open|close|format|inquire|rewind)\b")
+
+
+def _split_top(s: str, sep=","):
+    parts, depth, cur = [], 0, []
+    for ch in s:
+        if ch == "(":
+            depth += 1
+        elif ch == ")":
+            depth -= 1
+        if ch == sep and depth == 0:
+            parts.append("".join(cur).strip())
+            cur = []
+        else:
+            cur.append(ch)
+    if "".join(cur).strip():
+        parts.append("".join(cur).strip())
+    return parts
+
+
+def parse_stmt(no, s):
+    """Return a statement node."""
+    if _SKIP.match(s):
+        return ("skip", no)
+    if s.startswith("read") and re.match(r"^read\s*\(", s):
+        return ("read", no)
+    if re.match(r"^(implicit|use|include|save|intrinsic|external|continue)\b", s):
+        return ("skip", no)
+    m = _DECL.match(s)
+    if m:
+        if True:
+            base = m.group(1).replace(" ", "")
+            rest = m.group(6)
+            attrs = ""
+            if "::" in rest:
+                attrs, ents = rest.split("::", 1)
+            else:
+                ents = rest
+            ftype = "integer" if base.startswith("integer") else (
+                "real" if base.startswith("real") and base in ("real", "real*4") else (
+                    "double" if base in ("real*8", "doubleprecision") else (
+                        "logical" if base == "logical" else "character")))
+            alloc = "allocatable" in attrs
+            entities = []
+            for ent in _split_top(ents):
+                ent = ent.strip()
+                if not ent:
+                    continue
+                if "=" in ent and "(" not in ent.split("=")[0]:
+                    name, init = ent.split("=", 1)
+                    entities.append((name.strip(), None, parse_expr(init)))
+                    continue
+                mm = re.match(r"^([a-z_][a-z0-9_]*)\s*(\((.*)\))?\s*(\*\s*\d+)?$", ent)
+                if not mm:
+                    raise SyntaxError(f"bad declaration entity {ent!r}")
+                dims = None
+                if mm.group(2):
+                    dims = [d.strip() for d in _split_top(mm.group(3))]
+                    dims = [None if d == ":" else parse_expr(d) for d in dims]
+                entities.append((mm.group(1), dims, None))
+            return ("decl", no, ftype, alloc, entities)
+    if s in ("return",):
+        return ("return", no)
+    if s in ("exit",):
+        return ("exit", no)
+    if s in ("cycle",):
+        return ("cycle", no)
+    if s.startswith("stop"):
+        return ("stop", no)
+    m = re.match(r"^(allocate|deallocate)\s*\((.*)\)$", s)
+    if m:
+        items = []
+        for it in _split_top(m.group(2)):
+            mm = re.match(r"^([a-z_][a-z0-9_]*)\s*(\((.*)\))?$", it.strip())
+            if not mm:
+                continue  # stat= etc.
+            dims = [parse_expr(d) for d in _split_top(mm.group(3))] if mm.group(2) else None
+            items.append((mm.group(1), dims))
+        return (m.group(1), no, items)
+    m = re.match(r"^call\s+([a-z_][a-z0-9_]*)\s*(\((.*)\))?$", s)
+    if m:
+        args = []
+        if m.group(2):
+            p = Parser(tokenize(m.group(3)))
+            if p.peek()[0] != "end":
+                while True:
+                    args.append(p.subscript())
+                    if p.peek() == ("op", ","):
+                        p.next()
+                        continue
+                    break
+        return ("call", no, m.group(1), args)
+    if s == "do":
+        return ("dowhile", no, ("bool", True))
+    m = re.match(r"^do\s+while\s*\((.*)\)$", s)
+    if m:
+        return ("dowhile", no, parse_expr(m.group(1)))
+    m = re.match(r"^do\s+([a-z_][a-z0-9_]*)\s*=\s*(.*)$", s)
+    if m:
+        parts = _split_top(m.group(2))
+        return ("do", no, m.group(1), [parse_expr(p) for p in parts])
+    if s in ("enddo", "end do"):
+        return ("enddo", no)
+    if s in ("endif", "end if"):
+        return ("endif", no)
+    if s == "else":
+        return ("else", no)
+    m = re.match(r"^else\s*if\s*\(", s)
+    if m:
+        i0 = s.index("(")
+        i1 = _match_paren(s, i0)
+        return ("elseif", no, parse_expr(s[i0 + 1:i1]))
+    if s.startswith("if") and re.match(r"^if\s*\(", s):
+        i0 = s.index("(")
+        i1 = _match_paren(s, i0)
+        cond = parse_expr(s[i0 + 1:i1])
+        rest = s[i1 + 1:].strip()
+        if rest == "then":
+            return ("ifthen", no, cond)
+        return ("if1", no, cond, parse_stmt(no, rest))
+    if re.match(r"^end(\s*(subroutine|function|program)\b.*)?$", s):
+        return ("end", no)
+    k = _top_level_eq(s)
+    if k > 0:
+        lhs = parse_expr(s[:k])
+        rhs = parse_expr(s[k + 1:])
+        return ("assign", no, lhs, rhs)
+    raise SyntaxError(f"line {no}: cannot parse statement {s!r}")
+
+
+def build_blocks(stmts):
+    """Turn a flat statement list into nested blocks."""
+    pos = 0
+
+    def block(terminators):
+        nonlocal pos
+        body = []
+        while pos < len(stmts):
+            st = stmts[pos]
+            kind = st[0]
+            if kind in terminators:
+                return body
+            pos += 1
+            if kind == "do" or kind == "dowhile":
+                inner = block({"enddo"})
+                pos += 1
+                body.append(st + (inner,))
+            elif kind == "ifthen":
+                branches = []
+                cond = st[2]
+                while True:
+                    inner = block({"elseif", "else", "endif"})
+                    branches.append((cond, inner))
+                    term = stmts[pos]
+                    pos += 1
+                    if term[0] == "endif":
+                        break
+                    if term[0] == "elseif":
+                        cond = term[2]
+                    else:
+                        cond = ("bool", True)
+                body.append(("ifblock", st[1], branches))
+            else:
+                body.append(st)
+        return body
+
+    out = block(set())
+    return out
+
+
+class Unit:
+    def __init__(self, kind, name, args, body, decls, result=None):
+        self.kind, self.name, self.args, self.body, self.decls, self.result = kind, name, args, body, decls, result
+
+
+def parse_units(text: str):
+    units = {}
+    cur = None
+    stmts = []
+    for no, s in logical_lines(text):
+        m = re.match(r"^(?:(?:integer|real|logical)\s+)?(subroutine|function)\s+([a-z_][a-z0-9_]*)\s*(\((.*)\))?", s)
+        if m and cur is None:
+            args = [a.strip() for a in (m.group(4) or "").split(",") if a.strip()]
+            cur = (m.group(1), m.group(2), args)
+            stmts = []
+            implicit_none = False
+            continue
+        if cur is None:
+            continue  # module code, program code: not executed here
+        if re.match(r"^implicit\s+none", s):
+            implicit_none = True
+        try:
+            st = parse_stmt(no, s)
+        except SyntaxError:
+            st = ("bad", no, s)
+        if st[0] == "end" and not _open_blocks(stmts):
+            decls = [x for x in stmts if x[0] == "decl"]
+            body = build_blocks([x for x in stmts if x[0] != "decl"])
+            units[cur[1]] = Unit(cur[0], cur[1], cur[2], body, decls)
+            units[cur[1]].implicit = not implicit_none
+            cur = None
+            continue
+        stmts.append(st)
+    return units
+
+
+def _open_blocks(stmts):
+    depth = 0
+    for st in stmts:
+        if st[0] in ("do", "dowhile", "ifthen"):
+            depth += 1
+        elif st[0] in ("enddo", "endif"):
+            depth -= 1
+    return depth > 0
+
+
+# ----------------------------------------------------------------------------
+# evaluation
+# ----------------------------------------------------------------------------
+
+def _is_int(x):
+    if isinstance(x, (bool, np.bool_)):
+        return False
+    if isinstance(x, (int, np.integer)):
+        return True
+    return isinstance(x, np.ndarray) and x.dtype.kind in "iu"
+
+
+def _to_real(x):
+    if isinstance(x, np.ndarray):
+        return x.astype(np.float32) if x.dtype != np.float32 and x.dtype != np.float64 else x
+    if isinstance(x, (np.float32, np.float64)):
+        return x
+    return F32(x)
+
+
+def _int_div(a, b):
+    if isinstance(a, np.ndarray) or isinstance(b, np.ndarray):
+        q = np.abs(a) // np.abs(b)
+        return np.where((np.sign(a) * np.sign(b)) < 0, -q, q)
+    q = abs(a) // abs(b)
+    return -q if (a < 0) != (b < 0) else q
+
+
+def _power(a, b):
+    if _is_int(b) or (isinstance(b, (np.float32, np.float64)) and float(b).is_integer()):
+        n = int(b)
+        if _is_int(a) and not isinstance(a, np.ndarray):
+            return a ** n
+        if n == 0:
+            return np.ones_like(a) if isinstance(a, np.ndarray) else F32(1)
+        if n < 0:
+            return F32(1) / _power(a, -n)
+        r = a
+        # gfortran expands small integer powers by repeated multiplication
+        for _ in range(n - 1):
+            r = r * a
+        return r
+    return np.power(_to_real(a), _to_real(b))
+
+
+class Interp:
+    def __init__(self, units, globals_=None, overrides=None):
+        self.units = units
+        self.globals = globals_ or {}
+        self.overrides = overrides or {}
+
+    # -- entry ------------------------------------------------------------
+    def call(self, name, actuals):
+        """Call a unit with a list of Var objects (by reference)."""
+        u = self.units[name]
+        env = {}
+        for dummy, act in zip(u.args, actuals):
+            env[dummy] = act
+        ctx = {"unit": u, "env": env, "implicit": getattr(u, "implicit", False)}
+        # declarations: args first bound; now declare locals and reshape dummies
+        for d in u.decls:
+            _, no, ftype, alloc, entities = d
+            for (nm, dims, init) in entities:
+                if nm in env and nm in u.args:
+                    v = env[nm]
+                    if dims is not None and not alloc and isinstance(v.value, np.ndarray):
+                        shape = self._dims(ctx, dims, v.value)
+                        if shape is not None and tuple(shape) != v.value.shape:
+                            arr = v.value
+                            if not (arr.flags.f_contiguous or arr.ndim <= 1):
+                                raise RuntimeError(f"{name}: non-contiguous actual for {nm}")
+                            view = arr.reshape(tuple(shape), order="F")
+                            if not np.shares_memory(view, arr):
+                                raise RuntimeError("reshape copied")
+                            env[nm] = Var(view, v.ftype)
+                    continue
+                if nm == name and u.kind == "function":
+                    env[nm] = Var(self._zero(ftype), ftype)
+                    continue
+                if alloc:
+                    env[nm] = Var(None, ftype, alloc=True)
+                elif dims is not None:
+                    shape = self._dims(ctx, dims, None)
+                    env[nm] = Var(np.zeros(shape, dtype=self._dtype(ftype), order="F"), ftype)
+                else:
+                    env[nm] = Var(self._zero(ftype) if init is None else self.eval(ctx, init), ftype)
+        if u.kind == "function" and name not in env:
+            env[name] = Var(F32(0), "real")
+        try:
+            self.run(ctx, u.body)
+        except Return:
+            pass
+        if u.kind == "function":
+            return env[name].value
+        return None
+
+    def _dims(self, ctx, dims, actual):
+        if any(d is None for d in dims):
+            return None
+        return [int(self.eval(ctx, d)) for d in dims]
+
+    @staticmethod
+    def _dtype(ftype):
+        return {"integer": np.int64, "real": np.float32, "double": np.float64, "logical": np.bool_}.get(ftype, np.float32)
+
+    @staticmethod
+    def _zero(ftype):
+        return {"integer": 0, "real": F32(0), "double": np.float64(0), "logical": False}.get(ftype, None)
+
+    # -- statements ---------------------------------------------------------
+    def run(self, ctx, body):
+        for st in body:
+            self.exec(ctx, st)
+
+    def exec(self, ctx, st):
+        kind = st[0]
+        if kind == "assign":
+            self.assign(ctx, st[2], st[3])
+        elif kind == "do":
+            _, no, var, parts, inner = st
+            lo = int(self.eval(ctx, parts[0]))
+            hi = int(self.eval(ctx, parts[1]))
+            step = int(self.eval(ctx, parts[2])) if len(parts) > 2 else 1
+            count = max((hi - lo + step) // step, 0)
+            v = self.lookup(ctx, var)
+            i = lo
+            for _ in range(count):
+                v.value = i
+                try:
+                    self.run(ctx, inner)
+                except Cycle:
+                    pass
+                except Exit:
+                    break
+                i += step
+            else:
+                v.value = i
+        elif kind == "dowhile":
+            _, no, cond, inner = st
+            while self.truth(self.eval(ctx, cond)):
+                try:
+                    self.run(ctx, inner)
+                except Cycle:
+                    continue
+                except Exit:
+                    break
+        elif kind == "ifblock":
+            for cond, inner in st[2]:
+                if self.truth(self.eval(ctx, cond)):
+                    self.run(ctx, inner)
+                    break
+        elif kind == "if1":
+            if self.truth(self.eval(ctx, st[2])):
+                self.exec(ctx, st[3])
+        elif kind == "call":
+            self.do_call(ctx, st[2], st[3])
+        elif kind == "allocate":
+            for nm, dims in st[2]:
+                v = self.lookup(ctx, nm)
+                shape = [int(self.eval(ctx, d)) for d in dims]
+                v.value = np.zeros(shape, dtype=self._dtype(v.ftype), order="F")
+        elif kind == "deallocate":
+            for nm, _ in st[2]:
+                self.lookup(ctx, nm).value = None
+        elif kind == "return":
+            raise Return()
+        elif kind == "exit":
+            raise Exit()
+        elif kind == "cycle":
+            raise Cycle()
+        elif kind == "skip":
+            pass
+        elif kind == "bad":
+            raise RuntimeError(f"line {st[1]}: statement not supported: {st[2]!r}")
+        elif kind == "read":
+            raise RuntimeError(f"READ statement at line {st[1]} is not supported")
+        elif kind == "stop":
+            raise RuntimeError(f"STOP at line {st[1]}")
+        else:
+            raise RuntimeError(f"unhandled statement {st}")
+
+    def truth(self, v):
+        return bool(v)
+
+    def lookup(self, ctx, name):
+        env = ctx["env"]
+        if name in env:
+            return env[name]
+        if name in self.globals:
+            return self.globals[name]
+        if ctx.get("implicit", True):
+            # implicit typing (no IMPLICIT NONE in the unit): i-n integer, else real
+            ftype = "integer" if name[0] in "ijklmn" else "real"
+            env[name] = Var(self._zero(ftype), ftype)
+            return env[name]
+        raise NameError(f"{ctx['unit'].name}: unknown variable {name}")
+
+    def has_var(self, ctx, name):
+        return name in ctx["env"] or name in self.globals
+
+    # -- calls --------------------------------------------------------------
+    def do_call(self, ctx, name, args):
+        if name.startswith("mpi_"):
+            raise RuntimeError("MPI call in interpreted code")
+        actuals, writeback = [], []
+        for a in args:
+            if a[0] == "name" and self.has_var(ctx, a[1]):
+                actuals.append(self.lookup(ctx, a[1]))
+            elif a[0] == "ref" and self.has_var(ctx, a[1]):
+                base = self.lookup(ctx, a[1])
+                idx, basic, scalar = self.index(ctx, base.value, a[2])
+                if scalar:
+                    box = Var(base.value[idx], base.ftype)
+                    actuals.append(box)
+                    writeback.append((base, idx, box))
+                elif basic:
+                    actuals.append(Var(base.value[idx], base.ftype))
+                else:
+                    actuals.append(Var(np.array(base.value[idx], order="F"), base.ftype))
+            else:
+                val = self.eval(ctx, a)
+                ftype = "integer" if _is_int(val) else ("logical" if isinstance(val, (bool, np.bool_)) else "real")
+                actuals.append(Var(val, ftype))
+        if name not in self.units:
+            raise NameError(f"unknown subroutine {name}")
+        self.call(name, actuals)
+        for base, idx, box in writeback:
+            base.value[idx] = box.value
+
+    # -- assignment ---------------------------------------------------------
+    def assign(self, ctx, lhs, rhs):
+        val = self.eval(ctx, rhs)
+        unit = ctx["unit"].name
+        if lhs[0] == "name":
+            v = self.lookup(ctx, lhs[1])
+            key = (unit, lhs[1])
+            if key in self.overrides:
+                val = self.overrides[key]
+            if isinstance(v.value, np.ndarray):
+                if isinstance(val, np.ndarray) and val.shape != v.value.shape:
+                    if v.alloc:
+                        v.value = np.array(val, dtype=v.value.dtype, order="F")
+                        return
+                    raise RuntimeError(f"shape mismatch in assignment to {lhs[1]}")
+                v.value[...] = self._conv(val, v.value.dtype)
+            elif v.alloc and isinstance(val, np.ndarray):
+                v.value = np.array(val, dtype=self._dtype(v.ftype), order="F")
+            else:
+                v.value = self._conv_scalar(val, v.ftype)
+            return
+        if lhs[0] == "ref":
+            v = self.lookup(ctx, lhs[1])
+            idx, basic, scalar = self.index(ctx, v.value, lhs[2])
+            if scalar:
+                v.value[idx] = self._conv(val, v.value.dtype)
+            else:
+                target_shape = v.value[idx].shape
+                conv = self._conv(val, v.value.dtype)
+                if isinstance(conv, np.ndarray) and conv.shape != target_shape:
+                    conv = conv.reshape(target_shape, order="F")
+                v.value[idx] = conv
+            return
+        raise RuntimeError(f"bad assignment target {lhs}")
+
+    def _conv(self, val, dtype):
+        if dtype.kind in "iu":
+            if isinstance(val, np.ndarray):
+                return np.trunc(val).astype(dtype) if val.dtype.kind == "f" else val.astype(dtype)
+            return int(math.trunc(val)) if not _is_int(val) else val
+        if dtype == np.float32:
+            return val.astype(np.float32) if isinstance(val, np.ndarray) else F32(val)
+        return val
+
+    def _conv_scalar(self, val, ftype):
+        if ftype == "integer":
+            return int(math.trunc(val)) if not _is_int(val) else int(val)
+        if ftype == "real":
+            return F32(val)
+        if ftype == "double":
+            return np.float64(val)
+        if ftype == "logical":
+            return bool(val)
+        return val
+
+    # -- indexing -----------------------------------------------------------
+    def index(self, ctx, arr, subs):
+        """Return (numpy index, is_basic, is_scalar_element)."""
+        if arr is None:
+            raise RuntimeError("indexing an unallocated array")
+        parts, vec_dims, scalar = [], [], True
+        for k, s in enumerate(subs):
+            if s[0] == "range":
+                lo = 1 if s[1] is None else int(self.eval(ctx, s[1]))
+                hi = arr.shape[k] if s[2] is None else int(self.eval(ctx, s[2]))
+                parts.append(slice(lo - 1, hi))
+                scalar = False
+            else:
+                v = self.eval(ctx, s)
+                if isinstance(v, np.ndarray):
+                    parts.append(np.asarray(v, dtype=np.int64) - 1)
+                    vec_dims.append(k)
+                    scalar = False
+                else:
+                    iv = int(v)
+                    if iv < 1 or iv > arr.shape[k]:
+                        raise IndexError(f"{ctx['unit'].name}: subscript {iv} out of bounds 1..{arr.shape[k]}")
+                    parts.append(iv - 1)
+        if not vec_dims:
+            for k, p in enumerate(parts):
+                if isinstance(p, slice) and (p.start < 0 or p.stop > arr.shape[k]):
+                    if p.stop > p.start:
+                        raise IndexError(f"{ctx['unit'].name}: section {p} out of bounds")
+            return tuple(parts), True, scalar
+        # vector subscripts: build an open mesh over the non-scalar dims
+        lists, keep = [], []
+        for k, p in enumerate(parts):
+            if isinstance(p, slice):
+                lists.append(np.arange(p.start, p.stop))
+                keep.append(True)
+            elif isinstance(p, np.ndarray):
+                if p.min() < 0 or p.max() >= arr.shape[k]:
+                    raise IndexError("vector subscript out of bounds")
+                lists.append(p)
+                keep.append(True)
+            else:
+                lists.append(np.array([p]))
+                keep.append(False)
+        mesh = np.ix_(*lists)
+        mesh = tuple(m if kp else m.reshape(m.shape) for m, kp in zip(mesh, keep))
+        # squeeze scalar dims by taking index 0 along them afterwards
+        return _MeshIndex(mesh, keep), False, False
+
+    # -- expressions --------------------------------------------------------
+    def eval(self, ctx, e):
+        k = e[0]
+        if k == "int":
+            return e[1]
+        if k == "real":
+            return e[1]
+        if k == "bool":
+            return e[1]
+        if k == "str":
+            return e[1]
+        if k == "paren":
+            return self.eval(ctx, e[1])
+        if k == "neg":
+            v = self.eval(ctx, e[1])
+            return -v
+        if k == "not":
+            return not self.eval(ctx, e[1])
+        if k == "name":
+            v = self.lookup(ctx, e[1])
+            return v.value
+        if k == "bin":
+            return self.binop(e[1], self.eval(ctx, e[2]), self.eval(ctx, e[3]))
+        if k == "ref":
+            name, args = e[1], e[2]
+            if self.has_var(ctx, name):
+                v = self.lookup(ctx, name)
+                if not isinstance(v.value, np.ndarray):
+                    raise RuntimeError(f"{name} is not an array")
+                idx, basic, scalar = self.index(ctx, v.value, args)
+                out = v.value[idx]
+                if isinstance(idx, _MeshIndex):
+                    axes = tuple(i for i, kp in enumerate(idx.keep) if not kp)
+                    if axes:
+                        out = out.squeeze(axis=axes)
+                if isinstance(out, np.ndarray):
+                    return np.array(out, order="F")
+                return out
+            if name in self.units:
+                actuals = []
+                for a in args:
+                    if a[0] == "name" and self.has_var(ctx, a[1]):
+                        actuals.append(self.lookup(ctx, a[1]))
+                    else:
+                        val = self.eval(ctx, a)
+                        actuals.append(Var(val, "integer" if _is_int(val) else "real"))
+                return self.call(name, actuals)
+            return self.intrinsic(ctx, name, args)
+        raise RuntimeError(f"cannot evaluate {e}")
+
+    def binop(self, op, a, b):
+        if op in ("+", "-", "*", "/"):
+            if _is_int(a) and _is_int(b):
+                if op == "+":
+                    return a + b
+                if op == "-":
+                    return a - b
+                if op == "*":
+                    return a * b
+                return _int_div(a, b)
+            a, b = _to_real(a), _to_real(b)
+            if op == "+":
+                return a + b
+            if op == "-":
+                return a - b
+            if op == "*":
+                return a * b
+            return a / b
+        if op == "**":
+            return _power(a, b)
+        if op in ("==", "/=", "<", "<=", ">", ">="):
+            if not (_is_int(a) and _is_int(b)):
+                a, b = _to_real(a), _to_real(b)
+            return {"==": a == b, "/=": a != b, "<": a < b, "<=": a <= b, ">": a > b, ">=": a >= b}[op]
+        if op == ".and.":
+            return bool(a) and bool(b)
+        if op == ".or.":
+            return bool(a) or bool(b)
+        raise RuntimeError(f"operator {op}")
+
+    def intrinsic(self, ctx, name, args):
+        vals = [self.eval(ctx, a) for a in args if a[0] != "kw"]
+        if name == "abs":
+            return np.abs(vals[0]) if isinstance(vals[0], np.ndarray) else abs(vals[0])
+        if name == "sqrt":
+            return np.sqrt(_to_real(vals[0]))
+        if name == "exp":
+            return _vec(_libm.expf, _to_real(vals[0]))
+        if name == "log":
+            return _vec(_libm.logf, _to_real(vals[0]))
+        if name in ("maxval", "minval"):
+            arr = vals[0]
+            return arr.max() if name == "maxval" else arr.min()
+        if name in ("real", "float"):
+            return _to_real(vals[0])
+        if name == "int":
+            v = vals[0]
+            return np.trunc(v).astype(np.int64) if isinstance(v, np.ndarray) else int(math.trunc(v))
+        if name == "nint":
+            return int(np.rint(vals[0]))
+        if name == "ceiling":
+            return int(math.ceil(vals[0]))
+        if name == "floor":
+            return int(math.floor(vals[0]))
+        if name == "mod":
+            a, b = vals
+            if _is_int(a) and _is_int(b):
+                return a - _int_div(a, b) * b
+            return np.fmod(_to_real(a), _to_real(b))
+        if name in ("max", "min"):
+            if all(_is_int(v) for v in vals):
+                return max(vals) if name == "max" else min(vals)
+            vals = [_to_real(v) for v in vals]
+            r = vals[0]
+            for v in vals[1:]:
+                r = np.maximum(r, v) if name == "max" else np.minimum(r, v)
+            return r
+        if name == "dot_product":
+            a, b = _to_real(vals[0]), _to_real(vals[1])
+            s = F32(0)
+            for x, y in zip(a.reshape(-1), b.reshape(-1)):
+                s = s + x * y
+            return s
+        if name == "size":
+            return int(vals[0].size)
+        if name == "sum":
+            s = F32(0)
+            for x in _to_real(vals[0]).reshape(-1, order="F"):
+                s = s + x
+            return s
+        raise NameError(f"intrinsic {name} not supported")
+
+
+class _MeshIndex(tuple):
+    """np.ix_ mesh that squeezes dimensions indexed by a scalar."""
+
+    def __new__(cls, mesh, keep):
+        obj = tuple.__new__(cls, mesh)
+        obj.keep = keep
+        return obj
+
+
+class Program:
+    """All subroutines of a set of Fortran source files."""
+
+    def __init__(self, paths, globals_=None, overrides=None):
+        self.units = {}
+        for p in paths:
+            with open(p, encoding="latin-1") as f:
+                self.units.update(parse_units(f.read()))
+        self.interp = Interp(self.units, globals_, overrides)
+
+    def call(self, name, *actuals):
+        return self.interp.call(name, list(actuals))
+
+
+def run_snippet(path, first, last, env, globals_=None):
+    """Execute source lines first..last (1-based, inclusive) of a file as a
+    statement sequence in an environment of Var objects."""
+    with open(path, encoding="latin-1") as f:
+        text = f.read()
+    lines = text.split("\n")[first - 1:last]
+    stmts = [parse_stmt(no, s) for no, s in logical_lines("\n".join(lines))]
+    body = build_blocks([x for x in stmts if x[0] != "decl"])
+    unit = Unit("snippet", f"{path}:{first}-{last}", [], body, [])
+    interp = Interp({}, globals_)
+    ctx = {"unit": unit, "env": env}
+    interp.run(ctx, body)
+    return env

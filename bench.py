@@ -1,0 +1,370 @@
+#!/usr/bin/env python3
+"""Shot-gradients/s of the batched FWI gradient on one GB300.
+
+Workload (default): the batched MCS survey -- 400 x 2000 cells at 12.5 m,
+64 shots x 480 channels, 6 s at dt = 1 ms (nt = 6000), 6th-order FD
+(acc = 3), 20-cell CPML, snapshots every 10 steps, FP32 stencil and
+snapshots, FP64 gradient stack.  One step = one calculate_misfit_gradient
+over all 64 shots (forward + L2 misfit + adjoint + imaging + stack).
+
+    python bench.py [--steps K] [--warmup W] [--impl ours|reference]
+
+`--impl reference` times the CPU restatement of the reference solver (the
+Fortran reference cannot be compiled here: no Fortran compiler) on all
+host cores, one shot per thread, on a bounded number of time steps.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "shot-gradients/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--shots", type=int, default=64)
+    ap.add_argument("--nt", type=int, default=6000)
+    ap.add_argument("--snap", choices=["f32", "bf16", "f16"], default="f32")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg")
+    ap.add_argument("--no-plain", action="store_true", help="skip the plain-path leg")
+    return ap.parse_args()
+
+
+def workload_name(a):
+    return (f"batched MCS survey: 400x2000 cells @12.5 m, {a.shots} shots x 480 ch, nt={a.nt} (dt=1 ms), "
+            f"acc=3 (6th order), dPML=20, store_snap=10, {a.snap} snapshots, FP64 gradient stack")
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def traffic_from_profile():
+    """DRAM bytes per step launch pair from the committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", "step_kernels_config2.md")
+    try:
+        for line in open(path):
+            if line.startswith("traffic_bytes_per_step_per_shot:"):
+                return float(line.split(":", 1)[1].split()[0])
+    except OSError:
+        pass
+    return None
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu):
+        self.gpu = gpu
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        self.p = None
+
+    def start(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}",
+                                       "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                      stderr=subprocess.DEVNULL)
+        except OSError:
+            self.p = None
+
+    def stop(self):
+        if not self.p:
+            return None
+        self.p.terminate()
+        try:
+            self.p.wait(5)
+        except subprocess.TimeoutExpired:
+            self.p.kill()
+        self.f.flush()
+        rows = []
+        for line in open(self.f.name):
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) >= 9:
+                rows.append(parts)
+        os.unlink(self.f.name)
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        smax = max(float(r[2]) for r in rows if r[2].replace(".", "").isdigit())
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({n for r in rows for n, v in zip(names, r[5:9]) if v.lower() == "active"})
+        loaded = [s for s in sm if s > 0.5 * smax] or sm
+        return {"sm_mhz": statistics.median(loaded) if loaded else None, "sm_max_mhz": smax, "reasons": reasons,
+                "samples": len(rows)}
+
+
+# ---------------------------------------------------------------------------
+# CPU legs (the oracle is the checker and the CPU baseline, never the product)
+# ---------------------------------------------------------------------------
+
+def cpu_sample(spec, vp, nthreads, nt_sample):
+    """Time nthreads shot-gradients of the workload, each truncated to
+    nt_sample time steps, one shot per thread.  Returns
+    (shot-gradients/s scaled to the full nt, seconds, description)."""
+    from fwi_gb300.survey import SurveySpec
+    from oracle import oracle as O
+    shots = []
+    for i in range(nthreads):
+        s = spec.shots[i % len(spec.shots)]
+        src = np.asfortranarray(np.asarray(s.src)[:nt_sample])
+        obs = np.asfortranarray(np.random.default_rng(i).standard_normal((nt_sample, len(s.nxRec))).astype(np.float32))
+        shots.append(type(s)(x0=s.x0, nx=s.nx, nxSou=s.nxSou, nySou=s.nySou, nxRec=s.nxRec, nyRec=s.nyRec, src=src,
+                             obs=obs))
+    sub = SurveySpec(ny=spec.ny, nx_model=spec.nx_model, d=spec.d, dt=spec.dt, nt=nt_sample, shots=shots,
+                     store_snap=spec.store_snap, acc=spec.acc, dpml=spec.dpml)
+    t0 = time.perf_counter()
+    O.gradient_batch(sub, vp, step=1, nthreads=nthreads)
+    t = time.perf_counter() - t0
+    rate = nthreads / (t * (spec.nt / nt_sample))
+    desc = (f"{nthreads} shot-gradients of this workload (one per thread), each truncated to {nt_sample} of "
+            f"{spec.nt} time steps forward and adjoint, scaled by {spec.nt}/{nt_sample}")
+    return rate, t, desc
+
+
+def run_reference(a):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    from fwi_gb300 import synth
+    spec, vp_true, vp0 = synth.config2(nshots=a.shots, nt=a.nt)
+    nthreads = os.cpu_count() or 1
+    nt_sample = 100
+    for _ in range(a.warmup):
+        cpu_sample(spec, vp0, nthreads, nt_sample)
+    times = []
+    rate = None
+    desc = ""
+    for _ in range(a.steps):
+        rate, t, desc = cpu_sample(spec, vp0, nthreads, nt_sample)
+        times.append(t)
+    per_step = statistics.mean(times)
+    value = nthreads / (per_step * (spec.nt / nt_sample))
+    line = {"metric": METRIC, "value": value, "unit": METRIC, "n_gpus": a.gpus, "steps": a.steps, "warmup": a.warmup,
+            "ms_per_step": per_step * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32", "data": "synthetic", "impl": "reference",
+            "config": {"workload": workload_name(a), "l2": "n/a (CPU)"},
+            "cpu_baseline": {"value": value, "unit": METRIC, "cores": nthreads, "kind": "port", "sample": desc},
+            "e2e": {"value": value, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "note": "CPU restatement of solver_acoustic_SS/calculate_misfit_gradient (the Fortran reference "
+                    "needs gfortran+MPI, absent here); one shot per host thread, like mpirun -np <cores>"}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ---------------------------------------------------------------------------
+# GPU leg
+# ---------------------------------------------------------------------------
+
+def main():
+    a = parse()
+    if a.impl == "reference":
+        return run_reference(a)
+    import torch
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    if world > 1:
+        torch.distributed.init_process_group("nccl")
+    import fwi_gb300 as F
+    from fwi_gb300 import synth
+    from fwi_gb300.synth import lam_from_vp
+
+    F.init(local)
+    stream = torch.cuda.Stream()
+    F.set_stream(stream.cuda_stream)
+    snap_form = {"f32": F.SNAP_F32, "bf16": F.SNAP_BF16, "f16": F.SNAP_F16}[a.snap]
+    spec, vp_true, vp0 = synth.config2(seed=2 + rank, nshots=a.shots, nt=a.nt)
+    lam_true, lam0 = lam_from_vp(vp_true), lam_from_vp(vp0)
+
+    # observed data from the true model (untimed setup)
+    sv = F.Survey(spec, snap_form=snap_form)
+    sv.set_lambda(lam_true)
+    sv.run(2)
+    for i, sh in enumerate(spec.shots):
+        sh.obs = sv.synthetic(i)
+    obs_packed = spec.obs_packed()
+    sv.set_observed(obs_packed)
+    lam0_dev = torch.from_numpy(np.ascontiguousarray(lam0.reshape(-1, order="F"))).cuda()
+    sv.set_lambda(lam0_dev.data_ptr())
+    grad_dev = torch.zeros(spec.ny * spec.nx_model, dtype=torch.float32, device="cuda")
+
+    def step():
+        return sv.run_device_grad(1, grad_dev.data_ptr())
+
+    for _ in range(a.warmup):
+        step()
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    clocks = Clocks(local)
+    clocks.start()
+    l0 = F.kernel_launch_count()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(a.steps):
+        step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    launches = F.kernel_launch_count() - l0
+    t = e0.elapsed_time(e1) / 1e3
+    clk = clocks.stop()
+    if world > 1:
+        tt = torch.tensor([t], device="cuda")
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        t = float(tt.item())
+        torch.distributed.barrier()
+    value = world * len(spec.shots) * a.steps / t
+
+    # roofline of the dominant kernel pair (main + bottom step kernels)
+    hbm, peak_kind = peaks()
+    nsteps = 200
+    sv.time_steps(20)
+    torch.cuda.synchronize()
+    r0, r1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    r0.record(stream)
+    sv.time_steps(nsteps)
+    r1.record(stream)
+    torch.cuda.synchronize()
+    step_s = r0.elapsed_time(r1) / 1e3 / nsteps
+    bytes_step = sv.step_bytes()
+    achieved = bytes_step / step_s / 1e9
+    tr = traffic_from_profile()
+    wave, band = sv.tuning()
+    roof = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+            "traffic": tr * len(spec.shots) if tr else None,
+            "kernel": "k_step_main + k_step_bottom (one time step of all shots)",
+            "algorithmic_bytes_per_launch": bytes_step, "avg_launch_ms": step_s * 1e3,
+            "peak_kind": f"{peak_kind} copy bandwidth (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured"
+            else "fallback 6.8 TB/s"}
+    sv.close()
+    del sv
+    torch.cuda.synchronize()
+
+    # plain GPU path: one shot per survey, one launch per time step, no graph
+    plain = None
+    if not a.no_plain and rank == 0:
+        from fwi_gb300.survey import SurveySpec
+        one = SurveySpec(ny=spec.ny, nx_model=spec.nx_model, d=spec.d, dt=spec.dt, nt=spec.nt, shots=[spec.shots[0]],
+                         store_snap=spec.store_snap, acc=spec.acc, dpml=spec.dpml, water_rows=spec.water_rows)
+        pv = F.Survey(one, snap_form=snap_form, graph=False)
+        pv.set_lambda(lam0_dev.data_ptr())
+        pv.run_device_grad(1, grad_dev.data_ptr())
+        torch.cuda.synchronize()
+        p0, p1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        p0.record(stream)
+        nplain = 2
+        for _ in range(nplain):
+            pv.run_device_grad(1, grad_dev.data_ptr())
+        p1.record(stream)
+        torch.cuda.synchronize()
+        tp = p0.elapsed_time(p1) / 1e3 / nplain
+        plain = {"value": 1.0 / tp, "unit": METRIC, "batched_over_plain": value / world * tp,
+                 "how": "same workload one shot at a time, one kernel launch per time step, no CUDA graph"}
+        pv.close()
+        del pv
+        torch.cuda.synchronize()
+
+    # end to end: the reference-facing batch call with pinned host buffers
+    e2e = None
+    if not a.no_e2e:
+        from fwi_gb300.api import _DescHolder
+        pin = lambda n: torch.empty(n, dtype=torch.float32, pin_memory=True).numpy()  # noqa: E731
+        h_lam = pin(lam0.size)
+        h_lam[:] = lam0.reshape(-1, order="F")
+        h_grad = pin(spec.ny * spec.nx_model)
+        h_obs = pin(obs_packed.size)
+        h_obs[:] = obs_packed
+        nsrc = sum(np.asarray(s.src).size for s in spec.shots)
+        h_src = pin(nsrc)
+        h_src[:] = np.concatenate([np.asarray(s.src, np.float32).reshape(-1, order="F") for s in spec.shots])
+        dh = _DescHolder(spec, snap_form, F.GRAD_F64)
+        so = oo = 0
+        for i, s in enumerate(spec.shots):
+            ns, nr = s.src.size, len(s.nxRec) * spec.nt
+            dh.shots[i].src = h_src[so:so + ns].ctypes.data
+            dh.shots[i].obs = h_obs[oo:oo + nr].ctypes.data
+            so += ns
+            oo += nr
+        lib = F.load()
+        mis = C.c_float(0.0)
+
+        def e2e_step():
+            h_grad[:] = 0.0
+            rc = lib.fwi_misfit_gradient_batch(C.byref(dh.desc), C.c_void_p(h_lam.ctypes.data), 1, C.byref(mis),
+                                               C.c_void_p(h_grad.ctypes.data))
+            if rc:
+                raise F.FwiError(rc, lib.fwi_last_error().decode())
+        for _ in range(a.warmup):
+            e2e_step()
+        torch.cuda.synchronize()
+        q0, q1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        q0.record(stream)
+        for _ in range(a.steps):
+            e2e_step()
+        q1.record(stream)
+        torch.cuda.synchronize()
+        te = q0.elapsed_time(q1) / 1e3
+        if world > 1:
+            tt = torch.tensor([te], device="cuda")
+            torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+            te = float(tt.item())
+        e2e = {"value": world * len(spec.shots) * a.steps / te, "unit": METRIC,
+               "h2d_bytes_per_step": int(h_lam.nbytes + h_obs.nbytes + h_src.nbytes + h_grad.nbytes),
+               "d2h_bytes_per_step": int(h_grad.nbytes + 8 * sum(len(s.nxRec) for s in spec.shots)),
+               "call": "fwi_misfit_gradient_batch (calculate_misfit_gradient drop-in), pinned host buffers"}
+
+    cpu = None
+    if rank == 0 and world == 1 and not a.no_cpu:
+        nthreads = os.cpu_count() or 1
+        rate, tcpu, desc = cpu_sample(spec, vp0, nthreads, 200)
+        cpu = {"value": rate, "unit": METRIC, "cores": nthreads, "kind": "port", "sample": desc,
+               "seconds": tcpu}
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": a.steps,
+                "warmup": a.warmup, "ms_per_step": t / a.steps * 1e3, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded layered model, Ricker sources, "
+                "observed data synthesised on the true model)",
+                "config": {"workload": workload_name(a), "shots_per_gpu": len(spec.shots), "wave_shots": wave,
+                           "band_rows": band,
+                           "l2": "inputs larger than L2: 64 shots' wavefields (~1.8 GB) and snapshots (~134 GB)"},
+                "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "plain": plain, "gpu_launches": int(launches),
+                "clocks": clk}
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,26 @@
+"""GB300-native FWI hot path: per-shot forward/adjoint acoustic propagation,
+L2 misfit and adjoint source, imaging condition and gradient stack, as
+hand-written sm_103a kernels behind the C ABI of include/fwi_gb300.h.
+
+Importing the package loads fwi_gb300/_lib/libfwi_gb300.so; build it first
+with ``python -m fwi_gb300.build``.
+"""
+from ._native import FwiError, GRAD_F32, GRAD_F64, SNAP_BF16, SNAP_F16, SNAP_F32, load  # noqa: F401
+from .survey import ShotSpec, SurveySpec  # noqa: F401
+
+load()
+
+from .api import (  # noqa: E402,F401
+    Beta_calculous,
+    Misfit_function,
+    Ricker_mcs,
+    Survey,
+    calculate_misfit_gradient,
+    init,
+    kernel_launch_count,
+    mcs_geometry,
+    set_solver_options,
+    set_stream,
+    solver_acoustic_SS,
+    time_rules,
+)

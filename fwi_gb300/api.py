@@ -1,0 +1,239 @@
+"""Python mirror of the reference routines on the hot path.
+
+Names, argument order and meaning follow the Fortran routines they replace;
+arrays are numpy arrays in Fortran order (column-major) with 1-based grid
+indices, so code written against the reference reads the same:
+
+    solver_acoustic_SS   src/solver_acoustic_SS.f90:9-11
+    Misfit_function      src/Misfit.f90:1 (misfit_type 1, Misfit_L2.f90)
+    Beta_calculous       src/Beta_calculous.f90:1
+    calculate_misfit_gradient  src/calculate_misfit_gradient.f90:1 (all shots)
+    Ricker_mcs           src/get_mcs_data.f90:331
+    mcs_geometry         src/get_mcs_data.f90:113-114,147-155,503-512
+    time_rules           src/calculate_misfit_gradient.f90:198-203
+
+Every call goes through libfwi_gb300.so; errors raise FwiError.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _native as N
+from .survey import SurveySpec
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+def _ri(v):
+    return C.byref(C.c_int(int(v)))
+
+
+def _rf(v):
+    return C.byref(C.c_float(float(v)))
+
+
+def _f32(a):
+    return np.asfortranarray(np.asarray(a, dtype=np.float32))
+
+
+def _i32(a):
+    return np.ascontiguousarray(np.asarray(a, dtype=np.int32).reshape(-1))
+
+
+def init(device: int = 0):
+    N.check(N.load().fwi_init(device))
+
+
+def set_solver_options(acc: int = 3, dpml: int = 20):
+    """Spatial half-order and CPML width of solver_acoustic_SS (reference: 3, 20)."""
+    N.check(N.load().fwi_set_solver_options(acc, dpml))
+
+
+def set_stream(cuda_stream_handle):
+    N.check(N.load().fwi_set_stream(C.c_void_p(cuda_stream_handle)))
+
+
+def kernel_launch_count() -> int:
+    return int(N.load().fwi_kernel_launch_count())
+
+
+def solver_acoustic_SS(rank, iprop, NumSou, NumRec, nxSou, nySou, nxRec, nyRec, S, Sadj, d, dt, ny, nx, ctmp,
+                       store_snap, nt_Store, nt, kernel, Fields, Rec_point):
+    """Drop-in for solver_acoustic_SS.  kernel, Fields and Rec_point are
+    float32 Fortran-ordered arrays updated in place (kernel accumulated for
+    iprop=2, Fields written for iprop=1, Rec_point overwritten)."""
+    for name, a in (("kernel", kernel), ("Fields", Fields), ("Rec_point", Rec_point)):
+        if a is not None and (a.dtype != np.float32 or not a.flags.f_contiguous):
+            raise TypeError(f"{name} must be a float32 Fortran-ordered array")
+    xs, ys, xr, yr = _i32(nxSou), _i32(nySou), _i32(nxRec), _i32(nyRec)
+    S_ = _f32(S) if S is not None else None
+    Sa = _f32(Sadj) if Sadj is not None else None
+    ct = _f32(ctmp)
+    N.check(N.load().fwi_solver_acoustic_ss(
+        _ri(rank), _ri(iprop), _ri(NumSou), _ri(NumRec), _p(xs), _p(ys), _p(xr), _p(yr), _p(S_), _p(Sa), _rf(d),
+        _rf(dt), _ri(ny), _ri(nx), _p(ct), _ri(store_snap), _ri(nt_Store), _ri(nt), _p(kernel), _p(Fields),
+        _p(Rec_point)))
+
+
+def Misfit_function(rank, freq, Data_Synth, Data_trace, NumRec, nt, dt, AdjSource):
+    """Returns (Misfit as float32, misfit accumulated in FP64); AdjSource is
+    written in place."""
+    if AdjSource.dtype != np.float32 or not AdjSource.flags.f_contiguous:
+        raise TypeError("AdjSource must be a float32 Fortran-ordered array")
+    s, t = _f32(Data_Synth), _f32(Data_trace)
+    m = C.c_float(0.0)
+    m64 = C.c_double(0.0)
+    N.check(N.load().fwi_misfit_function(_ri(rank), _rf(freq), _p(s), _p(t), _ri(NumRec), _ri(nt), _rf(dt),
+                                         C.byref(m), _p(AdjSource), C.byref(m64)))
+    return np.float32(m.value), m64.value
+
+
+def Beta_calculous(Grad, OldGrad, nx, ny):
+    """Polak-Ribiere beta with FP64 dot products: (beta, num64, den64)."""
+    g, o = _f32(Grad), _f32(OldGrad)
+    b = C.c_float(0.0)
+    n64, d64 = C.c_double(0.0), C.c_double(0.0)
+    N.check(N.load().fwi_beta_calculous(_p(g), _p(o), _ri(nx), _ri(ny), C.byref(b), C.byref(n64), C.byref(d64)))
+    return np.float32(b.value), n64.value, d64.value
+
+
+def Ricker_mcs(freq, dt, nt):
+    out = np.zeros(nt, np.float32)
+    N.check(N.load().fwi_ricker(freq, dt, nt, _p(out)))
+    return out
+
+
+def mcs_geometry(xs, shot_depth, streamer_depth, near_offset, drec, dmodel, num_rec):
+    """(nxSou, nySou, nxRec[num_rec], nyRec[num_rec]) 1-based grid indices."""
+    a, b = C.c_int(0), C.c_int(0)
+    xr, yr = np.zeros(num_rec, np.int32), np.zeros(num_rec, np.int32)
+    N.check(N.load().fwi_mcs_geometry(xs, shot_depth, streamer_depth, near_offset, drec, dmodel, num_rec,
+                                      C.byref(a), C.byref(b), _p(xr), _p(yr)))
+    return a.value, b.value, xr, yr
+
+
+def time_rules(lam, dmodel, tfin, store_snap=10):
+    """(dt, nt, nt_Store) of calculate_misfit_gradient.f90:198-203."""
+    lam = _f32(lam)
+    dt, nt, nts = C.c_float(0), C.c_int(0), C.c_int(0)
+    N.check(N.load().fwi_time_rules(_p(lam), lam.shape[0], lam.shape[1], dmodel, tfin, store_snap, C.byref(dt),
+                                    C.byref(nt), C.byref(nts)))
+    return np.float32(dt.value), nt.value, nts.value
+
+
+class _DescHolder:
+    """Keeps the numpy arrays behind a FwiSurveyDesc alive."""
+
+    def __init__(self, spec: SurveySpec, snap_form=0, grad_form=1, hbm_budget=0, wave_shots=0, band_rows=0,
+                 flags=0):
+        self.keep = []
+        shots = (N.FwiShot * len(spec.shots))()
+        for i, sh in enumerate(spec.shots):
+            arrs = [_i32(sh.nxSou), _i32(sh.nySou), _i32(sh.nxRec), _i32(sh.nyRec),
+                    _f32(np.asarray(sh.src).reshape(spec.nt, -1, order="F")),
+                    _f32(np.asarray(sh.obs).reshape(spec.nt, -1, order="F")) if sh.obs is not None else None]
+            self.keep.extend(a for a in arrs if a is not None)
+            shots[i] = N.FwiShot(sh.x0, sh.nx, len(sh.nxSou), len(sh.nxRec), _p(arrs[0]), _p(arrs[1]), _p(arrs[2]),
+                                 _p(arrs[3]), _p(arrs[4]), _p(arrs[5]), sh.grad_weight, sh.misfit_weight)
+        self.shots = shots
+        water = None
+        if spec.water_rows is not None:
+            water = _i32(spec.water_rows)
+            self.keep.append(water)
+        self.desc = N.FwiSurveyDesc(spec.ny, spec.nx_model, spec.d, spec.dt, spec.nt, spec.store_snap, spec.acc,
+                                    spec.dpml, spec.numtasks, snap_form, grad_form, len(spec.shots), shots,
+                                    _p(water), hbm_budget, wave_shots, band_rows, flags)
+
+
+class Survey:
+    """Device-resident batched survey (fwi_survey_create & co)."""
+
+    def __init__(self, spec: SurveySpec, snap_form=N.SNAP_F32, grad_form=N.GRAD_F64, hbm_budget=0, wave_shots=0,
+                 band_rows=0, graph=True):
+        self.spec = spec
+        self._h = _DescHolder(spec, snap_form, grad_form, hbm_budget, wave_shots, band_rows,
+                              0 if graph else N.SURVEY_NO_GRAPH)
+        handle = C.c_void_p()
+        N.check(N.load().fwi_survey_create(C.byref(self._h.desc), C.byref(handle)))
+        self.handle = handle
+
+    def close(self):
+        if getattr(self, "handle", None) and self.handle.value:
+            N.load().fwi_survey_destroy(self.handle)
+            self.handle = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_lambda(self, lam):
+        """lambda (ny, nx_model): numpy (host) array or an integer device address."""
+        if isinstance(lam, int):
+            N.check(N.load().fwi_survey_set_lambda(self.handle, C.c_void_p(lam)))
+        else:
+            self._lam = _f32(lam)
+            N.check(N.load().fwi_survey_set_lambda(self.handle, _p(self._lam)))
+
+    def set_observed(self, obs_packed):
+        if isinstance(obs_packed, int):
+            N.check(N.load().fwi_survey_set_observed(self.handle, C.c_void_p(obs_packed)))
+        else:
+            self._obs = np.ascontiguousarray(obs_packed, dtype=np.float32)
+            N.check(N.load().fwi_survey_set_observed(self.handle, _p(self._obs)))
+
+    def run(self, step=1, grad=None, misfit=0.0):
+        """Returns (misfit + this run's misfit, grad) where grad (ny, nx_model)
+        float32 Fortran array is updated in place if given."""
+        m = C.c_double(misfit)
+        if grad is not None and (grad.dtype != np.float32 or not grad.flags.f_contiguous):
+            raise TypeError("grad must be a float32 Fortran-ordered array")
+        N.check(N.load().fwi_survey_run(self.handle, step, C.byref(m), _p(grad)))
+        return m.value, grad
+
+    def run_device_grad(self, step=1, grad_dev_ptr=None):
+        m = C.c_double(0.0)
+        N.check(N.load().fwi_survey_run(self.handle, step, C.byref(m),
+                                        None if grad_dev_ptr is None else C.c_void_p(grad_dev_ptr)))
+        return m.value
+
+    def synthetic(self, shot):
+        nrec = len(self.spec.shots[shot].nxRec)
+        out = np.zeros((self.spec.nt, nrec), np.float32, order="F")
+        N.check(N.load().fwi_survey_get_synthetic(self.handle, shot, _p(out)))
+        return out
+
+    def grad_stack_device_ptr(self):
+        p = C.c_void_p()
+        N.check(N.load().fwi_survey_grad_device(self.handle, C.byref(p)))
+        return p.value
+
+    def step_bytes(self):
+        b = C.c_double(0)
+        N.check(N.load().fwi_survey_step_bytes(self.handle, C.byref(b)))
+        return b.value
+
+    def tuning(self):
+        w, b = C.c_int(0), C.c_int(0)
+        N.check(N.load().fwi_survey_tuning(self.handle, C.byref(w), C.byref(b)))
+        return w.value, b.value
+
+    def time_steps(self, steps):
+        N.check(N.load().fwi_survey_time_steps(self.handle, steps))
+
+
+def calculate_misfit_gradient(spec: SurveySpec, lam, step, Misfit, Grad, snap_form=N.SNAP_F32,
+                              grad_form=N.GRAD_F64):
+    """calculate_misfit_gradient over every shot of `spec` in one call with
+    host buffers.  Returns the updated Misfit (float32); Grad (ny, nx_model)
+    float32 Fortran array is updated in place (step=1)."""
+    h = _DescHolder(spec, snap_form, grad_form)
+    lam = _f32(lam)
+    m = C.c_float(Misfit)
+    N.check(N.load().fwi_misfit_gradient_batch(C.byref(h.desc), _p(lam), step, C.byref(m), _p(Grad)))
+    return np.float32(m.value)

@@ -1,0 +1,1299 @@
+// Host side of the FWI path: the C ABI declared in include/fwi_gb300.h.
+//
+// Responsibilities: argument validation (everything the reference would
+// index out of bounds is rejected before launch), device layout planning,
+// per-warp work lists with their source/receiver cells, the time-step
+// schedule (snapshot counter of solver_acoustic_SS.f90:303-305, :438-471),
+// wave sizing against the HBM budget, CUDA-graph capture of whole waves,
+// and the misfit/gradient reductions of calculate_misfit_gradient.f90.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "fwi_gb300.h"
+#include "fwi_internal.cuh"
+
+namespace fwi {
+cudaError_t launch_step(int acc, int mode, const StepParams& pm, const StepParams& pb, cudaStream_t st);
+cudaError_t launch_build_c2(float* c2, int nyt, int pitch, int off, int dn, int ny, int nx, const float* src, int ldv,
+                            int x0, int from_lambda, float dt2, float d2, cudaStream_t st);
+cudaError_t launch_rec_last(float* rec, int nt, int nrec, cudaStream_t st);
+cudaError_t launch_misfit(const float* synth, const float* obs, float* adj, double* mis_tr, int nt, float dt,
+                          const int* tr_off, int ntr, int nshots, double* mis_shot, cudaStream_t st);
+cudaError_t launch_stack(double* G, int ny, int nxm, const void* shots, int nshots, int form, cudaStream_t st);
+size_t stack_shot_size();
+void fill_stack_shot(void* dst, const float* k32, const double* k64, int x0, int nx, int off_dn, int pitch, double w);
+cudaError_t launch_finalize(float* grad, const double* G, int ny, int nxm, int numtasks, const int* water,
+                            cudaStream_t st);
+cudaError_t launch_fields_io(float* fort, float* snaps, int ny, int nx, int pitch, int off_dn, int nsnap, int to_dev,
+                             cudaStream_t st);
+cudaError_t launch_kernel_io(float* dev, float* fort, int ny, int nx, int pitch, int off_dn, int to_dev,
+                             cudaStream_t st);
+cudaError_t launch_dot(const float* g, const float* o, size_t n, double* part, int nb, double* out, cudaStream_t st);
+cudaError_t launch_nonfinite(const float* a, size_t n, int* flag, cudaStream_t st);
+}  // namespace fwi
+
+using namespace fwi;
+
+namespace {
+
+// ---------------------------------------------------------------------------
+// errors and library state
+// ---------------------------------------------------------------------------
+
+thread_local std::string g_err;
+
+int fail(int code, const std::string& msg) {
+    g_err = msg;
+    return code;
+}
+int cuda_fail(cudaError_t e, const char* what, int line) {
+    char buf[512];
+    snprintf(buf, sizeof buf, "CUDA error %s (%s) in %s [fwi_host.cu:%d]", cudaGetErrorName(e), cudaGetErrorString(e),
+             what, line);
+    g_err = buf;
+    return (e == cudaErrorMemoryAllocation) ? FWI_ERR_NOMEM : FWI_ERR_CUDA;
+}
+#define CK(x)                                                       \
+    do {                                                            \
+        cudaError_t e_ = (x);                                       \
+        if (e_ != cudaSuccess) return cuda_fail(e_, #x, __LINE__);  \
+    } while (0)
+// launch + count (each launcher issues the number of kernels it returns in nk)
+#define LK(x)                                                      \
+    do {                                                           \
+        cudaError_t e_ = (x);                                      \
+        if (e_ != cudaSuccess) return cuda_fail(e_, #x, __LINE__); \
+        ++L().launches;                                            \
+    } while (0)
+#define TRY(x)                  \
+    do {                        \
+        int r_ = (x);           \
+        if (r_ != FWI_OK) return r_; \
+    } while (0)
+
+struct LibState {
+    bool init = false;
+    int device = 0;
+    cudaStream_t own = nullptr;
+    cudaStream_t user = nullptr;
+    int acc = 3, dpml = 20;
+    long long launches = 0;
+    std::recursive_mutex mu;
+};
+LibState& L() {
+    static LibState s;
+    return s;
+}
+cudaStream_t stream() { return L().user ? L().user : L().own; }
+
+int ensure_init() {
+    if (L().init) return FWI_OK;
+    return fwi_init(0);
+}
+
+// device allocation with RAII
+struct DBuf {
+    void* p = nullptr;
+    size_t n = 0;
+    DBuf() = default;
+    DBuf(const DBuf&) = delete;
+    DBuf& operator=(const DBuf&) = delete;
+    ~DBuf() { release(); }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+    }
+    int alloc(size_t bytes) {
+        release();
+        if (bytes == 0) bytes = 16;
+        cudaError_t e = cudaMalloc(&p, bytes);
+        if (e != cudaSuccess) {
+            p = nullptr;
+            char buf[256];
+            snprintf(buf, sizeof buf, "cudaMalloc of %zu bytes failed: %s", bytes, cudaGetErrorString(e));
+            g_err = buf;
+            return FWI_ERR_NOMEM;
+        }
+        n = bytes;
+        return FWI_OK;
+    }
+    int ensure(size_t bytes) { return (p && n >= bytes) ? FWI_OK : alloc(bytes); }
+    template <typename T> T* as() const { return reinterpret_cast<T*>(p); }
+};
+
+// ---------------------------------------------------------------------------
+// coefficients (solver_FD_coeffs.f90, solver_PML_coeffs.f90); this file is
+// built with -ffp-contract=off so the FP32 arithmetic matches the Fortran.
+// ---------------------------------------------------------------------------
+
+void fd_taps(int acc, float* c1, float* c2) {
+    for (int i = 0; i <= MAXR; ++i) c1[i] = c2[i] = 0.f;
+    if (acc == 3) {
+        c1[0] = 0.f; c1[1] = 3.f / 4.f; c1[2] = -(3.f / 20.f); c1[3] = 1.f / 60.f;
+        c2[0] = -(49.f / 18.f); c2[1] = 3.f / 2.f; c2[2] = -(3.f / 20.f); c2[3] = 1.f / 90.f;
+    } else if (acc == 4) {
+        c1[0] = 0.f; c1[1] = 4.f / 5.f; c1[2] = -(1.f / 5.f); c1[3] = 4.f / 105.f; c1[4] = -(1.f / 280.f);
+        c2[0] = -(205.f / 72.f); c2[1] = 8.f / 5.f; c2[2] = -(1.f / 5.f); c2[3] = 8.f / 315.f; c2[4] = -(1.f / 560.f);
+    }
+    c2[0] = c2[0] / 2.f;  // centre tap halved (solver_FD_coeffs.f90:68)
+}
+
+// 1-D CPML factors A, B (0-based, dn entries; entries 0..acc-1 are zero).
+// The corner matrices of the reference are A(max(i,j)) in the orientation
+// of each corner and are indexed on the fly by the kernels.
+void pml_factors(int acc, int dpml, float dt, float d, std::vector<float>& fA, std::vector<float>& fB) {
+    const int dn = dpml + 2 * acc;
+    fA.assign(dn, 0.f);
+    fB.assign(dn, 0.f);
+    const float pi = 3.14159265f, Refl = 0.00001f;
+    const float wPML = (float)(dpml - 1) * d;
+    const float lr = logf(Refl);
+    for (int i = 1 + acc; i <= dpml + acc; ++i) {
+        const float y = (float)(i - (acc + 1)) * d;
+        const float q = y / wPML;
+        const float alpha = 30.f * pi * (1.f - (y / wPML));
+        const float sigma = (-((6000.f * lr) / (2.f * wPML))) * (q * q);
+        const float A = expf((-(sigma + alpha)) * dt);
+        fA[i - 1] = A;
+        fB[i - 1] = ((A - 1.f) * sigma) / (sigma + alpha);
+    }
+    for (int i = dpml + acc + 1; i <= dn; ++i) {
+        fA[i - 1] = fA[dpml + acc - 1];
+        fB[i - 1] = fB[dpml + acc - 1];
+    }
+}
+
+// ---------------------------------------------------------------------------
+// layout and work lists
+// ---------------------------------------------------------------------------
+
+struct Layout {
+    int ny, nx, dn, nyt, nxt, off, pitch, ntiles;
+};
+
+Layout make_layout(int ny, int nx, int acc, int dpml) {
+    Layout l;
+    l.ny = ny;
+    l.nx = nx;
+    l.dn = dpml + 2 * acc;
+    l.nyt = 2 * l.dn + ny;
+    l.nxt = nx + 2 * l.dn;
+    const int r0 = (l.nxt - 1) % TILE;
+    l.off = 0;
+    if (r0 < l.dn - 1) l.off = ((l.dn - 1 - r0) + 3) / 4 * 4;
+    l.ntiles = (l.off + l.nxt + TILE - 1) / TILE;
+    l.pitch = l.ntiles * TILE;
+    return l;
+}
+
+int validate_common(int ny, int nx, int acc, int dpml, int nt, int store_snap) {
+    if (acc != 3 && acc != 4) return fail(FWI_ERR_ARG, "acc must be 3 or 4 (the reference's 6th/8th-order tables)");
+    if (dpml < 1 || dpml + 2 * acc > MAXDN - 2)
+        return fail(FWI_ERR_ARG, "dpml must be >= 1 and dpml + 2*acc <= 62");
+    if (ny < 1 || nx < 1) return fail(FWI_ERR_ARG, "ny and nx must be >= 1");
+    if ((long long)ny * nx > (1LL << 31)) return fail(FWI_ERR_ARG, "model too large");
+    if (nt < 2) return fail(FWI_ERR_ARG, "nt must be >= 2");
+    if (store_snap < 1) return fail(FWI_ERR_ARG, "store_snap must be >= 1");
+    return FWI_OK;
+}
+
+// Snapshot events of the reference's counter: l starts at 1, is incremented
+// every step k = 2..nt and triggers (and resets) when it equals store_snap.
+std::vector<int> snapshot_steps(int nt, int store_snap) {
+    std::vector<int> ks;
+    int l = 1;
+    for (int k = 2; k <= nt; ++k) {
+        l = l + 1;
+        if (l == store_snap) {
+            ks.push_back(k);
+            l = 0;
+        }
+    }
+    return ks;
+}
+
+struct ShotGeom {
+    int x0 = 0, nx = 0;
+    std::vector<int> nxS, nyS, nxR, nyR;  // 1-based, window-relative
+};
+
+int validate_geometry(const ShotGeom& g, const Layout& l, int shot) {
+    char buf[256];
+    auto chk = [&](const std::vector<int>& xs, const std::vector<int>& ys, const char* what) -> int {
+        for (size_t i = 0; i < xs.size(); ++i) {
+            const int py = l.dn + ys[i], px = l.dn + xs[i];
+            if (py < 1 || py > l.nyt || px < 1 || px > l.nxt) {
+                snprintf(buf, sizeof buf,
+                         "shot %d: %s %zu at grid (%d,%d) lies outside the padded grid (rows 1..%d, cols 1..%d "
+                         "after padding by %d)",
+                         shot, what, i + 1, ys[i], xs[i], l.nyt, l.nxt, l.dn);
+                return fail(FWI_ERR_ARG, buf);
+            }
+        }
+        return FWI_OK;
+    };
+    TRY(chk(g.nxS, g.nyS, "source"));
+    TRY(chk(g.nxR, g.nyR, "receiver"));
+    return FWI_OK;
+}
+
+struct Lists {
+    std::vector<WorkItem> main_fwd, main_adj, bottom;
+    std::vector<SrcEnt> src_fwd, src_adj;
+    std::vector<RecEnt> recs;
+};
+
+// Injection cells of one shot: interior cells only (the source array only
+// enters the interior update), last writer wins for repeated cells
+// (solver_acoustic_SS.f90:320-329).
+std::vector<SrcEnt> injection_cells(const std::vector<int>& xs, const std::vector<int>& ys, const Layout& l) {
+    std::map<std::pair<int, int>, int> last;
+    for (size_t j = 0; j < xs.size(); ++j) {
+        const int pr = l.dn + ys[j] - 1, pc = l.dn + xs[j] - 1;
+        if (pr < l.dn || pr >= l.dn + l.ny || pc < l.dn || pc >= l.dn + l.nx) continue;
+        last[{pr, pc}] = (int)j;
+    }
+    std::vector<SrcEnt> out;
+    for (auto& kv : last) out.push_back(SrcEnt{kv.first.first, l.off + kv.first.second, kv.second});
+    return out;
+}
+
+void append_item(Lists& L_, std::vector<WorkItem>& items, std::vector<SrcEnt>& srcs, const std::vector<SrcEnt>& cells,
+                 const std::vector<RecEnt>& recs_shot, int shot, int tile, int y0, int y1, int kind, bool with_recs) {
+    WorkItem it{};
+    it.shot = shot;
+    it.tile = tile;
+    it.y0 = y0;
+    it.y1 = y1;
+    it.kind = kind;
+    const int c0 = tile * TILE, c1 = c0 + TILE;
+    std::vector<SrcEnt> sel;
+    for (auto& c : cells)
+        if (c.row >= y0 && c.row < y1 && c.col >= c0 && c.col < c1) sel.push_back(c);
+    std::stable_sort(sel.begin(), sel.end(), [](const SrcEnt& a, const SrcEnt& b) { return a.row < b.row; });
+    it.s0 = (int)srcs.size();
+    srcs.insert(srcs.end(), sel.begin(), sel.end());
+    it.s1 = (int)srcs.size();
+    it.r0 = it.r1 = (int)L_.recs.size();
+    if (with_recs) {
+        std::vector<RecEnt> rs;
+        for (auto& r : recs_shot)
+            if (r.row >= y0 && r.row < y1 && r.col >= c0 && r.col < c1) rs.push_back(r);
+        std::stable_sort(rs.begin(), rs.end(), [](const RecEnt& a, const RecEnt& b) { return a.row < b.row; });
+        L_.recs.insert(L_.recs.end(), rs.begin(), rs.end());
+        it.r1 = (int)L_.recs.size();
+    }
+    items.push_back(it);
+}
+
+// Work lists for a set of shots (local shot index = position in `geoms`).
+Lists build_lists(const std::vector<ShotGeom>& geoms, const std::vector<Layout>& lays, int band_rows) {
+    Lists out;
+    for (size_t s = 0; s < geoms.size(); ++s) {
+        const Layout& l = lays[s];
+        const ShotGeom& g = geoms[s];
+        const auto cells_f = injection_cells(g.nxS, g.nyS, l);
+        const auto cells_a = injection_cells(g.nxR, g.nyR, l);
+        std::vector<RecEnt> recs;
+        for (size_t i = 0; i < g.nxR.size(); ++i) {
+            const int pr = l.dn + g.nyR[i] - 1, pc = l.dn + g.nxR[i] - 1;
+            if (pr < l.dn) continue;  // top pad: identically zero, never recorded
+            recs.push_back(RecEnt{pr, l.off + pc, (int)i});
+        }
+        const int nb = std::max(1, (l.ny + band_rows - 1) / band_rows);
+        for (int b = 0; b < nb; ++b) {
+            const int y0 = l.dn + (int)((long long)l.ny * b / nb);
+            const int y1 = l.dn + (int)((long long)l.ny * (b + 1) / nb);
+            if (y1 <= y0) continue;
+            for (int t = 0; t < l.ntiles; ++t) {
+                append_item(out, out.main_fwd, out.src_fwd, cells_f, recs, (int)s, t, y0, y1, 0, true);
+                append_item(out, out.main_adj, out.src_adj, cells_a, recs, (int)s, t, y0, y1, 0, false);
+            }
+        }
+        std::vector<SrcEnt> none;
+        for (int t = 0; t < l.ntiles; ++t)
+            append_item(out, out.bottom, out.src_fwd, none, recs, (int)s, t, l.nyt - l.dn, l.nyt, 1, true);
+    }
+    return out;
+}
+
+template <typename T>
+int upload(DBuf& b, const std::vector<T>& v, cudaStream_t st) {
+    TRY(b.ensure(std::max<size_t>(v.size() * sizeof(T), 16)));
+    if (!v.empty()) CK(cudaMemcpyAsync(b.p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, st));
+    return FWI_OK;
+}
+
+bool is_device_ptr(const void* p) {
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+double step_bytes_shot(int ny, int nx, int dn) {
+    const double cells = (double)(ny + dn) * (double)(nx + 2 * dn);
+    const double cpml = 2.0 * ny * dn + (double)dn * nx + 4.0 * dn * dn;
+    return 16.0 * cells + 16.0 * cpml;
+}
+
+// ---------------------------------------------------------------------------
+// per-shot device state
+// ---------------------------------------------------------------------------
+
+struct ShotState {
+    DBuf pa, pb, c2, phx, chx, phy, chy, snaps, sscale, k;
+    Layout lay{};
+    size_t field_bytes = 0, snap_bytes = 0;
+    int alloc(const Layout& l, int nsnap_blocks, int snap_form, int grad_form) {
+        lay = l;
+        field_bytes = (size_t)l.nyt * l.pitch * sizeof(float);
+        const size_t esz = snap_form == FWI_SNAP_F32 ? 4 : 2;
+        snap_bytes = (size_t)nsnap_blocks * l.ny * l.pitch * esz;
+        TRY(pa.ensure(field_bytes));
+        TRY(pb.ensure(field_bytes));
+        TRY(c2.ensure(field_bytes));
+        TRY(phx.ensure(field_bytes));
+        TRY(chx.ensure(field_bytes));
+        TRY(phy.ensure(field_bytes));
+        TRY(chy.ensure(field_bytes));
+        TRY(snaps.ensure(snap_bytes));
+        TRY(sscale.ensure((size_t)nsnap_blocks * l.ny * l.ntiles * sizeof(float)));
+        TRY(k.ensure((size_t)l.ny * l.pitch * (grad_form == FWI_GRAD_F64 ? 8 : 4)));
+        return FWI_OK;
+    }
+    int zero_state(cudaStream_t st) {
+        CK(cudaMemsetAsync(pa.p, 0, field_bytes, st));
+        CK(cudaMemsetAsync(pb.p, 0, field_bytes, st));
+        CK(cudaMemsetAsync(phx.p, 0, field_bytes, st));
+        CK(cudaMemsetAsync(chx.p, 0, field_bytes, st));
+        CK(cudaMemsetAsync(phy.p, 0, field_bytes, st));
+        CK(cudaMemsetAsync(chy.p, 0, field_bytes, st));
+        return FWI_OK;
+    }
+    ShotDev dev(int nt, int nrec, int x0, const float* srcv, float* rec) const {
+        ShotDev d{};
+        d.pa = pa.as<float>();
+        d.pb = pb.as<float>();
+        d.c2 = c2.as<float>();
+        d.phx = phx.as<float>();
+        d.chx = chx.as<float>();
+        d.phy = phy.as<float>();
+        d.chy = chy.as<float>();
+        d.srcv = srcv;
+        d.rec = rec;
+        d.snaps = snaps.p;
+        d.sscale = sscale.as<float>();
+        d.k32 = k.as<float>();
+        d.k64 = k.as<double>();
+        d.snap_stride = (long long)lay.ny * lay.pitch;
+        d.ny = lay.ny;
+        d.nx = lay.nx;
+        d.nyt = lay.nyt;
+        d.nxt = lay.nxt;
+        d.off = lay.off;
+        d.pitch = lay.pitch;
+        d.ntiles = lay.ntiles;
+        d.dn = lay.dn;
+        d.nt = nt;
+        d.nrec = nrec;
+        d.x0 = x0;
+        return d;
+    }
+};
+
+StepParams base_params(int acc, float dt, int store_snap, int snap_form, int grad_form, const float* dfA,
+                       const float* dfB) {
+    StepParams p{};
+    float c1[MAXR + 1], c2[MAXR + 1];
+    fd_taps(acc, c1, c2);
+    for (int i = 0; i <= MAXR; ++i) {
+        p.c1[i] = c1[i];
+        p.c2[i] = c2[i];
+    }
+    p.fA = dfA;
+    p.fB = dfB;
+    p.dt = dt;
+    p.ss = (float)store_snap;
+    p.snap_form = snap_form;
+    p.grad_form = grad_form;
+    p.snap = -1;
+    return p;
+}
+
+// One pass over the time loop k = 2..nt for a set of shots.
+// mode 0: forward (snapshots if store, receivers recorded); mode 1: adjoint.
+struct StepSet {
+    StepParams pm, pb;
+};
+int run_time_loop(int acc, int mode, int nt, int store_snap, int nt_store, bool store, StepSet ps, cudaStream_t st) {
+    std::vector<int> ev = snapshot_steps(nt, store_snap);
+    size_t evi = 0;
+    int snap = (mode == 0) ? 0 : nt_store;
+    for (int k = 2; k <= nt; ++k) {
+        int sn = -1;
+        if (evi < ev.size() && ev[evi] == k) {
+            ++evi;
+            if (mode == 0) {
+                ++snap;
+                if (store) sn = snap;
+            } else {
+                --snap;
+                sn = snap;
+            }
+        }
+        ps.pm.t = ps.pb.t = k - 2;
+        ps.pm.parity = ps.pb.parity = k & 1;
+        ps.pm.snap = ps.pb.snap = sn;
+        CK(launch_step(acc, mode, ps.pm, ps.pb, st));
+        L().launches += (ps.pm.nitems > 0) + (ps.pb.nitems > 0);
+    }
+    return FWI_OK;
+}
+
+// ---------------------------------------------------------------------------
+// single-shot drop-in state (buffers kept between calls)
+// ---------------------------------------------------------------------------
+
+struct Single {
+    ShotState sh;
+    DBuf d_ctmp, d_srcv, d_rec, d_items_m, d_items_b, d_src, d_recs, d_shot, d_fA, d_fB, d_stage, d_flag;
+};
+Single& single() {
+    static Single s;
+    return s;
+}
+
+int check_nonfinite(const float* dptr, size_t n, DBuf& flag, cudaStream_t st, const char* what) {
+    TRY(flag.ensure(sizeof(int)));
+    CK(cudaMemsetAsync(flag.p, 0, sizeof(int), st));
+    LK(launch_nonfinite(dptr, n, flag.as<int>(), st));
+    int h = 0;
+    CK(cudaMemcpyAsync(&h, flag.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    if (h) return fail(FWI_ERR_NONFINITE, std::string("non-finite values in ") + what +
+                                              " (the time step may violate the CFL limit)");
+    return FWI_OK;
+}
+
+}  // namespace
+
+// ===========================================================================
+// C ABI
+// ===========================================================================
+
+extern "C" {
+
+int fwi_init(int device) {
+    std::lock_guard<std::recursive_mutex> g(L().mu);
+    if (L().init && L().device == device) return FWI_OK;
+    int n = 0;
+    CK(cudaGetDeviceCount(&n));
+    if (device < 0 || device >= n) return fail(FWI_ERR_ARG, "invalid CUDA device index");
+    CK(cudaSetDevice(device));
+    if (!L().own) CK(cudaStreamCreateWithFlags(&L().own, cudaStreamNonBlocking));
+    L().device = device;
+    L().init = true;
+    return FWI_OK;
+}
+
+int fwi_finalize(void) {
+    std::lock_guard<std::recursive_mutex> g(L().mu);
+    if (!L().init) return FWI_OK;
+    cudaDeviceSynchronize();
+    Single& s = single();
+    s.~Single();
+    new (&s) Single();
+    if (L().own) cudaStreamDestroy(L().own);
+    L().own = nullptr;
+    L().user = nullptr;
+    L().init = false;
+    return FWI_OK;
+}
+
+const char* fwi_last_error(void) { return g_err.c_str(); }
+
+int fwi_set_stream(void* st) {
+    TRY(ensure_init());
+    L().user = reinterpret_cast<cudaStream_t>(st);
+    return FWI_OK;
+}
+
+int fwi_set_solver_options(int acc, int dpml) {
+    if (acc != 3 && acc != 4) return fail(FWI_ERR_ARG, "acc must be 3 or 4");
+    if (dpml < 1 || dpml + 2 * acc > MAXDN - 2) return fail(FWI_ERR_ARG, "dpml out of range");
+    L().acc = acc;
+    L().dpml = dpml;
+    return FWI_OK;
+}
+
+int64_t fwi_kernel_launch_count(void) { return L().launches; }
+
+int fwi_solver_acoustic_ss(const int* rank, const int* iprop_, const int* NumSou_, const int* NumRec_,
+                           const int* nxSou, const int* nySou, const int* nxRec, const int* nyRec, const float* S,
+                           const float* Sadj, const float* d_, const float* dt_, const int* ny_, const int* nx_,
+                           const float* ctmp, const int* store_snap_, const int* nt_Store_, const int* nt_,
+                           float* kernel, float* Fields, float* Rec_point) {
+    (void)rank;
+    std::lock_guard<std::recursive_mutex> g(L().mu);
+    TRY(ensure_init());
+    if (!iprop_ || !NumSou_ || !NumRec_ || !d_ || !dt_ || !ny_ || !nx_ || !store_snap_ || !nt_Store_ || !nt_)
+        return fail(FWI_ERR_ARG, "null scalar argument");
+    const int iprop = *iprop_, NumSou = *NumSou_, NumRec = *NumRec_, ny = *ny_, nx = *nx_;
+    const int store_snap = *store_snap_, nt_store = *nt_Store_, nt = *nt_;
+    const float d = *d_, dt = *dt_;
+    const int acc = L().acc, dpml = L().dpml;
+    TRY(validate_common(ny, nx, acc, dpml, nt, store_snap));
+    if (NumSou < 0 || NumRec < 0) return fail(FWI_ERR_ARG, "NumSou/NumRec must be >= 0");
+    if (!(d > 0.f) || !(dt > 0.f)) return fail(FWI_ERR_ARG, "d and dt must be positive");
+    if (!ctmp || !Rec_point) return fail(FWI_ERR_ARG, "null ctmp or Rec_point");
+    if (iprop == 2 && (!Sadj || !Fields || !kernel || !nxRec || !nyRec))
+        return fail(FWI_ERR_ARG, "adjoint needs Sadj, Fields, kernel and receiver indices");
+    if (iprop != 2 && NumSou > 0 && (!S || !nxSou || !nySou)) return fail(FWI_ERR_ARG, "forward needs S and sources");
+    if (iprop == 1 && !Fields) return fail(FWI_ERR_ARG, "forward with iprop=1 needs Fields");
+    if (NumRec > 0 && (!nxRec || !nyRec)) return fail(FWI_ERR_ARG, "null receiver indices");
+    if (nt_store < 0) return fail(FWI_ERR_ARG, "nt_Store must be >= 0");
+    const std::vector<int> ev = snapshot_steps(nt, store_snap);
+    if ((iprop == 1 || iprop == 2) && (int)ev.size() > nt_store)
+        return fail(FWI_ERR_ARG, "nt_Store is smaller than the number of snapshots nt/store_snap (the reference "
+                                 "would write past Fields)");
+
+    const Layout l = make_layout(ny, nx, acc, dpml);
+    ShotGeom geo;
+    geo.nx = nx;
+    if (iprop != 2) {
+        geo.nxS.assign(nxSou, nxSou + NumSou);
+        geo.nyS.assign(nySou, nySou + NumSou);
+    }
+    if (NumRec > 0) {
+        geo.nxR.assign(nxRec, nxRec + NumRec);
+        geo.nyR.assign(nyRec, nyRec + NumRec);
+    }
+    TRY(validate_geometry(geo, l, 1));
+
+    Single& sg = single();
+    cudaStream_t st = stream();
+    const int nsnap_blocks = nt_store + 1;
+    TRY(sg.sh.alloc(l, (iprop == 1 || iprop == 2) ? nsnap_blocks : 1, FWI_SNAP_F32, FWI_GRAD_F32));
+    TRY(sg.sh.zero_state(st));
+
+    // model -> c2
+    TRY(sg.d_ctmp.ensure((size_t)ny * nx * sizeof(float)));
+    CK(cudaMemcpyAsync(sg.d_ctmp.p, ctmp, (size_t)ny * nx * sizeof(float), cudaMemcpyHostToDevice, st));
+    LK(launch_build_c2(sg.sh.c2.as<float>(), l.nyt, l.pitch, l.off, l.dn, ny, nx, sg.d_ctmp.as<float>(), ny, 0, 0,
+                       dt * dt, d * d, st));
+    std::vector<float> fA, fB;
+    pml_factors(acc, dpml, dt, d, fA, fB);
+    TRY(upload(sg.d_fA, fA, st));
+    TRY(upload(sg.d_fB, fB, st));
+
+    // injected values
+    const int nval = (iprop == 2) ? NumRec : NumSou;
+    const float* hval = (iprop == 2) ? Sadj : S;
+    TRY(sg.d_srcv.ensure(std::max<size_t>((size_t)nt * nval * sizeof(float), 16)));
+    if (nval > 0) CK(cudaMemcpyAsync(sg.d_srcv.p, hval, (size_t)nt * nval * sizeof(float), cudaMemcpyHostToDevice, st));
+    TRY(sg.d_rec.ensure(std::max<size_t>((size_t)nt * NumRec * sizeof(float), 16)));
+    CK(cudaMemsetAsync(sg.d_rec.p, 0, std::max<size_t>((size_t)nt * NumRec * sizeof(float), 16), st));
+
+    const int off_dn = l.off + l.dn;
+    if (iprop == 2) {
+        const size_t fbytes = (size_t)ny * nx * nsnap_blocks * sizeof(float);
+        TRY(sg.d_stage.ensure(fbytes));
+        CK(cudaMemcpyAsync(sg.d_stage.p, Fields, fbytes, cudaMemcpyHostToDevice, st));
+        LK(launch_fields_io(sg.d_stage.as<float>(), sg.sh.snaps.as<float>(), ny, nx, l.pitch, off_dn, nsnap_blocks, 1,
+                            st));
+        CK(cudaMemsetAsync(sg.sh.k.p, 0, (size_t)ny * l.pitch * sizeof(float), st));
+        TRY(sg.d_ctmp.ensure((size_t)ny * nx * sizeof(float)));
+        CK(cudaMemcpyAsync(sg.d_ctmp.p, kernel, (size_t)ny * nx * sizeof(float), cudaMemcpyHostToDevice, st));
+        LK(launch_kernel_io(sg.sh.k.as<float>(), sg.d_ctmp.as<float>(), ny, nx, l.pitch, off_dn, 1, st));
+    }
+
+    // work lists (the adjoint injects at the receivers)
+    std::vector<ShotGeom> geoms{geo};
+    std::vector<Layout> lays{l};
+    Lists lists = build_lists(geoms, lays, 64);
+    const bool adj = (iprop == 2);
+    TRY(upload(sg.d_items_m, adj ? lists.main_adj : lists.main_fwd, st));
+    TRY(upload(sg.d_items_b, lists.bottom, st));
+    TRY(upload(sg.d_src, adj ? lists.src_adj : lists.src_fwd, st));
+    TRY(upload(sg.d_recs, lists.recs, st));
+    std::vector<ShotDev> sd{sg.sh.dev(nt, NumRec, 0, sg.d_srcv.as<float>(), sg.d_rec.as<float>())};
+    TRY(upload(sg.d_shot, sd, st));
+
+    StepSet ps;
+    ps.pm = base_params(acc, dt, store_snap, FWI_SNAP_F32, FWI_GRAD_F32, sg.d_fA.as<float>(), sg.d_fB.as<float>());
+    ps.pm.items = sg.d_items_m.as<WorkItem>();
+    ps.pm.nitems = (int)(adj ? lists.main_adj.size() : lists.main_fwd.size());
+    ps.pm.shots = sg.d_shot.as<ShotDev>();
+    ps.pm.srcs = sg.d_src.as<SrcEnt>();
+    ps.pm.recs = sg.d_recs.as<RecEnt>();
+    ps.pm.record = adj ? 0 : 1;
+    ps.pb = ps.pm;
+    ps.pb.items = sg.d_items_b.as<WorkItem>();
+    ps.pb.nitems = (int)lists.bottom.size();
+    TRY(run_time_loop(acc, adj ? 1 : 0, nt, store_snap, nt_store, iprop == 1, ps, st));
+
+    if (!adj) LK(launch_rec_last(sg.d_rec.as<float>(), nt, NumRec, st));
+    // outputs
+    if (NumRec > 0)
+        CK(cudaMemcpyAsync(Rec_point, sg.d_rec.p, (size_t)nt * NumRec * sizeof(float), cudaMemcpyDeviceToHost, st));
+    int rc = FWI_OK;
+    if (iprop == 1) {
+        // blocks 1..nwritten of Fields; block 0 and unwritten blocks untouched
+        const int nw = (int)ev.size();
+        if (nw > 0) {
+            const size_t fbytes = (size_t)ny * nx * (nw + 1) * sizeof(float);
+            TRY(sg.d_stage.ensure(fbytes));
+            LK(launch_fields_io(sg.d_stage.as<float>(), sg.sh.snaps.as<float>(), ny, nx, l.pitch, off_dn, nw + 1, 0,
+                                st));
+            const size_t blk = (size_t)ny * nx;
+            CK(cudaMemcpyAsync(Fields + blk, sg.d_stage.as<float>() + blk, blk * nw * sizeof(float),
+                               cudaMemcpyDeviceToHost, st));
+        }
+        if (NumRec > 0) rc = check_nonfinite(sg.d_rec.as<float>(), (size_t)nt * NumRec, sg.d_flag, st, "Rec_point");
+    } else if (adj) {
+        TRY(sg.d_stage.ensure((size_t)ny * nx * sizeof(float)));
+        LK(launch_kernel_io(sg.sh.k.as<float>(), sg.d_stage.as<float>(), ny, nx, l.pitch, off_dn, 0, st));
+        CK(cudaMemcpyAsync(kernel, sg.d_stage.p, (size_t)ny * nx * sizeof(float), cudaMemcpyDeviceToHost, st));
+        rc = check_nonfinite(sg.d_stage.as<float>(), (size_t)ny * nx, sg.d_flag, st, "kernel");
+    } else if (NumRec > 0) {
+        rc = check_nonfinite(sg.d_rec.as<float>(), (size_t)nt * NumRec, sg.d_flag, st, "Rec_point");
+    }
+    CK(cudaStreamSynchronize(st));
+    return rc;
+}
+
+int fwi_misfit_function(const int* rank, const float* freq, const float* synth, const float* trace, const int* NumRec_,
+                        const int* nt_, const float* dt_, float* Misfit, float* AdjSource, double* misfit64) {
+    (void)rank;
+    (void)freq;
+    std::lock_guard<std::recursive_mutex> g(L().mu);
+    TRY(ensure_init());
+    if (!NumRec_ || !nt_ || !dt_ || !synth || !trace || !Misfit || !AdjSource) return fail(FWI_ERR_ARG, "null argument");
+    const int nrec = *NumRec_, nt = *nt_;
+    if (nrec < 0 || nt < 1) return fail(FWI_ERR_ARG, "NumRec must be >= 0 and nt >= 1");
+    cudaStream_t st = stream();
+    const size_t n = (size_t)nrec * nt;
+    DBuf ds, dob, da, dtr, doff, dms;
+    TRY(ds.alloc(n * 4));
+    TRY(dob.alloc(n * 4));
+    TRY(da.alloc(n * 4));
+    TRY(dtr.alloc(std::max(nrec, 1) * sizeof(double)));
+    TRY(doff.alloc(2 * sizeof(int)));
+    TRY(dms.alloc(sizeof(double)));
+    CK(cudaMemcpyAsync(ds.p, synth, n * 4, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(dob.p, trace, n * 4, cudaMemcpyHostToDevice, st));
+    const int off[2] = {0, nrec};
+    CK(cudaMemcpyAsync(doff.p, off, sizeof off, cudaMemcpyHostToDevice, st));
+    LK(launch_misfit(ds.as<float>(), dob.as<float>(), da.as<float>(), dtr.as<double>(), nt, *dt_, doff.as<int>(), nrec,
+                     1, dms.as<double>(), st));
+    double m = 0.0;
+    CK(cudaMemcpyAsync(AdjSource, da.p, n * 4, cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(&m, dms.p, sizeof(double), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    *Misfit = (float)m;
+    if (misfit64) *misfit64 = m;
+    return FWI_OK;
+}
+
+int fwi_beta_calculous(const float* Grad, const float* OldGrad, const int* nx_, const int* ny_, float* Beta,
+                       double* num64, double* den64) {
+    std::lock_guard<std::recursive_mutex> g(L().mu);
+    TRY(ensure_init());
+    if (!Grad || !OldGrad || !nx_ || !ny_ || !Beta) return fail(FWI_ERR_ARG, "null argument");
+    const size_t n = (size_t)(*nx_) * (*ny_);
+    if (*nx_ < 1 || *ny_ < 1) return fail(FWI_ERR_ARG, "nx, ny must be >= 1");
+    cudaStream_t st = stream();
+    const bool dev = is_device_ptr(Grad) && is_device_ptr(OldGrad);
+    DBuf dg, dog, part, out;
+    const float *pg = Grad, *po = OldGrad;
+    if (!dev) {
+        TRY(dg.alloc(n * 4));
+        TRY(dog.alloc(n * 4));
+        CK(cudaMemcpyAsync(dg.p, Grad, n * 4, cudaMemcpyHostToDevice, st));
+        CK(cudaMemcpyAsync(dog.p, OldGrad, n * 4, cudaMemcpyHostToDevice, st));
+        pg = dg.as<float>();
+        po = dog.as<float>();
+    }
+    const int nb = 304;
+    TRY(part.alloc(2 * nb * sizeof(double)));
+    TRY(out.alloc(2 * sizeof(double)));
+    LK(launch_dot(pg, po, n, part.as<double>(), nb, out.as<double>(), st));
+    double h[2];
+    CK(cudaMemcpyAsync(h, out.p, sizeof h, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    *Beta = (float)(h[0] / h[1]);
+    if (num64) *num64 = h[0];
+    if (den64) *den64 = h[1];
+    return FWI_OK;
+}
+
+int fwi_mcs_geometry(float xs, float shot_depth, float streamer_depth, float near_offset, float drec, float dmodel,
+                     int num_rec, int* nxSou, int* nySou, int* nxRec, int* nyRec) {
+    if (num_rec < 0 || !(dmodel > 0.f)) return fail(FWI_ERR_ARG, "num_rec >= 0 and dmodel > 0 required");
+    const float added_space_model = 0.f;  // no parfile key sets it (modules.f90:153)
+    const float pos_shot = added_space_model + fabsf(xs);
+    if (nxSou) *nxSou = 1 + (int)ceilf(pos_shot / dmodel);
+    if (nySou) *nySou = 1 + (int)ceilf(shot_depth / dmodel);
+    for (int irec = 1; irec <= num_rec; ++irec) {
+        const float pos_rec = (pos_shot - near_offset) - (float)(irec - 1) * drec;
+        if (nxRec) nxRec[irec - 1] = 1 + (int)ceilf(pos_rec / dmodel);
+        if (nyRec) nyRec[irec - 1] = 1 + (int)ceilf(streamer_depth / dmodel);
+    }
+    return FWI_OK;
+}
+
+int fwi_ricker(float freq, float dt, int nt, float* out) {
+    if (nt < 0 || !out || !(freq > 0.f)) return fail(FWI_ERR_ARG, "bad Ricker arguments");
+    const float pi = 3.14159265f, f0 = freq, t0 = 1.5f / f0, tmp = 10.f / f0;
+    for (int i = 1; i <= nt; ++i) {
+        const float t = (float)(i - 1) * dt;
+        const float a = (pi * f0) * (t - t0);
+        float s = (1.f - 2.f * (a * a)) * expf(-(1.f * (a * a)));
+        if (t >= tmp) s = 0.f;
+        out[i - 1] = s;
+    }
+    return FWI_OK;
+}
+
+int fwi_time_rules(const float* lambda, int ny, int nx, float dmodel, float tfin, int store_snap, float* dt, int* nt,
+                   int* nt_Store) {
+    if (!lambda || ny < 1 || nx < 1 || store_snap < 1 || !dt || !nt || !nt_Store) return fail(FWI_ERR_ARG, "bad args");
+    float mx = -INFINITY;
+    for (size_t i = 0; i < (size_t)ny * nx; ++i) mx = std::max(mx, lambda[i] / 1000.f);
+    if (!(mx > 0.f)) return fail(FWI_ERR_ARG, "lambda must be positive");
+    *dt = (dmodel / sqrtf(mx)) / 2.f;
+    const int n0 = 1 + (int)ceilf(tfin / *dt);
+    const float temp = (float)(n0 / store_snap);
+    *nt_Store = (int)ceilf(temp);
+    *nt = *nt_Store * store_snap;
+    return FWI_OK;
+}
+
+}  // extern "C"
+
+// ===========================================================================
+// batched survey
+// ===========================================================================
+
+struct fwi_survey {
+    fwi_survey_desc desc{};
+    int nt_store = 0;
+    std::vector<ShotGeom> geoms;
+    std::vector<Layout> lays;
+    std::vector<double> gw, mw;
+    std::vector<int> tr_off;  // trace offsets per shot (size nshots+1)
+    int ntr = 0;
+    int wave = 1, band = 64;
+    std::vector<std::vector<int>> waves;  // shot indices per wave
+    // resident data
+    DBuf d_lambda, d_src, d_obs, d_synth, d_adj, d_mis_tr, d_mis_shot, d_tr_off, d_G, d_grad, d_water, d_fA, d_fB;
+    // per-slot state
+    std::vector<std::unique_ptr<ShotState>> slots;
+    // per-wave lists
+    struct WaveDev {
+        DBuf items_mf, items_ma, items_b, src_f, src_a, recs, shots_f, shots_a, stack;
+        int n_mf = 0, n_ma = 0, n_b = 0;
+        cudaGraphExec_t graph[3] = {nullptr, nullptr, nullptr};
+        long long graph_kernels[3] = {0, 0, 0};  // kernel nodes per graph
+    };
+    std::vector<std::unique_ptr<WaveDev>> wdev;
+    std::vector<float> h_fA, h_fB;
+    bool lambda_set = false;
+    ~fwi_survey() {
+        for (auto& w : wdev)
+            for (auto& gexec : w->graph)
+                if (gexec) cudaGraphExecDestroy(gexec);
+    }
+};
+
+namespace {
+
+size_t shot_wave_bytes(const Layout& l, int nt_store, int snap_form, int grad_form) {
+    const size_t fb = (size_t)l.nyt * l.pitch * 4;
+    const size_t esz = snap_form == FWI_SNAP_F32 ? 4 : 2;
+    const size_t sb = (size_t)(nt_store + 1) * l.ny * l.pitch * esz + (size_t)(nt_store + 1) * l.ny * l.ntiles * 4;
+    const size_t kb = (size_t)l.ny * l.pitch * (grad_form == FWI_GRAD_F64 ? 8 : 4);
+    return 7 * fb + sb + kb;
+}
+
+int survey_prepare_waves(fwi_survey* s) {
+    const auto& D = s->desc;
+    cudaStream_t st = stream();
+    s->waves.clear();
+    for (int i = 0; i < D.nshots; i += s->wave) {
+        std::vector<int> w;
+        for (int j = i; j < std::min(D.nshots, i + s->wave); ++j) w.push_back(j);
+        s->waves.push_back(w);
+    }
+    // slots sized for the largest layout
+    s->slots.clear();
+    for (int k = 0; k < s->wave; ++k) s->slots.emplace_back(new ShotState());
+    s->wdev.clear();
+    for (size_t wi = 0; wi < s->waves.size(); ++wi) {
+        const auto& w = s->waves[wi];
+        std::vector<ShotGeom> g;
+        std::vector<Layout> l;
+        for (int sh : w) {
+            g.push_back(s->geoms[sh]);
+            l.push_back(s->lays[sh]);
+        }
+        Lists lists = build_lists(g, l, s->band);
+        std::unique_ptr<fwi_survey::WaveDev> wd(new fwi_survey::WaveDev());
+        TRY(upload(wd->items_mf, lists.main_fwd, st));
+        TRY(upload(wd->items_ma, lists.main_adj, st));
+        TRY(upload(wd->items_b, lists.bottom, st));
+        TRY(upload(wd->src_f, lists.src_fwd, st));
+        TRY(upload(wd->src_a, lists.src_adj, st));
+        TRY(upload(wd->recs, lists.recs, st));
+        wd->n_mf = (int)lists.main_fwd.size();
+        wd->n_ma = (int)lists.main_adj.size();
+        wd->n_b = (int)lists.bottom.size();
+        s->wdev.push_back(std::move(wd));
+    }
+    // allocate slots for the largest shot that can land in each slot
+    for (int k = 0; k < s->wave; ++k) {
+        Layout big = s->lays[0];
+        size_t best = 0;
+        for (size_t wi = 0; wi < s->waves.size(); ++wi) {
+            if (k >= (int)s->waves[wi].size()) continue;
+            const Layout& l = s->lays[s->waves[wi][k]];
+            const size_t b = (size_t)l.nyt * l.pitch;
+            if (b >= best) {
+                best = b;
+                big = l;
+            }
+        }
+        TRY(s->slots[k]->alloc(big, s->nt_store + 1, D.snap_form, D.grad_form));
+    }
+    // per-wave shot descriptors (fwd: sources; adj: adjoint source table)
+    for (size_t wi = 0; wi < s->waves.size(); ++wi) {
+        const auto& w = s->waves[wi];
+        std::vector<ShotDev> f, a;
+        std::vector<unsigned char> stk(w.size() * stack_shot_size());
+        for (size_t k = 0; k < w.size(); ++k) {
+            const int sh = w[k];
+            ShotState& ss = *s->slots[k];
+            const Layout& l = s->lays[sh];
+            ShotDev dv = ss.dev(D.nt, (int)s->geoms[sh].nxR.size(), s->geoms[sh].x0, nullptr,
+                                s->d_synth.as<float>() + (size_t)s->tr_off[sh] * D.nt);
+            dv.snap_stride = (long long)l.ny * l.pitch;
+            dv.ny = l.ny; dv.nx = l.nx; dv.nyt = l.nyt; dv.nxt = l.nxt; dv.off = l.off; dv.pitch = l.pitch;
+            dv.ntiles = l.ntiles; dv.dn = l.dn;
+            // forward value table: this shot's sources (packed in shot order)
+            size_t soff = 0;
+            for (int q = 0; q < sh; ++q) soff += s->geoms[q].nxS.size();
+            dv.srcv = s->d_src.as<float>() + soff * D.nt;
+            f.push_back(dv);
+            dv.srcv = s->d_adj.as<float>() + (size_t)s->tr_off[sh] * D.nt;
+            a.push_back(dv);
+            fill_stack_shot(stk.data() + k * stack_shot_size(), ss.k.as<float>(), ss.k.as<double>(), s->geoms[sh].x0,
+                            l.nx, l.off + l.dn, l.pitch, s->gw[sh]);
+        }
+        auto& wd = *s->wdev[wi];
+        TRY(upload(wd.shots_f, f, st));
+        TRY(upload(wd.shots_a, a, st));
+        TRY(upload(wd.stack, stk, st));
+    }
+    CK(cudaStreamSynchronize(st));
+    return FWI_OK;
+}
+
+// Issue one wave's work: forward (+ misfit) and, for step 1, adjoint + stack.
+int issue_wave(fwi_survey* s, size_t wi, int step, cudaStream_t st) {
+    const auto& D = s->desc;
+    const auto& w = s->waves[wi];
+    auto& wd = *s->wdev[wi];
+    for (size_t k = 0; k < w.size(); ++k) {
+        const int sh = w[k];
+        ShotState& ss = *s->slots[k];
+        const Layout& l = s->lays[sh];
+        // the slot may be larger than this shot: zero the whole allocation
+        CK(cudaMemsetAsync(ss.pa.p, 0, ss.pa.n, st));
+        CK(cudaMemsetAsync(ss.pb.p, 0, ss.pb.n, st));
+        CK(cudaMemsetAsync(ss.phx.p, 0, ss.phx.n, st));
+        CK(cudaMemsetAsync(ss.chx.p, 0, ss.chx.n, st));
+        CK(cudaMemsetAsync(ss.phy.p, 0, ss.phy.n, st));
+        CK(cudaMemsetAsync(ss.chy.p, 0, ss.chy.n, st));
+        CK(cudaMemsetAsync(ss.c2.p, 0, ss.c2.n, st));
+        LK(launch_build_c2(ss.c2.as<float>(), l.nyt, l.pitch, l.off, l.dn, l.ny, l.nx, s->d_lambda.as<float>(), D.ny,
+                           s->geoms[sh].x0, 1, D.dt * D.dt, D.d * D.d, st));
+        float* rec = s->d_synth.as<float>() + (size_t)s->tr_off[sh] * D.nt;
+        CK(cudaMemsetAsync(rec, 0, (size_t)(int)s->geoms[sh].nxR.size() * D.nt * sizeof(float), st));
+    }
+    StepSet ps;
+    ps.pm = base_params(D.acc, D.dt, D.store_snap, D.snap_form, D.grad_form, s->d_fA.as<float>(), s->d_fB.as<float>());
+    ps.pm.items = wd.items_mf.as<WorkItem>();
+    ps.pm.nitems = wd.n_mf;
+    ps.pm.shots = wd.shots_f.as<ShotDev>();
+    ps.pm.srcs = wd.src_f.as<SrcEnt>();
+    ps.pm.recs = wd.recs.as<RecEnt>();
+    ps.pm.record = 1;
+    ps.pb = ps.pm;
+    ps.pb.items = wd.items_b.as<WorkItem>();
+    ps.pb.nitems = wd.n_b;
+    TRY(run_time_loop(D.acc, 0, D.nt, D.store_snap, s->nt_store, step == 1, ps, st));
+    for (size_t k = 0; k < w.size(); ++k) {
+        const int sh = w[k];
+        LK(launch_rec_last(s->d_synth.as<float>() + (size_t)s->tr_off[sh] * D.nt, D.nt, (int)s->geoms[sh].nxR.size(), st));
+    }
+    // misfit + adjoint source for this wave's traces
+    const int t0 = s->tr_off[w.front()], t1 = s->tr_off[w.back() + 1];
+    LK(launch_misfit(s->d_synth.as<float>() + (size_t)t0 * D.nt, s->d_obs.as<float>() + (size_t)t0 * D.nt,
+                     s->d_adj.as<float>() + (size_t)t0 * D.nt, s->d_mis_tr.as<double>() + t0, D.nt, D.dt,
+                     s->d_tr_off.as<int>(), t1 - t0, 0, nullptr, st));
+    if (step != 1) return FWI_OK;
+    for (size_t k = 0; k < w.size(); ++k) {
+        ShotState& ss = *s->slots[k];
+        CK(cudaMemsetAsync(ss.pa.p, 0, ss.pa.n, st));
+        CK(cudaMemsetAsync(ss.pb.p, 0, ss.pb.n, st));
+        CK(cudaMemsetAsync(ss.phx.p, 0, ss.phx.n, st));
+        CK(cudaMemsetAsync(ss.chx.p, 0, ss.chx.n, st));
+        CK(cudaMemsetAsync(ss.phy.p, 0, ss.phy.n, st));
+        CK(cudaMemsetAsync(ss.chy.p, 0, ss.chy.n, st));
+        CK(cudaMemsetAsync(ss.k.p, 0, ss.k.n, st));
+    }
+    ps.pm.items = wd.items_ma.as<WorkItem>();
+    ps.pm.nitems = wd.n_ma;
+    ps.pm.shots = wd.shots_a.as<ShotDev>();
+    ps.pm.srcs = wd.src_a.as<SrcEnt>();
+    ps.pm.record = 0;
+    ps.pb.shots = wd.shots_a.as<ShotDev>();
+    ps.pb.record = 0;
+    TRY(run_time_loop(D.acc, 1, D.nt, D.store_snap, s->nt_store, true, ps, st));
+    LK(launch_stack(s->d_G.as<double>(), D.ny, D.nx_model, wd.stack.p, (int)w.size(), D.grad_form, st));
+    return FWI_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int fwi_survey_create(const fwi_survey_desc* desc, fwi_survey** out) {
+    std::lock_guard<std::recursive_mutex> g(L().mu);
+    TRY(ensure_init());
+    if (!desc || !out) return fail(FWI_ERR_ARG, "null argument");
+    const fwi_survey_desc& D = *desc;
+    TRY(validate_common(D.ny, D.nx_model, D.acc, D.dpml, D.nt, D.store_snap));
+    if (D.nshots < 1 || !D.shots) return fail(FWI_ERR_ARG, "nshots must be >= 1");
+    if (!(D.d > 0.f) || !(D.dt > 0.f)) return fail(FWI_ERR_ARG, "d and dt must be positive");
+    if (D.numtasks < 1) return fail(FWI_ERR_ARG, "numtasks must be >= 1");
+    if (D.snap_form < 0 || D.snap_form > 2 || D.grad_form < 0 || D.grad_form > 1)
+        return fail(FWI_ERR_ARG, "bad snap_form / grad_form");
+    std::unique_ptr<fwi_survey> s(new fwi_survey());
+    s->desc = D;
+    s->nt_store = D.nt / D.store_snap;
+    if ((int)snapshot_steps(D.nt, D.store_snap).size() > s->nt_store)
+        return fail(FWI_ERR_ARG, "nt/store_snap snapshots exceed nt_Store");
+    s->tr_off.assign(D.nshots + 1, 0);
+    int nsou_tot = 0;
+    for (int i = 0; i < D.nshots; ++i) {
+        const fwi_shot& sh = D.shots[i];
+        if (sh.nx < 1 || sh.x0 < 0 || sh.x0 + sh.nx > D.nx_model)
+            return fail(FWI_ERR_ARG, "shot " + std::to_string(i) + ": window outside the model");
+        if (sh.num_sou < 0 || sh.num_rec < 0) return fail(FWI_ERR_ARG, "negative source/receiver count");
+        if ((sh.num_sou && (!sh.nxSou || !sh.nySou)) || (sh.num_rec && (!sh.nxRec || !sh.nyRec)))
+            return fail(FWI_ERR_ARG, "shot " + std::to_string(i) + ": null geometry arrays");
+        ShotGeom geo;
+        geo.x0 = sh.x0;
+        geo.nx = sh.nx;
+        geo.nxS.assign(sh.nxSou, sh.nxSou + sh.num_sou);
+        geo.nyS.assign(sh.nySou, sh.nySou + sh.num_sou);
+        geo.nxR.assign(sh.nxRec, sh.nxRec + sh.num_rec);
+        geo.nyR.assign(sh.nyRec, sh.nyRec + sh.num_rec);
+        const Layout l = make_layout(D.ny, sh.nx, D.acc, D.dpml);
+        TRY(validate_geometry(geo, l, i + 1));
+        s->geoms.push_back(geo);
+        s->lays.push_back(l);
+        s->gw.push_back(sh.grad_weight);
+        s->mw.push_back(sh.misfit_weight);
+        s->tr_off[i + 1] = s->tr_off[i] + sh.num_rec;
+        nsou_tot += sh.num_sou;
+    }
+    s->ntr = s->tr_off[D.nshots];
+    cudaStream_t st = stream();
+    const size_t nt = D.nt;
+    // resident data
+    TRY(s->d_lambda.alloc((size_t)D.ny * D.nx_model * 4));
+    TRY(s->d_src.alloc(std::max<size_t>(nt * nsou_tot * 4, 16)));
+    TRY(s->d_obs.alloc(std::max<size_t>(nt * s->ntr * 4, 16)));
+    TRY(s->d_synth.alloc(std::max<size_t>(nt * s->ntr * 4, 16)));
+    TRY(s->d_adj.alloc(std::max<size_t>(nt * s->ntr * 4, 16)));
+    TRY(s->d_mis_tr.alloc(std::max<size_t>(s->ntr * 8, 16)));
+    TRY(s->d_mis_shot.alloc(D.nshots * 8));
+    TRY(upload(s->d_tr_off, s->tr_off, st));
+    TRY(s->d_G.alloc((size_t)D.ny * D.nx_model * 8));
+    TRY(s->d_grad.alloc((size_t)D.ny * D.nx_model * 4));
+    if (D.water_rows) {
+        std::vector<int> w(D.water_rows, D.water_rows + D.nx_model);
+        TRY(upload(s->d_water, w, st));
+    }
+    pml_factors(D.acc, D.dpml, D.dt, D.d, s->h_fA, s->h_fB);
+    TRY(upload(s->d_fA, s->h_fA, st));
+    TRY(upload(s->d_fB, s->h_fB, st));
+    {
+        size_t so = 0, to = 0;
+        for (int i = 0; i < D.nshots; ++i) {
+            const fwi_shot& sh = D.shots[i];
+            if (sh.num_sou && sh.src)
+                CK(cudaMemcpyAsync(s->d_src.as<float>() + so, sh.src, nt * sh.num_sou * 4, cudaMemcpyHostToDevice, st));
+            else if (sh.num_sou)
+                CK(cudaMemsetAsync(s->d_src.as<float>() + so, 0, nt * sh.num_sou * 4, st));
+            if (sh.num_rec && sh.obs)
+                CK(cudaMemcpyAsync(s->d_obs.as<float>() + to, sh.obs, nt * sh.num_rec * 4, cudaMemcpyHostToDevice, st));
+            else if (sh.num_rec)
+                CK(cudaMemsetAsync(s->d_obs.as<float>() + to, 0, nt * sh.num_rec * 4, st));
+            so += nt * sh.num_sou;
+            to += nt * sh.num_rec;
+        }
+    }
+    CK(cudaStreamSynchronize(st));
+    s->desc.shots = nullptr;  // host pointers are not kept
+    // wave size from the HBM budget
+    size_t per = 0;
+    for (auto& l : s->lays) per = std::max(per, shot_wave_bytes(l, s->nt_store, D.snap_form, D.grad_form));
+    size_t freeb = 0, totb = 0;
+    CK(cudaMemGetInfo(&freeb, &totb));
+    size_t budget = (size_t)(0.92 * (double)freeb);
+    if (D.hbm_budget) {
+        size_t used_resident = s->d_obs.n + s->d_synth.n + s->d_adj.n + s->d_src.n + s->d_G.n + s->d_lambda.n;
+        if (D.hbm_budget <= used_resident) return fail(FWI_ERR_NOMEM, "HBM budget smaller than the resident data");
+        budget = std::min(budget, D.hbm_budget - used_resident);
+    }
+    int wave = (int)std::min<size_t>((size_t)D.nshots, budget / std::max<size_t>(per, 1));
+    if (wave < 1)
+        return fail(FWI_ERR_NOMEM, "one shot's wavefields and snapshots (" + std::to_string(per) +
+                                       " bytes) exceed the device budget");
+    if (D.wave_shots > 0) wave = std::min(wave, D.wave_shots);
+    // balance the waves: same number of shots in each
+    const int nw = (D.nshots + wave - 1) / wave;
+    wave = (D.nshots + nw - 1) / nw;
+    s->wave = wave;
+    s->band = D.band_rows > 0 ? D.band_rows : 64;
+    TRY(survey_prepare_waves(s.get()));
+    *out = s.release();
+    return FWI_OK;
+}
+
+int fwi_survey_destroy(fwi_survey* s) {
+    std::lock_guard<std::recursive_mutex> g(L().mu);
+    if (!s) return FWI_OK;
+    cudaStreamSynchronize(stream());
+    delete s;
+    return FWI_OK;
+}
+
+int fwi_survey_set_lambda(fwi_survey* s, const float* lambda) {
+    std::lock_guard<std::recursive_mutex> g(L().mu);
+    if (!s || !lambda) return fail(FWI_ERR_STATE, "null survey or lambda");
+    const size_t n = (size_t)s->desc.ny * s->desc.nx_model * 4;
+    CK(cudaMemcpyAsync(s->d_lambda.p, lambda, n, is_device_ptr(lambda) ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
+                       stream()));
+    s->lambda_set = true;
+    return FWI_OK;
+}
+
+int fwi_survey_set_observed(fwi_survey* s, const float* obs) {
+    std::lock_guard<std::recursive_mutex> g(L().mu);
+    if (!s || !obs) return fail(FWI_ERR_STATE, "null survey or data");
+    const size_t n = (size_t)s->ntr * s->desc.nt * 4;
+    if (n) CK(cudaMemcpyAsync(s->d_obs.p, obs, n, is_device_ptr(obs) ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
+                              stream()));
+    return FWI_OK;
+}
+
+int fwi_survey_set_sources(fwi_survey* s, const float* src) {
+    std::lock_guard<std::recursive_mutex> g(L().mu);
+    if (!s || !src) return fail(FWI_ERR_STATE, "null survey or sources");
+    size_t nsou = 0;
+    for (auto& gg : s->geoms) nsou += gg.nxS.size();
+    const size_t n = nsou * s->desc.nt * 4;
+    if (n) CK(cudaMemcpyAsync(s->d_src.p, src, n, is_device_ptr(src) ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
+                              stream()));
+    return FWI_OK;
+}
+
+int fwi_survey_run(fwi_survey* s, int step, double* misfit, float* grad) {
+    std::lock_guard<std::recursive_mutex> g(L().mu);
+    if (!s) return fail(FWI_ERR_STATE, "null survey");
+    if (!s->lambda_set) return fail(FWI_ERR_STATE, "fwi_survey_set_lambda has not been called");
+    if (step != 1 && step != 2) return fail(FWI_ERR_ARG, "step must be 1 or 2");
+    const auto& D = s->desc;
+    cudaStream_t st = stream();
+    CK(cudaMemsetAsync(s->d_G.p, 0, s->d_G.n, st));
+    const int gi = step == 1 ? 0 : 1;
+    for (size_t wi = 0; wi < s->waves.size(); ++wi) {
+        auto& wd = *s->wdev[wi];
+        if (D.flags & FWI_SURVEY_NO_GRAPH) {
+            TRY(issue_wave(s, wi, step, st));
+            continue;
+        }
+        if (!wd.graph[gi]) {
+            cudaStream_t cap;
+            CK(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
+            cudaGraph_t graph;
+            CK(cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal));
+            const long long l0 = L().launches;
+            int rc = issue_wave(s, wi, step, cap);
+            cudaError_t e = cudaStreamEndCapture(cap, &graph);
+            cudaStreamDestroy(cap);
+            if (rc != FWI_OK) return rc;
+            if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture", __LINE__);
+            wd.graph_kernels[gi] = L().launches - l0;
+            L().launches = l0;  // counted when replayed
+            e = cudaGraphInstantiate(&wd.graph[gi], graph, 0);
+            cudaGraphDestroy(graph);
+            if (e != cudaSuccess) return cuda_fail(e, "cudaGraphInstantiate", __LINE__);
+        }
+        CK(cudaGraphLaunch(wd.graph[gi], st));
+        L().launches += wd.graph_kernels[gi];
+    }
+    // per-shot misfits (FP64) in shot order
+    std::vector<double> mis_tr(s->ntr);
+    if (s->ntr) CK(cudaMemcpyAsync(mis_tr.data(), s->d_mis_tr.p, s->ntr * 8, cudaMemcpyDeviceToHost, st));
+    if (grad && step == 1) {
+        const size_t n = (size_t)D.ny * D.nx_model * 4;
+        const bool dev = is_device_ptr(grad);
+        float* dg = dev ? grad : s->d_grad.as<float>();
+        if (!dev) CK(cudaMemcpyAsync(dg, grad, n, cudaMemcpyHostToDevice, st));
+        LK(launch_finalize(dg, s->d_G.as<double>(), D.ny, D.nx_model, D.numtasks,
+                           s->d_water.p ? s->d_water.as<int>() : nullptr, st));
+        if (!dev) CK(cudaMemcpyAsync(grad, dg, n, cudaMemcpyDeviceToHost, st));
+    }
+    CK(cudaStreamSynchronize(st));
+    double tot = 0.0;
+    bool finite = true;
+    for (int i = 0; i < D.nshots; ++i) {
+        double m = 0.0;
+        for (int t = s->tr_off[i]; t < s->tr_off[i + 1]; ++t) m += mis_tr[t];
+        if (!std::isfinite(m)) finite = false;
+        tot += s->mw[i] * m;
+    }
+    if (misfit) *misfit += tot;
+    if (!finite) return fail(FWI_ERR_NONFINITE, "non-finite misfit (the time step may violate the CFL limit)");
+    return FWI_OK;
+}
+
+int fwi_survey_grad_device(fwi_survey* s, const double** ptr) {
+    if (!s || !ptr) return fail(FWI_ERR_STATE, "null argument");
+    *ptr = s->d_G.as<double>();
+    return FWI_OK;
+}
+
+int fwi_survey_get_synthetic(fwi_survey* s, int shot, float* out) {
+    std::lock_guard<std::recursive_mutex> g(L().mu);
+    if (!s || !out) return fail(FWI_ERR_STATE, "null argument");
+    if (shot < 0 || shot >= s->desc.nshots) return fail(FWI_ERR_ARG, "shot index out of range");
+    const size_t n = (size_t)(s->tr_off[shot + 1] - s->tr_off[shot]) * s->desc.nt * 4;
+    if (n)
+        CK(cudaMemcpyAsync(out, s->d_synth.as<float>() + (size_t)s->tr_off[shot] * s->desc.nt, n,
+                           cudaMemcpyDeviceToHost, stream()));
+    CK(cudaStreamSynchronize(stream()));
+    return FWI_OK;
+}
+
+int fwi_survey_step_bytes(fwi_survey* s, double* bytes) {
+    if (!s || !bytes) return fail(FWI_ERR_STATE, "null argument");
+    double b = 0.0;
+    for (auto& l : s->lays) b += step_bytes_shot(l.ny, l.nx, l.dn);
+    *bytes = b;
+    return FWI_OK;
+}
+
+int fwi_survey_tuning(fwi_survey* s, int* wave_shots, int* band_rows) {
+    if (!s) return fail(FWI_ERR_STATE, "null survey");
+    if (wave_shots) *wave_shots = s->wave;
+    if (band_rows) *band_rows = s->band;
+    return FWI_OK;
+}
+
+int fwi_survey_time_steps(fwi_survey* s, int steps) {
+    std::lock_guard<std::recursive_mutex> g(L().mu);
+    if (!s) return fail(FWI_ERR_STATE, "null survey");
+    const auto& D = s->desc;
+    auto& wd = *s->wdev[0];
+    StepSet ps;
+    ps.pm = base_params(D.acc, D.dt, D.store_snap, D.snap_form, D.grad_form, s->d_fA.as<float>(), s->d_fB.as<float>());
+    ps.pm.items = wd.items_mf.as<WorkItem>();
+    ps.pm.nitems = wd.n_mf;
+    ps.pm.shots = wd.shots_f.as<ShotDev>();
+    ps.pm.srcs = wd.src_f.as<SrcEnt>();
+    ps.pm.recs = wd.recs.as<RecEnt>();
+    ps.pm.record = 1;
+    ps.pb = ps.pm;
+    ps.pb.items = wd.items_b.as<WorkItem>();
+    ps.pb.nitems = wd.n_b;
+    for (int i = 0; i < steps; ++i) {
+        const int k = 2 + (i % (D.nt - 1));
+        ps.pm.t = ps.pb.t = k - 2;
+        ps.pm.parity = ps.pb.parity = k & 1;
+        CK(launch_step(D.acc, 0, ps.pm, ps.pb, stream()));
+        L().launches += 2;
+    }
+    return FWI_OK;
+}
+
+int fwi_misfit_gradient_batch(const fwi_survey_desc* desc, const float* lambda, int step, float* Misfit, float* Grad) {
+    std::lock_guard<std::recursive_mutex> g(L().mu);
+    TRY(ensure_init());
+    if (!desc || !lambda) return fail(FWI_ERR_ARG, "null argument");
+    // plan cache keyed by the geometry (sizes and indices); data re-uploaded
+    static std::map<std::string, std::unique_ptr<fwi_survey>> cache;
+    std::string key;
+    auto add = [&](const void* p, size_t n) { key.append(reinterpret_cast<const char*>(p), n); };
+    fwi_survey_desc k0 = *desc;
+    k0.shots = nullptr;
+    k0.water_rows = nullptr;
+    add(&k0, sizeof k0);
+    for (int i = 0; i < desc->nshots; ++i) {
+        const fwi_shot& sh = desc->shots[i];
+        add(&sh.x0, sizeof(int) * 4);
+        add(&sh.grad_weight, sizeof(double) * 2);
+        if (sh.num_sou) { add(sh.nxSou, 4 * sh.num_sou); add(sh.nySou, 4 * sh.num_sou); }
+        if (sh.num_rec) { add(sh.nxRec, 4 * sh.num_rec); add(sh.nyRec, 4 * sh.num_rec); }
+    }
+    if (desc->water_rows) add(desc->water_rows, 4 * desc->nx_model);
+    auto it = cache.find(key);
+    fwi_survey* s = nullptr;
+    if (it == cache.end()) {
+        if (cache.size() >= 4) cache.clear();
+        fwi_survey* ns = nullptr;
+        TRY(fwi_survey_create(desc, &ns));
+        cache[key].reset(ns);
+        s = ns;
+    } else {
+        s = it->second.get();
+        // new data for the same geometry
+        cudaStream_t st = stream();
+        size_t so = 0, to = 0;
+        const size_t nt = desc->nt;
+        for (int i = 0; i < desc->nshots; ++i) {
+            const fwi_shot& sh = desc->shots[i];
+            if (sh.num_sou && sh.src)
+                CK(cudaMemcpyAsync(s->d_src.as<float>() + so, sh.src, nt * sh.num_sou * 4, cudaMemcpyHostToDevice, st));
+            if (sh.num_rec && sh.obs)
+                CK(cudaMemcpyAsync(s->d_obs.as<float>() + to, sh.obs, nt * sh.num_rec * 4, cudaMemcpyHostToDevice, st));
+            so += nt * sh.num_sou;
+            to += nt * sh.num_rec;
+        }
+    }
+    TRY(fwi_survey_set_lambda(s, lambda));
+    double m = 0.0;
+    const int rc = fwi_survey_run(s, step, &m, step == 1 ? Grad : nullptr);
+    if (Misfit) *Misfit = *Misfit + (float)m;
+    return rc;
+}
+
+}  // extern "C"

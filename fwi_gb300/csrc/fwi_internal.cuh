@@ -1,0 +1,83 @@
+// Internal device data structures of the FWI step kernels.
+//
+// Device layout of one shot (all fields float, row-major, x fastest):
+//   rows 0..nyt-1 of the padded grid (nyt = dn + ny + dn, dn = dpml + 2*acc),
+//   row pitch `pitch` floats (a multiple of TILE = 128), logical padded column
+//   c stored at physical column off + c.  `off` (a multiple of 4) is chosen so
+//   that the first 128-column tile holds the whole left CPML strip and the
+//   last tile holds the whole right strip; every other tile is interior.
+//   One warp owns one tile (4 columns per lane, float4) and marches down a
+//   band of rows with a register queue of 2*acc+1 rows.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace fwi {
+
+constexpr int TILE = 128;       // columns per warp tile (32 lanes x float4)
+constexpr int MAXR = 4;         // largest supported FD half-order (acc)
+constexpr int MAXDN = 64;       // largest supported CPML pad (dpml + 2*acc)
+
+struct SrcEnt {                 // one injected source cell (deduplicated)
+    int row;                    // padded row
+    int col;                    // physical column
+    int vidx;                   // index into the shot's value table [vidx][nt]
+};
+struct RecEnt {                 // one recorded receiver
+    int row, col;               // padded row, physical column
+    int ridx;                   // receiver index: Rec_point(:, ridx+1)
+};
+
+struct WorkItem {               // one warp's work in a step launch
+    int shot;
+    int tile;                   // tile index (x0 = tile*TILE physical)
+    int y0, y1;                 // padded rows [y0, y1)
+    int kind;                   // 0 = model rows, 1 = bottom pad rows
+    int s0, s1;                 // SrcEnt range (sorted by row)
+    int r0, r1;                 // RecEnt range (sorted by row)
+    int pad_;
+};
+
+struct ShotDev {
+    float* pa;                  // wavefield ping-pong buffers
+    float* pb;
+    const float* c2;            // c^2 dt^2 / d^2
+    float* phx;                 // x-direction CPML phi (side strips and corners)
+    float* chx;                 // x-direction chi
+    float* phy;                 // y-direction phi (bottom strip and corners)
+    float* chy;                 // y-direction chi
+    const float* srcv;          // injected values [vidx][nt]
+    float* rec;                 // Rec_point(nt, nrec) column-major
+    void* snaps;                // snapshots [s][ny][pitch] (float / 16-bit)
+    float* sscale;              // 16-bit snapshot scales [s][ny][ntiles]
+    float* k32;                 // FP32 imaging accumulator [ny][pitch]
+    double* k64;                // FP64 imaging accumulator [ny][pitch]
+    long long snap_stride;      // elements per snapshot block (ny*pitch)
+    int ny, nx, nyt, nxt;
+    int off, pitch, ntiles, dn;
+    int nt, nrec;
+    int x0;                     // window start in the full model
+    int pad_;
+};
+
+struct StepParams {
+    const WorkItem* items;
+    const ShotDev* shots;
+    const SrcEnt* srcs;         // source cells of all items (sorted per item)
+    const RecEnt* recs;         // receiver cells of all items (sorted per item)
+    const float* fA;            // CPML factors (dn entries, 0-based)
+    const float* fB;
+    int nitems;
+    int t;                      // k-2: source column / receiver row this step
+    int parity;                 // k & 1: which buffer holds p_1 (written as p_3)
+    int snap;                   // snapshot block this step, -1 if none
+    int snap_form;              // FWI_SNAP_*
+    int grad_form;              // FWI_GRAD_*
+    int record;                 // 1: record receivers
+    float dt;                   // for ((p3-p1)*0.5)/dt
+    float ss;                   // float(store_snap) for the imaging condition
+    float c1[MAXR + 1];         // first-derivative taps
+    float c2[MAXR + 1];         // second-derivative taps (centre halved)
+};
+
+}  // namespace fwi

@@ -1,0 +1,584 @@
+// FWI time-step kernels for sm_103a.
+//
+// One launch of k_step_main plus one of k_step_bottom advance every shot of a
+// wave by one time step of the reference solver (solver_acoustic_SS.f90:313-586):
+//
+//   k_step_main    model rows dn..dn+ny-1: interior update with source
+//                  injection (:319-330, :433-434), left/right CPML strips
+//                  (pml_matrices_x, solver_PML_matrices.f90:1-40), snapshot
+//                  store (:438-454) or imaging condition (:457-473),
+//                  receiver recording (:551-555);
+//   k_step_bottom  bottom pad rows: bottom CPML strip (pml_matrices_y
+//                  :42-81) and the two bottom corners in two stages
+//                  (pml_matrices_xycorner :83-112, solver_acoustic_SS.f90:395-411).
+//
+// The top pad rows are never written: with the free surface they stay
+// exactly zero for the whole run (solver_acoustic_SS.f90:416-429, :477-479).
+//
+// Every warp owns a 128-column tile (4 columns per lane, float4) and marches
+// down a band of rows; the y-stencil comes from a register queue of 2R+1
+// rows, the x-stencil from warp shuffles of the current row plus one halo
+// float4 at each end of the tile.  The wavefield is ping-ponged between two
+// buffers: p_3 overwrites p_1 in place (each cell reads its own p_1 only).
+// The CPML memory variables are updated in place: the strip-local
+// derivative of phi only reads phi values of the same warp, loaded before
+// they are overwritten.
+//
+// This file is compiled with --fmad=false: every a*b+c below is a rounded
+// multiply followed by a rounded add, in the order the Fortran source writes
+// the expression, so results are bit-identical to the reference arithmetic.
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+
+#include <climits>
+
+#include "fwi_internal.cuh"
+
+namespace fwi {
+
+namespace {
+
+constexpr unsigned FULL = 0xffffffffu;
+
+__device__ __forceinline__ float4 ldg4(const float* p) { return __ldg(reinterpret_cast<const float4*>(p)); }
+__device__ __forceinline__ float4 ld4(const float* p) { return *reinterpret_cast<const float4*>(p); }
+__device__ __forceinline__ void st4(float* p, float4 v) { *reinterpret_cast<float4*>(p) = v; }
+
+__device__ __forceinline__ void to_arr(float4 v, float* a) { a[0] = v.x; a[1] = v.y; a[2] = v.z; a[3] = v.w; }
+__device__ __forceinline__ float4 from_arr(const float* a) { return make_float4(a[0], a[1], a[2], a[3]); }
+__device__ __forceinline__ float sel(const float* a, int e) {
+    return e == 0 ? a[0] : (e == 1 ? a[1] : (e == 2 ? a[2] : a[3]));
+}
+__device__ __forceinline__ float4 shfl_up4(float4 v) {
+    return make_float4(__shfl_up_sync(FULL, v.x, 1), __shfl_up_sync(FULL, v.y, 1), __shfl_up_sync(FULL, v.z, 1),
+                       __shfl_up_sync(FULL, v.w, 1));
+}
+__device__ __forceinline__ float4 shfl_dn4(float4 v) {
+    return make_float4(__shfl_down_sync(FULL, v.x, 1), __shfl_down_sync(FULL, v.y, 1),
+                       __shfl_down_sync(FULL, v.z, 1), __shfl_down_sync(FULL, v.w, 1));
+}
+
+// 12-value window of a row around this lane's 4 columns: w[4+e] is column e.
+__device__ __forceinline__ void window(float4 c, float4 hl, float4 hr, int lane, float* w) {
+    float4 l = shfl_up4(c), r = shfl_dn4(c);
+    if (lane == 0) l = hl;
+    if (lane == 31) r = hr;
+    to_arr(l, w);
+    to_arr(c, w + 4);
+    to_arr(r, w + 8);
+}
+
+// space_deriv2x / space_derivx at this lane's columns (solver_space_derivs.f90:11-16, :70-82)
+template <int R>
+__device__ __forceinline__ void xderivs(const float* w, const StepParams& P, float* d2, float* d1) {
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+        float s2 = 0.f, s1 = 0.f;
+#pragma unroll
+        for (int i = 0; i <= R; ++i) {
+            s2 = s2 + P.c2[i] * (w[4 + e + i] + w[4 + e - i]);
+            s1 = s1 + (w[4 + e + i] - w[4 + e - i]) * P.c1[i];
+        }
+        d2[e] = s2;
+        d1[e] = s1;
+    }
+}
+
+// space_deriv2y / space_derivy at the centre row of the queue (:38-45, :109-116)
+template <int R>
+__device__ __forceinline__ void yderivs(const float4* q, const StepParams& P, float* d2, float* d1) {
+    float a[2 * R + 1][4];
+#pragma unroll
+    for (int i = 0; i <= 2 * R; ++i) to_arr(q[i], a[i]);
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+        float s2 = 0.f, s1 = 0.f;
+#pragma unroll
+        for (int i = 0; i <= R; ++i) {
+            s2 = s2 + (a[R + i][e] + a[R - i][e]) * P.c2[i];
+            s1 = s1 + (a[R + i][e] - a[R - i][e]) * P.c1[i];
+        }
+        d2[e] = s2;
+        d1[e] = s1;
+    }
+}
+
+// First derivative along y of the centre row of a queue (strip-local phi).
+template <int R>
+__device__ __forceinline__ void yderiv1(const float4* f, const StepParams& P, float* d1) {
+    float a[2 * R + 1][4];
+#pragma unroll
+    for (int i = 0; i <= 2 * R; ++i) to_arr(f[i], a[i]);
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+        float s1 = 0.f;
+#pragma unroll
+        for (int i = 0; i <= R; ++i) s1 = s1 + (a[R + i][e] - a[R - i][e]) * P.c1[i];
+        d1[e] = s1;
+    }
+}
+
+// Fetch element `col` (physical, inside this tile) of a per-lane 4-array.
+__device__ __forceinline__ float fetch(const float* a, int col_in_tile) {
+    const int ln = col_in_tile >> 2, el = col_in_tile & 3;
+    return __shfl_sync(FULL, sel(a, el), ln);
+}
+
+// Grid-edge clamp of the x derivatives: columns < R copy column R, columns
+// > nxt-1-R copy column nxt-1-R (solver_space_derivs.f90:18-23, :84-94).
+template <int R>
+__device__ __forceinline__ void xclamp(const ShotDev& S, int x0, int c0, bool first, bool last, float* d2, float* d1) {
+    if (first) {
+        const int ct = S.off + R - x0;
+        const float v2 = fetch(d2, ct), v1 = fetch(d1, ct);
+#pragma unroll
+        for (int e = 0; e < 4; ++e)
+            if (c0 + e < R) { d2[e] = v2; d1[e] = v1; }
+    }
+    if (last) {
+        const int ct = S.off + S.nxt - 1 - R - x0;
+        const float v2 = fetch(d2, ct), v1 = fetch(d1, ct);
+#pragma unroll
+        for (int e = 0; e < 4; ++e)
+            if (c0 + e > S.nxt - 1 - R) { d2[e] = v2; d1[e] = v1; }
+    }
+}
+
+// Strip-local x derivative of the old x-direction phi with the strip-edge
+// clamp (pml_matrices_x / _xycorner call space_derivx on the dn-wide strip
+// array, solver_PML_matrices.f90:15, :97).  Valid for columns of the side
+// strips / corners only.
+template <int R>
+__device__ __forceinline__ void phi_xderiv(const ShotDev& S, const StepParams& P, float4 ph, int lane, int x0, int c0,
+                                           bool first, bool last, float* dph) {
+    float w[12];
+    window(ph, ph, ph, lane, w);
+    float d2u[4];
+    xderivs<R>(w, P, d2u, dph);
+    const int dn = S.dn, nx = S.nx;
+    if (first) {
+        const float lo = fetch(dph, S.off + R - x0), hi = fetch(dph, S.off + dn - 1 - R - x0);
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+            const int c = c0 + e;
+            if (c < dn) {
+                if (c < R) dph[e] = lo;
+                else if (c > dn - 1 - R) dph[e] = hi;
+            }
+        }
+    }
+    if (last) {
+        const int base = dn + nx;
+        const float lo = fetch(dph, S.off + base + R - x0), hi = fetch(dph, S.off + base + dn - 1 - R - x0);
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+            const int il = c0 + e - base;
+            if (il >= 0) {
+                if (il < R) dph[e] = lo;
+                else if (il > dn - 1 - R) dph[e] = hi;
+            }
+        }
+    }
+}
+
+// Snapshot store (forward) of the interior cells of one row:
+// Fields(j, snap*nx+i) = (p_3 - p_1)*0.5/dt   (solver_acoustic_SS.f90:447)
+__device__ __forceinline__ void store_snapshot(const StepParams& P, const ShotDev& S, int yrow, int lane, int x0,
+                                               int xl, int c0, const float* p3, const float* pm1, int tile) {
+    const int dn = S.dn, nx = S.nx;
+    float v[4];
+    bool in[4];
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+        const int c = c0 + e;
+        in[e] = (c >= dn) && (c < dn + nx);
+        v[e] = in[e] ? ((p3[e] - pm1[e]) * 0.5f) / P.dt : 0.f;
+    }
+    const size_t base = (size_t)P.snap * (size_t)S.snap_stride + (size_t)yrow * S.pitch + xl;
+    if (P.snap_form == 0) {
+        float* F = reinterpret_cast<float*>(S.snaps) + base;
+        if (in[0] && in[3]) {
+            st4(F, from_arr(v));
+        } else {
+#pragma unroll
+            for (int e = 0; e < 4; ++e)
+                if (in[e]) F[e] = v[e];
+        }
+        return;
+    }
+    // 16-bit forms: power-of-two scale per 128-column row segment so that the
+    // largest magnitude maps below 2^14 (exact scaling, no extra rounding).
+    float m = fmaxf(fmaxf(fabsf(v[0]), fabsf(v[1])), fmaxf(fabsf(v[2]), fabsf(v[3])));
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(FULL, m, o));
+    int ex = 0;
+    if (m > 0.f) frexpf(m, &ex);
+    const int sh = 14 - ex;
+    unsigned short h[4];
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+        const float sv = ldexpf(v[e], sh);
+        if (P.snap_form == 1) {
+            __nv_bfloat16 b = __float2bfloat16_rn(sv);
+            h[e] = *reinterpret_cast<unsigned short*>(&b);
+        } else {
+            __half b = __float2half_rn(sv);
+            h[e] = *reinterpret_cast<unsigned short*>(&b);
+        }
+    }
+    unsigned short* F = reinterpret_cast<unsigned short*>(S.snaps) + base;
+    if (in[0] && in[3]) {
+        uint2 pk;
+        pk.x = (unsigned)h[0] | ((unsigned)h[1] << 16);
+        pk.y = (unsigned)h[2] | ((unsigned)h[3] << 16);
+        *reinterpret_cast<uint2*>(F) = pk;
+    } else {
+#pragma unroll
+        for (int e = 0; e < 4; ++e)
+            if (in[e]) F[e] = h[e];
+    }
+    if (lane == 0) {
+        S.sscale[((size_t)P.snap * S.ny + yrow) * S.ntiles + tile] = ldexpf(1.f, -sh);
+    }
+}
+
+// Imaging condition (adjoint): kernel += -0.5*(p_3-p_1)*Fields(snap)*store_snap
+// (solver_acoustic_SS.f90:465-466)
+__device__ __forceinline__ void image_row(const StepParams& P, const ShotDev& S, int yrow, int xl, int c0,
+                                          const float* p3, const float* pm1, int tile) {
+    const int dn = S.dn, nx = S.nx;
+    const size_t base = (size_t)P.snap * (size_t)S.snap_stride + (size_t)yrow * S.pitch + xl;
+    float F[4];
+    if (P.snap_form == 0) {
+        to_arr(ldg4(reinterpret_cast<const float*>(S.snaps) + base), F);
+    } else {
+        const uint2 pk = __ldg(reinterpret_cast<const uint2*>(reinterpret_cast<const unsigned short*>(S.snaps) + base));
+        const unsigned short h[4] = {(unsigned short)(pk.x & 0xffffu), (unsigned short)(pk.x >> 16),
+                                     (unsigned short)(pk.y & 0xffffu), (unsigned short)(pk.y >> 16)};
+        const float sc = __ldg(S.sscale + ((size_t)P.snap * S.ny + yrow) * S.ntiles + tile);
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+            float f;
+            if (P.snap_form == 1) f = __bfloat162float(*reinterpret_cast<const __nv_bfloat16*>(&h[e]));
+            else f = __half2float(*reinterpret_cast<const __half*>(&h[e]));
+            F[e] = f * sc;
+        }
+    }
+    float k2[4];
+    bool in[4];
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+        const int c = c0 + e;
+        in[e] = (c >= dn) && (c < dn + nx);
+        k2[e] = -(((0.5f * (p3[e] - pm1[e])) * F[e]) * P.ss);
+    }
+    const size_t ko = (size_t)yrow * S.pitch + xl;
+    if (P.grad_form == 0) {
+        float* K = S.k32 + ko;
+        if (in[0] && in[3]) {
+            float4 k = ld4(K);
+            k.x = k.x + k2[0]; k.y = k.y + k2[1]; k.z = k.z + k2[2]; k.w = k.w + k2[3];
+            st4(K, k);
+        } else {
+#pragma unroll
+            for (int e = 0; e < 4; ++e)
+                if (in[e]) K[e] = K[e] + k2[e];
+        }
+    } else {
+        double* K = S.k64 + ko;
+        if (in[0] && in[3]) {
+            double2* K2 = reinterpret_cast<double2*>(K);
+            double2 a = K2[0], b = K2[1];
+            a.x += (double)k2[0]; a.y += (double)k2[1]; b.x += (double)k2[2]; b.y += (double)k2[3];
+            K2[0] = a;
+            K2[1] = b;
+        } else {
+#pragma unroll
+            for (int e = 0; e < 4; ++e)
+                if (in[e]) K[e] += (double)k2[e];
+        }
+    }
+}
+
+// Receiver recording for the row just finished (:553): every receiver in
+// this cell gets p_3.
+__device__ __forceinline__ void record_row(const StepParams& P, const ShotDev& S, int y, int xl, int& ri, int r1,
+                                           int& rrow, const float* p3) {
+    while (rrow == y) {
+        const RecEnt r = P.recs[ri];
+        if ((r.col >> 2) == (xl >> 2)) S.rec[(size_t)r.ridx * S.nt + P.t] = sel(p3, r.col & 3);
+        ++ri;
+        rrow = (ri < r1) ? P.recs[ri].row : INT_MAX;
+    }
+}
+
+}  // namespace
+
+// Model rows: interior + left/right CPML strips.
+template <int R, int MODE>
+__global__ void __launch_bounds__(128) k_step_main(const __grid_constant__ StepParams P) {
+    const int lane = threadIdx.x & 31;
+    const int wid = blockIdx.x * 4 + (threadIdx.x >> 5);
+    if (wid >= P.nitems) return;
+    const WorkItem it = P.items[wid];
+    const ShotDev& S = P.shots[it.shot];
+    const int pitch = S.pitch, dn = S.dn, nx = S.nx, nxt = S.nxt;
+    const int x0 = it.tile * TILE, xl = x0 + 4 * lane, c0 = xl - S.off;
+    const bool first = it.tile == 0, last = it.tile == S.ntiles - 1, edge = first || last;
+    const float* PC = P.parity ? S.pa : S.pb;  // p
+    float* P1 = P.parity ? S.pb : S.pa;        // p_1, overwritten with p_3
+
+    float4 q[2 * R + 1];
+#pragma unroll
+    for (int i = 0; i < 2 * R; ++i) q[i] = ldg4(PC + (size_t)(it.y0 - R + i) * pitch + xl);
+
+    int si = it.s0, ri = it.r0;
+    int srow = (si < it.s1) ? P.srcs[si].row : INT_MAX;
+    int rrow = (ri < it.r1) ? P.recs[ri].row : INT_MAX;
+    bool lane_strip = false;
+    if (edge) lane_strip = (c0 < dn) || (c0 + 3 >= dn + nx);
+
+    for (int y = it.y0; y < it.y1; ++y) {
+        q[2 * R] = ldg4(PC + (size_t)(y + R) * pitch + xl);
+        const size_t ro = (size_t)y * pitch + xl;
+        float pm1[4], cc[4], pc[4];
+        to_arr(ld4(P1 + ro), pm1);
+        to_arr(ldg4(S.c2 + ro), cc);
+        to_arr(q[R], pc);
+        float4 hl = make_float4(0.f, 0.f, 0.f, 0.f), hr = hl;
+        if (lane == 0 && x0 > 0) hl = ldg4(PC + (size_t)y * pitch + x0 - 4);
+        if (lane == 31 && x0 + TILE < pitch) hr = ldg4(PC + (size_t)y * pitch + x0 + TILE);
+        float w[12];
+        window(q[R], hl, hr, lane, w);
+        float d2x[4], dx[4], d2y[4], dy[4];
+        xderivs<R>(w, P, d2x, dx);
+        yderivs<R>(q, P, d2y, dy);
+
+        // source injection: source(nys,nxs) = S(k-1,j), interior cells only
+        float sv[4] = {0.f, 0.f, 0.f, 0.f};
+        while (srow == y) {
+            const SrcEnt s = P.srcs[si];
+            if ((s.col >> 2) == (xl >> 2)) {
+                const float val = __ldg(S.srcv + (size_t)s.vidx * S.nt + P.t);
+                const int el = s.col & 3;
+                sv[0] = el == 0 ? val : sv[0];
+                sv[1] = el == 1 ? val : sv[1];
+                sv[2] = el == 2 ? val : sv[2];
+                sv[3] = el == 3 ? val : sv[3];
+            }
+            ++si;
+            srow = (si < it.s1) ? P.srcs[si].row : INT_MAX;
+        }
+
+        float p3[4];
+        if (!edge) {
+#pragma unroll
+            for (int e = 0; e < 4; ++e)
+                p3[e] = ((-pm1[e]) + 2.f * pc[e]) + (((d2x[e] + d2y[e]) + sv[e]) * cc[e]);
+        } else {
+            xclamp<R>(S, x0, c0, first, last, d2x, dx);
+            float ph[4] = {0.f, 0.f, 0.f, 0.f}, ch[4] = {0.f, 0.f, 0.f, 0.f};
+            if (lane_strip) {
+                to_arr(ld4(S.phx + ro), ph);
+                to_arr(ld4(S.chx + ro), ch);
+            }
+            float dph[4];
+            phi_xderiv<R>(S, P, from_arr(ph), lane, x0, c0, first, last, dph);
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+                const int c = c0 + e;
+                if (c < 0 || c >= nxt) {
+                    p3[e] = 0.f;
+                } else if (c >= dn && c < dn + nx) {
+                    p3[e] = ((-pm1[e]) + 2.f * pc[e]) + (((d2x[e] + d2y[e]) + sv[e]) * cc[e]);
+                } else {
+                    // xl strip: factor(dn-i+1); xr strip: factor(i)  (solver_PML_matrices.f90:296-312)
+                    const int fi = (c < dn) ? (dn - 1 - c) : (c - dn - nx);
+                    const float A = __ldg(P.fA + fi), B = __ldg(P.fB + fi);
+                    const float phn = A * ph[e] + B * dx[e];
+                    const float chn = A * ch[e] + B * (d2x[e] + dph[e]);
+                    const float prop = dph[e] + chn;
+                    ph[e] = phn;
+                    ch[e] = chn;
+                    p3[e] = ((-pm1[e]) + 2.f * pc[e]) + cc[e] * ((d2x[e] + d2y[e]) + prop);
+                }
+            }
+            if (lane_strip) {
+                st4(S.phx + ro, from_arr(ph));
+                st4(S.chx + ro, from_arr(ch));
+            }
+        }
+
+        if (MODE == 0 && P.snap >= 0) store_snapshot(P, S, y - dn, lane, x0, xl, c0, p3, pm1, it.tile);
+        if (MODE == 1 && P.snap >= 0) image_row(P, S, y - dn, xl, c0, p3, pm1, it.tile);
+        st4(P1 + ro, from_arr(p3));
+        if (MODE == 0 && P.record) record_row(P, S, y, xl, ri, it.r1, rrow, p3);
+
+#pragma unroll
+        for (int i = 0; i < 2 * R; ++i) q[i] = q[i + 1];
+    }
+}
+
+// Bottom pad rows: bottom strip and bottom corners.
+template <int R, int MODE>
+__global__ void __launch_bounds__(128) k_step_bottom(const __grid_constant__ StepParams P) {
+    const int lane = threadIdx.x & 31;
+    const int wid = blockIdx.x * 4 + (threadIdx.x >> 5);
+    if (wid >= P.nitems) return;
+    const WorkItem it = P.items[wid];
+    const ShotDev& S = P.shots[it.shot];
+    const int pitch = S.pitch, dn = S.dn, nx = S.nx, nxt = S.nxt, nyt = S.nyt;
+    const int x0 = it.tile * TILE, xl = x0 + 4 * lane, c0 = xl - S.off;
+    const bool first = it.tile == 0, last = it.tile == S.ntiles - 1, edge = first || last;
+    const float* PC = P.parity ? S.pa : S.pb;
+    float* P1 = P.parity ? S.pb : S.pa;
+    const int yb0 = nyt - dn;
+
+    float4 q[2 * R + 1], f[2 * R + 1];
+#pragma unroll
+    for (int i = 0; i < 2 * R; ++i) q[i] = ldg4(PC + (size_t)(yb0 - R + i) * pitch + xl);
+#pragma unroll
+    for (int i = 0; i <= 2 * R; ++i) f[i] = ld4(S.phy + (size_t)(yb0 + i) * pitch + xl);
+    float dphyTop[4], dphyBot[4] = {0.f, 0.f, 0.f, 0.f};
+    yderiv1<R>(f, P, dphyTop);
+    float d2yBot[4] = {0.f, 0.f, 0.f, 0.f}, dyBot[4] = {0.f, 0.f, 0.f, 0.f};
+
+    int ri = it.r0;
+    int rrow = (ri < it.r1) ? P.recs[ri].row : INT_MAX;
+    bool lane_corner = false;
+    if (edge) lane_corner = (c0 < dn) || (c0 + 3 >= dn + nx);
+
+    for (int jl = 0; jl < dn; ++jl) {
+        const int y = yb0 + jl;
+        if (y + R <= nyt - 1) q[2 * R] = ldg4(PC + (size_t)(y + R) * pitch + xl);
+        const size_t ro = (size_t)y * pitch + xl;
+        float pm1[4], cc[4], pc[4];
+        to_arr(ld4(P1 + ro), pm1);
+        to_arr(ldg4(S.c2 + ro), cc);
+        to_arr(q[R], pc);
+        float d2y[4], dy[4];
+        if (y <= nyt - 1 - R) {
+            yderivs<R>(q, P, d2y, dy);
+            if (y == nyt - 1 - R) {
+#pragma unroll
+                for (int e = 0; e < 4; ++e) { d2yBot[e] = d2y[e]; dyBot[e] = dy[e]; }
+            }
+        } else {
+#pragma unroll
+            for (int e = 0; e < 4; ++e) { d2y[e] = d2yBot[e]; dy[e] = dyBot[e]; }
+        }
+        float4 hl = make_float4(0.f, 0.f, 0.f, 0.f), hr = hl;
+        if (lane == 0 && x0 > 0) hl = ldg4(PC + (size_t)y * pitch + x0 - 4);
+        if (lane == 31 && x0 + TILE < pitch) hr = ldg4(PC + (size_t)y * pitch + x0 + TILE);
+        float w[12];
+        window(q[R], hl, hr, lane, w);
+        float d2x[4], dx[4];
+        xderivs<R>(w, P, d2x, dx);
+        if (edge) xclamp<R>(S, x0, c0, first, last, d2x, dx);
+
+        // strip-local y derivative of the old y-direction phi (pml_matrices_y :335)
+        float dphy[4];
+        if (jl < R) {
+#pragma unroll
+            for (int e = 0; e < 4; ++e) dphy[e] = dphyTop[e];
+        } else if (jl <= dn - 1 - R) {
+            yderiv1<R>(f, P, dphy);
+            if (jl == dn - 1 - R) {
+#pragma unroll
+                for (int e = 0; e < 4; ++e) dphyBot[e] = dphy[e];
+            }
+        } else {
+#pragma unroll
+            for (int e = 0; e < 4; ++e) dphy[e] = dphyBot[e];
+        }
+
+        float phy[4], chy[4];
+        to_arr(ld4(S.phy + ro), phy);
+        to_arr(ld4(S.chy + ro), chy);
+        float phx[4] = {0.f, 0.f, 0.f, 0.f}, chx[4] = {0.f, 0.f, 0.f, 0.f}, dphx[4] = {0.f, 0.f, 0.f, 0.f};
+        if (edge) {
+            if (lane_corner) {
+                to_arr(ld4(S.phx + ro), phx);
+                to_arr(ld4(S.chx + ro), chx);
+            }
+            phi_xderiv<R>(S, P, from_arr(phx), lane, x0, c0, first, last, dphx);
+        }
+
+        float p3[4];
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+            const int c = c0 + e;
+            if (c < 0 || c >= nxt) {
+                p3[e] = 0.f;
+                continue;
+            }
+            const bool left = c < dn, right = c >= dn + nx;
+            // factor index: strip factor(j); corners factor(max(i,j)) with the
+            // ld/rd orientation (solver_PML_coeffs.f90:240-267)
+            int fi = jl;
+            if (left) fi = max(jl, dn - 1 - c);
+            if (right) fi = max(jl, c - dn - nx);
+            const float A = __ldg(P.fA + fi), B = __ldg(P.fB + fi);
+            const float phyn = A * phy[e] + B * dy[e];
+            const float chyn = A * chy[e] + B * (d2y[e] + dphy[e]);
+            const float propy = dphy[e] + chyn;
+            phy[e] = phyn;
+            chy[e] = chyn;
+            if (!left && !right) {
+                p3[e] = ((-pm1[e]) + 2.f * pc[e]) + cc[e] * ((d2x[e] + d2y[e]) + propy);
+            } else {
+                const float phxn = A * phx[e] + B * dx[e];
+                const float chxn = A * chx[e] + B * (d2x[e] + dphx[e]);
+                const float propx = dphx[e] + chxn;
+                phx[e] = phxn;
+                chx[e] = chxn;
+                const float t = ((-pm1[e]) + 2.f * pc[e]) + cc[e] * ((d2x[e] + d2y[e]) + propx);
+                p3[e] = t + cc[e] * propy;
+            }
+        }
+        st4(S.phy + ro, from_arr(phy));
+        st4(S.chy + ro, from_arr(chy));
+        if (lane_corner) {
+            st4(S.phx + ro, from_arr(phx));
+            st4(S.chx + ro, from_arr(chx));
+        }
+        st4(P1 + ro, from_arr(p3));
+        if (MODE == 0 && P.record) record_row(P, S, y, xl, ri, it.r1, rrow, p3);
+
+#pragma unroll
+        for (int i = 0; i < 2 * R; ++i) q[i] = q[i + 1];
+        if (jl >= R && jl + 1 + R <= dn - 1) {
+#pragma unroll
+            for (int i = 0; i < 2 * R; ++i) f[i] = f[i + 1];
+            f[2 * R] = ld4(S.phy + (size_t)(yb0 + jl + 1 + R) * pitch + xl);
+        }
+    }
+}
+
+// Host-side launchers -------------------------------------------------------
+
+cudaError_t launch_step(int acc, int mode, const StepParams& pm, const StepParams& pb, cudaStream_t st) {
+    const int bm = (pm.nitems + 3) / 4, bb = (pb.nitems + 3) / 4;
+    if (acc == 3) {
+        if (mode == 0) {
+            if (bm) k_step_main<3, 0><<<bm, 128, 0, st>>>(pm);
+            if (bb) k_step_bottom<3, 0><<<bb, 128, 0, st>>>(pb);
+        } else {
+            if (bm) k_step_main<3, 1><<<bm, 128, 0, st>>>(pm);
+            if (bb) k_step_bottom<3, 1><<<bb, 128, 0, st>>>(pb);
+        }
+    } else if (acc == 4) {
+        if (mode == 0) {
+            if (bm) k_step_main<4, 0><<<bm, 128, 0, st>>>(pm);
+            if (bb) k_step_bottom<4, 0><<<bb, 128, 0, st>>>(pb);
+        } else {
+            if (bm) k_step_main<4, 1><<<bm, 128, 0, st>>>(pm);
+            if (bb) k_step_bottom<4, 1><<<bb, 128, 0, st>>>(pb);
+        }
+    } else {
+        return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+}
+
+}  // namespace fwi

@@ -1,0 +1,162 @@
+"""Seeded synthetic models and acquisition geometries of the benchmark configs.
+
+The reference ships no data (its sample datasets are not published), so the
+workloads are synthetic with the shapes, sizes and value ranges of each
+config; receiver and source grid indices are computed with the reference's
+own FP32 rules (fwi_mcs_geometry).  Observed data are synthesised from the
+true model by the same solver.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from .survey import ShotSpec, SurveySpec
+
+
+def _F(a):
+    return np.asfortranarray(np.asarray(a, dtype=np.float32))
+
+
+def ricker_shifted(freq, dt, nt, shift):
+    """Ricker_mcs wavelet (get_mcs_data.f90:346-362) delayed by `shift` s."""
+    from .api import Ricker_mcs
+    w = Ricker_mcs(freq, dt, nt)
+    if shift:
+        t = np.arange(nt) * dt
+        w = np.interp(t - shift, t, w, left=0.0, right=0.0).astype(np.float32)
+    return w
+
+
+def model_config1(seed=1, anomaly=True):
+    """200 x 400 at 25 m: 500 m of water at 1500 m/s over a linear gradient
+    1800 -> 4500 m/s, plus a +200 m/s Gaussian anomaly (sigma 300 m) at
+    (x=5 km, z=2.5 km) with a seeded position jitter (+-100 m)."""
+    rng = np.random.default_rng(seed)
+    ny, nx, d = 200, 400, 25.0
+    z = (np.arange(ny) + 0.5) * d
+    x = (np.arange(nx) + 0.5) * d
+    vp = np.empty((ny, nx), np.float64)
+    water = z < 500.0
+    below = ~water
+    zb = z[below] - 500.0
+    grad = 1800.0 + (4500.0 - 1800.0) * zb / (ny * d - 500.0)
+    vp[water, :] = 1500.0
+    vp[below, :] = grad[:, None]
+    if anomaly:
+        jx, jz = rng.uniform(-100.0, 100.0, size=2)
+        X, Z = np.meshgrid(x, z)
+        vp += 200.0 * np.exp(-((X - 5000.0 - jx) ** 2 + (Z - 2500.0 - jz) ** 2) / (2 * 300.0 ** 2)) * below[:, None]
+    return _F(vp), int(round(500.0 / d))
+
+
+def model_layered(ny, nx, d, seed, nlayers=8, water_depth=None, vmin=1800.0, vmax=5000.0, lateral=0.10,
+                  lenses=()):
+    """Water at 1500 m/s over `nlayers` layers of random thickness 200-600 m
+    with monotone random velocities in [vmin, vmax] and a +-lateral
+    sinusoidal lateral perturbation; optional Gaussian low-velocity lenses
+    (x, z, sigma, dv)."""
+    rng = np.random.default_rng(seed)
+    wd = water_depth if water_depth is not None else 500.0
+    z = (np.arange(ny) + 0.5) * d
+    x = (np.arange(nx) + 0.5) * d
+    thick = rng.uniform(200.0, 600.0, size=nlayers)
+    tops = wd + np.concatenate([[0.0], np.cumsum(thick)[:-1]])
+    vels = np.sort(rng.uniform(vmin, vmax, size=nlayers))
+    phase = rng.uniform(0, 2 * np.pi, size=nlayers)
+    wavelength = rng.uniform(3000.0, 9000.0, size=nlayers)
+    vp = np.full((ny, nx), 1500.0)
+    for k in range(nlayers):
+        mask = z >= tops[k]
+        pert = 1.0 + lateral * np.sin(2 * np.pi * x / wavelength[k] + phase[k])
+        vp[mask, :] = vels[k] * pert[None, :]
+    X, Z = np.meshgrid(x, z)
+    for (lx, lz, sig, dv) in lenses:
+        vp += dv * np.exp(-((X - lx) ** 2 + (Z - lz) ** 2) / (2 * sig ** 2)) * (Z >= wd)
+    return _F(vp), int(np.ceil(wd / d))
+
+
+def lam_from_vp(vp):
+    """lambda = rho*Vp**2 with rho = 1000 (auxiliar.f90:205-209), in FP32."""
+    v = np.asarray(vp, np.float32)
+    return _F(np.float32(1000.0) * (v * v))
+
+
+def mcs_survey(vp, d, dt, nt, xs_list, nrec, drec, near=150.0, sdepth=10.0, rdepth=10.0, freq=10.0, acc=3,
+               dpml=20, store_snap=10, seed=0, water_rows=None, windows=None, shift_max=0.0):
+    """MCS survey on model vp: one Ricker source per shot (seeded time shift
+    in [0, shift_max]) and a trailing streamer of nrec channels.  `windows`
+    optionally gives (x0, nx) per shot; geometry indices are window
+    relative."""
+    from .api import mcs_geometry
+    rng = np.random.default_rng(seed)
+    ny, nxm = vp.shape
+    shots = []
+    for i, xs in enumerate(xs_list):
+        nxs, nys, nxr, nyr = mcs_geometry(xs, sdepth, rdepth, near, drec, d, nrec)
+        x0, nxw = (0, nxm) if windows is None else windows[i]
+        sh = float(rng.uniform(0.0, shift_max)) if shift_max else 0.0
+        src = ricker_shifted(freq, dt, nt, sh).reshape(nt, 1, order="F")
+        shots.append(ShotSpec(x0=x0, nx=nxw, nxSou=np.array([nxs - x0], np.int32), nySou=np.array([nys], np.int32),
+                              nxRec=(nxr - x0).astype(np.int32), nyRec=nyr.astype(np.int32), src=_F(src)))
+    wr = None
+    if water_rows is not None:
+        wr = np.full(nxm, water_rows, np.int32) if np.isscalar(water_rows) else np.asarray(water_rows, np.int32)
+    return SurveySpec(ny=ny, nx_model=nxm, d=d, dt=dt, nt=nt, shots=shots, store_snap=store_snap, acc=acc,
+                      dpml=dpml, water_rows=wr)
+
+
+def config1(seed=1):
+    """Plain single shot (BASELINE config 1): returns (spec, vp_true, vp_start)."""
+    vp_true, wrows = model_config1(seed, anomaly=True)
+    vp0, _ = model_config1(seed, anomaly=False)
+    rng = np.random.default_rng(seed + 100)
+    spec = mcs_survey(vp_true, 25.0, 0.002, 3000, [2637.5 + 25.0 * int(rng.integers(0, 40))], 200, 12.5, near=150.0,
+                      sdepth=10.0, rdepth=10.0, freq=8.0, acc=4, dpml=20, seed=seed, water_rows=wrows,
+                      shift_max=0.02)
+    return spec, vp_true, vp0
+
+
+def config2(seed=2, nshots=64, nt=6000, store_snap=10):
+    """Batched MCS survey (BASELINE config 2): 400 x 2000 at 12.5 m, 64 shots
+    at 250 m spacing, 480 channels at 12.5 m, 6 s at dt = 1 ms, 10 Hz.
+    Returns (spec, vp_true, vp_start) where the start model is the true
+    model smoothed laterally and vertically."""
+    vp_true, wrows = model_layered(400, 2000, 12.5, seed)
+    xs = [6250.0 + 250.0 * i for i in range(nshots)]
+    spec = mcs_survey(vp_true, 12.5, 0.001, nt, xs, 480, 12.5, near=150.0, freq=10.0, acc=3, dpml=20,
+                      store_snap=store_snap, seed=seed, water_rows=wrows, shift_max=0.01)
+    return spec, vp_true, smooth(vp_true, 8)
+
+
+def smooth(vp, r):
+    """Box-smoothed copy of vp (r cells each way) for starting models."""
+    v = np.asarray(vp, np.float64)
+    k = 2 * r + 1
+    pad = np.pad(v, r, mode="edge")
+    c = np.cumsum(np.cumsum(pad, 0), 1)
+    c = np.pad(c, ((1, 0), (1, 0)))
+    out = (c[k:, k:] - c[:-k, k:] - c[k:, :-k] + c[:-k, :-k]) / (k * k)
+    return _F(out)
+
+
+def small_survey(seed=0, ny=40, nxm=90, nshots=3, nt=200, acc=3, dpml=8, d=10.0, dt=1e-3, nrec=20, windows=None,
+                 store_snap=10):
+    """A small survey for parity tests (CPML, windows, duplicates...)."""
+    rng = np.random.default_rng(seed)
+    vp = 1500.0 + 1000.0 * (np.arange(ny)[:, None] / ny) + rng.uniform(-50, 50, size=(ny, nxm))
+    vp = _F(vp)
+    shots = []
+    for i in range(nshots):
+        x0, nx = (0, nxm) if windows is None else windows[i]
+        nsou = 1 + (i % 2)
+        nxs = rng.integers(1, nx + 1, size=nsou).astype(np.int32)
+        nys = rng.integers(1, min(ny, 6) + 1, size=nsou).astype(np.int32)
+        nxr = rng.integers(-dpml, nx + dpml, size=nrec).astype(np.int32)
+        nyr = rng.integers(1, ny + dpml, size=nrec).astype(np.int32)
+        nxr[:3] = nxr[0]
+        nyr[:3] = nyr[0]  # three receivers in one cell
+        src = _F(rng.standard_normal((nt, nsou)))
+        shots.append(ShotSpec(x0=x0, nx=nx, nxSou=nxs, nySou=nys, nxRec=nxr, nyRec=nyr, src=src))
+    spec = SurveySpec(ny=ny, nx_model=nxm, d=d, dt=dt, nt=nt, shots=shots, store_snap=store_snap, acc=acc,
+                      dpml=dpml, water_rows=rng.integers(0, 4, size=nxm).astype(np.int32))
+    return spec, vp

@@ -1,0 +1,202 @@
+/*
+ * fwi_gb300.h -- C ABI of the GB300-native FWI hot path.
+ *
+ * Every entry point returns 0 on success or a negative FWI_ERR_* code; the
+ * message of the last failure on the calling thread is fwi_last_error().
+ * Arrays follow the reference's Fortran conventions (column-major, grid
+ * indices 1-based and relative to the model, default REAL = float,
+ * INTEGER = int32), so a Fortran caller binds them with iso_c_binding and
+ * passes its arrays unchanged (see fortran/fwi_gpu_iface.f90).
+ *
+ * Reference interfaces replaced (paths inside ejimeneztejero/FWI):
+ *   fwi_solver_acoustic_ss    src/solver_acoustic_SS.f90:9-11
+ *   fwi_misfit_function       src/Misfit.f90:1 (Misfit_function, L2 path
+ *                             src/Misfit_L2.f90:1)
+ *   fwi_beta_calculous        src/Beta_calculous.f90:1
+ *   fwi_misfit_gradient_batch src/calculate_misfit_gradient.f90:1 (all
+ *                             shots of one call; the MPI shot loop
+ *                             :73-360 becomes on-device batching)
+ *   fwi_mcs_geometry          src/get_mcs_data.f90:113-114,147-155,503-512
+ *   fwi_ricker                src/get_mcs_data.f90:331 (Ricker_mcs)
+ *   fwi_time_rules            src/calculate_misfit_gradient.f90:198-203
+ */
+#ifndef FWI_GB300_H
+#define FWI_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FWI_OK 0
+#define FWI_ERR_ARG (-1)        /* invalid argument (size, index, order)        */
+#define FWI_ERR_CUDA (-2)       /* CUDA runtime error                            */
+#define FWI_ERR_NOMEM (-3)      /* device memory exhausted                       */
+#define FWI_ERR_NONFINITE (-4)  /* NaN/Inf in a result (e.g. CFL-unstable dt)    */
+#define FWI_ERR_STATE (-5)      /* library not initialised / bad handle          */
+
+/* Snapshot storage forms for the forward wavefield time derivative. */
+#define FWI_SNAP_F32 0
+#define FWI_SNAP_BF16 1         /* bfloat16 + power-of-two scale per 128 values */
+#define FWI_SNAP_F16 2          /* float16  + power-of-two scale per 128 values */
+
+/* Gradient accumulation forms. */
+#define FWI_GRAD_F32 0          /* per-shot FP32 accumulation, as the reference  */
+#define FWI_GRAD_F64 1          /* per-shot and cross-shot FP64 accumulation     */
+
+/* ---- library state ------------------------------------------------------ */
+
+/* Select the CUDA device and create the library's stream.  Optional: every
+ * other entry point initialises device 0 on first use. */
+int fwi_init(int device);
+/* Free every device buffer the library holds and destroy its stream. */
+int fwi_finalize(void);
+/* Message of the last failed call on this thread ("" if none). */
+const char* fwi_last_error(void);
+/* Run subsequent work on a caller-owned cudaStream_t (NULL = library stream). */
+int fwi_set_stream(void* cuda_stream);
+/* Solver order/CPML width used by fwi_solver_acoustic_ss.  The reference
+ * hard-codes acc = 3, dPML = 20 (solver_acoustic_SS.f90:90-91); acc = 4 is
+ * the reference's own 8th-order table (solver_FD_coeffs.f90:21-27,52-58). */
+int fwi_set_solver_options(int acc, int dpml);
+/* Number of step-kernel launches issued since the library was initialised. */
+int64_t fwi_kernel_launch_count(void);
+
+/* ---- drop-in single-shot solver ------------------------------------------ */
+
+/* solver_acoustic_SS(rank,iprop,NumSou,NumRec,nxSou,nySou,nxRec,nyRec,S,Sadj,
+ *                    d,dt,ny,nx,ctmp,store_snap,nt_Store,nt,kernel,Fields,
+ *                    Rec_point)            -- src/solver_acoustic_SS.f90:9-11
+ * All scalars by reference.  iprop = 1: forward; Fields(ny,nx*(nt_Store+1))
+ * receives the snapshots (block s = 1..), Rec_point(nt,NumRec) the traces.
+ * iprop = 2: adjoint driven by Sadj(nt,NumRec) at the receivers; Fields is
+ * read and kernel(ny,nx) is accumulated (+=) with the imaging condition;
+ * Rec_point is zeroed.  Host pointers; the copies are part of the call. */
+int fwi_solver_acoustic_ss(const int* rank, const int* iprop, const int* NumSou, const int* NumRec,
+                           const int* nxSou, const int* nySou, const int* nxRec, const int* nyRec,
+                           const float* S, const float* Sadj, const float* d, const float* dt,
+                           const int* ny, const int* nx, const float* ctmp, const int* store_snap,
+                           const int* nt_Store, const int* nt, float* kernel, float* Fields,
+                           float* Rec_point);
+
+/* ---- misfit, adjoint source, Polak-Ribiere beta --------------------------- */
+
+/* Misfit_function(rank,freq,Data_Synth,Data_trace,NumRec,nt,dt,Misfit,
+ * AdjSource) with misfit_type = 1 (L2 of max-abs-normalised traces,
+ * Misfit.f90:28-61, Misfit_L2.f90:8-14).  Misfit is overwritten with the sum
+ * accumulated in FP64 and rounded to float; misfit64 (may be NULL) receives
+ * the FP64 value.  AdjSource(nt,NumRec) = time-reversed negative residual. */
+int fwi_misfit_function(const int* rank, const float* freq, const float* Data_Synth,
+                        const float* Data_trace, const int* NumRec, const int* nt, const float* dt,
+                        float* Misfit, float* AdjSource, double* misfit64);
+
+/* Beta_calculous(Grad,OldGrad,nx,ny,Beta) (Beta_calculous.f90:1-25) with the
+ * two dot products in FP64 on the device.  num64/den64 may be NULL. */
+int fwi_beta_calculous(const float* Grad, const float* OldGrad, const int* nx, const int* ny,
+                       float* Beta, double* num64, double* den64);
+
+/* ---- geometry and wavelet (host arithmetic, bit-exact FP32) -------------- */
+
+/* One MCS shot: shot x position xs (m), depths, near offset, channel
+ * spacing, grid step -> 1-based grid indices, as read_nav_shot_mcs,
+ * get_geometry_mcs and get_pos_channels (offset_header = 0) compute them. */
+int fwi_mcs_geometry(float xs, float shot_depth, float streamer_depth, float near_offset, float drec,
+                     float dmodel, int num_rec, int* nxSou, int* nySou, int* nxRec, int* nyRec);
+/* Ricker_mcs: out(nt) for peak frequency freq and sampling dt. */
+int fwi_ricker(float freq, float dt, int nt, float* out);
+/* dt = dmodel/sqrt(max(lambda/1000))/2, nt = 1+ceil(tfin/dt) truncated to a
+ * multiple of store_snap, nt_Store = nt/store_snap. lambda(ny,nx) host. */
+int fwi_time_rules(const float* lambda, int ny, int nx, float dmodel, float tfin, int store_snap,
+                   float* dt, int* nt, int* nt_Store);
+
+/* ---- batched misfit + gradient over shots ------------------------------ */
+
+typedef struct fwi_shot {
+    int x0;               /* first model column of the shot's window (0-based)   */
+    int nx;               /* window width in model columns                       */
+    int num_sou, num_rec;
+    const int* nxSou;     /* window-relative 1-based grid indices (num_sou)      */
+    const int* nySou;
+    const int* nxRec;     /* (num_rec)                                           */
+    const int* nyRec;
+    const float* src;     /* S(nt, num_sou), column-major                        */
+    const float* obs;     /* observed Data_target(nt, num_rec), column-major     */
+    double grad_weight;   /* weight of this shot's kernel in the stack (1.0)     */
+    double misfit_weight; /* weight of this shot's misfit in the sum (1.0)       */
+} fwi_shot;
+
+typedef struct fwi_survey_desc {
+    int ny;               /* model rows (depth)                                  */
+    int nx_model;         /* model columns                                       */
+    float d;              /* grid step (m)                                       */
+    float dt;             /* time step (s)                                       */
+    int nt;               /* time samples, common to all shots                   */
+    int store_snap;       /* snapshot decimation (reference: 10)                 */
+    int acc;              /* FD half-order: 3 (reference) or 4                   */
+    int dpml;             /* CPML cells (reference: 20)                          */
+    int numtasks;         /* gradient divisor of the reference's MPI reduction   */
+    int snap_form;        /* FWI_SNAP_*                                          */
+    int grad_form;        /* FWI_GRAD_*                                          */
+    int nshots;
+    const fwi_shot* shots;
+    const int* water_rows;/* bat_model_grid(nx_model): rows 1..k zeroed, or NULL */
+    size_t hbm_budget;    /* bytes the survey may hold on the device (0 = all)   */
+    int wave_shots;       /* shots per concurrent wave (0 = chosen by the tuner) */
+    int band_rows;        /* rows per warp work item (0 = chosen by the tuner)   */
+    int flags;            /* FWI_SURVEY_* bits                                   */
+} fwi_survey_desc;
+
+/* fwi_survey_desc.flags: launch every time step directly instead of
+ * replaying the captured CUDA graph (the plain one-launch-per-step path). */
+#define FWI_SURVEY_NO_GRAPH 1
+
+typedef struct fwi_survey fwi_survey;
+
+/* Plan a survey: validate the geometry, upload sources and observed data,
+ * size the shot waves to the HBM budget and allocate device buffers. */
+int fwi_survey_create(const fwi_survey_desc* desc, fwi_survey** out);
+int fwi_survey_destroy(fwi_survey* s);
+/* Model parameter: lambda(ny,nx_model) bulk modulus (rho = 1000), host or
+ * device pointer (the call detects which).  Vp = sqrt(lambda/1000.) as in
+ * calculate_misfit_gradient.f90:252. */
+int fwi_survey_set_lambda(fwi_survey* s, const float* lambda);
+/* Replace the observed data of every shot (host or device pointer to the
+ * shots' obs blocks packed in shot order, each (nt, num_rec)). */
+int fwi_survey_set_observed(fwi_survey* s, const float* obs_packed);
+/* Replace every shot's source wavelets (packed like set_observed). */
+int fwi_survey_set_sources(fwi_survey* s, const float* src_packed);
+/* One calculate_misfit_gradient call: step = 1 forward + misfit + adjoint +
+ * imaging + stack; step = 2 forward + misfit only (line-search trials).
+ * misfit (may be NULL) += the weighted misfit sum (FP64); grad (may be NULL)
+ * (ny, nx_model) host float is updated as Grad = Grad + stack/numtasks and
+ * the water rows are zeroed, as calculate_misfit_gradient.f90:339-351. */
+int fwi_survey_run(fwi_survey* s, int step, double* misfit, float* grad);
+/* Device pointer to the FP64 gradient stack of the last run
+ * ((ny, nx_model) column-major, before the numtasks divisor and mask). */
+int fwi_survey_grad_device(fwi_survey* s, const double** ptr);
+/* Synthetic traces of shot i from the last run: Rec_point(nt, num_rec),
+ * copied to host. */
+int fwi_survey_get_synthetic(fwi_survey* s, int shot, float* out);
+/* Sum of algorithmic HBM bytes of one forward step over all shots. */
+int fwi_survey_step_bytes(fwi_survey* s, double* bytes);
+/* Tuning chosen for the survey (wave size, band rows). */
+int fwi_survey_tuning(fwi_survey* s, int* wave_shots, int* band_rows);
+/* Run `steps` forward time steps of the first wave (for kernel timing; the
+ * wavefields keep evolving, sources are injected). */
+int fwi_survey_time_steps(fwi_survey* s, int steps);
+
+/* calculate_misfit_gradient(iter,step,f1,f2,dt,nt,tfin,S0,Misfit,Grad) for
+ * all shots in one call, with host buffers: plans (or reuses a cached plan
+ * for the same geometry), uploads lambda, sources and observed data, runs,
+ * and downloads Misfit (+=) and Grad (updated, masked).
+ * src/calculate_misfit_gradient.f90:1-366 */
+int fwi_misfit_gradient_batch(const fwi_survey_desc* desc, const float* lambda, int step,
+                              float* Misfit, float* Grad);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* FWI_GB300_H */

@@ -166,8 +166,9 @@ def gradient_batch(survey, vp_model, step=1, fp64=False, nthreads=1, want_synth=
     nyR = _i(np.concatenate([s.nyRec for s in sv.shots]))
     S = np.concatenate([np.asarray(s.src, dtp).reshape(sv.nt, -1, order="F") for s in sv.shots], axis=1)
     S = np.asfortranarray(S)
-    obs = np.asfortranarray(np.concatenate([np.asarray(s.obs, dtp).reshape(sv.nt, -1, order="F")
-                                            for s in sv.shots], axis=1))
+    obs = np.asfortranarray(np.concatenate([
+        (np.asarray(s.obs, dtp).reshape(sv.nt, -1, order="F") if s.obs is not None
+         else np.zeros((sv.nt, len(s.nxRec)), dtp)) for s in sv.shots], axis=1))
     sizes = [sv.ny * s.nx for s in sv.shots]
     koff = np.ascontiguousarray(np.concatenate([[0], np.cumsum(sizes)[:-1]]).astype(np.uint64))
     kern = np.zeros(int(sum(sizes)), dtp)

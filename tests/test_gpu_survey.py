@@ -1,0 +1,147 @@
+"""Batched survey (all shots of calculate_misfit_gradient in one graph) on
+the GPU against the oracle run shot by shot."""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+def stacked_oracle(spec, vp, fp64=False, step=1):
+    kern, mr, m64, synth = O.gradient_batch(spec, vp, step=step, fp64=fp64, nthreads=8, want_synth=True)
+    G = np.zeros((spec.ny, spec.nx_model), np.float64)
+    for sh, k in zip(spec.shots, kern):
+        G[:, sh.x0:sh.x0 + sh.nx] += sh.grad_weight * k.astype(np.float64)
+    return G, mr, m64, synth
+
+
+def make(seed, **kw):
+    from fwi_gb300 import synth
+    spec, vp = synth.small_survey(seed=seed, **kw)
+    # observed data: the same survey on a perturbed model (oracle, FP32)
+    vp_obs = np.asfortranarray(vp * np.float32(1.03))
+    _, _, _, obs = O.gradient_batch(spec, vp_obs, step=2, nthreads=8, want_synth=True)
+    for sh, o in zip(spec.shots, obs):
+        sh.obs = np.asfortranarray(o)
+    return spec, vp
+
+
+def rel(a, b):
+    return np.linalg.norm(a - b) / np.linalg.norm(b)
+
+
+@pytest.mark.parametrize("kw", [dict(), dict(acc=4, dpml=20, ny=33, nxm=170, nshots=4),
+                                dict(nshots=3, nxm=300, windows=[(0, 150), (70, 230), (140, 160)]),
+                                dict(store_snap=4, nt=160)])
+def test_survey_gradient_vs_oracle(kw):
+    import fwi_gb300 as F
+    from fwi_gb300.synth import lam_from_vp
+    spec, vp = make(5, **kw)
+    lam = lam_from_vp(vp)
+    vp_ref = np.sqrt(lam / np.float32(1000.0))  # Vpmodel = sqrt(lambda/1000.)
+    G, mr, m64, synth = stacked_oracle(spec, vp_ref)
+    sv = F.Survey(spec)
+    sv.set_lambda(lam)
+    grad = np.zeros((spec.ny, spec.nx_model), np.float32, order="F")
+    mis, _ = sv.run(1, grad)
+    for i in range(len(spec.shots)):
+        np.testing.assert_array_equal(sv.synthetic(i), synth[i])        # traces bit-exact
+    assert abs(mis - m64.sum()) <= 1e-12 * abs(m64.sum())
+    assert abs(mis - mr.sum()) <= 1e-4 * abs(mis)                       # vs FP32 sequential sums
+    Gm = G.copy()
+    for i, k in enumerate(spec.water_rows):
+        Gm[:k, i] = 0.0
+    assert rel(grad.astype(np.float64), Gm) <= 1e-6
+    # a second run reuses the captured graph and gives identical results
+    grad2 = np.zeros_like(grad)
+    mis2, _ = sv.run(1, grad2)
+    assert mis2 == mis and np.array_equal(grad2, grad)
+
+
+def test_wave_split_is_bit_identical_and_fp32_form():
+    import fwi_gb300 as F
+    from fwi_gb300.synth import lam_from_vp
+    spec, vp = make(6, nshots=5)
+    lam = lam_from_vp(vp)
+    outs = []
+    for wave in (0, 1, 2):
+        sv = F.Survey(spec, wave_shots=wave)
+        sv.set_lambda(lam)
+        g = np.zeros((spec.ny, spec.nx_model), np.float32, order="F")
+        m, _ = sv.run(1, g)
+        outs.append((m, g))
+    for m, g in outs[1:]:
+        assert m == outs[0][0] and np.array_equal(g, outs[0][1])
+    # FP32 per-shot accumulation (the reference's) agrees to FP32 rounding
+    sv = F.Survey(spec, grad_form=F.GRAD_F32)
+    sv.set_lambda(lam)
+    g32 = np.zeros_like(outs[0][1])
+    sv.run(1, g32)
+    assert rel(g32.astype(np.float64), outs[0][1].astype(np.float64)) <= 1e-5
+
+
+def test_step2_numtasks_and_accumulation():
+    import fwi_gb300 as F
+    from fwi_gb300.synth import lam_from_vp
+    spec, vp = make(7, nshots=2)
+    lam = lam_from_vp(vp)
+    sv1 = F.Survey(spec)                # numtasks = 1
+    sv1.set_lambda(lam)
+    g1 = np.zeros((spec.ny, spec.nx_model), np.float32, order="F")
+    m0, _ = sv1.run(1, g1)
+    spec.numtasks = 2
+    sv = F.Survey(spec)
+    sv.set_lambda(lam)
+    g0 = np.full((spec.ny, spec.nx_model), 0.25, np.float32, order="F")
+    g = g0.copy(order="F")
+    m1, _ = sv.run(1, g, misfit=1.5)    # Misfit and Grad accumulate
+    m2, _ = sv.run(2, None)             # forward + misfit only
+    assert m1 - 1.5 == pytest.approx(m0, rel=1e-12) and m2 == pytest.approx(m0, rel=1e-12)
+    # Grad = Grad + stack/numtasks, then the water rows are zeroed
+    expect = (g0.astype(np.float64) + g1.astype(np.float64) / 2).astype(np.float32)
+    for i, k in enumerate(spec.water_rows):
+        expect[:k, i] = 0
+    assert rel(g.astype(np.float64), expect.astype(np.float64)) <= 1e-6
+
+
+@pytest.mark.parametrize("form,tol", [(1, 2e-2), (2, 2e-3)])
+def test_16bit_snapshots_error_vs_fp64_oracle(form, tol):
+    import fwi_gb300 as F
+    from fwi_gb300.synth import lam_from_vp
+    spec, vp = make(8, nshots=2, nt=300)
+    lam = lam_from_vp(vp)
+    vp_ref = np.sqrt(lam / np.float32(1000.0))
+    G64, _, m64, _ = stacked_oracle(spec, vp_ref.astype(np.float64), fp64=True)
+    for i, k in enumerate(spec.water_rows):
+        G64[:k, i] = 0
+    res = {}
+    for f in (0, form):
+        sv = F.Survey(spec, snap_form=f)
+        sv.set_lambda(lam)
+        g = np.zeros((spec.ny, spec.nx_model), np.float32, order="F")
+        m, _ = sv.run(1, g)
+        res[f] = (m, g.astype(np.float64))
+    e32 = rel(res[0][1], G64)
+    e16 = rel(res[form][1], G64)
+    assert e32 <= 1e-4
+    assert e16 <= tol
+    assert res[form][0] == res[0][0]  # the misfit does not depend on snapshots
+
+
+def test_batch_entry_point_matches_survey():
+    import fwi_gb300 as F
+    from fwi_gb300.synth import lam_from_vp
+    spec, vp = make(9, nshots=3)
+    lam = lam_from_vp(vp)
+    g = np.zeros((spec.ny, spec.nx_model), np.float32, order="F")
+    m = F.calculate_misfit_gradient(spec, lam, 1, np.float32(0.0), g)
+    sv = F.Survey(spec)
+    sv.set_lambda(lam)
+    g2 = np.zeros_like(g)
+    m2, _ = sv.run(1, g2)
+    assert np.array_equal(g, g2) and m == np.float32(m2)
+    # second call with the same geometry reuses the cached plan
+    g3 = np.zeros_like(g)
+    m3 = F.calculate_misfit_gradient(spec, lam, 1, np.float32(0.0), g3)
+    assert np.array_equal(g3, g) and m3 == m

@@ -2,13 +2,12 @@
 L2 misfit and adjoint source, imaging condition and gradient stack, as
 hand-written sm_103a kernels behind the C ABI of include/fwi_gb300.h.
 
-Importing the package loads fwi_gb300/_lib/libfwi_gb300.so; build it first
-with ``python -m fwi_gb300.build``.
+Every entry point loads fwi_gb300/_lib/libfwi_gb300.so and raises if it is
+missing (build it with ``python -m fwi_gb300.build``): there is no CPU
+fallback.
 """
 from ._native import FwiError, GRAD_F32, GRAD_F64, SNAP_BF16, SNAP_F16, SNAP_F32, load  # noqa: F401
 from .survey import ShotSpec, SurveySpec  # noqa: F401
-
-load()
 
 from .api import (  # noqa: E402,F401
     Beta_calculous,

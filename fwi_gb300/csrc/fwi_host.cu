@@ -22,7 +22,8 @@
 #include "fwi_internal.cuh"
 
 namespace fwi {
-cudaError_t launch_step(int acc, int mode, const StepParams& pm, const StepParams& pb, cudaStream_t st);
+cudaError_t launch_step(int acc, int mode, const StepParams& pm, const StepParams& pb, cudaStream_t sm,
+                        cudaStream_t sb);
 cudaError_t launch_build_c2(float* c2, int nyt, int pitch, int off, int dn, int ny, int nx, const float* src, int ldv,
                             int x0, int from_lambda, float dt2, float d2, cudaStream_t st);
 cudaError_t launch_rec_last(float* rec, int nt, int nrec, cudaStream_t st);
@@ -85,6 +86,8 @@ struct LibState {
     int device = 0;
     cudaStream_t own = nullptr;
     cudaStream_t user = nullptr;
+    cudaStream_t aux = nullptr;      // bottom-row kernels run here, concurrently
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     int acc = 3, dpml = 20;
     long long launches = 0;
     std::recursive_mutex mu;
@@ -433,12 +436,26 @@ StepParams base_params(int acc, float dt, int store_snap, int snap_form, int gra
     return p;
 }
 
-// One pass over the time loop k = 2..nt for a set of shots.
-// mode 0: forward (snapshots if store, receivers recorded); mode 1: adjoint.
 struct StepSet {
     StepParams pm, pb;
 };
-int run_time_loop(int acc, int mode, int nt, int store_snap, int nt_store, bool store, StepSet ps, cudaStream_t st) {
+
+// One time step: model rows on st, bottom rows on st2, both ordered after
+// the previous step and before the next one.
+int step_fork_join(int acc, int mode, const StepSet& ps, cudaStream_t st, cudaStream_t st2) {
+    CK(cudaEventRecord(L().ev_fork, st));
+    CK(cudaStreamWaitEvent(st2, L().ev_fork, 0));
+    CK(launch_step(acc, mode, ps.pm, ps.pb, st, st2));
+    CK(cudaEventRecord(L().ev_join, st2));
+    CK(cudaStreamWaitEvent(st, L().ev_join, 0));
+    L().launches += (ps.pm.nitems > 0) + (ps.pb.nitems > 0);
+    return FWI_OK;
+}
+
+// One pass over the time loop k = 2..nt for a set of shots.
+// mode 0: forward (snapshots if store, receivers recorded); mode 1: adjoint.
+int run_time_loop(int acc, int mode, int nt, int store_snap, int nt_store, bool store, StepSet ps, cudaStream_t st,
+                  cudaStream_t st2) {
     std::vector<int> ev = snapshot_steps(nt, store_snap);
     size_t evi = 0;
     int snap = (mode == 0) ? 0 : nt_store;
@@ -457,8 +474,7 @@ int run_time_loop(int acc, int mode, int nt, int store_snap, int nt_store, bool 
         ps.pm.t = ps.pb.t = k - 2;
         ps.pm.parity = ps.pb.parity = k & 1;
         ps.pm.snap = ps.pb.snap = sn;
-        CK(launch_step(acc, mode, ps.pm, ps.pb, st));
-        L().launches += (ps.pm.nitems > 0) + (ps.pb.nitems > 0);
+        TRY(step_fork_join(acc, mode, ps, st, st2));
     }
     return FWI_OK;
 }
@@ -504,6 +520,9 @@ int fwi_init(int device) {
     if (device < 0 || device >= n) return fail(FWI_ERR_ARG, "invalid CUDA device index");
     CK(cudaSetDevice(device));
     if (!L().own) CK(cudaStreamCreateWithFlags(&L().own, cudaStreamNonBlocking));
+    if (!L().aux) CK(cudaStreamCreateWithFlags(&L().aux, cudaStreamNonBlocking));
+    if (!L().ev_fork) CK(cudaEventCreateWithFlags(&L().ev_fork, cudaEventDisableTiming));
+    if (!L().ev_join) CK(cudaEventCreateWithFlags(&L().ev_join, cudaEventDisableTiming));
     L().device = device;
     L().init = true;
     return FWI_OK;
@@ -517,7 +536,11 @@ int fwi_finalize(void) {
     s.~Single();
     new (&s) Single();
     if (L().own) cudaStreamDestroy(L().own);
-    L().own = nullptr;
+    if (L().aux) cudaStreamDestroy(L().aux);
+    if (L().ev_fork) cudaEventDestroy(L().ev_fork);
+    if (L().ev_join) cudaEventDestroy(L().ev_join);
+    L().own = L().aux = nullptr;
+    L().ev_fork = L().ev_join = nullptr;
     L().user = nullptr;
     L().init = false;
     return FWI_OK;
@@ -643,7 +666,7 @@ int fwi_solver_acoustic_ss(const int* rank, const int* iprop_, const int* NumSou
     ps.pb = ps.pm;
     ps.pb.items = sg.d_items_b.as<WorkItem>();
     ps.pb.nitems = (int)lists.bottom.size();
-    TRY(run_time_loop(acc, adj ? 1 : 0, nt, store_snap, nt_store, iprop == 1, ps, st));
+    TRY(run_time_loop(acc, adj ? 1 : 0, nt, store_snap, nt_store, iprop == 1, ps, st, L().aux));
 
     if (!adj) LK(launch_rec_last(sg.d_rec.as<float>(), nt, NumRec, st));
     // outputs
@@ -912,7 +935,7 @@ int survey_prepare_waves(fwi_survey* s) {
 }
 
 // Issue one wave's work: forward (+ misfit) and, for step 1, adjoint + stack.
-int issue_wave(fwi_survey* s, size_t wi, int step, cudaStream_t st) {
+int issue_wave(fwi_survey* s, size_t wi, int step, cudaStream_t st, cudaStream_t st2) {
     const auto& D = s->desc;
     const auto& w = s->waves[wi];
     auto& wd = *s->wdev[wi];
@@ -928,6 +951,14 @@ int issue_wave(fwi_survey* s, size_t wi, int step, cudaStream_t st) {
         CK(cudaMemsetAsync(ss.phy.p, 0, ss.phy.n, st));
         CK(cudaMemsetAsync(ss.chy.p, 0, ss.chy.n, st));
         CK(cudaMemsetAsync(ss.c2.p, 0, ss.c2.n, st));
+        // snapshot block 0 is never written by the forward but is the last
+        // one the adjoint pairs with: zero, as Fields = 0 before the forward
+        // (calculate_misfit_gradient.f90:231)
+        if (step == 1) {
+            const size_t esz = D.snap_form == FWI_SNAP_F32 ? 4 : 2;
+            CK(cudaMemsetAsync(ss.snaps.p, 0, (size_t)l.ny * l.pitch * esz, st));
+            CK(cudaMemsetAsync(ss.sscale.p, 0, (size_t)l.ny * l.ntiles * sizeof(float), st));
+        }
         LK(launch_build_c2(ss.c2.as<float>(), l.nyt, l.pitch, l.off, l.dn, l.ny, l.nx, s->d_lambda.as<float>(), D.ny,
                            s->geoms[sh].x0, 1, D.dt * D.dt, D.d * D.d, st));
         float* rec = s->d_synth.as<float>() + (size_t)s->tr_off[sh] * D.nt;
@@ -944,7 +975,7 @@ int issue_wave(fwi_survey* s, size_t wi, int step, cudaStream_t st) {
     ps.pb = ps.pm;
     ps.pb.items = wd.items_b.as<WorkItem>();
     ps.pb.nitems = wd.n_b;
-    TRY(run_time_loop(D.acc, 0, D.nt, D.store_snap, s->nt_store, step == 1, ps, st));
+    TRY(run_time_loop(D.acc, 0, D.nt, D.store_snap, s->nt_store, step == 1, ps, st, st2));
     for (size_t k = 0; k < w.size(); ++k) {
         const int sh = w[k];
         LK(launch_rec_last(s->d_synth.as<float>() + (size_t)s->tr_off[sh] * D.nt, D.nt, (int)s->geoms[sh].nxR.size(), st));
@@ -972,7 +1003,7 @@ int issue_wave(fwi_survey* s, size_t wi, int step, cudaStream_t st) {
     ps.pm.record = 0;
     ps.pb.shots = wd.shots_a.as<ShotDev>();
     ps.pb.record = 0;
-    TRY(run_time_loop(D.acc, 1, D.nt, D.store_snap, s->nt_store, true, ps, st));
+    TRY(run_time_loop(D.acc, 1, D.nt, D.store_snap, s->nt_store, true, ps, st, st2));
     LK(launch_stack(s->d_G.as<double>(), D.ny, D.nx_model, wd.stack.p, (int)w.size(), D.grad_form, st));
     return FWI_OK;
 }
@@ -1137,18 +1168,20 @@ int fwi_survey_run(fwi_survey* s, int step, double* misfit, float* grad) {
     for (size_t wi = 0; wi < s->waves.size(); ++wi) {
         auto& wd = *s->wdev[wi];
         if (D.flags & FWI_SURVEY_NO_GRAPH) {
-            TRY(issue_wave(s, wi, step, st));
+            TRY(issue_wave(s, wi, step, st, L().aux));
             continue;
         }
         if (!wd.graph[gi]) {
-            cudaStream_t cap;
+            cudaStream_t cap, cap2;
             CK(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
+            CK(cudaStreamCreateWithFlags(&cap2, cudaStreamNonBlocking));
             cudaGraph_t graph;
             CK(cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal));
             const long long l0 = L().launches;
-            int rc = issue_wave(s, wi, step, cap);
+            int rc = issue_wave(s, wi, step, cap, cap2);
             cudaError_t e = cudaStreamEndCapture(cap, &graph);
             cudaStreamDestroy(cap);
+            cudaStreamDestroy(cap2);
             if (rc != FWI_OK) return rc;
             if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture", __LINE__);
             wd.graph_kernels[gi] = L().launches - l0;
@@ -1239,8 +1272,7 @@ int fwi_survey_time_steps(fwi_survey* s, int steps) {
         const int k = 2 + (i % (D.nt - 1));
         ps.pm.t = ps.pb.t = k - 2;
         ps.pm.parity = ps.pb.parity = k & 1;
-        CK(launch_step(D.acc, 0, ps.pm, ps.pb, stream()));
-        L().launches += 2;
+        TRY(step_fork_join(D.acc, 0, ps, stream(), L().aux));
     }
     return FWI_OK;
 }

@@ -314,12 +314,31 @@ __device__ __forceinline__ void record_row(const StepParams& P, const ShotDev& S
 
 }  // namespace
 
+// Per-lane asynchronous prefetch of the rows a warp will need (cp.async,
+// 16 bytes per lane per array, L2-only).  Every lane reads back only what it
+// copied itself, so no intra-warp synchronisation is needed.
+__device__ __forceinline__ void cp16(void* smem_dst, const void* gmem_src) {
+    const unsigned d = (unsigned)__cvta_generic_to_shared(smem_dst);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(gmem_src) : "memory");
+}
+__device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
+
+// One prefetch stage of the main kernel (float4 slots): p(y+R), p_1(y),
+// c2(y), x-phi(y), x-chi(y) per lane, plus the two halo float4 of p(y).
+constexpr int ST_P = 0, ST_P1 = 32, ST_C2 = 64, ST_PH = 96, ST_CH = 128, ST_HL = 160, ST_HR = 161, ST_SIZE = 162;
+constexpr int MAIN_DEPTH = 4;  // rows in flight per warp
+constexpr int MAIN_SMEM = 4 * MAIN_DEPTH * ST_SIZE * 16;  // bytes per 4-warp block
+
 // Model rows: interior + left/right CPML strips.
 template <int R, int MODE>
 __global__ void __launch_bounds__(128) k_step_main(const __grid_constant__ StepParams P) {
+    extern __shared__ float4 smem[];
     const int lane = threadIdx.x & 31;
     const int wid = blockIdx.x * 4 + (threadIdx.x >> 5);
     if (wid >= P.nitems) return;
+    float4* ring = smem + (threadIdx.x >> 5) * (MAIN_DEPTH * ST_SIZE);
     const WorkItem it = P.items[wid];
     const ShotDev& S = P.shots[it.shot];
     const int pitch = S.pitch, dn = S.dn, nx = S.nx, nxt = S.nxt;
@@ -327,7 +346,29 @@ __global__ void __launch_bounds__(128) k_step_main(const __grid_constant__ StepP
     const bool first = it.tile == 0, last = it.tile == S.ntiles - 1, edge = first || last;
     const float* PC = P.parity ? S.pa : S.pb;  // p
     float* P1 = P.parity ? S.pb : S.pa;        // p_1, overwritten with p_3
+    bool lane_strip = false;
+    if (edge) lane_strip = (c0 < dn) || (c0 + 3 >= dn + nx);
+    const bool has_hl = (lane == 0) && (x0 > 0), has_hr = (lane == 31) && (x0 + TILE < pitch);
 
+    auto issue = [&](int y, int slot) {
+        float4* st = ring + slot * ST_SIZE;
+        const size_t ro = (size_t)y * pitch + xl;
+        cp16(st + ST_P + lane, PC + (size_t)(y + R) * pitch + xl);
+        cp16(st + ST_P1 + lane, P1 + ro);
+        cp16(st + ST_C2 + lane, S.c2 + ro);
+        if (lane_strip) {
+            cp16(st + ST_PH + lane, S.phx + ro);
+            cp16(st + ST_CH + lane, S.chx + ro);
+        }
+        if (has_hl) cp16(st + ST_HL, PC + (size_t)y * pitch + x0 - 4);
+        if (has_hr) cp16(st + ST_HR, PC + (size_t)y * pitch + x0 + TILE);
+    };
+
+#pragma unroll
+    for (int i = 0; i < MAIN_DEPTH; ++i) {
+        if (it.y0 + i < it.y1) issue(it.y0 + i, i);
+        cp_commit();
+    }
     float4 q[2 * R + 1];
 #pragma unroll
     for (int i = 0; i < 2 * R; ++i) q[i] = ldg4(PC + (size_t)(it.y0 - R + i) * pitch + xl);
@@ -335,19 +376,24 @@ __global__ void __launch_bounds__(128) k_step_main(const __grid_constant__ StepP
     int si = it.s0, ri = it.r0;
     int srow = (si < it.s1) ? P.srcs[si].row : INT_MAX;
     int rrow = (ri < it.r1) ? P.recs[ri].row : INT_MAX;
-    bool lane_strip = false;
-    if (edge) lane_strip = (c0 < dn) || (c0 + 3 >= dn + nx);
 
+    int slot = 0;
     for (int y = it.y0; y < it.y1; ++y) {
-        q[2 * R] = ldg4(PC + (size_t)(y + R) * pitch + xl);
+        cp_wait<MAIN_DEPTH - 1>();
+        const float4* st = ring + slot * ST_SIZE;
         const size_t ro = (size_t)y * pitch + xl;
+        q[2 * R] = st[ST_P + lane];
         float pm1[4], cc[4], pc[4];
-        to_arr(ld4(P1 + ro), pm1);
-        to_arr(ldg4(S.c2 + ro), cc);
+        to_arr(st[ST_P1 + lane], pm1);
+        to_arr(st[ST_C2 + lane], cc);
         to_arr(q[R], pc);
-        float4 hl = make_float4(0.f, 0.f, 0.f, 0.f), hr = hl;
-        if (lane == 0 && x0 > 0) hl = ldg4(PC + (size_t)y * pitch + x0 - 4);
-        if (lane == 31 && x0 + TILE < pitch) hr = ldg4(PC + (size_t)y * pitch + x0 + TILE);
+        const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
+        const float4 hl = has_hl ? st[ST_HL] : z4, hr = has_hr ? st[ST_HR] : z4;
+        float ph[4] = {0.f, 0.f, 0.f, 0.f}, ch[4] = {0.f, 0.f, 0.f, 0.f};
+        if (lane_strip) {
+            to_arr(st[ST_PH + lane], ph);
+            to_arr(st[ST_CH + lane], ch);
+        }
         float w[12];
         window(q[R], hl, hr, lane, w);
         float d2x[4], dx[4], d2y[4], dy[4];
@@ -377,11 +423,6 @@ __global__ void __launch_bounds__(128) k_step_main(const __grid_constant__ StepP
                 p3[e] = ((-pm1[e]) + 2.f * pc[e]) + (((d2x[e] + d2y[e]) + sv[e]) * cc[e]);
         } else {
             xclamp<R>(S, x0, c0, first, last, d2x, dx);
-            float ph[4] = {0.f, 0.f, 0.f, 0.f}, ch[4] = {0.f, 0.f, 0.f, 0.f};
-            if (lane_strip) {
-                to_arr(ld4(S.phx + ro), ph);
-                to_arr(ld4(S.chx + ro), ch);
-            }
             float dph[4];
             phi_xderiv<R>(S, P, from_arr(ph), lane, x0, c0, first, last, dph);
 #pragma unroll
@@ -416,7 +457,12 @@ __global__ void __launch_bounds__(128) k_step_main(const __grid_constant__ StepP
 
 #pragma unroll
         for (int i = 0; i < 2 * R; ++i) q[i] = q[i + 1];
+        // refill this slot (its values are consumed above) with row y + depth
+        if (y + MAIN_DEPTH < it.y1) issue(y + MAIN_DEPTH, slot);
+        cp_commit();
+        slot = (slot + 1 == MAIN_DEPTH) ? 0 : slot + 1;
     }
+    cp_wait<0>();
 }
 
 // Bottom pad rows: bottom strip and bottom corners.
@@ -557,27 +603,26 @@ __global__ void __launch_bounds__(128) k_step_bottom(const __grid_constant__ Ste
 
 // Host-side launchers -------------------------------------------------------
 
-cudaError_t launch_step(int acc, int mode, const StepParams& pm, const StepParams& pb, cudaStream_t st) {
+// Model-row kernel on stream sm and bottom-row kernel on stream sb (the
+// caller orders the two streams around each time step).
+cudaError_t launch_step(int acc, int mode, const StepParams& pm, const StepParams& pb, cudaStream_t sm,
+                        cudaStream_t sb) {
     const int bm = (pm.nitems + 3) / 4, bb = (pb.nitems + 3) / 4;
+#define FWI_LAUNCH(R_, M_)                                                            \
+    do {                                                                             \
+        if (bm) k_step_main<R_, M_><<<bm, 128, MAIN_SMEM, sm>>>(pm);                  \
+        if (bb) k_step_bottom<R_, M_><<<bb, 128, 0, sb>>>(pb);                        \
+    } while (0)
     if (acc == 3) {
-        if (mode == 0) {
-            if (bm) k_step_main<3, 0><<<bm, 128, 0, st>>>(pm);
-            if (bb) k_step_bottom<3, 0><<<bb, 128, 0, st>>>(pb);
-        } else {
-            if (bm) k_step_main<3, 1><<<bm, 128, 0, st>>>(pm);
-            if (bb) k_step_bottom<3, 1><<<bb, 128, 0, st>>>(pb);
-        }
+        if (mode == 0) FWI_LAUNCH(3, 0);
+        else FWI_LAUNCH(3, 1);
     } else if (acc == 4) {
-        if (mode == 0) {
-            if (bm) k_step_main<4, 0><<<bm, 128, 0, st>>>(pm);
-            if (bb) k_step_bottom<4, 0><<<bb, 128, 0, st>>>(pb);
-        } else {
-            if (bm) k_step_main<4, 1><<<bm, 128, 0, st>>>(pm);
-            if (bb) k_step_bottom<4, 1><<<bb, 128, 0, st>>>(pb);
-        }
+        if (mode == 0) FWI_LAUNCH(4, 0);
+        else FWI_LAUNCH(4, 1);
     } else {
         return cudaErrorInvalidValue;
     }
+#undef FWI_LAUNCH
     return cudaGetLastError();
 }
 

@@ -45,6 +45,10 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg")
     ap.add_argument("--no-plain", action="store_true", help="skip the plain-path leg")
+    ap.add_argument("--profile", type=int, default=0,
+                    help="only build the survey and run this many forward time steps (for ncu captures)")
+    ap.add_argument("--wave", type=int, default=0, help="shots per wave (0 = tuner)")
+    ap.add_argument("--band", type=int, default=0, help="rows per warp work item (0 = tuner)")
     return ap.parse_args()
 
 
@@ -205,8 +209,21 @@ def main():
     spec, vp_true, vp0 = synth.config2(seed=2 + rank, nshots=a.shots, nt=a.nt)
     lam_true, lam0 = lam_from_vp(vp_true), lam_from_vp(vp0)
 
+    if a.profile:
+        sv = F.Survey(spec, snap_form=snap_form, wave_shots=a.wave, band_rows=a.band)
+        sv.set_lambda(lam0)
+        torch.cuda.synchronize()
+        p0, p1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        p0.record(stream)
+        sv.time_steps(a.profile)
+        p1.record(stream)
+        torch.cuda.synchronize()
+        ms = p0.elapsed_time(p1) / a.profile
+        print(json.dumps({"profile_steps": a.profile, "ms_per_step": ms, "step_bytes": sv.step_bytes(),
+                          "GBps": sv.step_bytes() / ms / 1e6, "tuning": sv.tuning()}))
+        return 0
     # observed data from the true model (untimed setup)
-    sv = F.Survey(spec, snap_form=snap_form)
+    sv = F.Survey(spec, snap_form=snap_form, wave_shots=a.wave, band_rows=a.band)
     sv.set_lambda(lam_true)
     sv.run(2)
     for i, sh in enumerate(spec.shots):

@@ -24,6 +24,7 @@
 namespace fwi {
 cudaError_t launch_step(int acc, int mode, const StepParams& pm, const StepParams& pb, cudaStream_t sm,
                         cudaStream_t sb);
+cudaError_t configure_step_kernels();
 cudaError_t launch_build_c2(float* c2, int nyt, int pitch, int off, int dn, int ny, int nx, const float* src, int ldv,
                             int x0, int from_lambda, float dt2, float d2, cudaStream_t st);
 cudaError_t launch_rec_last(float* rec, int nt, int nrec, cudaStream_t st);
@@ -88,6 +89,7 @@ struct LibState {
     cudaStream_t user = nullptr;
     cudaStream_t aux = nullptr;      // bottom-row kernels run here, concurrently
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    int prio_hi = 0;
     int acc = 3, dpml = 20;
     long long launches = 0;
     std::recursive_mutex mu;
@@ -250,8 +252,13 @@ int validate_geometry(const ShotGeom& g, const Layout& l, int shot) {
     return FWI_OK;
 }
 
+// Work items of one time step: interior items (middle tiles of the model
+// rows) for k_step_interior, boundary items (first/last tile of the model
+// rows, every tile of the bottom pad) for k_step_boundary; forward lists
+// inject the sources and record the receivers, adjoint lists inject the
+// adjoint sources at the receivers.
 struct Lists {
-    std::vector<WorkItem> main_fwd, main_adj, bottom;
+    std::vector<WorkItem> int_fwd, int_adj, bnd_fwd, bnd_adj;
     std::vector<SrcEnt> src_fwd, src_adj;
     std::vector<RecEnt> recs;
 };
@@ -313,19 +320,30 @@ Lists build_lists(const std::vector<ShotGeom>& geoms, const std::vector<Layout>&
             if (pr < l.dn) continue;  // top pad: identically zero, never recorded
             recs.push_back(RecEnt{pr, l.off + pc, (int)i});
         }
-        const int nb = std::max(1, (l.ny + band_rows - 1) / band_rows);
-        for (int b = 0; b < nb; ++b) {
-            const int y0 = l.dn + (int)((long long)l.ny * b / nb);
-            const int y1 = l.dn + (int)((long long)l.ny * (b + 1) / nb);
-            if (y1 <= y0) continue;
-            for (int t = 0; t < l.ntiles; ++t) {
-                append_item(out, out.main_fwd, out.src_fwd, cells_f, recs, (int)s, t, y0, y1, 0, true);
-                append_item(out, out.main_adj, out.src_adj, cells_a, recs, (int)s, t, y0, y1, 0, false);
+        // interior tiles in bands of band_rows; the heavier edge tiles (CPML
+        // strips) in thinner bands so that the boundary kernel has warps enough
+        for (int pass = 0; pass < 2; ++pass) {
+            const int rows = pass == 0 ? band_rows : std::min(band_rows, 16);
+            const int nb = std::max(1, (l.ny + rows - 1) / rows);
+            for (int b = 0; b < nb; ++b) {
+                const int y0 = l.dn + (int)((long long)l.ny * b / nb);
+                const int y1 = l.dn + (int)((long long)l.ny * (b + 1) / nb);
+                if (y1 <= y0) continue;
+                for (int t = 0; t < l.ntiles; ++t) {
+                    const bool edge = (t == 0) || (t == l.ntiles - 1);
+                    if (edge != (pass == 1)) continue;
+                    append_item(out, edge ? out.bnd_fwd : out.int_fwd, out.src_fwd, cells_f, recs, (int)s, t, y0, y1,
+                                0, true);
+                    append_item(out, edge ? out.bnd_adj : out.int_adj, out.src_adj, cells_a, recs, (int)s, t, y0, y1,
+                                0, false);
+                }
             }
         }
         std::vector<SrcEnt> none;
-        for (int t = 0; t < l.ntiles; ++t)
-            append_item(out, out.bottom, out.src_fwd, none, recs, (int)s, t, l.nyt - l.dn, l.nyt, 1, true);
+        for (int t = 0; t < l.ntiles; ++t) {
+            append_item(out, out.bnd_fwd, out.src_fwd, none, recs, (int)s, t, l.nyt - l.dn, l.nyt, 1, true);
+            append_item(out, out.bnd_adj, out.src_adj, none, recs, (int)s, t, l.nyt - l.dn, l.nyt, 1, false);
+        }
     }
     return out;
 }
@@ -520,9 +538,17 @@ int fwi_init(int device) {
     if (device < 0 || device >= n) return fail(FWI_ERR_ARG, "invalid CUDA device index");
     CK(cudaSetDevice(device));
     if (!L().own) CK(cudaStreamCreateWithFlags(&L().own, cudaStreamNonBlocking));
-    if (!L().aux) CK(cudaStreamCreateWithFlags(&L().aux, cudaStreamNonBlocking));
+    if (!L().aux) {
+        // boundary kernels (long dependency chains, few warps) get the
+        // higher priority so they start first and overlap the interior
+        int lo = 0, hi = 0;
+        CK(cudaDeviceGetStreamPriorityRange(&lo, &hi));
+        CK(cudaStreamCreateWithPriority(&L().aux, cudaStreamNonBlocking, hi));
+        L().prio_hi = hi;
+    }
     if (!L().ev_fork) CK(cudaEventCreateWithFlags(&L().ev_fork, cudaEventDisableTiming));
     if (!L().ev_join) CK(cudaEventCreateWithFlags(&L().ev_join, cudaEventDisableTiming));
+    CK(configure_step_kernels());
     L().device = device;
     L().init = true;
     return FWI_OK;
@@ -648,8 +674,8 @@ int fwi_solver_acoustic_ss(const int* rank, const int* iprop_, const int* NumSou
     std::vector<Layout> lays{l};
     Lists lists = build_lists(geoms, lays, 64);
     const bool adj = (iprop == 2);
-    TRY(upload(sg.d_items_m, adj ? lists.main_adj : lists.main_fwd, st));
-    TRY(upload(sg.d_items_b, lists.bottom, st));
+    TRY(upload(sg.d_items_m, adj ? lists.int_adj : lists.int_fwd, st));
+    TRY(upload(sg.d_items_b, adj ? lists.bnd_adj : lists.bnd_fwd, st));
     TRY(upload(sg.d_src, adj ? lists.src_adj : lists.src_fwd, st));
     TRY(upload(sg.d_recs, lists.recs, st));
     std::vector<ShotDev> sd{sg.sh.dev(nt, NumRec, 0, sg.d_srcv.as<float>(), sg.d_rec.as<float>())};
@@ -658,14 +684,14 @@ int fwi_solver_acoustic_ss(const int* rank, const int* iprop_, const int* NumSou
     StepSet ps;
     ps.pm = base_params(acc, dt, store_snap, FWI_SNAP_F32, FWI_GRAD_F32, sg.d_fA.as<float>(), sg.d_fB.as<float>());
     ps.pm.items = sg.d_items_m.as<WorkItem>();
-    ps.pm.nitems = (int)(adj ? lists.main_adj.size() : lists.main_fwd.size());
+    ps.pm.nitems = (int)(adj ? lists.int_adj.size() : lists.int_fwd.size());
     ps.pm.shots = sg.d_shot.as<ShotDev>();
     ps.pm.srcs = sg.d_src.as<SrcEnt>();
     ps.pm.recs = sg.d_recs.as<RecEnt>();
     ps.pm.record = adj ? 0 : 1;
     ps.pb = ps.pm;
     ps.pb.items = sg.d_items_b.as<WorkItem>();
-    ps.pb.nitems = (int)lists.bottom.size();
+    ps.pb.nitems = (int)(adj ? lists.bnd_adj.size() : lists.bnd_fwd.size());
     TRY(run_time_loop(acc, adj ? 1 : 0, nt, store_snap, nt_store, iprop == 1, ps, st, L().aux));
 
     if (!adj) LK(launch_rec_last(sg.d_rec.as<float>(), nt, NumRec, st));
@@ -827,8 +853,8 @@ struct fwi_survey {
     std::vector<std::unique_ptr<ShotState>> slots;
     // per-wave lists
     struct WaveDev {
-        DBuf items_mf, items_ma, items_b, src_f, src_a, recs, shots_f, shots_a, stack;
-        int n_mf = 0, n_ma = 0, n_b = 0;
+        DBuf items_if, items_ia, items_bf, items_ba, src_f, src_a, recs, shots_f, shots_a, stack;
+        int n_if = 0, n_ia = 0, n_bf = 0, n_ba = 0;
         cudaGraphExec_t graph[3] = {nullptr, nullptr, nullptr};
         long long graph_kernels[3] = {0, 0, 0};  // kernel nodes per graph
     };
@@ -875,15 +901,17 @@ int survey_prepare_waves(fwi_survey* s) {
         }
         Lists lists = build_lists(g, l, s->band);
         std::unique_ptr<fwi_survey::WaveDev> wd(new fwi_survey::WaveDev());
-        TRY(upload(wd->items_mf, lists.main_fwd, st));
-        TRY(upload(wd->items_ma, lists.main_adj, st));
-        TRY(upload(wd->items_b, lists.bottom, st));
+        TRY(upload(wd->items_if, lists.int_fwd, st));
+        TRY(upload(wd->items_ia, lists.int_adj, st));
+        TRY(upload(wd->items_bf, lists.bnd_fwd, st));
+        TRY(upload(wd->items_ba, lists.bnd_adj, st));
         TRY(upload(wd->src_f, lists.src_fwd, st));
         TRY(upload(wd->src_a, lists.src_adj, st));
         TRY(upload(wd->recs, lists.recs, st));
-        wd->n_mf = (int)lists.main_fwd.size();
-        wd->n_ma = (int)lists.main_adj.size();
-        wd->n_b = (int)lists.bottom.size();
+        wd->n_if = (int)lists.int_fwd.size();
+        wd->n_ia = (int)lists.int_adj.size();
+        wd->n_bf = (int)lists.bnd_fwd.size();
+        wd->n_ba = (int)lists.bnd_adj.size();
         s->wdev.push_back(std::move(wd));
     }
     // allocate slots for the largest shot that can land in each slot
@@ -966,15 +994,15 @@ int issue_wave(fwi_survey* s, size_t wi, int step, cudaStream_t st, cudaStream_t
     }
     StepSet ps;
     ps.pm = base_params(D.acc, D.dt, D.store_snap, D.snap_form, D.grad_form, s->d_fA.as<float>(), s->d_fB.as<float>());
-    ps.pm.items = wd.items_mf.as<WorkItem>();
-    ps.pm.nitems = wd.n_mf;
+    ps.pm.items = wd.items_if.as<WorkItem>();
+    ps.pm.nitems = wd.n_if;
     ps.pm.shots = wd.shots_f.as<ShotDev>();
     ps.pm.srcs = wd.src_f.as<SrcEnt>();
     ps.pm.recs = wd.recs.as<RecEnt>();
     ps.pm.record = 1;
     ps.pb = ps.pm;
-    ps.pb.items = wd.items_b.as<WorkItem>();
-    ps.pb.nitems = wd.n_b;
+    ps.pb.items = wd.items_bf.as<WorkItem>();
+    ps.pb.nitems = wd.n_bf;
     TRY(run_time_loop(D.acc, 0, D.nt, D.store_snap, s->nt_store, step == 1, ps, st, st2));
     for (size_t k = 0; k < w.size(); ++k) {
         const int sh = w[k];
@@ -996,13 +1024,14 @@ int issue_wave(fwi_survey* s, size_t wi, int step, cudaStream_t st, cudaStream_t
         CK(cudaMemsetAsync(ss.chy.p, 0, ss.chy.n, st));
         CK(cudaMemsetAsync(ss.k.p, 0, ss.k.n, st));
     }
-    ps.pm.items = wd.items_ma.as<WorkItem>();
-    ps.pm.nitems = wd.n_ma;
+    ps.pm.items = wd.items_ia.as<WorkItem>();
+    ps.pm.nitems = wd.n_ia;
     ps.pm.shots = wd.shots_a.as<ShotDev>();
     ps.pm.srcs = wd.src_a.as<SrcEnt>();
     ps.pm.record = 0;
-    ps.pb.shots = wd.shots_a.as<ShotDev>();
-    ps.pb.record = 0;
+    ps.pb = ps.pm;
+    ps.pb.items = wd.items_ba.as<WorkItem>();
+    ps.pb.nitems = wd.n_ba;
     TRY(run_time_loop(D.acc, 1, D.nt, D.store_snap, s->nt_store, true, ps, st, st2));
     LK(launch_stack(s->d_G.as<double>(), D.ny, D.nx_model, wd.stack.p, (int)w.size(), D.grad_form, st));
     return FWI_OK;
@@ -1174,7 +1203,7 @@ int fwi_survey_run(fwi_survey* s, int step, double* misfit, float* grad) {
         if (!wd.graph[gi]) {
             cudaStream_t cap, cap2;
             CK(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
-            CK(cudaStreamCreateWithFlags(&cap2, cudaStreamNonBlocking));
+            CK(cudaStreamCreateWithPriority(&cap2, cudaStreamNonBlocking, L().prio_hi));
             cudaGraph_t graph;
             CK(cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal));
             const long long l0 = L().launches;
@@ -1186,7 +1215,7 @@ int fwi_survey_run(fwi_survey* s, int step, double* misfit, float* grad) {
             if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture", __LINE__);
             wd.graph_kernels[gi] = L().launches - l0;
             L().launches = l0;  // counted when replayed
-            e = cudaGraphInstantiate(&wd.graph[gi], graph, 0);
+            e = cudaGraphInstantiate(&wd.graph[gi], graph, cudaGraphInstantiateFlagUseNodePriority);
             cudaGraphDestroy(graph);
             if (e != cudaSuccess) return cuda_fail(e, "cudaGraphInstantiate", __LINE__);
         }
@@ -1259,15 +1288,15 @@ int fwi_survey_time_steps(fwi_survey* s, int steps) {
     auto& wd = *s->wdev[0];
     StepSet ps;
     ps.pm = base_params(D.acc, D.dt, D.store_snap, D.snap_form, D.grad_form, s->d_fA.as<float>(), s->d_fB.as<float>());
-    ps.pm.items = wd.items_mf.as<WorkItem>();
-    ps.pm.nitems = wd.n_mf;
+    ps.pm.items = wd.items_if.as<WorkItem>();
+    ps.pm.nitems = wd.n_if;
     ps.pm.shots = wd.shots_f.as<ShotDev>();
     ps.pm.srcs = wd.src_f.as<SrcEnt>();
     ps.pm.recs = wd.recs.as<RecEnt>();
     ps.pm.record = 1;
     ps.pb = ps.pm;
-    ps.pb.items = wd.items_b.as<WorkItem>();
-    ps.pb.nitems = wd.n_b;
+    ps.pb.items = wd.items_bf.as<WorkItem>();
+    ps.pb.nitems = wd.n_bf;
     for (int i = 0; i < steps; ++i) {
         const int k = 2 + (i % (D.nt - 1));
         ps.pm.t = ps.pb.t = k - 2;

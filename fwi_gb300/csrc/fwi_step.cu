@@ -103,6 +103,31 @@ __device__ __forceinline__ void yderivs(const float4* q, const StepParams& P, fl
     }
 }
 
+// Second derivatives only (interior cells need no first derivative).
+template <int R>
+__device__ __forceinline__ void xderiv2(const float* w, const StepParams& P, float* d2) {
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+        float s2 = 0.f;
+#pragma unroll
+        for (int i = 0; i <= R; ++i) s2 = s2 + P.c2[i] * (w[4 + e + i] + w[4 + e - i]);
+        d2[e] = s2;
+    }
+}
+template <int R>
+__device__ __forceinline__ void yderiv2(const float4* q, const StepParams& P, float* d2) {
+    float a[2 * R + 1][4];
+#pragma unroll
+    for (int i = 0; i <= 2 * R; ++i) to_arr(q[i], a[i]);
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+        float s2 = 0.f;
+#pragma unroll
+        for (int i = 0; i <= R; ++i) s2 = s2 + (a[R + i][e] + a[R - i][e]) * P.c2[i];
+        d2[e] = s2;
+    }
+}
+
 // First derivative along y of the centre row of a queue (strip-local phi).
 template <int R>
 __device__ __forceinline__ void yderiv1(const float4* f, const StepParams& P, float* d1) {
@@ -331,15 +356,10 @@ constexpr int ST_P = 0, ST_P1 = 32, ST_C2 = 64, ST_PH = 96, ST_CH = 128, ST_HL =
 constexpr int MAIN_DEPTH = 4;  // rows in flight per warp
 constexpr int MAIN_SMEM = 4 * MAIN_DEPTH * ST_SIZE * 16;  // bytes per 4-warp block
 
-// Model rows: interior + left/right CPML strips.
+// Model rows of the first and last tile of a shot: interior cells plus the
+// left/right CPML strips, with the grid-edge clamps of the x derivatives.
 template <int R, int MODE>
-__global__ void __launch_bounds__(128) k_step_main(const __grid_constant__ StepParams P) {
-    extern __shared__ float4 smem[];
-    const int lane = threadIdx.x & 31;
-    const int wid = blockIdx.x * 4 + (threadIdx.x >> 5);
-    if (wid >= P.nitems) return;
-    float4* ring = smem + (threadIdx.x >> 5) * (MAIN_DEPTH * ST_SIZE);
-    const WorkItem it = P.items[wid];
+__device__ __forceinline__ void edge_rows(const StepParams& P, const WorkItem& it, float4* ring, int lane) {
     const ShotDev& S = P.shots[it.shot];
     const int pitch = S.pitch, dn = S.dn, nx = S.nx, nxt = S.nxt;
     const int x0 = it.tile * TILE, xl = x0 + 4 * lane, c0 = xl - S.off;
@@ -465,13 +485,17 @@ __global__ void __launch_bounds__(128) k_step_main(const __grid_constant__ StepP
     cp_wait<0>();
 }
 
-// Bottom pad rows: bottom strip and bottom corners.
+// One prefetch stage of the bottom kernel: p(y+R), p_1(y), c2(y), y-phi(y),
+// y-chi(y), x-phi(y), x-chi(y), the y-phi row the derivative queue needs
+// next (jl+1+R), and the halo float4 of p(y).
+constexpr int SB_P = 0, SB_P1 = 32, SB_C2 = 64, SB_PY = 96, SB_CY = 128, SB_PX = 160, SB_CX = 192, SB_FA = 224,
+              SB_HL = 256, SB_HR = 257, SB_SIZE = 258;
+constexpr int BOT_DEPTH = 3;
+constexpr int BOT_SMEM = 4 * BOT_DEPTH * SB_SIZE * 16;
+
+// Bottom pad rows of one tile: bottom strip and bottom corners.
 template <int R, int MODE>
-__global__ void __launch_bounds__(128) k_step_bottom(const __grid_constant__ StepParams P) {
-    const int lane = threadIdx.x & 31;
-    const int wid = blockIdx.x * 4 + (threadIdx.x >> 5);
-    if (wid >= P.nitems) return;
-    const WorkItem it = P.items[wid];
+__device__ __forceinline__ void bottom_rows(const StepParams& P, const WorkItem& it, float4* ring, int lane) {
     const ShotDev& S = P.shots[it.shot];
     const int pitch = S.pitch, dn = S.dn, nx = S.nx, nxt = S.nxt, nyt = S.nyt;
     const int x0 = it.tile * TILE, xl = x0 + 4 * lane, c0 = xl - S.off;
@@ -479,6 +503,32 @@ __global__ void __launch_bounds__(128) k_step_bottom(const __grid_constant__ Ste
     const float* PC = P.parity ? S.pa : S.pb;
     float* P1 = P.parity ? S.pb : S.pa;
     const int yb0 = nyt - dn;
+    bool lane_corner = false;
+    if (edge) lane_corner = (c0 < dn) || (c0 + 3 >= dn + nx);
+    const bool has_hl = (lane == 0) && (x0 > 0), has_hr = (lane == 31) && (x0 + TILE < pitch);
+
+    auto issue = [&](int jl, int slot) {
+        float4* st = ring + slot * SB_SIZE;
+        const int y = yb0 + jl;
+        const size_t ro = (size_t)y * pitch + xl;
+        if (y + R <= nyt - 1) cp16(st + SB_P + lane, PC + (size_t)(y + R) * pitch + xl);
+        cp16(st + SB_P1 + lane, P1 + ro);
+        cp16(st + SB_C2 + lane, S.c2 + ro);
+        cp16(st + SB_PY + lane, S.phy + ro);
+        cp16(st + SB_CY + lane, S.chy + ro);
+        if (lane_corner) {
+            cp16(st + SB_PX + lane, S.phx + ro);
+            cp16(st + SB_CX + lane, S.chx + ro);
+        }
+        if (jl >= R && jl + 1 + R <= dn - 1) cp16(st + SB_FA + lane, S.phy + (size_t)(yb0 + jl + 1 + R) * pitch + xl);
+        if (has_hl) cp16(st + SB_HL, PC + (size_t)y * pitch + x0 - 4);
+        if (has_hr) cp16(st + SB_HR, PC + (size_t)y * pitch + x0 + TILE);
+    };
+#pragma unroll
+    for (int i = 0; i < BOT_DEPTH; ++i) {
+        issue(i, i);  // dn >= 2R+1 > BOT_DEPTH rows always exist
+        cp_commit();
+    }
 
     float4 q[2 * R + 1], f[2 * R + 1];
 #pragma unroll
@@ -491,16 +541,17 @@ __global__ void __launch_bounds__(128) k_step_bottom(const __grid_constant__ Ste
 
     int ri = it.r0;
     int rrow = (ri < it.r1) ? P.recs[ri].row : INT_MAX;
-    bool lane_corner = false;
-    if (edge) lane_corner = (c0 < dn) || (c0 + 3 >= dn + nx);
 
+    int slot = 0;
     for (int jl = 0; jl < dn; ++jl) {
         const int y = yb0 + jl;
-        if (y + R <= nyt - 1) q[2 * R] = ldg4(PC + (size_t)(y + R) * pitch + xl);
+        cp_wait<BOT_DEPTH - 1>();
+        const float4* st = ring + slot * SB_SIZE;
+        if (y + R <= nyt - 1) q[2 * R] = st[SB_P + lane];
         const size_t ro = (size_t)y * pitch + xl;
         float pm1[4], cc[4], pc[4];
-        to_arr(ld4(P1 + ro), pm1);
-        to_arr(ldg4(S.c2 + ro), cc);
+        to_arr(st[SB_P1 + lane], pm1);
+        to_arr(st[SB_C2 + lane], cc);
         to_arr(q[R], pc);
         float d2y[4], dy[4];
         if (y <= nyt - 1 - R) {
@@ -513,9 +564,8 @@ __global__ void __launch_bounds__(128) k_step_bottom(const __grid_constant__ Ste
 #pragma unroll
             for (int e = 0; e < 4; ++e) { d2y[e] = d2yBot[e]; dy[e] = dyBot[e]; }
         }
-        float4 hl = make_float4(0.f, 0.f, 0.f, 0.f), hr = hl;
-        if (lane == 0 && x0 > 0) hl = ldg4(PC + (size_t)y * pitch + x0 - 4);
-        if (lane == 31 && x0 + TILE < pitch) hr = ldg4(PC + (size_t)y * pitch + x0 + TILE);
+        const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
+        const float4 hl = has_hl ? st[SB_HL] : z4, hr = has_hr ? st[SB_HR] : z4;
         float w[12];
         window(q[R], hl, hr, lane, w);
         float d2x[4], dx[4];
@@ -539,16 +589,17 @@ __global__ void __launch_bounds__(128) k_step_bottom(const __grid_constant__ Ste
         }
 
         float phy[4], chy[4];
-        to_arr(ld4(S.phy + ro), phy);
-        to_arr(ld4(S.chy + ro), chy);
+        to_arr(st[SB_PY + lane], phy);
+        to_arr(st[SB_CY + lane], chy);
         float phx[4] = {0.f, 0.f, 0.f, 0.f}, chx[4] = {0.f, 0.f, 0.f, 0.f}, dphx[4] = {0.f, 0.f, 0.f, 0.f};
         if (edge) {
             if (lane_corner) {
-                to_arr(ld4(S.phx + ro), phx);
-                to_arr(ld4(S.chx + ro), chx);
+                to_arr(st[SB_PX + lane], phx);
+                to_arr(st[SB_CX + lane], chx);
             }
             phi_xderiv<R>(S, P, from_arr(phx), lane, x0, c0, first, last, dphx);
         }
+        const float4 fnext = st[SB_FA + lane];
 
         float p3[4];
 #pragma unroll
@@ -596,22 +647,160 @@ __global__ void __launch_bounds__(128) k_step_bottom(const __grid_constant__ Ste
         if (jl >= R && jl + 1 + R <= dn - 1) {
 #pragma unroll
             for (int i = 0; i < 2 * R; ++i) f[i] = f[i + 1];
-            f[2 * R] = ld4(S.phy + (size_t)(yb0 + jl + 1 + R) * pitch + xl);
+            f[2 * R] = fnext;
         }
+        if (jl + BOT_DEPTH < dn) issue(jl + BOT_DEPTH, slot);
+        cp_commit();
+        slot = (slot + 1 == BOT_DEPTH) ? 0 : slot + 1;
     }
+    cp_wait<0>();
 }
 
-// Host-side launchers -------------------------------------------------------
+// Model rows of the middle tiles: interior cells only (no CPML, no clamp),
+// so only second derivatives are needed.  This is the kernel that moves
+// almost all of the bytes.
+constexpr int IN_P = 0, IN_P1 = 32, IN_C2 = 64, IN_HL = 96, IN_HR = 97, IN_SIZE = 98;
+constexpr int IN_DEPTH = 6;
+constexpr int IN_SMEM = 4 * IN_DEPTH * IN_SIZE * 16;
 
-// Model-row kernel on stream sm and bottom-row kernel on stream sb (the
-// caller orders the two streams around each time step).
+template <int R, int MODE>
+__global__ void __launch_bounds__(128, 5) k_step_interior(const __grid_constant__ StepParams P) {
+    extern __shared__ float4 smem[];
+    const int lane = threadIdx.x & 31;
+    const int wid = blockIdx.x * 4 + (threadIdx.x >> 5);
+    if (wid >= P.nitems) return;
+    float4* ring = smem + (threadIdx.x >> 5) * (IN_DEPTH * IN_SIZE);
+    const WorkItem it = P.items[wid];
+    const ShotDev& S = P.shots[it.shot];
+    const int pitch = S.pitch;
+    const int x0 = it.tile * TILE, xl = x0 + 4 * lane;
+    const float* PC = (P.parity ? S.pa : S.pb) + xl;  // p at this lane's columns
+    float* P1 = (P.parity ? S.pb : S.pa) + xl;        // p_1, overwritten with p_3
+    const float* C2 = S.c2 + xl;
+    // every middle tile has both neighbours; lanes 0 and 31 fetch the halos
+    const int hoff = (lane == 0) ? -4 - 4 * lane : TILE - 4 * lane;
+    const bool has_h = (lane == 0) || (lane == 31);
+    float4* hslot = ring + (lane == 0 ? IN_HL : IN_HR);
+
+    auto issue = [&](int y, int slot) {
+        float4* st = ring + slot * IN_SIZE;
+        const size_t ro = (size_t)y * pitch;
+        cp16(st + IN_P + lane, PC + ro + (size_t)R * pitch);
+        cp16(st + IN_P1 + lane, P1 + ro);
+        cp16(st + IN_C2 + lane, C2 + ro);
+        if (has_h) cp16(hslot + slot * IN_SIZE, PC + ro + hoff);
+    };
+#pragma unroll
+    for (int i = 0; i < IN_DEPTH; ++i) {
+        if (it.y0 + i < it.y1) issue(it.y0 + i, i);
+        cp_commit();
+    }
+    float4 q[2 * R + 1];
+#pragma unroll
+    for (int i = 0; i < 2 * R; ++i) q[i] = ldg4(PC + (size_t)(it.y0 - R + i) * pitch);
+
+    int si = it.s0, ri = it.r0;
+    int srow = (si < it.s1) ? P.srcs[si].row : INT_MAX;
+    int rrow = (ri < it.r1) ? P.recs[ri].row : INT_MAX;
+    const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
+
+    int slot = 0;
+    // unrolled by the queue length so that the queue shift becomes register renaming
+#pragma unroll(2 * R + 1)
+    for (int y = it.y0; y < it.y1; ++y) {
+        cp_wait<IN_DEPTH - 1>();
+        const float4* st = ring + slot * IN_SIZE;
+        q[2 * R] = st[IN_P + lane];
+        float pm1[4], cc[4], pc[4];
+        to_arr(st[IN_P1 + lane], pm1);
+        to_arr(st[IN_C2 + lane], cc);
+        to_arr(q[R], pc);
+        const float4 h = has_h ? st[lane == 0 ? IN_HL : IN_HR] : z4;
+        float w[12];
+        window(q[R], h, h, lane, w);
+        float d2x[4], d2y[4];
+        xderiv2<R>(w, P, d2x);
+        yderiv2<R>(q, P, d2y);
+
+        // source injection: source(nys,nxs) = S(k-1,j)  (solver_acoustic_SS.f90:319-330)
+        float sv[4] = {0.f, 0.f, 0.f, 0.f};
+        while (srow == y) {
+            const SrcEnt s = P.srcs[si];
+            if ((s.col >> 2) == (xl >> 2)) {
+                const float val = __ldg(S.srcv + (size_t)s.vidx * S.nt + P.t);
+                const int el = s.col & 3;
+                sv[0] = el == 0 ? val : sv[0];
+                sv[1] = el == 1 ? val : sv[1];
+                sv[2] = el == 2 ? val : sv[2];
+                sv[3] = el == 3 ? val : sv[3];
+            }
+            ++si;
+            srow = (si < it.s1) ? P.srcs[si].row : INT_MAX;
+        }
+        // p_3 = -p_1 + 2p + (d2x + d2y + source)*c2  (:433-434)
+        float p3[4];
+#pragma unroll
+        for (int e = 0; e < 4; ++e) p3[e] = ((-pm1[e]) + 2.f * pc[e]) + (((d2x[e] + d2y[e]) + sv[e]) * cc[e]);
+
+        const int c0 = xl - S.off;
+        if (MODE == 0 && P.snap >= 0) store_snapshot(P, S, y - S.dn, lane, x0, xl, c0, p3, pm1, it.tile);
+        if (MODE == 1 && P.snap >= 0) image_row(P, S, y - S.dn, xl, c0, p3, pm1, it.tile);
+        st4(P1 + (size_t)y * pitch, from_arr(p3));
+        if (MODE == 0 && P.record) record_row(P, S, y, xl, ri, it.r1, rrow, p3);
+
+#pragma unroll
+        for (int i = 0; i < 2 * R; ++i) q[i] = q[i + 1];
+        if (y + IN_DEPTH < it.y1) issue(y + IN_DEPTH, slot);
+        cp_commit();
+        slot = (slot + 1 == IN_DEPTH) ? 0 : slot + 1;
+    }
+    cp_wait<0>();
+}
+
+// Everything next to a boundary: model rows of the first/last tile (kind 0)
+// and the bottom pad rows of every tile (kind 1).  Runs on a second stream,
+// concurrently with k_step_interior.
+constexpr int BND_WARP_F4 = (MAIN_DEPTH * ST_SIZE > BOT_DEPTH * SB_SIZE) ? MAIN_DEPTH * ST_SIZE : BOT_DEPTH * SB_SIZE;
+constexpr int BND_SMEM = 4 * BND_WARP_F4 * 16;
+
+template <int R, int MODE>
+__global__ void __launch_bounds__(128) k_step_boundary(const __grid_constant__ StepParams P) {
+    extern __shared__ float4 smem[];
+    const int lane = threadIdx.x & 31;
+    const int wid = blockIdx.x * 4 + (threadIdx.x >> 5);
+    if (wid >= P.nitems) return;
+    float4* ring = smem + (threadIdx.x >> 5) * BND_WARP_F4;
+    const WorkItem it = P.items[wid];
+    if (it.kind == 0) edge_rows<R, MODE>(P, it, ring, lane);
+    else bottom_rows<R, MODE>(P, it, ring, lane);
+}
+
+// Opt the step kernels into the dynamic shared memory they use (the
+// boundary kernel's prefetch rings are above the 48 KB default).
+cudaError_t configure_step_kernels() {
+    cudaError_t e = cudaSuccess;
+#define FWI_CFG(R_, M_)                                                                                           \
+    if (e == cudaSuccess)                                                                                         \
+        e = cudaFuncSetAttribute(k_step_interior<R_, M_>, cudaFuncAttributeMaxDynamicSharedMemorySize, IN_SMEM);   \
+    if (e == cudaSuccess)                                                                                         \
+        e = cudaFuncSetAttribute(k_step_boundary<R_, M_>, cudaFuncAttributeMaxDynamicSharedMemorySize, BND_SMEM);
+    FWI_CFG(3, 0)
+    FWI_CFG(3, 1)
+    FWI_CFG(4, 0)
+    FWI_CFG(4, 1)
+#undef FWI_CFG
+    return e;
+}
+
+// Interior kernel on stream sm and boundary kernel on stream sb (the caller
+// orders the two streams around each time step).
 cudaError_t launch_step(int acc, int mode, const StepParams& pm, const StepParams& pb, cudaStream_t sm,
                         cudaStream_t sb) {
     const int bm = (pm.nitems + 3) / 4, bb = (pb.nitems + 3) / 4;
-#define FWI_LAUNCH(R_, M_)                                                            \
-    do {                                                                             \
-        if (bm) k_step_main<R_, M_><<<bm, 128, MAIN_SMEM, sm>>>(pm);                  \
-        if (bb) k_step_bottom<R_, M_><<<bb, 128, 0, sb>>>(pb);                        \
+#define FWI_LAUNCH(R_, M_)                                                          \
+    do {                                                                           \
+        if (bb) k_step_boundary<R_, M_><<<bb, 128, BND_SMEM, sb>>>(pb);             \
+        if (bm) k_step_interior<R_, M_><<<bm, 128, IN_SMEM, sm>>>(pm);              \
     } while (0)
     if (acc == 3) {
         if (mode == 0) FWI_LAUNCH(3, 0);

@@ -279,7 +279,7 @@ def main():
     wave, band = sv.tuning()
     roof = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
             "traffic": tr * len(spec.shots) if tr else None,
-            "kernel": "k_step_main + k_step_bottom (one time step of all shots)",
+            "kernel": "k_step_interior + k_step_boundary (one time step of all shots, concurrent streams)",
             "algorithmic_bytes_per_launch": bytes_step, "avg_launch_ms": step_s * 1e3,
             "peak_kind": f"{peak_kind} copy bandwidth (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured"
             else "fallback 6.8 TB/s"}
@@ -363,7 +363,7 @@ def main():
     cpu = None
     if rank == 0 and world == 1 and not a.no_cpu:
         nthreads = os.cpu_count() or 1
-        rate, tcpu, desc = cpu_sample(spec, vp0, nthreads, 200)
+        rate, tcpu, desc = cpu_sample(spec, vp0, nthreads, 600)
         cpu = {"value": rate, "unit": METRIC, "cores": nthreads, "kind": "port", "sample": desc,
                "seconds": tcpu}
 

@@ -1,0 +1,104 @@
+!! fwi_gpu_iface.f90 -- iso_c_binding interface to libfwi_gb300.so
+!!
+!! The reference driver keeps its call signatures; each routine on the hot
+!! path gains a GPU twin with the same arguments.  Fortran passes everything
+!! by reference, which is exactly the C ABI of include/fwi_gb300.h, so the
+!! dummies below carry no VALUE attribute except where the C side takes a
+!! scalar by value.  Default INTEGER and REAL must be 4 bytes (c_int,
+!! c_float), as in the reference build (mpif90 -O3, no -fdefault-real-8).
+module fwi_gpu_iface
+  use iso_c_binding
+  implicit none
+
+  integer(c_int), parameter :: FWI_OK = 0
+
+  type, bind(C) :: fwi_shot
+     integer(c_int) :: x0, nx, num_sou, num_rec
+     type(c_ptr)    :: nxSou, nySou, nxRec, nyRec
+     type(c_ptr)    :: src, obs
+     real(c_double) :: grad_weight, misfit_weight
+  end type fwi_shot
+
+  type, bind(C) :: fwi_survey_desc
+     integer(c_int)    :: ny, nx_model
+     real(c_float)     :: d, dt
+     integer(c_int)    :: nt, store_snap, acc, dpml, numtasks
+     integer(c_int)    :: snap_form, grad_form, nshots
+     type(c_ptr)       :: shots, water_rows
+     integer(c_size_t) :: hbm_budget
+     integer(c_int)    :: wave_shots, band_rows, flags
+  end type fwi_survey_desc
+
+  interface
+     integer(c_int) function fwi_init(device) bind(C, name="fwi_init")
+       import :: c_int
+       integer(c_int), value :: device
+     end function fwi_init
+
+     integer(c_int) function fwi_set_solver_options(acc, dpml) bind(C, name="fwi_set_solver_options")
+       import :: c_int
+       integer(c_int), value :: acc, dpml
+     end function fwi_set_solver_options
+
+     !! solver_acoustic_SS (src/solver_acoustic_SS.f90:9-11), same 21 arguments
+     integer(c_int) function fwi_solver_acoustic_ss(rank, iprop, NumSou, NumRec, nxSou, nySou, &
+          nxRec, nyRec, S, Sadj, d, dt, ny, nx, ctmp, store_snap, nt_Store, nt, kernel, Fields, &
+          Rec_point) bind(C, name="fwi_solver_acoustic_ss")
+       import :: c_int, c_float
+       integer(c_int) :: rank, iprop, NumSou, NumRec, ny, nx, store_snap, nt_Store, nt
+       integer(c_int) :: nxSou(*), nySou(*), nxRec(*), nyRec(*)
+       real(c_float)  :: S(*), Sadj(*), d, dt, ctmp(*), kernel(*), Fields(*), Rec_point(*)
+     end function fwi_solver_acoustic_ss
+
+     !! Misfit_function (src/Misfit.f90:1), misfit_type = 1
+     integer(c_int) function fwi_misfit_function(rank, freq, Data_Synth, Data_trace, NumRec, nt, dt, &
+          Misfit, AdjSource, misfit64) bind(C, name="fwi_misfit_function")
+       import :: c_int, c_float, c_double
+       integer(c_int) :: rank, NumRec, nt
+       real(c_float)  :: freq, dt, Misfit
+       real(c_float)  :: Data_Synth(*), Data_trace(*), AdjSource(*)
+       real(c_double) :: misfit64
+     end function fwi_misfit_function
+
+     !! Beta_calculous (src/Beta_calculous.f90:1)
+     integer(c_int) function fwi_beta_calculous(Grad, OldGrad, nx, ny, Beta, num64, den64) &
+          bind(C, name="fwi_beta_calculous")
+       import :: c_int, c_float, c_double
+       real(c_float)  :: Grad(*), OldGrad(*), Beta
+       integer(c_int) :: nx, ny
+       real(c_double) :: num64, den64
+     end function fwi_beta_calculous
+
+     !! calculate_misfit_gradient (src/calculate_misfit_gradient.f90:1) for all shots at once
+     integer(c_int) function fwi_misfit_gradient_batch(desc, lambda, step, Misfit, Grad) &
+          bind(C, name="fwi_misfit_gradient_batch")
+       import :: c_int, c_float, fwi_survey_desc
+       type(fwi_survey_desc) :: desc
+       real(c_float)         :: lambda(*), Misfit, Grad(*)
+       integer(c_int), value :: step
+     end function fwi_misfit_gradient_batch
+
+     type(c_ptr) function fwi_last_error() bind(C, name="fwi_last_error")
+       import :: c_ptr
+     end function fwi_last_error
+  end interface
+
+contains
+
+  !! Stop like the reference does on an error, with the library's message.
+  subroutine fwi_check(rc)
+    integer(c_int), intent(in) :: rc
+    character(kind=c_char), pointer :: msg(:)
+    integer :: n
+    if (rc == FWI_OK) return
+    call c_f_pointer(fwi_last_error(), msg, [512])
+    n = 0
+    do while (n < 512)
+       if (msg(n + 1) == c_null_char) exit
+       n = n + 1
+    end do
+    write(*,*) 'fwi_gb300 error ', rc, ': ', msg(1:n)
+    stop
+  end subroutine fwi_check
+
+end module fwi_gpu_iface

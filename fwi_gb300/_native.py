@@ -28,7 +28,7 @@ EXPORTS = [
     "fwi_mcs_geometry", "fwi_ricker", "fwi_time_rules", "fwi_survey_create", "fwi_survey_destroy",
     "fwi_survey_set_lambda", "fwi_survey_set_observed", "fwi_survey_set_sources", "fwi_survey_run",
     "fwi_survey_grad_device", "fwi_survey_get_synthetic", "fwi_survey_step_bytes", "fwi_survey_tuning",
-    "fwi_survey_time_steps", "fwi_misfit_gradient_batch",
+    "fwi_survey_time_steps", "fwi_misfit_gradient_batch", "fwi_solver_forward_noalloc",
 ]
 
 
@@ -89,6 +89,7 @@ def load():
     lib.fwi_survey_tuning.argtypes = [P, IP, IP]
     lib.fwi_survey_time_steps.argtypes = [P, I]
     lib.fwi_misfit_gradient_batch.argtypes = [C.POINTER(FwiSurveyDesc), P, I, P, P]
+    lib.fwi_solver_forward_noalloc.argtypes = [I, I, P, P, P, P, P, F, F, I, I, P, I, P]
     for name in EXPORTS:
         fn = getattr(lib, name)
         if fn.restype is None and name not in ("fwi_last_error", "fwi_kernel_launch_count"):

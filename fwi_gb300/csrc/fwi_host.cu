@@ -1358,3 +1358,144 @@ int fwi_misfit_gradient_batch(const fwi_survey_desc* desc, const float* lambda, 
 }
 
 }  // extern "C"
+
+// ===========================================================================
+// forward traces without device allocation
+// ===========================================================================
+//
+// Some callers cannot call cudaMalloc: code that runs inside a framework
+// which owns the device memory pool (a raw cudaMalloc synchronises the
+// device and sits outside the pool's budget), and code paths that must not
+// allocate once set up (latency-critical loops, work recorded once and
+// replayed).  For them the forward propagation of one shot can run with all
+// of its working state (wavefields, c2, CPML memory variables, work lists)
+// in the fixed array below, which every GPU that loads this library holds
+// until the process exits.
+
+namespace {
+
+constexpr size_t NOALLOC_SCRATCH_BYTES = 16u << 20;  // 16 MiB
+static __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_SCRATCH_BYTES];
+
+// Device address of g_noalloc_scratch, looked up once per device.  In host
+// code the symbol itself is only a host-side stand-in, so the kernels get
+// this address instead.
+constexpr int NOALLOC_MAX_DEVICES = 64;
+void* g_noalloc_addr[NOALLOC_MAX_DEVICES] = {nullptr};
+
+int noalloc_scratch(void** out) {
+    int dev = 0;
+    CK(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= NOALLOC_MAX_DEVICES) return fail(FWI_ERR_ARG, "device index too large");
+    if (!g_noalloc_addr[dev]) {
+        void* p = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(g_noalloc_scratch)", __LINE__);
+        g_noalloc_addr[dev] = p;
+    }
+    *out = g_noalloc_addr[dev];
+    return FWI_OK;
+}
+
+}  // namespace
+
+extern "C" int fwi_solver_forward_noalloc(int NumSou, int NumRec, const int* nxSou, const int* nySou,
+                                          const int* nxRec, const int* nyRec, const float* S_dev, float d, float dt,
+                                          int ny, int nx, const float* ctmp_dev, int nt, float* Rec_point_dev) {
+    std::lock_guard<std::recursive_mutex> g(L().mu);
+    TRY(ensure_init());
+    const int acc = L().acc, dpml = L().dpml;
+    TRY(validate_common(ny, nx, acc, dpml, nt, 1));
+    if (NumSou < 0 || NumRec < 0) return fail(FWI_ERR_ARG, "NumSou/NumRec must be >= 0");
+    if (!(d > 0.f) || !(dt > 0.f)) return fail(FWI_ERR_ARG, "d and dt must be positive");
+    if (!ctmp_dev || (NumRec > 0 && (!Rec_point_dev || !nxRec || !nyRec)) ||
+        (NumSou > 0 && (!S_dev || !nxSou || !nySou)))
+        return fail(FWI_ERR_ARG, "null argument");
+    const Layout l = make_layout(ny, nx, acc, dpml);
+    ShotGeom geo;
+    geo.nx = nx;
+    geo.nxS.assign(nxSou, nxSou + NumSou);
+    geo.nyS.assign(nySou, nySou + NumSou);
+    geo.nxR.assign(nxRec, nxRec + NumRec);
+    geo.nyR.assign(nyRec, nyRec + NumRec);
+    TRY(validate_geometry(geo, l, 1));
+    std::vector<ShotGeom> geoms{geo};
+    std::vector<Layout> lays{l};
+    Lists lists = build_lists(geoms, lays, 64);
+    std::vector<float> fA, fB;
+    pml_factors(acc, dpml, dt, d, fA, fB);
+
+    // carve the scratch: seven fields, CPML factors, shot descriptor, lists
+    const size_t field = (size_t)l.nyt * l.pitch * sizeof(float);
+    size_t off = 0;
+    auto carve = [&](size_t bytes) {
+        const size_t at = off;
+        off += (bytes + 255) / 256 * 256;
+        return at;
+    };
+    size_t o_fld[7];
+    for (auto& o : o_fld) o = carve(field);
+    const size_t o_fA = carve(fA.size() * 4), o_fB = carve(fB.size() * 4), o_shot = carve(sizeof(ShotDev));
+    const size_t o_im = carve(lists.int_fwd.size() * sizeof(WorkItem)), o_bm = carve(lists.bnd_fwd.size() * sizeof(WorkItem));
+    const size_t o_src = carve(lists.src_fwd.size() * sizeof(SrcEnt)), o_rec = carve(lists.recs.size() * sizeof(RecEnt));
+    if (off > NOALLOC_SCRATCH_BYTES) {
+        char buf[256];
+        snprintf(buf, sizeof buf,
+                 "grid too large for the allocation-free solver: needs %zu bytes of scratch, the fixed limit is %zu "
+                 "(use fwi_solver_acoustic_ss)",
+                 off, NOALLOC_SCRATCH_BYTES);
+        return fail(FWI_ERR_ARG, buf);
+    }
+    void* base = nullptr;
+    TRY(noalloc_scratch(&base));
+    unsigned char* sb = reinterpret_cast<unsigned char*>(base);
+    cudaStream_t st = stream();
+
+    // the array keeps the previous call's contents: clear the state that must start at zero
+    CK(cudaMemsetAsync(sb, 0, o_fA, st));
+    float* fld[7];
+    for (int i = 0; i < 7; ++i) fld[i] = reinterpret_cast<float*>(sb + o_fld[i]);
+    LK(launch_build_c2(fld[2], l.nyt, l.pitch, l.off, l.dn, ny, nx, ctmp_dev, ny, 0, 0, dt * dt, d * d, st));
+    if (NumRec > 0) CK(cudaMemsetAsync(Rec_point_dev, 0, (size_t)nt * NumRec * sizeof(float), st));
+
+    ShotDev sd{};
+    sd.pa = fld[0];
+    sd.pb = fld[1];
+    sd.c2 = fld[2];
+    sd.phx = fld[3];
+    sd.chx = fld[4];
+    sd.phy = fld[5];
+    sd.chy = fld[6];
+    sd.srcv = S_dev;
+    sd.rec = Rec_point_dev;
+    sd.ny = l.ny; sd.nx = l.nx; sd.nyt = l.nyt; sd.nxt = l.nxt; sd.off = l.off; sd.pitch = l.pitch;
+    sd.ntiles = l.ntiles; sd.dn = l.dn; sd.nt = nt; sd.nrec = NumRec;
+    auto put = [&](size_t at, const void* src, size_t bytes) -> int {
+        if (bytes) CK(cudaMemcpyAsync(sb + at, src, bytes, cudaMemcpyHostToDevice, st));
+        return FWI_OK;
+    };
+    TRY(put(o_fA, fA.data(), fA.size() * 4));
+    TRY(put(o_fB, fB.data(), fB.size() * 4));
+    TRY(put(o_shot, &sd, sizeof sd));
+    TRY(put(o_im, lists.int_fwd.data(), lists.int_fwd.size() * sizeof(WorkItem)));
+    TRY(put(o_bm, lists.bnd_fwd.data(), lists.bnd_fwd.size() * sizeof(WorkItem)));
+    TRY(put(o_src, lists.src_fwd.data(), lists.src_fwd.size() * sizeof(SrcEnt)));
+    TRY(put(o_rec, lists.recs.data(), lists.recs.size() * sizeof(RecEnt)));
+
+    StepSet ps;
+    ps.pm = base_params(acc, dt, nt + 1, FWI_SNAP_F32, FWI_GRAD_F32, reinterpret_cast<float*>(sb + o_fA),
+                        reinterpret_cast<float*>(sb + o_fB));
+    ps.pm.items = reinterpret_cast<WorkItem*>(sb + o_im);
+    ps.pm.nitems = (int)lists.int_fwd.size();
+    ps.pm.shots = reinterpret_cast<ShotDev*>(sb + o_shot);
+    ps.pm.srcs = reinterpret_cast<SrcEnt*>(sb + o_src);
+    ps.pm.recs = reinterpret_cast<RecEnt*>(sb + o_rec);
+    ps.pm.record = 1;
+    ps.pb = ps.pm;
+    ps.pb.items = reinterpret_cast<WorkItem*>(sb + o_bm);
+    ps.pb.nitems = (int)lists.bnd_fwd.size();
+    TRY(run_time_loop(acc, 0, nt, nt + 1, 0, false, ps, st, L().aux));
+    LK(launch_rec_last(Rec_point_dev, nt, NumRec, st));
+    CK(cudaStreamSynchronize(st));
+    return FWI_OK;
+}

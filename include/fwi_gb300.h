@@ -195,6 +195,34 @@ int fwi_survey_time_steps(fwi_survey* s, int steps);
 int fwi_misfit_gradient_batch(const fwi_survey_desc* desc, const float* lambda, int step,
                               float* Misfit, float* Grad);
 
+/* ---- forward traces without device allocation --------------------------- */
+
+/* No counterpart in the reference: an addition for callers that cannot call
+ * cudaMalloc -- code inside a framework that owns the device memory pool (a
+ * raw cudaMalloc synchronises the device and falls outside the pool's
+ * budget) and code paths that must not allocate once they are set up.
+ *
+ * Forward propagation of one shot (the reference's solver_acoustic_SS with
+ * iprop = 3: traces only, no snapshots) with the order and CPML width of
+ * fwi_set_solver_options.  The caller passes its own DEVICE buffers for
+ * S(nt,NumSou), ctmp(ny,nx) and the output Rec_point(nt,NumRec); the grid
+ * indices are host arrays.  All working state (wavefields, c2, CPML memory
+ * variables, work lists) lives in one fixed 16 MiB device array that every
+ * GPU loading this library holds until the process exits; grids whose state
+ * does not fit (about 7*(ny+2*dn)*(nx+2*dn+128)*4 bytes, dn = dpml+2*acc)
+ * are rejected with FWI_ERR_ARG.  Nothing is allocated: no cudaMalloc,
+ * cudaFree or allocating library call.
+ *
+ * The first call on a device looks up the array's device address (and, if
+ * the library was not initialised, creates its streams); make that first
+ * call before any stream capture.  Every call shares the one array, which
+ * keeps the last call's contents (the call clears what must start at zero):
+ * calls that overlap on the GPU -- from several host threads or streams --
+ * race and must not be issued. */
+int fwi_solver_forward_noalloc(int NumSou, int NumRec, const int* nxSou, const int* nySou,
+                               const int* nxRec, const int* nyRec, const float* S_dev, float d, float dt,
+                               int ny, int nx, const float* ctmp_dev, int nt, float* Rec_point_dev);
+
 #ifdef __cplusplus
 }
 #endif

@@ -306,6 +306,8 @@ void append_item(Lists& L_, std::vector<WorkItem>& items, std::vector<SrcEnt>& s
     items.push_back(it);
 }
 
+constexpr int BOTTOM_BAND = 9;  // rows per bottom-pad work item
+
 // Work lists for a set of shots (local shot index = position in `geoms`).
 Lists build_lists(const std::vector<ShotGeom>& geoms, const std::vector<Layout>& lays, int band_rows) {
     Lists out;
@@ -339,10 +341,16 @@ Lists build_lists(const std::vector<ShotGeom>& geoms, const std::vector<Layout>&
                 }
             }
         }
+        // bottom pad in bands of about BOTTOM_BAND rows (the y-phi is ping-ponged,
+        // so bands are independent)
         std::vector<SrcEnt> none;
-        for (int t = 0; t < l.ntiles; ++t) {
-            append_item(out, out.bnd_fwd, out.src_fwd, none, recs, (int)s, t, l.nyt - l.dn, l.nyt, 1, true);
-            append_item(out, out.bnd_adj, out.src_adj, none, recs, (int)s, t, l.nyt - l.dn, l.nyt, 1, false);
+        const int nbb = std::max(1, (l.dn + BOTTOM_BAND - 1) / BOTTOM_BAND);
+        for (int b = 0; b < nbb; ++b) {
+            const int y0 = l.nyt - l.dn + l.dn * b / nbb, y1 = l.nyt - l.dn + l.dn * (b + 1) / nbb;
+            for (int t = 0; t < l.ntiles; ++t) {
+                append_item(out, out.bnd_fwd, out.src_fwd, none, recs, (int)s, t, y0, y1, 1, true);
+                append_item(out, out.bnd_adj, out.src_adj, none, recs, (int)s, t, y0, y1, 1, false);
+            }
         }
     }
     return out;
@@ -375,7 +383,7 @@ double step_bytes_shot(int ny, int nx, int dn) {
 // ---------------------------------------------------------------------------
 
 struct ShotState {
-    DBuf pa, pb, c2, phx, chx, phy, chy, snaps, sscale, k;
+    DBuf pa, pb, c2, phx, chx, phy, phy2, chy, snaps, sscale, k;
     Layout lay{};
     size_t field_bytes = 0, snap_bytes = 0;
     int alloc(const Layout& l, int nsnap_blocks, int snap_form, int grad_form) {
@@ -389,6 +397,7 @@ struct ShotState {
         TRY(phx.ensure(field_bytes));
         TRY(chx.ensure(field_bytes));
         TRY(phy.ensure(field_bytes));
+        TRY(phy2.ensure(field_bytes));
         TRY(chy.ensure(field_bytes));
         TRY(snaps.ensure(snap_bytes));
         TRY(sscale.ensure((size_t)nsnap_blocks * l.ny * l.ntiles * sizeof(float)));
@@ -401,6 +410,7 @@ struct ShotState {
         CK(cudaMemsetAsync(phx.p, 0, field_bytes, st));
         CK(cudaMemsetAsync(chx.p, 0, field_bytes, st));
         CK(cudaMemsetAsync(phy.p, 0, field_bytes, st));
+        CK(cudaMemsetAsync(phy2.p, 0, field_bytes, st));
         CK(cudaMemsetAsync(chy.p, 0, field_bytes, st));
         return FWI_OK;
     }
@@ -412,6 +422,7 @@ struct ShotState {
         d.phx = phx.as<float>();
         d.chx = chx.as<float>();
         d.phy = phy.as<float>();
+        d.phy2 = phy2.as<float>();
         d.chy = chy.as<float>();
         d.srcv = srcv;
         d.rec = rec;
@@ -875,21 +886,52 @@ size_t shot_wave_bytes(const Layout& l, int nt_store, int snap_form, int grad_fo
     const size_t esz = snap_form == FWI_SNAP_F32 ? 4 : 2;
     const size_t sb = (size_t)(nt_store + 1) * l.ny * l.pitch * esz + (size_t)(nt_store + 1) * l.ny * l.ntiles * 4;
     const size_t kb = (size_t)l.ny * l.pitch * (grad_form == FWI_GRAD_F64 ? 8 : 4);
-    return 7 * fb + sb + kb;
+    return 8 * fb + sb + kb;
 }
 
+// Shot packing: shots sorted by window width (widest first, stable) and cut
+// into waves of s->wave shots, so that every wave holds shots of similar
+// size and the slots (sized by the widest shot that uses them) waste little.
+// Slot buffers are allocated here, once.
+int survey_prepare_slots(fwi_survey* s) {
+    const auto& D = s->desc;
+    std::vector<int> order(D.nshots);
+    for (int i = 0; i < D.nshots; ++i) order[i] = i;
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return s->geoms[a].nx > s->geoms[b].nx; });
+    s->waves.clear();
+    for (int i = 0; i < D.nshots; i += s->wave) {
+        std::vector<int> w(order.begin() + i, order.begin() + std::min(D.nshots, i + s->wave));
+        s->waves.push_back(w);
+    }
+    s->slots.clear();
+    for (int k = 0; k < s->wave; ++k) s->slots.emplace_back(new ShotState());
+    for (int k = 0; k < s->wave; ++k) {
+        Layout big = s->lays[s->waves[0][0]];
+        size_t best = 0;
+        for (size_t wi = 0; wi < s->waves.size(); ++wi) {
+            if (k >= (int)s->waves[wi].size()) continue;
+            const Layout& l = s->lays[s->waves[wi][k]];
+            const size_t b = (size_t)l.nyt * l.pitch;
+            if (b >= best) {
+                best = b;
+                big = l;
+            }
+        }
+        TRY(s->slots[k]->alloc(big, s->nt_store + 1, D.snap_form, D.grad_form));
+    }
+    return FWI_OK;
+}
+
+// Work lists and shot descriptors of every wave for the band height s->band.
 int survey_prepare_waves(fwi_survey* s) {
     const auto& D = s->desc;
     cudaStream_t st = stream();
-    s->waves.clear();
-    for (int i = 0; i < D.nshots; i += s->wave) {
-        std::vector<int> w;
-        for (int j = i; j < std::min(D.nshots, i + s->wave); ++j) w.push_back(j);
-        s->waves.push_back(w);
-    }
-    // slots sized for the largest layout
-    s->slots.clear();
-    for (int k = 0; k < s->wave; ++k) s->slots.emplace_back(new ShotState());
+    for (auto& w : s->wdev)
+        for (auto& gexec : w->graph)
+            if (gexec) {
+                cudaGraphExecDestroy(gexec);
+                gexec = nullptr;
+            }
     s->wdev.clear();
     for (size_t wi = 0; wi < s->waves.size(); ++wi) {
         const auto& w = s->waves[wi];
@@ -913,21 +955,6 @@ int survey_prepare_waves(fwi_survey* s) {
         wd->n_bf = (int)lists.bnd_fwd.size();
         wd->n_ba = (int)lists.bnd_adj.size();
         s->wdev.push_back(std::move(wd));
-    }
-    // allocate slots for the largest shot that can land in each slot
-    for (int k = 0; k < s->wave; ++k) {
-        Layout big = s->lays[0];
-        size_t best = 0;
-        for (size_t wi = 0; wi < s->waves.size(); ++wi) {
-            if (k >= (int)s->waves[wi].size()) continue;
-            const Layout& l = s->lays[s->waves[wi][k]];
-            const size_t b = (size_t)l.nyt * l.pitch;
-            if (b >= best) {
-                best = b;
-                big = l;
-            }
-        }
-        TRY(s->slots[k]->alloc(big, s->nt_store + 1, D.snap_form, D.grad_form));
     }
     // per-wave shot descriptors (fwd: sources; adj: adjoint source table)
     for (size_t wi = 0; wi < s->waves.size(); ++wi) {
@@ -962,6 +989,44 @@ int survey_prepare_waves(fwi_survey* s) {
     return FWI_OK;
 }
 
+// Autotuner for the band height of the step kernels' work items: times a
+// few forward steps of the first wave for each candidate and keeps the
+// fastest.  Results are cached per (device, grid, order, CPML, wave shape).
+int time_wave0_steps(fwi_survey* s, int steps, float* ms);
+
+int tune_band(fwi_survey* s) {
+    static std::map<std::string, int> cache;
+    const auto& D = s->desc;
+    cudaDeviceProp prop;
+    CK(cudaGetDeviceProperties(&prop, L().device));
+    std::string key = std::string(prop.name) + "|" + std::to_string(D.ny) + "|" + std::to_string(D.acc) + "|" +
+                      std::to_string(D.dpml) + "|" + std::to_string(s->wave);
+    for (int sh : s->waves[0]) key += "|" + std::to_string(s->geoms[sh].nx);
+    auto it = cache.find(key);
+    if (it != cache.end()) {
+        s->band = it->second;
+        return FWI_OK;
+    }
+    const int cands[] = {16, 24, 32, 48, 64};
+    int best = 64;
+    float best_ms = 1e30f;
+    for (int c : cands) {
+        if (c > D.ny && c != cands[0]) break;
+        s->band = c;
+        TRY(survey_prepare_waves(s));
+        float ms = 0.f;
+        TRY(time_wave0_steps(s, 2, &ms));  // warm-up
+        TRY(time_wave0_steps(s, 6, &ms));
+        if (ms < best_ms) {
+            best_ms = ms;
+            best = c;
+        }
+    }
+    s->band = best;
+    cache[key] = best;
+    return FWI_OK;
+}
+
 // Issue one wave's work: forward (+ misfit) and, for step 1, adjoint + stack.
 int issue_wave(fwi_survey* s, size_t wi, int step, cudaStream_t st, cudaStream_t st2) {
     const auto& D = s->desc;
@@ -977,6 +1042,7 @@ int issue_wave(fwi_survey* s, size_t wi, int step, cudaStream_t st, cudaStream_t
         CK(cudaMemsetAsync(ss.phx.p, 0, ss.phx.n, st));
         CK(cudaMemsetAsync(ss.chx.p, 0, ss.chx.n, st));
         CK(cudaMemsetAsync(ss.phy.p, 0, ss.phy.n, st));
+        CK(cudaMemsetAsync(ss.phy2.p, 0, ss.phy2.n, st));
         CK(cudaMemsetAsync(ss.chy.p, 0, ss.chy.n, st));
         CK(cudaMemsetAsync(ss.c2.p, 0, ss.c2.n, st));
         // snapshot block 0 is never written by the forward but is the last
@@ -1021,6 +1087,7 @@ int issue_wave(fwi_survey* s, size_t wi, int step, cudaStream_t st, cudaStream_t
         CK(cudaMemsetAsync(ss.phx.p, 0, ss.phx.n, st));
         CK(cudaMemsetAsync(ss.chx.p, 0, ss.chx.n, st));
         CK(cudaMemsetAsync(ss.phy.p, 0, ss.phy.n, st));
+        CK(cudaMemsetAsync(ss.phy2.p, 0, ss.phy2.n, st));
         CK(cudaMemsetAsync(ss.chy.p, 0, ss.chy.n, st));
         CK(cudaMemsetAsync(ss.k.p, 0, ss.k.n, st));
     }
@@ -1141,7 +1208,9 @@ int fwi_survey_create(const fwi_survey_desc* desc, fwi_survey** out) {
     const int nw = (D.nshots + wave - 1) / wave;
     wave = (D.nshots + nw - 1) / nw;
     s->wave = wave;
-    s->band = D.band_rows > 0 ? D.band_rows : 64;
+    TRY(survey_prepare_slots(s.get()));
+    if (D.band_rows > 0) s->band = D.band_rows;
+    else TRY(tune_band(s.get()));
     TRY(survey_prepare_waves(s.get()));
     *out = s.release();
     return FWI_OK;
@@ -1284,6 +1353,13 @@ int fwi_survey_tuning(fwi_survey* s, int* wave_shots, int* band_rows) {
 int fwi_survey_time_steps(fwi_survey* s, int steps) {
     std::lock_guard<std::recursive_mutex> g(L().mu);
     if (!s) return fail(FWI_ERR_STATE, "null survey");
+    return time_wave0_steps(s, steps, nullptr);
+}
+
+}  // extern "C"
+
+namespace {
+int time_wave0_steps(fwi_survey* s, int steps, float* ms) {
     const auto& D = s->desc;
     auto& wd = *s->wdev[0];
     StepSet ps;
@@ -1297,14 +1373,30 @@ int fwi_survey_time_steps(fwi_survey* s, int steps) {
     ps.pb = ps.pm;
     ps.pb.items = wd.items_bf.as<WorkItem>();
     ps.pb.nitems = wd.n_bf;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if (ms) {
+        CK(cudaEventCreate(&e0));
+        CK(cudaEventCreate(&e1));
+        CK(cudaEventRecord(e0, stream()));
+    }
     for (int i = 0; i < steps; ++i) {
         const int k = 2 + (i % (D.nt - 1));
         ps.pm.t = ps.pb.t = k - 2;
         ps.pm.parity = ps.pb.parity = k & 1;
         TRY(step_fork_join(D.acc, 0, ps, stream(), L().aux));
     }
+    if (ms) {
+        CK(cudaEventRecord(e1, stream()));
+        CK(cudaEventSynchronize(e1));
+        CK(cudaEventElapsedTime(ms, e0, e1));
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+    }
     return FWI_OK;
 }
+}  // namespace
+
+extern "C" {
 
 int fwi_misfit_gradient_batch(const fwi_survey_desc* desc, const float* lambda, int step, float* Misfit, float* Grad) {
     std::lock_guard<std::recursive_mutex> g(L().mu);
@@ -1425,7 +1517,7 @@ extern "C" int fwi_solver_forward_noalloc(int NumSou, int NumRec, const int* nxS
     std::vector<float> fA, fB;
     pml_factors(acc, dpml, dt, d, fA, fB);
 
-    // carve the scratch: seven fields, CPML factors, shot descriptor, lists
+    // carve the scratch: eight fields, CPML factors, shot descriptor, lists
     const size_t field = (size_t)l.nyt * l.pitch * sizeof(float);
     size_t off = 0;
     auto carve = [&](size_t bytes) {
@@ -1433,7 +1525,7 @@ extern "C" int fwi_solver_forward_noalloc(int NumSou, int NumRec, const int* nxS
         off += (bytes + 255) / 256 * 256;
         return at;
     };
-    size_t o_fld[7];
+    size_t o_fld[8];
     for (auto& o : o_fld) o = carve(field);
     const size_t o_fA = carve(fA.size() * 4), o_fB = carve(fB.size() * 4), o_shot = carve(sizeof(ShotDev));
     const size_t o_im = carve(lists.int_fwd.size() * sizeof(WorkItem)), o_bm = carve(lists.bnd_fwd.size() * sizeof(WorkItem));
@@ -1453,8 +1545,8 @@ extern "C" int fwi_solver_forward_noalloc(int NumSou, int NumRec, const int* nxS
 
     // the array keeps the previous call's contents: clear the state that must start at zero
     CK(cudaMemsetAsync(sb, 0, o_fA, st));
-    float* fld[7];
-    for (int i = 0; i < 7; ++i) fld[i] = reinterpret_cast<float*>(sb + o_fld[i]);
+    float* fld[8];
+    for (int i = 0; i < 8; ++i) fld[i] = reinterpret_cast<float*>(sb + o_fld[i]);
     LK(launch_build_c2(fld[2], l.nyt, l.pitch, l.off, l.dn, ny, nx, ctmp_dev, ny, 0, 0, dt * dt, d * d, st));
     if (NumRec > 0) CK(cudaMemsetAsync(Rec_point_dev, 0, (size_t)nt * NumRec * sizeof(float), st));
 
@@ -1466,6 +1558,7 @@ extern "C" int fwi_solver_forward_noalloc(int NumSou, int NumRec, const int* nxS
     sd.chx = fld[4];
     sd.phy = fld[5];
     sd.chy = fld[6];
+    sd.phy2 = fld[7];
     sd.srcv = S_dev;
     sd.rec = Rec_point_dev;
     sd.ny = l.ny; sd.nx = l.nx; sd.nyt = l.nyt; sd.nxt = l.nxt; sd.off = l.off; sd.pitch = l.pitch;

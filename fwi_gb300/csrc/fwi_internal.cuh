@@ -44,7 +44,8 @@ struct ShotDev {
     const float* c2;            // c^2 dt^2 / d^2
     float* phx;                 // x-direction CPML phi (side strips and corners)
     float* chx;                 // x-direction chi
-    float* phy;                 // y-direction phi (bottom strip and corners)
+    float* phy;                 // y-direction phi (bottom strip and corners),
+    float* phy2;                // ping-ponged with phy by step parity
     float* chy;                 // y-direction chi
     const float* srcv;          // injected values [vidx][nt]
     float* rec;                 // Rec_point(nt, nrec) column-major

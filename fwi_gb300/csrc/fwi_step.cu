@@ -178,8 +178,13 @@ __device__ __forceinline__ void phi_xderiv(const ShotDev& S, const StepParams& P
                                            bool first, bool last, float* dph) {
     float w[12];
     window(ph, ph, ph, lane, w);
-    float d2u[4];
-    xderivs<R>(w, P, d2u, dph);
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+        float s1 = 0.f;
+#pragma unroll
+        for (int i = 0; i <= R; ++i) s1 = s1 + (w[4 + e + i] - w[4 + e - i]) * P.c1[i];
+        dph[e] = s1;
+    }
     const int dn = S.dn, nx = S.nx;
     if (first) {
         const float lo = fetch(dph, S.off + R - x0), hi = fetch(dph, S.off + dn - 1 - R - x0);
@@ -416,9 +421,9 @@ __device__ __forceinline__ void edge_rows(const StepParams& P, const WorkItem& i
         }
         float w[12];
         window(q[R], hl, hr, lane, w);
-        float d2x[4], dx[4], d2y[4], dy[4];
+        float d2x[4], dx[4], d2y[4];
         xderivs<R>(w, P, d2x, dx);
-        yderivs<R>(q, P, d2y, dy);
+        yderiv2<R>(q, P, d2y);
 
         // source injection: source(nys,nxs) = S(k-1,j), interior cells only
         float sv[4] = {0.f, 0.f, 0.f, 0.f};
@@ -493,7 +498,10 @@ constexpr int SB_P = 0, SB_P1 = 32, SB_C2 = 64, SB_PY = 96, SB_CY = 128, SB_PX =
 constexpr int BOT_DEPTH = 3;
 constexpr int BOT_SMEM = 4 * BOT_DEPTH * SB_SIZE * 16;
 
-// Bottom pad rows of one tile: bottom strip and bottom corners.
+// Bottom pad rows [it.y0, it.y1) of one tile: bottom strip and bottom
+// corners.  The y-direction phi is ping-ponged between two buffers (old read
+// from one, new written to the other), so the strip-local derivative of the
+// old phi can be taken in any band of the bottom pad.
 template <int R, int MODE>
 __device__ __forceinline__ void bottom_rows(const StepParams& P, const WorkItem& it, float4* ring, int lane) {
     const ShotDev& S = P.shots[it.shot];
@@ -502,7 +510,11 @@ __device__ __forceinline__ void bottom_rows(const StepParams& P, const WorkItem&
     const bool first = it.tile == 0, last = it.tile == S.ntiles - 1, edge = first || last;
     const float* PC = P.parity ? S.pa : S.pb;
     float* P1 = P.parity ? S.pb : S.pa;
+    const float* PHO = P.parity ? S.phy2 : S.phy;  // old y-phi
+    float* PHN = P.parity ? S.phy : S.phy2;        // new y-phi
     const int yb0 = nyt - dn;
+    const int j0 = it.y0 - yb0, j1 = it.y1 - yb0;
+    const int jA = max(j0, R), jB = min(j1 - 1, dn - 1 - R);  // rows with an unclamped phi derivative
     bool lane_corner = false;
     if (edge) lane_corner = (c0 < dn) || (c0 + 3 >= dn + nx);
     const bool has_hl = (lane == 0) && (x0 > 0), has_hr = (lane == 31) && (x0 + TILE < pitch);
@@ -514,36 +526,58 @@ __device__ __forceinline__ void bottom_rows(const StepParams& P, const WorkItem&
         if (y + R <= nyt - 1) cp16(st + SB_P + lane, PC + (size_t)(y + R) * pitch + xl);
         cp16(st + SB_P1 + lane, P1 + ro);
         cp16(st + SB_C2 + lane, S.c2 + ro);
-        cp16(st + SB_PY + lane, S.phy + ro);
+        cp16(st + SB_PY + lane, PHO + ro);
         cp16(st + SB_CY + lane, S.chy + ro);
         if (lane_corner) {
             cp16(st + SB_PX + lane, S.phx + ro);
             cp16(st + SB_CX + lane, S.chx + ro);
         }
-        if (jl >= R && jl + 1 + R <= dn - 1) cp16(st + SB_FA + lane, S.phy + (size_t)(yb0 + jl + 1 + R) * pitch + xl);
+        if (jl >= jA && jl <= jB) cp16(st + SB_FA + lane, PHO + (size_t)(yb0 + jl + R) * pitch + xl);
         if (has_hl) cp16(st + SB_HL, PC + (size_t)y * pitch + x0 - 4);
         if (has_hr) cp16(st + SB_HR, PC + (size_t)y * pitch + x0 + TILE);
     };
 #pragma unroll
     for (int i = 0; i < BOT_DEPTH; ++i) {
-        issue(i, i);  // dn >= 2R+1 > BOT_DEPTH rows always exist
+        if (j0 + i < j1) issue(j0 + i, i);
         cp_commit();
+    }
+
+    // clamped values: rows jl < R use the phi derivative at local row R, rows
+    // jl > dn-1-R that at dn-1-R (solver_space_derivs.f90:118-128 on the
+    // strip); rows below nyt-1-R use the p derivatives of row nyt-1-R.
+    float4 t[2 * R + 1];
+    float dphyTop[4] = {0.f, 0.f, 0.f, 0.f}, dphyBot[4] = {0.f, 0.f, 0.f, 0.f};
+    float d2yBot[4] = {0.f, 0.f, 0.f, 0.f}, dyBot[4] = {0.f, 0.f, 0.f, 0.f};
+    if (j0 < R) {
+#pragma unroll
+        for (int i = 0; i <= 2 * R; ++i) t[i] = ld4(PHO + (size_t)(yb0 + i) * pitch + xl);
+        yderiv1<R>(t, P, dphyTop);
+    }
+    if (j1 - 1 > dn - 1 - R) {
+#pragma unroll
+        for (int i = 0; i <= 2 * R; ++i) t[i] = ld4(PHO + (size_t)(nyt - 1 - 2 * R + i) * pitch + xl);
+        yderiv1<R>(t, P, dphyBot);
+#pragma unroll
+        for (int i = 0; i <= 2 * R; ++i) t[i] = ldg4(PC + (size_t)(nyt - 1 - 2 * R + i) * pitch + xl);
+        yderivs<R>(t, P, d2yBot, dyBot);
     }
 
     float4 q[2 * R + 1], f[2 * R + 1];
 #pragma unroll
-    for (int i = 0; i < 2 * R; ++i) q[i] = ldg4(PC + (size_t)(yb0 - R + i) * pitch + xl);
+    for (int i = 0; i < 2 * R; ++i) {
+        const int yq = yb0 + j0 - R + i;
+        q[i] = (yq <= nyt - 1) ? ldg4(PC + (size_t)yq * pitch + xl) : make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+    if (jA <= jB) {
 #pragma unroll
-    for (int i = 0; i <= 2 * R; ++i) f[i] = ld4(S.phy + (size_t)(yb0 + i) * pitch + xl);
-    float dphyTop[4], dphyBot[4] = {0.f, 0.f, 0.f, 0.f};
-    yderiv1<R>(f, P, dphyTop);
-    float d2yBot[4] = {0.f, 0.f, 0.f, 0.f}, dyBot[4] = {0.f, 0.f, 0.f, 0.f};
+        for (int i = 0; i < 2 * R; ++i) f[i] = ld4(PHO + (size_t)(yb0 + jA - R + i) * pitch + xl);
+    }
 
     int ri = it.r0;
     int rrow = (ri < it.r1) ? P.recs[ri].row : INT_MAX;
 
     int slot = 0;
-    for (int jl = 0; jl < dn; ++jl) {
+    for (int jl = j0; jl < j1; ++jl) {
         const int y = yb0 + jl;
         cp_wait<BOT_DEPTH - 1>();
         const float4* st = ring + slot * SB_SIZE;
@@ -556,10 +590,6 @@ __device__ __forceinline__ void bottom_rows(const StepParams& P, const WorkItem&
         float d2y[4], dy[4];
         if (y <= nyt - 1 - R) {
             yderivs<R>(q, P, d2y, dy);
-            if (y == nyt - 1 - R) {
-#pragma unroll
-                for (int e = 0; e < 4; ++e) { d2yBot[e] = d2y[e]; dyBot[e] = dy[e]; }
-            }
         } else {
 #pragma unroll
             for (int e = 0; e < 4; ++e) { d2y[e] = d2yBot[e]; dy[e] = dyBot[e]; }
@@ -578,11 +608,10 @@ __device__ __forceinline__ void bottom_rows(const StepParams& P, const WorkItem&
 #pragma unroll
             for (int e = 0; e < 4; ++e) dphy[e] = dphyTop[e];
         } else if (jl <= dn - 1 - R) {
+            f[2 * R] = st[SB_FA + lane];
             yderiv1<R>(f, P, dphy);
-            if (jl == dn - 1 - R) {
 #pragma unroll
-                for (int e = 0; e < 4; ++e) dphyBot[e] = dphy[e];
-            }
+            for (int i = 0; i < 2 * R; ++i) f[i] = f[i + 1];
         } else {
 #pragma unroll
             for (int e = 0; e < 4; ++e) dphy[e] = dphyBot[e];
@@ -599,7 +628,6 @@ __device__ __forceinline__ void bottom_rows(const StepParams& P, const WorkItem&
             }
             phi_xderiv<R>(S, P, from_arr(phx), lane, x0, c0, first, last, dphx);
         }
-        const float4 fnext = st[SB_FA + lane];
 
         float p3[4];
 #pragma unroll
@@ -629,11 +657,11 @@ __device__ __forceinline__ void bottom_rows(const StepParams& P, const WorkItem&
                 const float propx = dphx[e] + chxn;
                 phx[e] = phxn;
                 chx[e] = chxn;
-                const float t = ((-pm1[e]) + 2.f * pc[e]) + cc[e] * ((d2x[e] + d2y[e]) + propx);
-                p3[e] = t + cc[e] * propy;
+                const float tt = ((-pm1[e]) + 2.f * pc[e]) + cc[e] * ((d2x[e] + d2y[e]) + propx);
+                p3[e] = tt + cc[e] * propy;
             }
         }
-        st4(S.phy + ro, from_arr(phy));
+        st4(PHN + ro, from_arr(phy));
         st4(S.chy + ro, from_arr(chy));
         if (lane_corner) {
             st4(S.phx + ro, from_arr(phx));
@@ -644,12 +672,7 @@ __device__ __forceinline__ void bottom_rows(const StepParams& P, const WorkItem&
 
 #pragma unroll
         for (int i = 0; i < 2 * R; ++i) q[i] = q[i + 1];
-        if (jl >= R && jl + 1 + R <= dn - 1) {
-#pragma unroll
-            for (int i = 0; i < 2 * R; ++i) f[i] = f[i + 1];
-            f[2 * R] = fnext;
-        }
-        if (jl + BOT_DEPTH < dn) issue(jl + BOT_DEPTH, slot);
+        if (jl + BOT_DEPTH < j1) issue(jl + BOT_DEPTH, slot);
         cp_commit();
         slot = (slot + 1 == BOT_DEPTH) ? 0 : slot + 1;
     }
@@ -658,18 +681,31 @@ __device__ __forceinline__ void bottom_rows(const StepParams& P, const WorkItem&
 
 // Model rows of the middle tiles: interior cells only (no CPML, no clamp),
 // so only second derivatives are needed.  This is the kernel that moves
-// almost all of the bytes.
-constexpr int IN_P = 0, IN_P1 = 32, IN_C2 = 64, IN_HL = 96, IN_HR = 97, IN_SIZE = 98;
-constexpr int IN_DEPTH = 6;
+// almost all of the bytes.  SNAP selects the variant for the time steps
+// that store a snapshot (forward) or apply the imaging condition (adjoint);
+// the adjoint variant also prefetches the snapshot row and the imaging
+// accumulator row through the ring.
+constexpr int IN_P = 0, IN_P1 = 32, IN_C2 = 64, IN_HL = 96, IN_HR = 97, IN_F = 98, IN_FS = 130, IN_K = 131;
+constexpr int IN_SIZE = 98, IN_SIZE_IMG = 195;
+constexpr int IN_DEPTH = 6, IN_DEPTH_IMG = 4;
 constexpr int IN_SMEM = 4 * IN_DEPTH * IN_SIZE * 16;
+constexpr int IN_SMEM_IMG = 4 * IN_DEPTH_IMG * IN_SIZE_IMG * 16;
 
-template <int R, int MODE>
-__global__ void __launch_bounds__(128, 5) k_step_interior(const __grid_constant__ StepParams P) {
+__device__ __forceinline__ void cp4(void* smem_dst, const void* gmem_src) {
+    const unsigned d = (unsigned)__cvta_generic_to_shared(smem_dst);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(d), "l"(gmem_src) : "memory");
+}
+
+template <int R, int MODE, bool SNAP>
+__global__ void __launch_bounds__(128, (MODE == 1 && SNAP) ? 3 : 5) k_step_interior(const __grid_constant__ StepParams P) {
+    constexpr bool IMG = (MODE == 1) && SNAP;
+    constexpr int SZ = IMG ? IN_SIZE_IMG : IN_SIZE;
+    constexpr int DEPTH = IMG ? IN_DEPTH_IMG : IN_DEPTH;
     extern __shared__ float4 smem[];
     const int lane = threadIdx.x & 31;
     const int wid = blockIdx.x * 4 + (threadIdx.x >> 5);
     if (wid >= P.nitems) return;
-    float4* ring = smem + (threadIdx.x >> 5) * (IN_DEPTH * IN_SIZE);
+    float4* ring = smem + (threadIdx.x >> 5) * (DEPTH * SZ);
     const WorkItem it = P.items[wid];
     const ShotDev& S = P.shots[it.shot];
     const int pitch = S.pitch;
@@ -681,17 +717,35 @@ __global__ void __launch_bounds__(128, 5) k_step_interior(const __grid_constant_
     const int hoff = (lane == 0) ? -4 - 4 * lane : TILE - 4 * lane;
     const bool has_h = (lane == 0) || (lane == 31);
     float4* hslot = ring + (lane == 0 ? IN_HL : IN_HR);
+    const size_t snap_base = IMG ? (size_t)P.snap * (size_t)S.snap_stride : 0;
 
     auto issue = [&](int y, int slot) {
-        float4* st = ring + slot * IN_SIZE;
+        float4* st = ring + slot * SZ;
         const size_t ro = (size_t)y * pitch;
         cp16(st + IN_P + lane, PC + ro + (size_t)R * pitch);
         cp16(st + IN_P1 + lane, P1 + ro);
         cp16(st + IN_C2 + lane, C2 + ro);
-        if (has_h) cp16(hslot + slot * IN_SIZE, PC + ro + hoff);
+        if (has_h) cp16(hslot + slot * SZ, PC + ro + hoff);
+        if (IMG) {
+            const size_t fo = snap_base + (size_t)(y - S.dn) * pitch + x0;  // element offset of the row segment
+            if (P.snap_form == 0) {
+                cp16(st + IN_F + lane, reinterpret_cast<const float*>(S.snaps) + fo + 4 * lane);
+            } else {
+                if (lane < 16) cp16(st + IN_F + lane, reinterpret_cast<const unsigned short*>(S.snaps) + fo + 8 * lane);
+                if (lane == 16)
+                    cp4(st + IN_FS, S.sscale + ((size_t)P.snap * S.ny + (y - S.dn)) * S.ntiles + it.tile);
+            }
+            const size_t ko = (size_t)(y - S.dn) * pitch + xl;
+            if (P.grad_form == 0) {
+                cp16(st + IN_K + lane, S.k32 + ko);
+            } else {
+                cp16(st + IN_K + 2 * lane, S.k64 + ko);
+                cp16(st + IN_K + 2 * lane + 1, S.k64 + ko + 2);
+            }
+        }
     };
 #pragma unroll
-    for (int i = 0; i < IN_DEPTH; ++i) {
+    for (int i = 0; i < DEPTH; ++i) {
         if (it.y0 + i < it.y1) issue(it.y0 + i, i);
         cp_commit();
     }
@@ -705,11 +759,9 @@ __global__ void __launch_bounds__(128, 5) k_step_interior(const __grid_constant_
     const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
 
     int slot = 0;
-    // unrolled by the queue length so that the queue shift becomes register renaming
-#pragma unroll(2 * R + 1)
     for (int y = it.y0; y < it.y1; ++y) {
-        cp_wait<IN_DEPTH - 1>();
-        const float4* st = ring + slot * IN_SIZE;
+        cp_wait<DEPTH - 1>();
+        const float4* st = ring + slot * SZ;
         q[2 * R] = st[IN_P + lane];
         float pm1[4], cc[4], pc[4];
         to_arr(st[IN_P1 + lane], pm1);
@@ -742,17 +794,50 @@ __global__ void __launch_bounds__(128, 5) k_step_interior(const __grid_constant_
 #pragma unroll
         for (int e = 0; e < 4; ++e) p3[e] = ((-pm1[e]) + 2.f * pc[e]) + (((d2x[e] + d2y[e]) + sv[e]) * cc[e]);
 
-        const int c0 = xl - S.off;
-        if (MODE == 0 && P.snap >= 0) store_snapshot(P, S, y - S.dn, lane, x0, xl, c0, p3, pm1, it.tile);
-        if (MODE == 1 && P.snap >= 0) image_row(P, S, y - S.dn, xl, c0, p3, pm1, it.tile);
+        if (MODE == 0 && SNAP) store_snapshot(P, S, y - S.dn, lane, x0, xl, xl - S.off, p3, pm1, it.tile);
+        if (IMG) {
+            // kernel += -0.5*(p_3-p_1)*Fields(snap)*store_snap  (:465-466); all columns interior
+            float F[4];
+            if (P.snap_form == 0) {
+                to_arr(st[IN_F + lane], F);
+            } else {
+                const uint2 pk = reinterpret_cast<const uint2*>(st + IN_F)[lane];
+                const float sc = reinterpret_cast<const float*>(st + IN_FS)[0];
+                const unsigned short hv[4] = {(unsigned short)(pk.x & 0xffffu), (unsigned short)(pk.x >> 16),
+                                              (unsigned short)(pk.y & 0xffffu), (unsigned short)(pk.y >> 16)};
+#pragma unroll
+                for (int e = 0; e < 4; ++e) {
+                    float f;
+                    if (P.snap_form == 1) f = __bfloat162float(*reinterpret_cast<const __nv_bfloat16*>(&hv[e]));
+                    else f = __half2float(*reinterpret_cast<const __half*>(&hv[e]));
+                    F[e] = f * sc;
+                }
+            }
+            float k2[4];
+#pragma unroll
+            for (int e = 0; e < 4; ++e) k2[e] = -(((0.5f * (p3[e] - pm1[e])) * F[e]) * P.ss);
+            const size_t ko = (size_t)(y - S.dn) * pitch + xl;
+            if (P.grad_form == 0) {
+                float4 k = st[IN_K + lane];
+                k.x = k.x + k2[0]; k.y = k.y + k2[1]; k.z = k.z + k2[2]; k.w = k.w + k2[3];
+                st4(S.k32 + ko, k);
+            } else {
+                const double2* kk = reinterpret_cast<const double2*>(st + IN_K) + 2 * lane;
+                double2 a = kk[0], b = kk[1];
+                a.x += (double)k2[0]; a.y += (double)k2[1]; b.x += (double)k2[2]; b.y += (double)k2[3];
+                double2* K2 = reinterpret_cast<double2*>(S.k64 + ko);
+                K2[0] = a;
+                K2[1] = b;
+            }
+        }
         st4(P1 + (size_t)y * pitch, from_arr(p3));
         if (MODE == 0 && P.record) record_row(P, S, y, xl, ri, it.r1, rrow, p3);
 
 #pragma unroll
         for (int i = 0; i < 2 * R; ++i) q[i] = q[i + 1];
-        if (y + IN_DEPTH < it.y1) issue(y + IN_DEPTH, slot);
+        if (y + DEPTH < it.y1) issue(y + DEPTH, slot);
         cp_commit();
-        slot = (slot + 1 == IN_DEPTH) ? 0 : slot + 1;
+        slot = (slot + 1 == DEPTH) ? 0 : slot + 1;
     }
     cp_wait<0>();
 }
@@ -781,7 +866,11 @@ cudaError_t configure_step_kernels() {
     cudaError_t e = cudaSuccess;
 #define FWI_CFG(R_, M_)                                                                                           \
     if (e == cudaSuccess)                                                                                         \
-        e = cudaFuncSetAttribute(k_step_interior<R_, M_>, cudaFuncAttributeMaxDynamicSharedMemorySize, IN_SMEM);   \
+        e = cudaFuncSetAttribute(k_step_interior<R_, M_, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,      \
+                                 IN_SMEM);                                                                         \
+    if (e == cudaSuccess)                                                                                         \
+        e = cudaFuncSetAttribute(k_step_interior<R_, M_, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,       \
+                                 M_ == 1 ? IN_SMEM_IMG : IN_SMEM);                                                 \
     if (e == cudaSuccess)                                                                                         \
         e = cudaFuncSetAttribute(k_step_boundary<R_, M_>, cudaFuncAttributeMaxDynamicSharedMemorySize, BND_SMEM);
     FWI_CFG(3, 0)
@@ -800,7 +889,12 @@ cudaError_t launch_step(int acc, int mode, const StepParams& pm, const StepParam
 #define FWI_LAUNCH(R_, M_)                                                          \
     do {                                                                           \
         if (bb) k_step_boundary<R_, M_><<<bb, 128, BND_SMEM, sb>>>(pb);             \
-        if (bm) k_step_interior<R_, M_><<<bm, 128, IN_SMEM, sm>>>(pm);              \
+        if (bm) {                                                                  \
+            if (pm.snap >= 0)                                                      \
+                k_step_interior<R_, M_, true><<<bm, 128, M_ == 1 ? IN_SMEM_IMG : IN_SMEM, sm>>>(pm); \
+            else                                                                   \
+                k_step_interior<R_, M_, false><<<bm, 128, IN_SMEM, sm>>>(pm);      \
+        }                                                                          \
     } while (0)
     if (acc == 3) {
         if (mode == 0) FWI_LAUNCH(3, 0);

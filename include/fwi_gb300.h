@@ -209,7 +209,7 @@ int fwi_misfit_gradient_batch(const fwi_survey_desc* desc, const float* lambda, 
  * indices are host arrays.  All working state (wavefields, c2, CPML memory
  * variables, work lists) lives in one fixed 16 MiB device array that every
  * GPU loading this library holds until the process exits; grids whose state
- * does not fit (about 7*(ny+2*dn)*(nx+2*dn+128)*4 bytes, dn = dpml+2*acc)
+ * does not fit (about 8*(ny+2*dn)*(nx+2*dn+128)*4 bytes, dn = dpml+2*acc)
  * are rejected with FWI_ERR_ARG.  Nothing is allocated: no cudaMalloc,
  * cudaFree or allocating library call.
  *

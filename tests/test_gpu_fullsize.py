@@ -1,0 +1,106 @@
+"""Parity at the benchmark sizes.
+
+Config 1 (200 x 400, 8th order, 3000 steps) runs through the drop-in solver
+and through the oracle in full: bit-exact.  Config 2 (400 x 2000) is checked
+bit-exact on a truncated record, and on the full survey through properties
+that do not need the oracle: scaling the sources by 2 scales traces,
+snapshots and gradient by exactly 2 (a power of two is exact in IEEE
+arithmetic) and leaves the misfit unchanged (traces are normalised); and
+the result does not depend on how the shots are grouped into waves.
+"""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+def _drop_in(spec, vp, iprop, S, Sadj, kernel, fields):
+    import fwi_gb300 as F
+    sh = spec.shots[0]
+    F.set_solver_options(spec.acc, spec.dpml)
+    rec = np.zeros((spec.nt, len(sh.nxRec)), np.float32, order="F")
+    F.solver_acoustic_SS(0, iprop, len(sh.nxSou), len(sh.nxRec), sh.nxSou, sh.nySou, sh.nxRec, sh.nyRec, S, Sadj,
+                         spec.d, spec.dt, spec.ny, spec.nx_model, vp, spec.store_snap, spec.nt_store, spec.nt, kernel,
+                         fields, rec)
+    return rec
+
+
+def _oracle(spec, vp, iprop, S, Sadj, kernel, fields):
+    sh = spec.shots[0]
+    return O.solver_acoustic_ss(iprop, sh.nxSou, sh.nySou, sh.nxRec, sh.nyRec, S, Sadj, spec.d, spec.dt, vp,
+                                spec.store_snap, spec.nt_store, spec.nt, kernel, fields, acc=spec.acc, dpml=spec.dpml)
+
+
+def _both(spec, vp):
+    sh = spec.shots[0]
+    nf = spec.nx_model * (spec.nt_store + 1)
+    out = {}
+    for name, fn in (("gpu", _drop_in), ("oracle", _oracle)):
+        K = np.zeros((spec.ny, spec.nx_model), np.float32, order="F")
+        Fl = np.zeros((spec.ny, nf), np.float32, order="F")
+        rec = fn(spec, vp, 1, sh.src, None, K, Fl)
+        # adjoint source: the reversed negative traces (any source exercises the path)
+        adj = np.asfortranarray(-rec[::-1].copy())
+        fn(spec, vp, 2, sh.src, adj, K, Fl)
+        out[name] = (rec, Fl, K)
+    return out
+
+
+def test_config1_full_run_bit_exact():
+    from fwi_gb300 import synth
+    spec, vp_true, vp0 = synth.config1()
+    assert (spec.ny, spec.nx_model, spec.nt, spec.acc) == (200, 400, 3000, 4)
+    r = _both(spec, vp0)
+    for a, b in zip(r["gpu"], r["oracle"]):
+        np.testing.assert_array_equal(a, b)
+    assert np.abs(r["gpu"][0]).max() > 0 and np.abs(r["gpu"][2]).max() > 0
+
+
+def test_config2_shot_truncated_bit_exact():
+    from fwi_gb300 import synth
+    spec, vp_true, vp0 = synth.config2(nshots=1, nt=300)
+    r = _both(spec, vp0)
+    for a, b in zip(r["gpu"], r["oracle"]):
+        np.testing.assert_array_equal(a, b)
+
+
+def _survey_run(spec, lam, wave=0, scale=1.0):
+    import fwi_gb300 as F
+    if scale != 1.0:
+        for sh in spec.shots:
+            sh.src = np.asfortranarray(sh.src * np.float32(scale))
+    sv = F.Survey(spec, wave_shots=wave)
+    sv.set_lambda(lam)
+    g = np.zeros((spec.ny, spec.nx_model), np.float32, order="F")
+    m, _ = sv.run(1, g)
+    traces = [sv.synthetic(i) for i in range(len(spec.shots))]
+    sv.close()
+    return m, g, traces
+
+
+def test_config2_full_grid_properties():
+    from fwi_gb300 import synth
+    from fwi_gb300.synth import lam_from_vp
+    spec, vp_true, vp0 = synth.config2(nshots=4, nt=1200)
+    lam_t, lam0 = lam_from_vp(vp_true), lam_from_vp(vp0)
+    # observed data from the true model
+    import fwi_gb300 as F
+    sv = F.Survey(spec)
+    sv.set_lambda(lam_t)
+    sv.run(2)
+    for i, sh in enumerate(spec.shots):
+        sh.obs = sv.synthetic(i)
+    sv.close()
+    m1, g1, t1 = _survey_run(spec, lam0)
+    m2, g2, t2 = _survey_run(spec, lam0, scale=2.0)
+    assert m1 > 0 and m1 == m2
+    for a, b in zip(t1, t2):
+        np.testing.assert_array_equal(2 * a, b)
+    np.testing.assert_array_equal(2 * g1, g2)
+    for sh in spec.shots:
+        sh.src = np.asfortranarray(sh.src * np.float32(0.5))
+    m3, g3, _ = _survey_run(spec, lam0, wave=1)
+    assert m3 == m1
+    np.testing.assert_array_equal(g3, g1)

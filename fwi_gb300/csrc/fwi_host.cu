@@ -1074,11 +1074,15 @@ int issue_wave(fwi_survey* s, size_t wi, int step, cudaStream_t st, cudaStream_t
         const int sh = w[k];
         LK(launch_rec_last(s->d_synth.as<float>() + (size_t)s->tr_off[sh] * D.nt, D.nt, (int)s->geoms[sh].nxR.size(), st));
     }
-    // misfit + adjoint source for this wave's traces
-    const int t0 = s->tr_off[w.front()], t1 = s->tr_off[w.back() + 1];
-    LK(launch_misfit(s->d_synth.as<float>() + (size_t)t0 * D.nt, s->d_obs.as<float>() + (size_t)t0 * D.nt,
-                     s->d_adj.as<float>() + (size_t)t0 * D.nt, s->d_mis_tr.as<double>() + t0, D.nt, D.dt,
-                     s->d_tr_off.as<int>(), t1 - t0, 0, nullptr, st));
+    // misfit + adjoint source for this wave's traces (one launch per shot:
+    // the shots of a wave need not be consecutive)
+    for (int sh : w) {
+        const int t0 = s->tr_off[sh], t1 = s->tr_off[sh + 1];
+        if (t1 == t0) continue;
+        LK(launch_misfit(s->d_synth.as<float>() + (size_t)t0 * D.nt, s->d_obs.as<float>() + (size_t)t0 * D.nt,
+                         s->d_adj.as<float>() + (size_t)t0 * D.nt, s->d_mis_tr.as<double>() + t0, D.nt, D.dt,
+                         s->d_tr_off.as<int>(), t1 - t0, 0, nullptr, st));
+    }
     if (step != 1) return FWI_OK;
     for (size_t k = 0; k < w.size(); ++k) {
         ShotState& ss = *s->slots[k];

@@ -3,10 +3,12 @@
 Config 1 (200 x 400, 8th order, 3000 steps) runs through the drop-in solver
 and through the oracle in full: bit-exact.  Config 2 (400 x 2000) is checked
 bit-exact on a truncated record, and on the full survey through properties
-that do not need the oracle: scaling the sources by 2 scales traces,
-snapshots and gradient by exactly 2 (a power of two is exact in IEEE
-arithmetic) and leaves the misfit unchanged (traces are normalised); and
-the result does not depend on how the shots are grouped into waves.
+that do not need the oracle: the result does not depend on how the shots are
+grouped into waves or on graph replay versus direct launches (bit-exact),
+and scaling the sources by 2 scales traces and gradient by 2 and leaves the
+misfit unchanged.  The last holds only to FP32 rounding, not bit for bit:
+values in the subnormal range round in absolute units, and those differences
+change later rounding decisions (the CPU oracle shows the same, ~1e-7).
 """
 import numpy as np
 import pytest
@@ -80,6 +82,10 @@ def _survey_run(spec, lam, wave=0, scale=1.0):
     return m, g, traces
 
 
+def _rel(a, b):
+    return float(np.linalg.norm((a - b).astype(np.float64)) / np.linalg.norm(b.astype(np.float64)))
+
+
 def test_config2_full_grid_properties():
     from fwi_gb300 import synth
     from fwi_gb300.synth import lam_from_vp
@@ -95,12 +101,14 @@ def test_config2_full_grid_properties():
     sv.close()
     m1, g1, t1 = _survey_run(spec, lam0)
     m2, g2, t2 = _survey_run(spec, lam0, scale=2.0)
-    assert m1 > 0 and m1 == m2
+    assert m1 > 0 and abs(m2 - m1) <= 1e-4 * m1
     for a, b in zip(t1, t2):
-        np.testing.assert_array_equal(2 * a, b)
-    np.testing.assert_array_equal(2 * g1, g2)
+        assert _rel(2 * a, b) <= 1e-5
+    assert _rel(2 * g1, g2) <= 1e-5
     for sh in spec.shots:
         sh.src = np.asfortranarray(sh.src * np.float32(0.5))
-    m3, g3, _ = _survey_run(spec, lam0, wave=1)
+    m3, g3, t3 = _survey_run(spec, lam0, wave=1)
     assert m3 == m1
     np.testing.assert_array_equal(g3, g1)
+    for a, b in zip(t1, t3):
+        np.testing.assert_array_equal(a, b)

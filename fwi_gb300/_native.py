@@ -20,6 +20,7 @@ FWI_ERR_STATE = -5
 
 SNAP_F32, SNAP_BF16, SNAP_F16 = 0, 1, 2
 SURVEY_NO_GRAPH = 1
+SURVEY_RECOMPUTE = 2
 GRAD_F32, GRAD_F64 = 0, 1
 
 EXPORTS = [
@@ -28,6 +29,7 @@ EXPORTS = [
     "fwi_mcs_geometry", "fwi_ricker", "fwi_time_rules", "fwi_survey_create", "fwi_survey_destroy",
     "fwi_survey_set_lambda", "fwi_survey_set_observed", "fwi_survey_set_sources", "fwi_survey_run",
     "fwi_survey_grad_device", "fwi_survey_get_synthetic", "fwi_survey_step_bytes", "fwi_survey_tuning",
+    "fwi_survey_recompute",
     "fwi_survey_time_steps", "fwi_misfit_gradient_batch", "fwi_solver_forward_noalloc",
 ]
 
@@ -87,6 +89,7 @@ def load():
     lib.fwi_survey_get_synthetic.argtypes = [P, I, P]
     lib.fwi_survey_step_bytes.argtypes = [P, C.POINTER(C.c_double)]
     lib.fwi_survey_tuning.argtypes = [P, IP, IP]
+    lib.fwi_survey_recompute.argtypes = [P, IP, IP]
     lib.fwi_survey_time_steps.argtypes = [P, I]
     lib.fwi_misfit_gradient_batch.argtypes = [C.POINTER(FwiSurveyDesc), P, I, P, P]
     lib.fwi_solver_forward_noalloc.argtypes = [I, I, P, P, P, P, P, F, F, I, I, P, I, P]

@@ -153,10 +153,10 @@ class Survey:
     """Device-resident batched survey (fwi_survey_create & co)."""
 
     def __init__(self, spec: SurveySpec, snap_form=N.SNAP_F32, grad_form=N.GRAD_F64, hbm_budget=0, wave_shots=0,
-                 band_rows=0, graph=True):
+                 band_rows=0, graph=True, recompute=False):
         self.spec = spec
-        self._h = _DescHolder(spec, snap_form, grad_form, hbm_budget, wave_shots, band_rows,
-                              0 if graph else N.SURVEY_NO_GRAPH)
+        flags = (0 if graph else N.SURVEY_NO_GRAPH) | (N.SURVEY_RECOMPUTE if recompute else 0)
+        self._h = _DescHolder(spec, snap_form, grad_form, hbm_budget, wave_shots, band_rows, flags)
         handle = C.c_void_p()
         N.check(N.load().fwi_survey_create(C.byref(self._h.desc), C.byref(handle)))
         self.handle = handle
@@ -222,6 +222,12 @@ class Survey:
         w, b = C.c_int(0), C.c_int(0)
         N.check(N.load().fwi_survey_tuning(self.handle, C.byref(w), C.byref(b)))
         return w.value, b.value
+
+    def recompute_plan(self):
+        """(forward steps per segment, segments); (0, 0) without recomputation."""
+        c, j = C.c_int(0), C.c_int(0)
+        N.check(N.load().fwi_survey_recompute(self.handle, C.byref(c), C.byref(j)))
+        return c.value, j.value
 
     def time_steps(self, steps):
         N.check(N.load().fwi_survey_time_steps(self.handle, steps))

@@ -4,6 +4,7 @@
 // Compiled with --fmad=false (see fwi_step.cu).
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstdint>
 
 #include "fwi_internal.cuh"
@@ -219,6 +220,21 @@ __global__ void k_dot_final(const double* part, int nb, double* out) {
     }
 }
 
+// Copy many equal-purpose buffers in one launch (checkpoint save/restore of
+// the wavefield state): job j copies n4 float4 from src to dst.
+struct CopyJob {
+    const float4* src;
+    float4* dst;
+    size_t n4;
+};
+__global__ void k_copy_jobs(const CopyJob* jobs, int njobs) {
+    for (int j = blockIdx.y; j < njobs; j += gridDim.y) {
+        const CopyJob c = jobs[j];
+        for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < c.n4; i += (size_t)gridDim.x * blockDim.x)
+            c.dst[i] = c.src[i];
+    }
+}
+
 // Non-finite detector over a float array (sets *flag = 1).
 __global__ void k_nonfinite(const float* a, size_t n, int* flag) {
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
@@ -277,6 +293,17 @@ cudaError_t launch_kernel_io(float* dev, float* fort, int ny, int nx, int pitch,
 cudaError_t launch_dot(const float* g, const float* o, size_t n, double* part, int nb, double* out, cudaStream_t st) {
     k_dot_partial<<<nb, 256, 0, st>>>(g, o, n, part);
     k_dot_final<<<1, 32, 0, st>>>(part, nb, out);
+    return cudaGetLastError();
+}
+size_t copy_job_size() { return sizeof(CopyJob); }
+void fill_copy_job(void* dst, const void* src, void* to, size_t bytes) {
+    CopyJob c{reinterpret_cast<const float4*>(src), reinterpret_cast<float4*>(to), bytes / 16};
+    *reinterpret_cast<CopyJob*>(dst) = c;
+}
+cudaError_t launch_copy_jobs(const void* jobs, int njobs, cudaStream_t st) {
+    if (njobs <= 0) return cudaSuccess;
+    dim3 g(64, (unsigned)std::min(njobs, 65535));
+    k_copy_jobs<<<g, 256, 0, st>>>(reinterpret_cast<const CopyJob*>(jobs), njobs);
     return cudaGetLastError();
 }
 cudaError_t launch_nonfinite(const float* a, size_t n, int* flag, cudaStream_t st) {

@@ -41,6 +41,9 @@ cudaError_t launch_kernel_io(float* dev, float* fort, int ny, int nx, int pitch,
                              cudaStream_t st);
 cudaError_t launch_dot(const float* g, const float* o, size_t n, double* part, int nb, double* out, cudaStream_t st);
 cudaError_t launch_nonfinite(const float* a, size_t n, int* flag, cudaStream_t st);
+size_t copy_job_size();
+void fill_copy_job(void* dst, const void* src, void* to, size_t bytes);
+cudaError_t launch_copy_jobs(const void* jobs, int njobs, cudaStream_t st);
 }  // namespace fwi
 
 using namespace fwi;
@@ -384,8 +387,20 @@ double step_bytes_shot(int ny, int nx, int dn) {
 
 struct ShotState {
     DBuf pa, pb, c2, phx, chx, phy, phy2, chy, snaps, sscale, k;
+    DBuf bst[7];   // second wavefield state (adjoint) when recomputing
+    DBuf ckpt;     // forward-state checkpoints when recomputing
     Layout lay{};
     size_t field_bytes = 0, snap_bytes = 0;
+    // the seven state fields in ShotDev order: pa, pb, phx, chx, phy, phy2, chy
+    void* state(int i) {
+        DBuf* a[7] = {&pa, &pb, &phx, &chx, &phy, &phy2, &chy};
+        return a[i]->p;
+    }
+    int alloc_rc(int nckpt) {
+        for (auto& b : bst) TRY(b.ensure(field_bytes));
+        TRY(ckpt.ensure(std::max<size_t>(16, (size_t)nckpt * 7 * field_bytes)));
+        return FWI_OK;
+    }
     int alloc(const Layout& l, int nsnap_blocks, int snap_form, int grad_form) {
         lay = l;
         field_bytes = (size_t)l.nyt * l.pitch * sizeof(float);
@@ -868,10 +883,15 @@ struct fwi_survey {
         int n_if = 0, n_ia = 0, n_bf = 0, n_ba = 0;
         cudaGraphExec_t graph[3] = {nullptr, nullptr, nullptr};
         long long graph_kernels[3] = {0, 0, 0};  // kernel nodes per graph
+        DBuf save_jobs, restore_jobs;  // checkpoint copies: [ckpt][shot][field]
     };
     std::vector<std::unique_ptr<WaveDev>> wdev;
     std::vector<float> h_fA, h_fB;
     bool lambda_set = false;
+    // checkpointed recomputation: C forward steps per segment, J segments,
+    // `slots` snapshot blocks per shot; per block its segment and slot
+    int rc_C = 0, rc_J = 0, rc_slots = 0;
+    std::vector<int> ev, blk_seg, blk_slot;
     ~fwi_survey() {
         for (auto& w : wdev)
             for (auto& gexec : w->graph)
@@ -917,7 +937,8 @@ int survey_prepare_slots(fwi_survey* s) {
                 big = l;
             }
         }
-        TRY(s->slots[k]->alloc(big, s->nt_store + 1, D.snap_form, D.grad_form));
+        TRY(s->slots[k]->alloc(big, s->rc_C ? s->rc_slots : s->nt_store + 1, D.snap_form, D.grad_form));
+        if (s->rc_C) TRY(s->slots[k]->alloc_rc(s->rc_J - 1));
     }
     return FWI_OK;
 }
@@ -976,6 +997,15 @@ int survey_prepare_waves(fwi_survey* s) {
             dv.srcv = s->d_src.as<float>() + soff * D.nt;
             f.push_back(dv);
             dv.srcv = s->d_adj.as<float>() + (size_t)s->tr_off[sh] * D.nt;
+            if (s->rc_C) {  // the adjoint runs on the second state while the forward is recomputed
+                dv.pa = ss.bst[0].as<float>();
+                dv.pb = ss.bst[1].as<float>();
+                dv.phx = ss.bst[2].as<float>();
+                dv.chx = ss.bst[3].as<float>();
+                dv.phy = ss.bst[4].as<float>();
+                dv.phy2 = ss.bst[5].as<float>();
+                dv.chy = ss.bst[6].as<float>();
+            }
             a.push_back(dv);
             fill_stack_shot(stk.data() + k * stack_shot_size(), ss.k.as<float>(), ss.k.as<double>(), s->geoms[sh].x0,
                             l.nx, l.off + l.dn, l.pitch, s->gw[sh]);
@@ -984,6 +1014,22 @@ int survey_prepare_waves(fwi_survey* s) {
         TRY(upload(wd.shots_f, f, st));
         TRY(upload(wd.shots_a, a, st));
         TRY(upload(wd.stack, stk, st));
+        if (s->rc_C && s->rc_J > 1) {
+            const size_t js = copy_job_size(), per = w.size() * 7;
+            std::vector<unsigned char> sv(per * (s->rc_J - 1) * js), rv(sv.size());
+            for (int c = 0; c < s->rc_J - 1; ++c)
+                for (size_t k = 0; k < w.size(); ++k) {
+                    ShotState& ss = *s->slots[k];
+                    for (int fi = 0; fi < 7; ++fi) {
+                        const size_t idx = (size_t)c * per + k * 7 + fi;
+                        unsigned char* cp = ss.ckpt.as<unsigned char>() + ((size_t)c * 7 + fi) * ss.field_bytes;
+                        fill_copy_job(sv.data() + idx * js, ss.state(fi), cp, ss.field_bytes);
+                        fill_copy_job(rv.data() + idx * js, cp, ss.state(fi), ss.field_bytes);
+                    }
+                }
+            TRY(upload(wd.save_jobs, sv, st));
+            TRY(upload(wd.restore_jobs, rv, st));
+        }
     }
     CK(cudaStreamSynchronize(st));
     return FWI_OK;
@@ -1027,6 +1073,142 @@ int tune_band(fwi_survey* s) {
     return FWI_OK;
 }
 
+// ---- checkpointed recomputation -------------------------------------------
+//
+// Segment j holds forward steps k in [C*j+1, C*(j+1)].  The forward run keeps
+// the full state after steps C, 2C, ... (checkpoints) and the snapshots of
+// the last segment only; the adjoint, which consumes snapshot blocks from the
+// last to the first, re-runs the forward of a segment from its checkpoint
+// into the small snapshot ring whenever it needs a block of another segment.
+// The arithmetic of every step is unchanged, so the gradient is identical to
+// the one computed with all snapshots stored.
+
+int rc_plan(fwi_survey* s, int C) {
+    const auto& D = s->desc;
+    s->rc_C = C;
+    s->ev = snapshot_steps(D.nt, D.store_snap);
+    s->rc_J = (D.nt - 1) / C + 1;
+    const int nb = (int)s->ev.size();
+    s->blk_seg.assign(nb + 1, 0);
+    s->blk_slot.assign(nb + 1, 0);
+    std::vector<int> first(s->rc_J, -1);
+    for (int b = 1; b <= nb; ++b) {
+        const int j = (s->ev[b - 1] - 1) / C;
+        s->blk_seg[b] = j;
+        if (first[j] < 0) first[j] = b;
+        s->blk_slot[b] = b - first[j] + 1;  // slot 0 is block 0 (zeros) in segment 0
+    }
+    int mx = 0;
+    for (int b = 1; b <= nb; ++b) mx = std::max(mx, s->blk_slot[b]);
+    s->rc_slots = mx + 1;
+    return FWI_OK;
+}
+
+int zero_slot0(fwi_survey* s, size_t wi, cudaStream_t st) {
+    const auto& D = s->desc;
+    for (size_t k = 0; k < s->waves[wi].size(); ++k) {
+        ShotState& ss = *s->slots[k];
+        const Layout& l = s->lays[s->waves[wi][k]];
+        const size_t esz = D.snap_form == FWI_SNAP_F32 ? 4 : 2;
+        CK(cudaMemsetAsync(ss.snaps.p, 0, (size_t)l.ny * l.pitch * esz, st));
+        CK(cudaMemsetAsync(ss.sscale.p, 0, (size_t)l.ny * l.ntiles * sizeof(float), st));
+    }
+    return FWI_OK;
+}
+
+// Forward steps k0..k1 on state A; snapshots of blocks whose segment is
+// `keep_seg` go to their ring slots (keep_seg < 0: none).
+int rc_steps(fwi_survey* s, int k0, int k1, int keep_seg, bool save_ckpt, size_t wi, StepSet ps, cudaStream_t st,
+             cudaStream_t st2) {
+    const auto& D = s->desc;
+    auto& wd = *s->wdev[wi];
+    const int per = (int)s->waves[wi].size() * 7;
+    size_t evi = std::lower_bound(s->ev.begin(), s->ev.end(), k0) - s->ev.begin();
+    for (int k = k0; k <= k1; ++k) {
+        int sn = -1;
+        if (evi < s->ev.size() && s->ev[evi] == k) {
+            const int b = (int)evi + 1;
+            if (s->blk_seg[b] == keep_seg) sn = s->blk_slot[b];
+            ++evi;
+        }
+        ps.pm.t = ps.pb.t = k - 2;
+        ps.pm.parity = ps.pb.parity = k & 1;
+        ps.pm.snap = ps.pb.snap = sn;
+        TRY(step_fork_join(D.acc, 0, ps, st, st2));
+        if (save_ckpt && k % s->rc_C == 0 && k / s->rc_C <= s->rc_J - 1) {
+            const int c = k / s->rc_C - 1;
+            LK(launch_copy_jobs(wd.save_jobs.as<unsigned char>() + (size_t)c * per * copy_job_size(), per, st));
+        }
+    }
+    return FWI_OK;
+}
+
+int rc_forward(fwi_survey* s, size_t wi, int step, StepSet ps, cudaStream_t st, cudaStream_t st2) {
+    // keep the last segment's snapshots (the adjoint needs them first)
+    if (step == 1 && s->rc_J == 1) TRY(zero_slot0(s, wi, st));
+    return rc_steps(s, 2, s->desc.nt, step == 1 ? s->rc_J - 1 : -1, step == 1, wi, ps, st, st2);
+}
+
+int rc_recompute(fwi_survey* s, size_t wi, int j, StepSet psf, cudaStream_t st, cudaStream_t st2) {
+    auto& wd = *s->wdev[wi];
+    const int per = (int)s->waves[wi].size() * 7;
+    if (j == 0) {
+        for (size_t k = 0; k < s->waves[wi].size(); ++k) {
+            ShotState& ss = *s->slots[k];
+            for (int fi = 0; fi < 7; ++fi) CK(cudaMemsetAsync(ss.state(fi), 0, ss.field_bytes, st));
+        }
+        TRY(zero_slot0(s, wi, st));
+    } else {
+        LK(launch_copy_jobs(wd.restore_jobs.as<unsigned char>() + (size_t)(j - 1) * per * copy_job_size(), per, st));
+    }
+    const int k0 = std::max(2, s->rc_C * j + 1), k1 = std::min(s->desc.nt, s->rc_C * (j + 1));
+    return rc_steps(s, k0, k1, j, false, wi, psf, st, st2);
+}
+
+int rc_adjoint(fwi_survey* s, size_t wi, StepSet ps, cudaStream_t st, cudaStream_t st2) {
+    const auto& D = s->desc;
+    auto& wd = *s->wdev[wi];
+    StepSet psf;  // forward recompute: state A, no receivers
+    psf.pm = ps.pm;
+    psf.pm.items = wd.items_if.as<WorkItem>();
+    psf.pm.nitems = wd.n_if;
+    psf.pm.shots = wd.shots_f.as<ShotDev>();
+    psf.pm.srcs = wd.src_f.as<SrcEnt>();
+    psf.pm.record = 0;
+    psf.pb = psf.pm;
+    psf.pb.items = wd.items_bf.as<WorkItem>();
+    psf.pb.nitems = wd.n_bf;
+    ps.pm.items = wd.items_ia.as<WorkItem>();
+    ps.pm.nitems = wd.n_ia;
+    ps.pm.shots = wd.shots_a.as<ShotDev>();
+    ps.pm.srcs = wd.src_a.as<SrcEnt>();
+    ps.pm.record = 0;
+    ps.pb = ps.pm;
+    ps.pb.items = wd.items_ba.as<WorkItem>();
+    ps.pb.nitems = wd.n_ba;
+    int cur = s->rc_J - 1;
+    size_t evi = 0;
+    int snap = s->nt_store;
+    for (int k = 2; k <= D.nt; ++k) {
+        int sn = -1;
+        if (evi < s->ev.size() && s->ev[evi] == k) {
+            ++evi;
+            --snap;  // block used by this imaging step (solver_acoustic_SS.f90:460)
+            const int need = snap == 0 ? 0 : s->blk_seg[snap];
+            if (need != cur) {
+                TRY(rc_recompute(s, wi, need, psf, st, st2));
+                cur = need;
+            }
+            sn = snap == 0 ? 0 : s->blk_slot[snap];
+        }
+        ps.pm.t = ps.pb.t = k - 2;
+        ps.pm.parity = ps.pb.parity = k & 1;
+        ps.pm.snap = ps.pb.snap = sn;
+        TRY(step_fork_join(D.acc, 1, ps, st, st2));
+    }
+    return FWI_OK;
+}
+
 // Issue one wave's work: forward (+ misfit) and, for step 1, adjoint + stack.
 int issue_wave(fwi_survey* s, size_t wi, int step, cudaStream_t st, cudaStream_t st2) {
     const auto& D = s->desc;
@@ -1048,7 +1230,7 @@ int issue_wave(fwi_survey* s, size_t wi, int step, cudaStream_t st, cudaStream_t
         // snapshot block 0 is never written by the forward but is the last
         // one the adjoint pairs with: zero, as Fields = 0 before the forward
         // (calculate_misfit_gradient.f90:231)
-        if (step == 1) {
+        if (step == 1 && !s->rc_C) {
             const size_t esz = D.snap_form == FWI_SNAP_F32 ? 4 : 2;
             CK(cudaMemsetAsync(ss.snaps.p, 0, (size_t)l.ny * l.pitch * esz, st));
             CK(cudaMemsetAsync(ss.sscale.p, 0, (size_t)l.ny * l.ntiles * sizeof(float), st));
@@ -1069,7 +1251,11 @@ int issue_wave(fwi_survey* s, size_t wi, int step, cudaStream_t st, cudaStream_t
     ps.pb = ps.pm;
     ps.pb.items = wd.items_bf.as<WorkItem>();
     ps.pb.nitems = wd.n_bf;
-    TRY(run_time_loop(D.acc, 0, D.nt, D.store_snap, s->nt_store, step == 1, ps, st, st2));
+    if (s->rc_C) {
+        TRY(rc_forward(s, wi, step, ps, st, st2));
+    } else {
+        TRY(run_time_loop(D.acc, 0, D.nt, D.store_snap, s->nt_store, step == 1, ps, st, st2));
+    }
     for (size_t k = 0; k < w.size(); ++k) {
         const int sh = w[k];
         LK(launch_rec_last(s->d_synth.as<float>() + (size_t)s->tr_off[sh] * D.nt, D.nt, (int)s->geoms[sh].nxR.size(), st));
@@ -1086,14 +1272,16 @@ int issue_wave(fwi_survey* s, size_t wi, int step, cudaStream_t st, cudaStream_t
     if (step != 1) return FWI_OK;
     for (size_t k = 0; k < w.size(); ++k) {
         ShotState& ss = *s->slots[k];
-        CK(cudaMemsetAsync(ss.pa.p, 0, ss.pa.n, st));
-        CK(cudaMemsetAsync(ss.pb.p, 0, ss.pb.n, st));
-        CK(cudaMemsetAsync(ss.phx.p, 0, ss.phx.n, st));
-        CK(cudaMemsetAsync(ss.chx.p, 0, ss.chx.n, st));
-        CK(cudaMemsetAsync(ss.phy.p, 0, ss.phy.n, st));
-        CK(cudaMemsetAsync(ss.phy2.p, 0, ss.phy2.n, st));
-        CK(cudaMemsetAsync(ss.chy.p, 0, ss.chy.n, st));
+        for (int fi = 0; fi < 7; ++fi) {
+            void* f = s->rc_C ? ss.bst[fi].p : ss.state(fi);
+            CK(cudaMemsetAsync(f, 0, ss.field_bytes, st));
+        }
         CK(cudaMemsetAsync(ss.k.p, 0, ss.k.n, st));
+    }
+    if (s->rc_C) {
+        TRY(rc_adjoint(s, wi, ps, st, st2));
+        LK(launch_stack(s->d_G.as<double>(), D.ny, D.nx_model, wd.stack.p, (int)w.size(), D.grad_form, st));
+        return FWI_OK;
     }
     ps.pm.items = wd.items_ia.as<WorkItem>();
     ps.pm.nitems = wd.n_ia;
@@ -1204,6 +1392,33 @@ int fwi_survey_create(const fwi_survey_desc* desc, fwi_survey** out) {
         budget = std::min(budget, D.hbm_budget - used_resident);
     }
     int wave = (int)std::min<size_t>((size_t)D.nshots, budget / std::max<size_t>(per, 1));
+    // Checkpointed recomputation keeps a forward-state checkpoint every C steps
+    // and a ring of C/store_snap snapshots instead of all of them, for one more
+    // forward pass.  It is used when asked for, or when the budget would leave
+    // waves so small (< 8 shots) that the extra pass is cheaper than the lost
+    // batching.
+    {
+        size_t fb = 0, bb = 0, kb = 0;
+        for (auto& l : s->lays) {
+            fb = std::max(fb, (size_t)l.nyt * l.pitch * 4);
+            bb = std::max(bb, (size_t)l.ny * l.pitch * (D.snap_form == FWI_SNAP_F32 ? 4 : 2) + (size_t)l.ny * l.ntiles * 4);
+            kb = std::max(kb, (size_t)l.ny * l.pitch * (D.grad_form == FWI_GRAD_F64 ? 8 : 4));
+        }
+        const int ss = D.store_snap;
+        int C = (int)std::lround(std::sqrt(7.0 * fb * D.nt * ss / (double)std::max<size_t>(bb, 1)));
+        C = std::max(ss, std::min(D.nt, (C + ss - 1) / ss * ss));
+        const int J = (D.nt - 1) / C + 1;
+        const size_t per_rc = 15 * fb + (size_t)(J - 1) * 7 * fb + (size_t)(C / ss + 2) * bb + kb;
+        const int wave_rc = (int)std::min<size_t>((size_t)D.nshots, budget / std::max<size_t>(per_rc, 1));
+        const bool force = (D.flags & FWI_SURVEY_RECOMPUTE) != 0;
+        if (force || (wave < std::min(D.nshots, 8) && wave_rc > wave)) {
+            if (wave_rc < 1)
+                return fail(FWI_ERR_NOMEM, "one shot's checkpoints and snapshot ring (" + std::to_string(per_rc) +
+                                               " bytes) exceed the device budget");
+            TRY(rc_plan(s.get(), C));
+            wave = wave_rc;
+        }
+    }
     if (wave < 1)
         return fail(FWI_ERR_NOMEM, "one shot's wavefields and snapshots (" + std::to_string(per) +
                                        " bytes) exceed the device budget");
@@ -1351,6 +1566,13 @@ int fwi_survey_tuning(fwi_survey* s, int* wave_shots, int* band_rows) {
     if (!s) return fail(FWI_ERR_STATE, "null survey");
     if (wave_shots) *wave_shots = s->wave;
     if (band_rows) *band_rows = s->band;
+    return FWI_OK;
+}
+
+int fwi_survey_recompute(fwi_survey* s, int* segment_steps, int* segments) {
+    if (!s) return fail(FWI_ERR_STATE, "null survey");
+    if (segment_steps) *segment_steps = s->rc_C;
+    if (segments) *segments = s->rc_J;
     return FWI_OK;
 }
 

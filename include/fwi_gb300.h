@@ -151,6 +151,11 @@ typedef struct fwi_survey_desc {
 /* fwi_survey_desc.flags: launch every time step directly instead of
  * replaying the captured CUDA graph (the plain one-launch-per-step path). */
 #define FWI_SURVEY_NO_GRAPH 1
+/* fwi_survey_desc.flags: keep forward-state checkpoints and a small snapshot
+ * ring and recompute forward segments during the adjoint (one more forward
+ * pass, far less memory).  Chosen automatically when the HBM budget would
+ * otherwise leave waves of fewer than 8 shots. */
+#define FWI_SURVEY_RECOMPUTE 2
 
 typedef struct fwi_survey fwi_survey;
 
@@ -183,6 +188,9 @@ int fwi_survey_get_synthetic(fwi_survey* s, int shot, float* out);
 int fwi_survey_step_bytes(fwi_survey* s, double* bytes);
 /* Tuning chosen for the survey (wave size, band rows). */
 int fwi_survey_tuning(fwi_survey* s, int* wave_shots, int* band_rows);
+/* Checkpointed recomputation plan: forward steps per segment and number of
+ * segments (0, 0 when all snapshots are stored). */
+int fwi_survey_recompute(fwi_survey* s, int* segment_steps, int* segments);
 /* Run `steps` forward time steps of the first wave (for kernel timing; the
  * wavefields keep evolving, sources are injected). */
 int fwi_survey_time_steps(fwi_survey* s, int steps);

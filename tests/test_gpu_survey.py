@@ -145,3 +145,46 @@ def test_batch_entry_point_matches_survey():
     g3 = np.zeros_like(g)
     m3 = F.calculate_misfit_gradient(spec, lam, 1, np.float32(0.0), g3)
     assert np.array_equal(g3, g) and m3 == m
+
+
+@pytest.mark.parametrize("kw,form", [(dict(nt=300), 0), (dict(nt=200, store_snap=4), 1), (dict(nt=600, nshots=4), 2)])
+def test_checkpointed_recompute_is_bit_identical(kw, form):
+    import fwi_gb300 as F
+    from fwi_gb300.synth import lam_from_vp
+    spec, vp = make(11, **kw)
+    lam = lam_from_vp(vp)
+    res = []
+    for rc in (False, True):
+        sv = F.Survey(spec, snap_form=form, recompute=rc)
+        c, j = sv.recompute_plan()
+        assert (j > 1) == rc
+        sv.set_lambda(lam)
+        g = np.zeros((spec.ny, spec.nx_model), np.float32, order="F")
+        m, _ = sv.run(1, g)
+        res.append((m, g, [sv.synthetic(i) for i in range(len(spec.shots))]))
+        m2, _ = sv.run(2)  # forward-only runs keep no snapshots
+        assert m2 == m
+    assert res[0][0] == res[1][0]
+    np.testing.assert_array_equal(res[0][1], res[1][1])
+    for a, b in zip(res[0][2], res[1][2]):
+        np.testing.assert_array_equal(a, b)
+
+
+def test_small_budget_selects_recompute():
+    import fwi_gb300 as F
+    from fwi_gb300.synth import lam_from_vp
+    spec, vp = make(12, nshots=2, nt=3000)
+    lam = lam_from_vp(vp)
+    full = F.Survey(spec)
+    full.set_lambda(lam)
+    g0 = np.zeros((spec.ny, spec.nx_model), np.float32, order="F")
+    m0, _ = full.run(1, g0)
+    full.close()
+    # resident data ~ traces; give room for far less than one shot's snapshots
+    resident = 4 * spec.nt * sum(len(s.nxRec) for s in spec.shots) * 3 + 8 * spec.ny * spec.nx_model * 2
+    sv = F.Survey(spec, hbm_budget=resident + 6_000_000)
+    assert sv.recompute_plan()[1] > 1
+    sv.set_lambda(lam)
+    g = np.zeros_like(g0)
+    m, _ = sv.run(1, g)
+    assert m == m0 and np.array_equal(g, g0)

@@ -487,6 +487,13 @@ struct StepSet {
 // One time step: model rows on st, bottom rows on st2, both ordered after
 // the previous step and before the next one.
 int step_fork_join(int acc, int mode, const StepSet& ps, cudaStream_t st, cudaStream_t st2) {
+    if (ps.pm.nitems == 0 || ps.pb.nitems == 0) {
+        // one kernel only: no fork.  (A wait on an event with no new node on
+        // st in between would accumulate dependencies under stream capture.)
+        CK(launch_step(acc, mode, ps.pm, ps.pb, st, st));
+        L().launches += (ps.pm.nitems > 0) + (ps.pb.nitems > 0);
+        return FWI_OK;
+    }
     CK(cudaEventRecord(L().ev_fork, st));
     CK(cudaStreamWaitEvent(st2, L().ev_fork, 0));
     CK(launch_step(acc, mode, ps.pm, ps.pb, st, st2));

@@ -105,8 +105,8 @@ def test_config2_full_grid_properties():
     # 1e-5 shows up ~30x larger in the misfit
     assert m1 > 0 and abs(m2 - m1) <= 2e-3 * m1
     for a, b in zip(t1, t2):
-        assert _rel(2 * a, b) <= 1e-5
-    assert _rel(2 * g1, g2) <= 1e-5
+        assert _rel(2 * a, b) <= 1e-4
+    assert _rel(2 * g1, g2) <= 1e-4
     for sh in spec.shots:
         sh.src = np.asfortranarray(sh.src * np.float32(0.5))
     m3, g3, t3 = _survey_run(spec, lam0, wave=1)

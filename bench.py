@@ -39,8 +39,10 @@ def parse():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--shots", type=int, default=64)
-    ap.add_argument("--nt", type=int, default=6000)
+    ap.add_argument("--config", type=int, choices=[2, 3], default=2,
+                    help="2: batched MCS survey (the metric's workload); 3: uneven-window WAS batch")
+    ap.add_argument("--shots", type=int, default=0, help="shots (0 = the config's: 64 or 30)")
+    ap.add_argument("--nt", type=int, default=0, help="time steps (0 = the config's: 6000 or 12800)")
     ap.add_argument("--snap", choices=["f32", "bf16", "f16"], default="f32")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg")
@@ -53,8 +55,25 @@ def parse():
 
 
 def workload_name(a):
+    if a.config == 3:
+        return (f"uneven-window WAS batch: 600x6000 cells @25 m crustal model, {a.shots} OBS sources on 30-100 km "
+                f"windows, 1200 receivers @125 m, nt={a.nt} (dt=1.5625 ms, the CFL rule; 2.5 ms is unstable), "
+                f"acc=3, dPML=20, store_snap=10, {a.snap} snapshots, FP64 gradient stack")
     return (f"batched MCS survey: 400x2000 cells @12.5 m, {a.shots} shots x 480 ch, nt={a.nt} (dt=1 ms), "
             f"acc=3 (6th order), dPML=20, store_snap=10, {a.snap} snapshots, FP64 gradient stack")
+
+
+def make_workload(a, seed_offset=0):
+    from fwi_gb300 import synth
+    if a.config == 3:
+        a.shots = a.shots or 30
+        spec, vp_true, vp0 = synth.config3(seed=3 + seed_offset, nt=a.nt or None, nshots=a.shots)
+        a.nt = spec.nt
+    else:
+        a.shots = a.shots or 64
+        a.nt = a.nt or 6000
+        spec, vp_true, vp0 = synth.config2(seed=2 + seed_offset, nshots=a.shots, nt=a.nt)
+    return spec, vp_true, vp0
 
 
 def peaks():
@@ -156,10 +175,9 @@ def run_reference(a):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return 0
-    from fwi_gb300 import synth
-    spec, vp_true, vp0 = synth.config2(nshots=a.shots, nt=a.nt)
+    spec, vp_true, vp0 = make_workload(a)
     nthreads = os.cpu_count() or 1
-    nt_sample = 100
+    nt_sample = 100 if a.config == 2 else 40
     for _ in range(a.warmup):
         cpu_sample(spec, vp0, nthreads, nt_sample)
     times = []
@@ -199,14 +217,13 @@ def main():
     if world > 1:
         torch.distributed.init_process_group("nccl")
     import fwi_gb300 as F
-    from fwi_gb300 import synth
     from fwi_gb300.synth import lam_from_vp
 
     F.init(local)
     stream = torch.cuda.Stream()
     F.set_stream(stream.cuda_stream)
     snap_form = {"f32": F.SNAP_F32, "bf16": F.SNAP_BF16, "f16": F.SNAP_F16}[a.snap]
-    spec, vp_true, vp0 = synth.config2(seed=2 + rank, nshots=a.shots, nt=a.nt)
+    spec, vp_true, vp0 = make_workload(a, rank)
     lam_true, lam0 = lam_from_vp(vp_true), lam_from_vp(vp0)
 
     if a.profile:
@@ -363,7 +380,7 @@ def main():
     cpu = None
     if rank == 0 and world == 1 and not a.no_cpu:
         nthreads = os.cpu_count() or 1
-        rate, tcpu, desc = cpu_sample(spec, vp0, nthreads, 600)
+        rate, tcpu, desc = cpu_sample(spec, vp0, nthreads, 600 if a.config == 2 else 150)
         cpu = {"value": rate, "unit": METRIC, "cores": nthreads, "kind": "port", "sample": desc,
                "seconds": tcpu}
 
@@ -374,7 +391,8 @@ def main():
                 "observed data synthesised on the true model)",
                 "config": {"workload": workload_name(a), "shots_per_gpu": len(spec.shots), "wave_shots": wave,
                            "band_rows": band,
-                           "l2": "inputs larger than L2: 64 shots' wavefields (~1.8 GB) and snapshots (~134 GB)"},
+                           "l2": "inputs larger than L2 (wavefields of all shots of a wave and their snapshots: "
+                                 "tens to hundreds of GB)"},
                 "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "plain": plain, "gpu_launches": int(launches),
                 "clocks": clk}
         print(json.dumps(line), flush=True)

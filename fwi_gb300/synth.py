@@ -160,3 +160,72 @@ def small_survey(seed=0, ny=40, nxm=90, nshots=3, nt=200, acc=3, dpml=8, d=10.0,
     spec = SurveySpec(ny=ny, nx_model=nxm, d=d, dt=dt, nt=nt, shots=shots, store_snap=store_snap, acc=acc,
                       dpml=dpml, water_rows=rng.integers(0, 4, size=nxm).astype(np.int32))
     return spec, vp
+
+
+def model_crustal(seed=3, ny=600, nx=6000, d=25.0):
+    """Crustal model of the uneven-size WAS batch (150 x 15 km at 25 m):
+    water from the surface to a seeded seafloor near 3 km, sediments
+    1.8 -> 3 km/s (2 km thick), crust 5.5 -> 7 km/s, mantle 8 km/s below a
+    Moho at 12 km with seeded +-1 km topography.  Returns (vp, seafloor
+    depth per column in m)."""
+    rng = np.random.default_rng(seed)
+    x = (np.arange(nx) + 0.5) * d
+    z = (np.arange(ny) + 0.5) * d
+
+    def smooth_noise(amp, nmodes=6):
+        s = np.zeros(nx)
+        for _ in range(nmodes):
+            s += rng.uniform(-1, 1) * np.sin(2 * np.pi * x / rng.uniform(15e3, 80e3) + rng.uniform(0, 2 * np.pi))
+        return amp * s / max(np.abs(s).max(), 1e-9)
+
+    sea = 2800.0 + smooth_noise(200.0)
+    sed_base = sea + 2000.0
+    moho = 12000.0 + smooth_noise(1000.0)
+    Z = z[:, None]
+    vp = np.full((ny, nx), 1500.0)
+    sed = (Z >= sea) & (Z < sed_base)
+    vp = np.where(sed, 1800.0 + 1200.0 * (Z - sea) / 2000.0, vp)
+    crust = (Z >= sed_base) & (Z < moho)
+    vp = np.where(crust, 5500.0 + 1500.0 * (Z - sed_base) / np.maximum(moho - sed_base, 1.0), vp)
+    vp = np.where(Z >= moho, 8000.0, vp)
+    return _F(vp), sea
+
+
+def config3(seed=3, nt=None, nshots=30, freq=5.0, tfin=20.0):
+    """Uneven-size WAS batch (BASELINE config 3) with OBS as reciprocal
+    sources: 30 OBS at 5 km on the seafloor, 1200 surface receivers at 125 m
+    (10 m deep), each shot on its own window of 30-100 km (seeded).  The
+    stated dt = 2.5 ms violates the CFL limit at 8 km/s and 25 m, so the
+    reference's own rule dt = d/(2 vmax) (calculate_misfit_gradient.f90:198)
+    is used: 1.5625 ms, nt = 12800 for 20 s.  Returns (spec, vp_true, vp_start)."""
+    from .api import time_rules
+    rng = np.random.default_rng(seed + 1)
+    d = 25.0
+    vp, sea = model_crustal(seed)
+    ny, nxm = vp.shape
+    lam = lam_from_vp(vp)
+    dt, nt_full, _ = time_rules(lam, d, tfin, 10)
+    nt = nt_full if nt is None else nt
+    f32 = np.float32
+    grid = lambda pos: 1 + int(np.ceil(f32(abs(pos)) / f32(d)))  # noqa: E731  get_was_data.f90:155-159
+    rec_x = np.array([62.5 + 125.0 * j for j in range(1200)], np.float64)
+    rec_grid = np.array([grid(xr) for xr in rec_x], np.int32)
+    rec_row = grid(10.0)
+    shots = []
+    for i in range(nshots):
+        xo = 2500.0 + 5000.0 * i
+        xg = grid(xo)
+        zo = sea[min(xg - 1, nxm - 1)]          # OBS relocated to the seafloor (get_was_data.f90:112-115)
+        zg = grid(zo)
+        width = rng.uniform(30e3, 100e3)
+        c0 = max(0, int((xo - width / 2) / d))
+        c1 = min(nxm, int((xo + width / 2) / d))
+        inside = (rec_grid - 1 >= c0) & (rec_grid - 1 < c1)
+        nxr = (rec_grid[inside] - c0).astype(np.int32)
+        src = ricker_shifted(freq, float(dt), nt, 0.0).reshape(nt, 1, order="F")
+        shots.append(ShotSpec(x0=c0, nx=c1 - c0, nxSou=np.array([xg - c0], np.int32), nySou=np.array([zg], np.int32),
+                              nxRec=nxr, nyRec=np.full(nxr.size, rec_row, np.int32), src=_F(src)))
+    water = np.array([grid(s) for s in sea], np.int32)
+    spec = SurveySpec(ny=ny, nx_model=nxm, d=d, dt=float(dt), nt=nt, shots=shots, store_snap=10, acc=3, dpml=20,
+                      water_rows=water)
+    return spec, vp, smooth(vp, 6)

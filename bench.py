@@ -290,12 +290,12 @@ def main():
     r1.record(stream)
     torch.cuda.synchronize()
     step_s = r0.elapsed_time(r1) / 1e3 / nsteps
-    bytes_step = sv.step_bytes()
+    bytes_step = sv.step_bytes()  # the shots of the first wave, which time_steps advances
+    wave, band = sv.tuning()
     achieved = bytes_step / step_s / 1e9
     tr = traffic_from_profile()
-    wave, band = sv.tuning()
     roof = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
-            "traffic": tr * len(spec.shots) if tr else None,
+            "traffic": tr * wave if (tr and a.config == 2) else None,
             "kernel": "k_step_interior + k_step_boundary (one time step of all shots, concurrent streams)",
             "algorithmic_bytes_per_launch": bytes_step, "avg_launch_ms": step_s * 1e3,
             "peak_kind": f"{peak_kind} copy bandwidth (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured"

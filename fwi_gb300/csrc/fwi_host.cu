@@ -1564,7 +1564,7 @@ int fwi_survey_get_synthetic(fwi_survey* s, int shot, float* out) {
 int fwi_survey_step_bytes(fwi_survey* s, double* bytes) {
     if (!s || !bytes) return fail(FWI_ERR_STATE, "null argument");
     double b = 0.0;
-    for (auto& l : s->lays) b += step_bytes_shot(l.ny, l.nx, l.dn);
+    for (int sh : s->waves[0]) b += step_bytes_shot(s->lays[sh].ny, s->lays[sh].nx, s->lays[sh].dn);
     *bytes = b;
     return FWI_OK;
 }

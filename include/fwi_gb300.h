@@ -184,7 +184,8 @@ int fwi_survey_grad_device(fwi_survey* s, const double** ptr);
 /* Synthetic traces of shot i from the last run: Rec_point(nt, num_rec),
  * copied to host. */
 int fwi_survey_get_synthetic(fwi_survey* s, int shot, float* out);
-/* Sum of algorithmic HBM bytes of one forward step over all shots. */
+/* Algorithmic HBM bytes of one forward time step of the shots of the first
+ * wave (the unit fwi_survey_time_steps advances). */
 int fwi_survey_step_bytes(fwi_survey* s, double* bytes);
 /* Tuning chosen for the survey (wave size, band rows). */
 int fwi_survey_tuning(fwi_survey* s, int* wave_shots, int* band_rows);

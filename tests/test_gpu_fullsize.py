@@ -123,9 +123,15 @@ def test_config3_uneven_windows_truncated():
     import fwi_gb300 as F
     from fwi_gb300 import synth
     from fwi_gb300.synth import lam_from_vp
-    spec, vp_true, vp0 = synth.config3(nt=120)
+    spec, vp_true, vp0 = synth.config3(nt=150)
     order = np.argsort([s.nx for s in spec.shots])
     spec.shots = [spec.shots[i] for i in (order[0], order[len(order) // 2], order[-1])]
+    # 150 steps are too short for the seafloor OBS to reach the surface
+    # receivers: move the sources up next to them and keep the gradient
+    # unmasked, so that traces, misfit and imaging are all non-trivial
+    for sh in spec.shots:
+        sh.nySou = np.array([2], np.int32)
+    spec.water_rows = None
     lam_t, lam0 = lam_from_vp(vp_true), lam_from_vp(vp0)
     sv = F.Survey(spec)
     sv.set_lambda(lam_t)
@@ -145,7 +151,6 @@ def test_config3_uneven_windows_truncated():
     G = np.zeros((spec.ny, spec.nx_model))
     for sh, k in zip(spec.shots, kern):
         G[:, sh.x0:sh.x0 + sh.nx] += k
-    for i, kk in enumerate(spec.water_rows):
-        G[:kk, i] = 0.0
-    assert abs(m - m64.sum()) <= 1e-12 * abs(m64.sum())
+    assert m > 0 and abs(m - m64.sum()) <= 1e-12 * abs(m64.sum())
+    assert np.abs(G).max() > 0
     assert _rel(g.astype(np.float64), G) <= 1e-6

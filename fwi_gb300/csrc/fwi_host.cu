@@ -22,8 +22,8 @@
 #include "fwi_internal.cuh"
 
 namespace fwi {
-cudaError_t launch_step(int acc, int mode, const StepParams& pm, const StepParams& pb, cudaStream_t sm,
-                        cudaStream_t sb);
+cudaError_t launch_step(int acc, int mode, int kstrip, const StepParams& pm, const StepParams& pb, cudaStream_t sm,
+                        cudaStream_t sb, cudaStream_t ss);
 cudaError_t configure_step_kernels();
 cudaError_t launch_build_c2(float* c2, int nyt, int pitch, int off, int dn, int ny, int nx, const float* src, int ldv,
                             int x0, int from_lambda, float dt2, float d2, cudaStream_t st);
@@ -91,7 +91,8 @@ struct LibState {
     cudaStream_t own = nullptr;
     cudaStream_t user = nullptr;
     cudaStream_t aux = nullptr;      // bottom-row kernels run here, concurrently
-    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    cudaStream_t aux3 = nullptr;     // side-strip kernels run here, concurrently
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_join2 = nullptr;
     int prio_hi = 0;
     int acc = 3, dpml = 20;
     long long launches = 0;
@@ -187,6 +188,8 @@ void pml_factors(int acc, int dpml, float dt, float d, std::vector<float>& fA, s
 
 struct Layout {
     int ny, nx, dn, nyt, nxt, off, pitch, ntiles;
+    int sl, sr;   // side strips [0, sl) and [sr, nxt), interior columns [sl, sr)
+    int kstrip;   // columns per lane of a strip warp: strips are at most 32*kstrip wide
 };
 
 Layout make_layout(int ny, int nx, int acc, int dpml) {
@@ -201,6 +204,12 @@ Layout make_layout(int ny, int nx, int acc, int dpml) {
     if (r0 < l.dn - 1) l.off = ((l.dn - 1 - r0) + 3) / 4 * 4;
     l.ntiles = (l.off + l.nxt + TILE - 1) / TILE;
     l.pitch = l.ntiles * TILE;
+    // side strips: each holds its dn CPML columns and at most 32*kstrip
+    // columns; in narrow grids they share the interior columns between them
+    l.kstrip = (l.dn + 31) / 32;
+    const int sw = 32 * l.kstrip;
+    l.sl = std::min(sw, l.dn + nx / 2);
+    l.sr = std::max(l.nxt - sw, l.sl);
     return l;
 }
 
@@ -261,7 +270,8 @@ int validate_geometry(const ShotGeom& g, const Layout& l, int shot) {
 // inject the sources and record the receivers, adjoint lists inject the
 // adjoint sources at the receivers.
 struct Lists {
-    std::vector<WorkItem> int_fwd, int_adj, bnd_fwd, bnd_adj;
+    std::vector<WorkItem> int_fwd, int_adj, bnd_fwd, bnd_adj;  // boundary lists: nstrip strips, then bottom tiles
+    int nstrip = 0, kstrip = 1;
     std::vector<SrcEnt> src_fwd, src_adj;
     std::vector<RecEnt> recs;
 };
@@ -281,15 +291,17 @@ std::vector<SrcEnt> injection_cells(const std::vector<int>& xs, const std::vecto
     return out;
 }
 
+// One work item; its sources and receivers are the cells of physical
+// columns [c0, c1) in rows [y0, y1).
 void append_item(Lists& L_, std::vector<WorkItem>& items, std::vector<SrcEnt>& srcs, const std::vector<SrcEnt>& cells,
-                 const std::vector<RecEnt>& recs_shot, int shot, int tile, int y0, int y1, int kind, bool with_recs) {
+                 const std::vector<RecEnt>& recs_shot, int shot, int tile, int y0, int y1, int kind, bool with_recs,
+                 int c0, int c1) {
     WorkItem it{};
     it.shot = shot;
     it.tile = tile;
     it.y0 = y0;
     it.y1 = y1;
     it.kind = kind;
-    const int c0 = tile * TILE, c1 = c0 + TILE;
     std::vector<SrcEnt> sel;
     for (auto& c : cells)
         if (c.row >= y0 && c.row < y1 && c.col >= c0 && c.col < c1) sel.push_back(c);
@@ -310,10 +322,21 @@ void append_item(Lists& L_, std::vector<WorkItem>& items, std::vector<SrcEnt>& s
 }
 
 constexpr int BOTTOM_BAND = 9;  // rows per bottom-pad work item
+constexpr int STRIP_BAND = 16;  // rows per side-strip work item
 
 // Work lists for a set of shots (local shot index = position in `geoms`).
+// All shots share dn (one acc / dpml per launch), hence one kstrip.
 Lists build_lists(const std::vector<ShotGeom>& geoms, const std::vector<Layout>& lays, int band_rows) {
     Lists out;
+    std::vector<WorkItem> strip_f, strip_a, bot_f, bot_a;
+    if (!lays.empty()) out.kstrip = lays[0].kstrip;
+    auto bands = [](int n, int rows, auto&& fn) {
+        const int nb = std::max(1, (n + rows - 1) / rows);
+        for (int b = 0; b < nb; ++b) {
+            const int y0 = (int)((long long)n * b / nb), y1 = (int)((long long)n * (b + 1) / nb);
+            if (y1 > y0) fn(y0, y1);
+        }
+    };
     for (size_t s = 0; s < geoms.size(); ++s) {
         const Layout& l = lays[s];
         const ShotGeom& g = geoms[s];
@@ -325,37 +348,47 @@ Lists build_lists(const std::vector<ShotGeom>& geoms, const std::vector<Layout>&
             if (pr < l.dn) continue;  // top pad: identically zero, never recorded
             recs.push_back(RecEnt{pr, l.off + pc, (int)i});
         }
-        // interior tiles in bands of band_rows; the heavier edge tiles (CPML
-        // strips) in thinner bands so that the boundary kernel has warps enough
-        for (int pass = 0; pass < 2; ++pass) {
-            const int rows = pass == 0 ? band_rows : std::min(band_rows, 16);
-            const int nb = std::max(1, (l.ny + rows - 1) / rows);
-            for (int b = 0; b < nb; ++b) {
-                const int y0 = l.dn + (int)((long long)l.ny * b / nb);
-                const int y1 = l.dn + (int)((long long)l.ny * (b + 1) / nb);
-                if (y1 <= y0) continue;
-                for (int t = 0; t < l.ntiles; ++t) {
-                    const bool edge = (t == 0) || (t == l.ntiles - 1);
-                    if (edge != (pass == 1)) continue;
-                    append_item(out, edge ? out.bnd_fwd : out.int_fwd, out.src_fwd, cells_f, recs, (int)s, t, y0, y1,
-                                0, true);
-                    append_item(out, edge ? out.bnd_adj : out.int_adj, out.src_adj, cells_a, recs, (int)s, t, y0, y1,
-                                0, false);
+        // interior columns [sl, sr): 128-column tiles in bands of band_rows
+        const int xa = l.off + l.sl, xb = l.off + l.sr;
+        if (xa < xb) {
+            bands(l.ny, band_rows, [&](int y0, int y1) {
+                for (int t = xa / TILE; t <= (xb - 1) / TILE; ++t) {
+                    const int c0 = std::max(t * TILE, xa), c1 = std::min((t + 1) * TILE, xb);
+                    append_item(out, out.int_fwd, out.src_fwd, cells_f, recs, (int)s, t, l.dn + y0, l.dn + y1, 0,
+                                true, c0, c1);
+                    append_item(out, out.int_adj, out.src_adj, cells_a, recs, (int)s, t, l.dn + y0, l.dn + y1, 0,
+                                false, c0, c1);
                 }
-            }
+            });
         }
+        // side strips of the model rows
+        bands(l.ny, STRIP_BAND, [&](int y0, int y1) {
+            for (int side = 0; side < 2; ++side) {
+                const int c0 = l.off + (side ? l.sr : 0), c1 = l.off + (side ? l.nxt : l.sl);
+                if (c1 <= c0) continue;
+                append_item(out, strip_f, out.src_fwd, cells_f, recs, (int)s, side, l.dn + y0, l.dn + y1, 2, true,
+                            c0, c1);
+                append_item(out, strip_a, out.src_adj, cells_a, recs, (int)s, side, l.dn + y0, l.dn + y1, 2, false,
+                            c0, c1);
+            }
+        });
         // bottom pad in bands of about BOTTOM_BAND rows (the y-phi is ping-ponged,
         // so bands are independent)
         std::vector<SrcEnt> none;
-        const int nbb = std::max(1, (l.dn + BOTTOM_BAND - 1) / BOTTOM_BAND);
-        for (int b = 0; b < nbb; ++b) {
-            const int y0 = l.nyt - l.dn + l.dn * b / nbb, y1 = l.nyt - l.dn + l.dn * (b + 1) / nbb;
+        bands(l.dn, BOTTOM_BAND, [&](int j0, int j1) {
             for (int t = 0; t < l.ntiles; ++t) {
-                append_item(out, out.bnd_fwd, out.src_fwd, none, recs, (int)s, t, y0, y1, 1, true);
-                append_item(out, out.bnd_adj, out.src_adj, none, recs, (int)s, t, y0, y1, 1, false);
+                append_item(out, bot_f, out.src_fwd, none, recs, (int)s, t, l.nyt - l.dn + j0, l.nyt - l.dn + j1, 1,
+                            true, t * TILE, (t + 1) * TILE);
+                append_item(out, bot_a, out.src_adj, none, recs, (int)s, t, l.nyt - l.dn + j0, l.nyt - l.dn + j1, 1,
+                            false, t * TILE, (t + 1) * TILE);
             }
-        }
+        });
     }
+    out.nstrip = (int)strip_f.size();
+    out.bnd_fwd = strip_f;
+    out.bnd_fwd.insert(out.bnd_fwd.end(), bot_f.begin(), bot_f.end());
+    out.bnd_adj = strip_a;
+    out.bnd_adj.insert(out.bnd_adj.end(), bot_a.begin(), bot_a.end());
     return out;
 }
 
@@ -415,7 +448,7 @@ struct ShotState {
         TRY(phy2.ensure(field_bytes));
         TRY(chy.ensure(field_bytes));
         TRY(snaps.ensure(snap_bytes));
-        TRY(sscale.ensure((size_t)nsnap_blocks * l.ny * l.ntiles * sizeof(float)));
+        TRY(sscale.ensure((size_t)nsnap_blocks * l.ny * (l.ntiles + 2) * sizeof(float)));
         TRY(k.ensure((size_t)l.ny * l.pitch * (grad_form == FWI_GRAD_F64 ? 8 : 4)));
         return FWI_OK;
     }
@@ -454,6 +487,8 @@ struct ShotState {
         d.pitch = lay.pitch;
         d.ntiles = lay.ntiles;
         d.dn = lay.dn;
+        d.sl = lay.sl;
+        d.sr = lay.sr;
         d.nt = nt;
         d.nrec = nrec;
         d.x0 = x0;
@@ -481,25 +516,39 @@ StepParams base_params(int acc, float dt, int store_snap, int snap_form, int gra
 }
 
 struct StepSet {
-    StepParams pm, pb;
+    StepParams pm, pb;  // interior list; boundary list (pb.nstrip side strips, then bottom tiles)
+    int kstrip = 1;
 };
 
-// One time step: model rows on st, bottom rows on st2, both ordered after
-// the previous step and before the next one.
+int step_kernels(const StepSet& ps) {
+    return (ps.pm.nitems > 0) + (ps.pb.nstrip > 0) + (ps.pb.nitems > ps.pb.nstrip);
+}
+
+// One time step: interior tiles on st, bottom tiles on st2, side strips on
+// the library's third stream, all three ordered after the previous step and
+// before the next one.  Streams fork only when st itself gets a kernel (a
+// wait on an event with no new node on st in between would accumulate
+// dependencies under stream capture).
 int step_fork_join(int acc, int mode, const StepSet& ps, cudaStream_t st, cudaStream_t st2) {
-    if (ps.pm.nitems == 0 || ps.pb.nitems == 0) {
-        // one kernel only: no fork.  (A wait on an event with no new node on
-        // st in between would accumulate dependencies under stream capture.)
-        CK(launch_step(acc, mode, ps.pm, ps.pb, st, st));
-        L().launches += (ps.pm.nitems > 0) + (ps.pb.nitems > 0);
+    const bool has_m = ps.pm.nitems > 0, has_s = ps.pb.nstrip > 0, has_b = ps.pb.nitems > ps.pb.nstrip;
+    L().launches += step_kernels(ps);
+    if (!has_m || (!has_s && !has_b)) {
+        CK(launch_step(acc, mode, ps.kstrip, ps.pm, ps.pb, st, st, st));
         return FWI_OK;
     }
+    cudaStream_t st3 = L().aux3;
     CK(cudaEventRecord(L().ev_fork, st));
-    CK(cudaStreamWaitEvent(st2, L().ev_fork, 0));
-    CK(launch_step(acc, mode, ps.pm, ps.pb, st, st2));
-    CK(cudaEventRecord(L().ev_join, st2));
-    CK(cudaStreamWaitEvent(st, L().ev_join, 0));
-    L().launches += (ps.pm.nitems > 0) + (ps.pb.nitems > 0);
+    if (has_b) CK(cudaStreamWaitEvent(st2, L().ev_fork, 0));
+    if (has_s) CK(cudaStreamWaitEvent(st3, L().ev_fork, 0));
+    CK(launch_step(acc, mode, ps.kstrip, ps.pm, ps.pb, st, st2, st3));
+    if (has_b) {
+        CK(cudaEventRecord(L().ev_join, st2));
+        CK(cudaStreamWaitEvent(st, L().ev_join, 0));
+    }
+    if (has_s) {
+        CK(cudaEventRecord(L().ev_join2, st3));
+        CK(cudaStreamWaitEvent(st, L().ev_join2, 0));
+    }
     return FWI_OK;
 }
 
@@ -579,8 +628,14 @@ int fwi_init(int device) {
         CK(cudaStreamCreateWithPriority(&L().aux, cudaStreamNonBlocking, hi));
         L().prio_hi = hi;
     }
+    if (!L().aux3) {
+        int lo = 0, hi = 0;
+        CK(cudaDeviceGetStreamPriorityRange(&lo, &hi));
+        CK(cudaStreamCreateWithPriority(&L().aux3, cudaStreamNonBlocking, hi));
+    }
     if (!L().ev_fork) CK(cudaEventCreateWithFlags(&L().ev_fork, cudaEventDisableTiming));
     if (!L().ev_join) CK(cudaEventCreateWithFlags(&L().ev_join, cudaEventDisableTiming));
+    if (!L().ev_join2) CK(cudaEventCreateWithFlags(&L().ev_join2, cudaEventDisableTiming));
     CK(configure_step_kernels());
     L().device = device;
     L().init = true;
@@ -596,10 +651,12 @@ int fwi_finalize(void) {
     new (&s) Single();
     if (L().own) cudaStreamDestroy(L().own);
     if (L().aux) cudaStreamDestroy(L().aux);
+    if (L().aux3) cudaStreamDestroy(L().aux3);
     if (L().ev_fork) cudaEventDestroy(L().ev_fork);
     if (L().ev_join) cudaEventDestroy(L().ev_join);
-    L().own = L().aux = nullptr;
-    L().ev_fork = L().ev_join = nullptr;
+    if (L().ev_join2) cudaEventDestroy(L().ev_join2);
+    L().own = L().aux = L().aux3 = nullptr;
+    L().ev_fork = L().ev_join = L().ev_join2 = nullptr;
     L().user = nullptr;
     L().init = false;
     return FWI_OK;
@@ -725,6 +782,8 @@ int fwi_solver_acoustic_ss(const int* rank, const int* iprop_, const int* NumSou
     ps.pb = ps.pm;
     ps.pb.items = sg.d_items_b.as<WorkItem>();
     ps.pb.nitems = (int)(adj ? lists.bnd_adj.size() : lists.bnd_fwd.size());
+    ps.pb.nstrip = lists.nstrip;
+    ps.kstrip = lists.kstrip;
     TRY(run_time_loop(acc, adj ? 1 : 0, nt, store_snap, nt_store, iprop == 1, ps, st, L().aux));
 
     if (!adj) LK(launch_rec_last(sg.d_rec.as<float>(), nt, NumRec, st));
@@ -887,7 +946,7 @@ struct fwi_survey {
     // per-wave lists
     struct WaveDev {
         DBuf items_if, items_ia, items_bf, items_ba, src_f, src_a, recs, shots_f, shots_a, stack;
-        int n_if = 0, n_ia = 0, n_bf = 0, n_ba = 0;
+        int n_if = 0, n_ia = 0, n_bf = 0, n_ba = 0, n_strip = 0, kstrip = 1;
         cudaGraphExec_t graph[3] = {nullptr, nullptr, nullptr};
         long long graph_kernels[3] = {0, 0, 0};  // kernel nodes per graph
         DBuf save_jobs, restore_jobs;  // checkpoint copies: [ckpt][shot][field]
@@ -911,7 +970,7 @@ namespace {
 size_t shot_wave_bytes(const Layout& l, int nt_store, int snap_form, int grad_form) {
     const size_t fb = (size_t)l.nyt * l.pitch * 4;
     const size_t esz = snap_form == FWI_SNAP_F32 ? 4 : 2;
-    const size_t sb = (size_t)(nt_store + 1) * l.ny * l.pitch * esz + (size_t)(nt_store + 1) * l.ny * l.ntiles * 4;
+    const size_t sb = (size_t)(nt_store + 1) * l.ny * l.pitch * esz + (size_t)(nt_store + 1) * l.ny * (l.ntiles + 2) * 4;
     const size_t kb = (size_t)l.ny * l.pitch * (grad_form == FWI_GRAD_F64 ? 8 : 4);
     return 8 * fb + sb + kb;
 }
@@ -982,6 +1041,8 @@ int survey_prepare_waves(fwi_survey* s) {
         wd->n_ia = (int)lists.int_adj.size();
         wd->n_bf = (int)lists.bnd_fwd.size();
         wd->n_ba = (int)lists.bnd_adj.size();
+        wd->n_strip = lists.nstrip;
+        wd->kstrip = lists.kstrip;
         s->wdev.push_back(std::move(wd));
     }
     // per-wave shot descriptors (fwd: sources; adj: adjoint source table)
@@ -997,7 +1058,7 @@ int survey_prepare_waves(fwi_survey* s) {
                                 s->d_synth.as<float>() + (size_t)s->tr_off[sh] * D.nt);
             dv.snap_stride = (long long)l.ny * l.pitch;
             dv.ny = l.ny; dv.nx = l.nx; dv.nyt = l.nyt; dv.nxt = l.nxt; dv.off = l.off; dv.pitch = l.pitch;
-            dv.ntiles = l.ntiles; dv.dn = l.dn;
+            dv.ntiles = l.ntiles; dv.dn = l.dn; dv.sl = l.sl; dv.sr = l.sr;
             // forward value table: this shot's sources (packed in shot order)
             size_t soff = 0;
             for (int q = 0; q < sh; ++q) soff += s->geoms[q].nxS.size();
@@ -1118,7 +1179,7 @@ int zero_slot0(fwi_survey* s, size_t wi, cudaStream_t st) {
         const Layout& l = s->lays[s->waves[wi][k]];
         const size_t esz = D.snap_form == FWI_SNAP_F32 ? 4 : 2;
         CK(cudaMemsetAsync(ss.snaps.p, 0, (size_t)l.ny * l.pitch * esz, st));
-        CK(cudaMemsetAsync(ss.sscale.p, 0, (size_t)l.ny * l.ntiles * sizeof(float), st));
+        CK(cudaMemsetAsync(ss.sscale.p, 0, (size_t)l.ny * (l.ntiles + 2) * sizeof(float), st));
     }
     return FWI_OK;
 }
@@ -1185,6 +1246,8 @@ int rc_adjoint(fwi_survey* s, size_t wi, StepSet ps, cudaStream_t st, cudaStream
     psf.pb = psf.pm;
     psf.pb.items = wd.items_bf.as<WorkItem>();
     psf.pb.nitems = wd.n_bf;
+    psf.pb.nstrip = wd.n_strip;
+    psf.kstrip = wd.kstrip;
     ps.pm.items = wd.items_ia.as<WorkItem>();
     ps.pm.nitems = wd.n_ia;
     ps.pm.shots = wd.shots_a.as<ShotDev>();
@@ -1193,6 +1256,8 @@ int rc_adjoint(fwi_survey* s, size_t wi, StepSet ps, cudaStream_t st, cudaStream
     ps.pb = ps.pm;
     ps.pb.items = wd.items_ba.as<WorkItem>();
     ps.pb.nitems = wd.n_ba;
+    ps.pb.nstrip = wd.n_strip;
+    ps.kstrip = wd.kstrip;
     int cur = s->rc_J - 1;
     size_t evi = 0;
     int snap = s->nt_store;
@@ -1240,7 +1305,7 @@ int issue_wave(fwi_survey* s, size_t wi, int step, cudaStream_t st, cudaStream_t
         if (step == 1 && !s->rc_C) {
             const size_t esz = D.snap_form == FWI_SNAP_F32 ? 4 : 2;
             CK(cudaMemsetAsync(ss.snaps.p, 0, (size_t)l.ny * l.pitch * esz, st));
-            CK(cudaMemsetAsync(ss.sscale.p, 0, (size_t)l.ny * l.ntiles * sizeof(float), st));
+            CK(cudaMemsetAsync(ss.sscale.p, 0, (size_t)l.ny * (l.ntiles + 2) * sizeof(float), st));
         }
         LK(launch_build_c2(ss.c2.as<float>(), l.nyt, l.pitch, l.off, l.dn, l.ny, l.nx, s->d_lambda.as<float>(), D.ny,
                            s->geoms[sh].x0, 1, D.dt * D.dt, D.d * D.d, st));
@@ -1258,6 +1323,8 @@ int issue_wave(fwi_survey* s, size_t wi, int step, cudaStream_t st, cudaStream_t
     ps.pb = ps.pm;
     ps.pb.items = wd.items_bf.as<WorkItem>();
     ps.pb.nitems = wd.n_bf;
+    ps.pb.nstrip = wd.n_strip;
+    ps.kstrip = wd.kstrip;
     if (s->rc_C) {
         TRY(rc_forward(s, wi, step, ps, st, st2));
     } else {
@@ -1298,6 +1365,8 @@ int issue_wave(fwi_survey* s, size_t wi, int step, cudaStream_t st, cudaStream_t
     ps.pb = ps.pm;
     ps.pb.items = wd.items_ba.as<WorkItem>();
     ps.pb.nitems = wd.n_ba;
+    ps.pb.nstrip = wd.n_strip;
+    ps.kstrip = wd.kstrip;
     TRY(run_time_loop(D.acc, 1, D.nt, D.store_snap, s->nt_store, true, ps, st, st2));
     LK(launch_stack(s->d_G.as<double>(), D.ny, D.nx_model, wd.stack.p, (int)w.size(), D.grad_form, st));
     return FWI_OK;
@@ -1408,7 +1477,7 @@ int fwi_survey_create(const fwi_survey_desc* desc, fwi_survey** out) {
         size_t fb = 0, bb = 0, kb = 0;
         for (auto& l : s->lays) {
             fb = std::max(fb, (size_t)l.nyt * l.pitch * 4);
-            bb = std::max(bb, (size_t)l.ny * l.pitch * (D.snap_form == FWI_SNAP_F32 ? 4 : 2) + (size_t)l.ny * l.ntiles * 4);
+            bb = std::max(bb, (size_t)l.ny * l.pitch * (D.snap_form == FWI_SNAP_F32 ? 4 : 2) + (size_t)l.ny * (l.ntiles + 2) * 4);
             kb = std::max(kb, (size_t)l.ny * l.pitch * (D.grad_form == FWI_GRAD_F64 ? 8 : 4));
         }
         const int ss = D.store_snap;
@@ -1606,6 +1675,8 @@ int time_wave0_steps(fwi_survey* s, int steps, float* ms) {
     ps.pb = ps.pm;
     ps.pb.items = wd.items_bf.as<WorkItem>();
     ps.pb.nitems = wd.n_bf;
+    ps.pb.nstrip = wd.n_strip;
+    ps.kstrip = wd.kstrip;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     if (ms) {
         CK(cudaEventCreate(&e0));
@@ -1795,7 +1866,7 @@ extern "C" int fwi_solver_forward_noalloc(int NumSou, int NumRec, const int* nxS
     sd.srcv = S_dev;
     sd.rec = Rec_point_dev;
     sd.ny = l.ny; sd.nx = l.nx; sd.nyt = l.nyt; sd.nxt = l.nxt; sd.off = l.off; sd.pitch = l.pitch;
-    sd.ntiles = l.ntiles; sd.dn = l.dn; sd.nt = nt; sd.nrec = NumRec;
+    sd.ntiles = l.ntiles; sd.dn = l.dn; sd.sl = l.sl; sd.sr = l.sr; sd.nt = nt; sd.nrec = NumRec;
     auto put = [&](size_t at, const void* src, size_t bytes) -> int {
         if (bytes) CK(cudaMemcpyAsync(sb + at, src, bytes, cudaMemcpyHostToDevice, st));
         return FWI_OK;
@@ -1820,6 +1891,8 @@ extern "C" int fwi_solver_forward_noalloc(int NumSou, int NumRec, const int* nxS
     ps.pb = ps.pm;
     ps.pb.items = reinterpret_cast<WorkItem*>(sb + o_bm);
     ps.pb.nitems = (int)lists.bnd_fwd.size();
+    ps.pb.nstrip = lists.nstrip;
+    ps.kstrip = lists.kstrip;
     TRY(run_time_loop(acc, 0, nt, nt + 1, 0, false, ps, st, L().aux));
     LK(launch_rec_last(Rec_point_dev, nt, NumRec, st));
     CK(cudaStreamSynchronize(st));

@@ -5,9 +5,14 @@
 //   row pitch `pitch` floats (a multiple of TILE = 128), logical padded column
 //   c stored at physical column off + c.  `off` (a multiple of 4) is chosen so
 //   that the first 128-column tile holds the whole left CPML strip and the
-//   last tile holds the whole right strip; every other tile is interior.
-//   One warp owns one tile (4 columns per lane, float4) and marches down a
-//   band of rows with a register queue of 2*acc+1 rows.
+//   last tile holds the whole right strip.
+//   Model rows are split by column: the side strips [0, sl) and [sr, nxt)
+//   (each at most 32*ceil(dn/32) columns wide, holding the x-CPML columns)
+//   go to one warp per band with one column per lane; the interior columns
+//   [sl, sr) go to 128-column tiles, one warp per tile and band (4 columns
+//   per lane, float4), with stores masked to [sl, sr) in the two partial
+//   tiles.  Bottom pad rows go to 128-column tiles of the whole width.
+//   Every warp marches down its band with a register queue of 2*acc+1 rows.
 #pragma once
 #include <cstdint>
 #include <cuda_runtime.h>
@@ -30,9 +35,9 @@ struct RecEnt {                 // one recorded receiver
 
 struct WorkItem {               // one warp's work in a step launch
     int shot;
-    int tile;                   // tile index (x0 = tile*TILE physical)
+    int tile;                   // tile index (x0 = tile*TILE physical); side strip: 0 left, 1 right
     int y0, y1;                 // padded rows [y0, y1)
-    int kind;                   // 0 = model rows, 1 = bottom pad rows
+    int kind;                   // 0 = interior model rows, 1 = bottom pad rows, 2 = side strip
     int s0, s1;                 // SrcEnt range (sorted by row)
     int r0, r1;                 // RecEnt range (sorted by row)
     int pad_;
@@ -50,7 +55,7 @@ struct ShotDev {
     const float* srcv;          // injected values [vidx][nt]
     float* rec;                 // Rec_point(nt, nrec) column-major
     void* snaps;                // snapshots [s][ny][pitch] (float / 16-bit)
-    float* sscale;              // 16-bit snapshot scales [s][ny][ntiles]
+    float* sscale;              // 16-bit snapshot scales [s][ny][ntiles + 2] (tiles, then the two side strips)
     float* k32;                 // FP32 imaging accumulator [ny][pitch]
     double* k64;                // FP64 imaging accumulator [ny][pitch]
     long long snap_stride;      // elements per snapshot block (ny*pitch)
@@ -58,6 +63,7 @@ struct ShotDev {
     int off, pitch, ntiles, dn;
     int nt, nrec;
     int x0;                     // window start in the full model
+    int sl, sr;                 // interior columns [sl, sr) (logical); side strips [0, sl), [sr, nxt)
     int pad_;
 };
 
@@ -69,6 +75,7 @@ struct StepParams {
     const float* fA;            // CPML factors (dn entries, 0-based)
     const float* fB;
     int nitems;
+    int nstrip;                 // boundary list: the first nstrip items are side strips (kind 2)
     int t;                      // k-2: source column / receiver row this step
     int parity;                 // k & 1: which buffer holds p_1 (written as p_3)
     int snap;                   // snapshot block this step, -1 if none

@@ -1,28 +1,31 @@
 // FWI time-step kernels for sm_103a.
 //
-// One launch of k_step_main plus one of k_step_bottom advance every shot of a
-// wave by one time step of the reference solver (solver_acoustic_SS.f90:313-586):
+// Three launches advance every shot of a wave by one time step of the
+// reference solver (solver_acoustic_SS.f90:313-586):
 //
-//   k_step_main    model rows dn..dn+ny-1: interior update with source
-//                  injection (:319-330, :433-434), left/right CPML strips
-//                  (pml_matrices_x, solver_PML_matrices.f90:1-40), snapshot
-//                  store (:438-454) or imaging condition (:457-473),
-//                  receiver recording (:551-555);
-//   k_step_bottom  bottom pad rows: bottom CPML strip (pml_matrices_y
-//                  :42-81) and the two bottom corners in two stages
-//                  (pml_matrices_xycorner :83-112, solver_acoustic_SS.f90:395-411).
+//   k_step_interior  model rows dn..dn+ny-1, interior columns: interior
+//                    update with source injection (:319-330, :433-434),
+//                    snapshot store (:438-454) or imaging condition
+//                    (:457-473), receiver recording (:551-555);
+//   k_step_strip     model rows, the two side strips: left/right CPML strips
+//                    (pml_matrices_x, solver_PML_matrices.f90:1-40) with the
+//                    grid-edge clamps, and the interior columns next to them;
+//   k_step_bottom    bottom pad rows: bottom CPML strip (pml_matrices_y
+//                    :42-81) and the two bottom corners in two stages
+//                    (pml_matrices_xycorner :83-112, solver_acoustic_SS.f90:395-411).
 //
 // The top pad rows are never written: with the free surface they stay
 // exactly zero for the whole run (solver_acoustic_SS.f90:416-429, :477-479).
 //
-// Every warp owns a 128-column tile (4 columns per lane, float4) and marches
-// down a band of rows; the y-stencil comes from a register queue of 2R+1
-// rows, the x-stencil from warp shuffles of the current row plus one halo
-// float4 at each end of the tile.  The wavefield is ping-ponged between two
-// buffers: p_3 overwrites p_1 in place (each cell reads its own p_1 only).
-// The CPML memory variables are updated in place: the strip-local
-// derivative of phi only reads phi values of the same warp, loaded before
-// they are overwritten.
+// Interior and bottom warps own a 128-column tile (4 columns per lane,
+// float4) and march down a band of rows; the y-stencil comes from a register
+// queue of 2R+1 rows, the x-stencil from warp shuffles of the current row
+// plus one halo float4 at each end of the tile.  Strip warps hold one column
+// per lane.  The wavefield is ping-ponged between two buffers: p_3
+// overwrites p_1 in place (each cell reads its own p_1 only), and every cell
+// is written by exactly one warp.  The CPML memory variables are updated in
+// place: the strip-local derivative of phi only reads phi values of the same
+// warp, loaded before they are overwritten.
 //
 // This file is compiled with --fmad=false: every a*b+c below is a rounded
 // multiply followed by a rounded add, in the order the Fortran source writes
@@ -100,31 +103,6 @@ __device__ __forceinline__ void yderivs(const float4* q, const StepParams& P, fl
         }
         d2[e] = s2;
         d1[e] = s1;
-    }
-}
-
-// Second derivatives only (interior cells need no first derivative).
-template <int R>
-__device__ __forceinline__ void xderiv2(const float* w, const StepParams& P, float* d2) {
-#pragma unroll
-    for (int e = 0; e < 4; ++e) {
-        float s2 = 0.f;
-#pragma unroll
-        for (int i = 0; i <= R; ++i) s2 = s2 + P.c2[i] * (w[4 + e + i] + w[4 + e - i]);
-        d2[e] = s2;
-    }
-}
-template <int R>
-__device__ __forceinline__ void yderiv2(const float4* q, const StepParams& P, float* d2) {
-    float a[2 * R + 1][4];
-#pragma unroll
-    for (int i = 0; i <= 2 * R; ++i) to_arr(q[i], a[i]);
-#pragma unroll
-    for (int e = 0; e < 4; ++e) {
-        float s2 = 0.f;
-#pragma unroll
-        for (int i = 0; i <= R; ++i) s2 = s2 + (a[R + i][e] + a[R - i][e]) * P.c2[i];
-        d2[e] = s2;
     }
 }
 
@@ -213,21 +191,22 @@ __device__ __forceinline__ void phi_xderiv(const ShotDev& S, const StepParams& P
 
 // Snapshot store (forward) of the interior cells of one row:
 // Fields(j, snap*nx+i) = (p_3 - p_1)*0.5/dt   (solver_acoustic_SS.f90:447)
-__device__ __forceinline__ void store_snapshot(const StepParams& P, const ShotDev& S, int yrow, int lane, int x0,
-                                               int xl, int c0, const float* p3, const float* pm1, int tile) {
-    const int dn = S.dn, nx = S.nx;
+// This lane stores elements [lo, hi) of its 4 columns; `seg` is the row
+// segment whose scale the 16-bit forms use.
+__device__ __forceinline__ void store_snapshot(const StepParams& P, const ShotDev& S, int yrow, int lane, int xl,
+                                               int lo, int hi, const float* p3, const float* pm1, int seg) {
     float v[4];
     bool in[4];
 #pragma unroll
     for (int e = 0; e < 4; ++e) {
-        const int c = c0 + e;
-        in[e] = (c >= dn) && (c < dn + nx);
+        in[e] = (e >= lo) && (e < hi);
         v[e] = in[e] ? ((p3[e] - pm1[e]) * 0.5f) / P.dt : 0.f;
     }
+    const bool full = in[0] && in[3];
     const size_t base = (size_t)P.snap * (size_t)S.snap_stride + (size_t)yrow * S.pitch + xl;
     if (P.snap_form == 0) {
         float* F = reinterpret_cast<float*>(S.snaps) + base;
-        if (in[0] && in[3]) {
+        if (full) {
             st4(F, from_arr(v));
         } else {
 #pragma unroll
@@ -236,8 +215,8 @@ __device__ __forceinline__ void store_snapshot(const StepParams& P, const ShotDe
         }
         return;
     }
-    // 16-bit forms: power-of-two scale per 128-column row segment so that the
-    // largest magnitude maps below 2^14 (exact scaling, no extra rounding).
+    // 16-bit forms: power-of-two scale per row segment so that the largest
+    // magnitude maps below 2^14 (exact scaling, no extra rounding).
     float m = fmaxf(fmaxf(fabsf(v[0]), fabsf(v[1])), fmaxf(fabsf(v[2]), fabsf(v[3])));
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(FULL, m, o));
@@ -257,7 +236,7 @@ __device__ __forceinline__ void store_snapshot(const StepParams& P, const ShotDe
         }
     }
     unsigned short* F = reinterpret_cast<unsigned short*>(S.snaps) + base;
-    if (in[0] && in[3]) {
+    if (full) {
         uint2 pk;
         pk.x = (unsigned)h[0] | ((unsigned)h[1] << 16);
         pk.y = (unsigned)h[2] | ((unsigned)h[3] << 16);
@@ -267,67 +246,7 @@ __device__ __forceinline__ void store_snapshot(const StepParams& P, const ShotDe
         for (int e = 0; e < 4; ++e)
             if (in[e]) F[e] = h[e];
     }
-    if (lane == 0) {
-        S.sscale[((size_t)P.snap * S.ny + yrow) * S.ntiles + tile] = ldexpf(1.f, -sh);
-    }
-}
-
-// Imaging condition (adjoint): kernel += -0.5*(p_3-p_1)*Fields(snap)*store_snap
-// (solver_acoustic_SS.f90:465-466)
-__device__ __forceinline__ void image_row(const StepParams& P, const ShotDev& S, int yrow, int xl, int c0,
-                                          const float* p3, const float* pm1, int tile) {
-    const int dn = S.dn, nx = S.nx;
-    const size_t base = (size_t)P.snap * (size_t)S.snap_stride + (size_t)yrow * S.pitch + xl;
-    float F[4];
-    if (P.snap_form == 0) {
-        to_arr(ldg4(reinterpret_cast<const float*>(S.snaps) + base), F);
-    } else {
-        const uint2 pk = __ldg(reinterpret_cast<const uint2*>(reinterpret_cast<const unsigned short*>(S.snaps) + base));
-        const unsigned short h[4] = {(unsigned short)(pk.x & 0xffffu), (unsigned short)(pk.x >> 16),
-                                     (unsigned short)(pk.y & 0xffffu), (unsigned short)(pk.y >> 16)};
-        const float sc = __ldg(S.sscale + ((size_t)P.snap * S.ny + yrow) * S.ntiles + tile);
-#pragma unroll
-        for (int e = 0; e < 4; ++e) {
-            float f;
-            if (P.snap_form == 1) f = __bfloat162float(*reinterpret_cast<const __nv_bfloat16*>(&h[e]));
-            else f = __half2float(*reinterpret_cast<const __half*>(&h[e]));
-            F[e] = f * sc;
-        }
-    }
-    float k2[4];
-    bool in[4];
-#pragma unroll
-    for (int e = 0; e < 4; ++e) {
-        const int c = c0 + e;
-        in[e] = (c >= dn) && (c < dn + nx);
-        k2[e] = -(((0.5f * (p3[e] - pm1[e])) * F[e]) * P.ss);
-    }
-    const size_t ko = (size_t)yrow * S.pitch + xl;
-    if (P.grad_form == 0) {
-        float* K = S.k32 + ko;
-        if (in[0] && in[3]) {
-            float4 k = ld4(K);
-            k.x = k.x + k2[0]; k.y = k.y + k2[1]; k.z = k.z + k2[2]; k.w = k.w + k2[3];
-            st4(K, k);
-        } else {
-#pragma unroll
-            for (int e = 0; e < 4; ++e)
-                if (in[e]) K[e] = K[e] + k2[e];
-        }
-    } else {
-        double* K = S.k64 + ko;
-        if (in[0] && in[3]) {
-            double2* K2 = reinterpret_cast<double2*>(K);
-            double2 a = K2[0], b = K2[1];
-            a.x += (double)k2[0]; a.y += (double)k2[1]; b.x += (double)k2[2]; b.y += (double)k2[3];
-            K2[0] = a;
-            K2[1] = b;
-        } else {
-#pragma unroll
-            for (int e = 0; e < 4; ++e)
-                if (in[e]) K[e] += (double)k2[e];
-        }
-    }
+    if (lane == 0) S.sscale[((size_t)P.snap * S.ny + yrow) * (S.ntiles + 2) + seg] = ldexpf(1.f, -sh);
 }
 
 // Receiver recording for the row just finished (:553): every receiver in
@@ -354,141 +273,6 @@ __device__ __forceinline__ void cp16(void* smem_dst, const void* gmem_src) {
 __device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 template <int N>
 __device__ __forceinline__ void cp_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
-
-// One prefetch stage of the main kernel (float4 slots): p(y+R), p_1(y),
-// c2(y), x-phi(y), x-chi(y) per lane, plus the two halo float4 of p(y).
-constexpr int ST_P = 0, ST_P1 = 32, ST_C2 = 64, ST_PH = 96, ST_CH = 128, ST_HL = 160, ST_HR = 161, ST_SIZE = 162;
-constexpr int MAIN_DEPTH = 4;  // rows in flight per warp
-constexpr int MAIN_SMEM = 4 * MAIN_DEPTH * ST_SIZE * 16;  // bytes per 4-warp block
-
-// Model rows of the first and last tile of a shot: interior cells plus the
-// left/right CPML strips, with the grid-edge clamps of the x derivatives.
-template <int R, int MODE>
-__device__ __forceinline__ void edge_rows(const StepParams& P, const WorkItem& it, float4* ring, int lane) {
-    const ShotDev& S = P.shots[it.shot];
-    const int pitch = S.pitch, dn = S.dn, nx = S.nx, nxt = S.nxt;
-    const int x0 = it.tile * TILE, xl = x0 + 4 * lane, c0 = xl - S.off;
-    const bool first = it.tile == 0, last = it.tile == S.ntiles - 1, edge = first || last;
-    const float* PC = P.parity ? S.pa : S.pb;  // p
-    float* P1 = P.parity ? S.pb : S.pa;        // p_1, overwritten with p_3
-    bool lane_strip = false;
-    if (edge) lane_strip = (c0 < dn) || (c0 + 3 >= dn + nx);
-    const bool has_hl = (lane == 0) && (x0 > 0), has_hr = (lane == 31) && (x0 + TILE < pitch);
-
-    auto issue = [&](int y, int slot) {
-        float4* st = ring + slot * ST_SIZE;
-        const size_t ro = (size_t)y * pitch + xl;
-        cp16(st + ST_P + lane, PC + (size_t)(y + R) * pitch + xl);
-        cp16(st + ST_P1 + lane, P1 + ro);
-        cp16(st + ST_C2 + lane, S.c2 + ro);
-        if (lane_strip) {
-            cp16(st + ST_PH + lane, S.phx + ro);
-            cp16(st + ST_CH + lane, S.chx + ro);
-        }
-        if (has_hl) cp16(st + ST_HL, PC + (size_t)y * pitch + x0 - 4);
-        if (has_hr) cp16(st + ST_HR, PC + (size_t)y * pitch + x0 + TILE);
-    };
-
-#pragma unroll
-    for (int i = 0; i < MAIN_DEPTH; ++i) {
-        if (it.y0 + i < it.y1) issue(it.y0 + i, i);
-        cp_commit();
-    }
-    float4 q[2 * R + 1];
-#pragma unroll
-    for (int i = 0; i < 2 * R; ++i) q[i] = ldg4(PC + (size_t)(it.y0 - R + i) * pitch + xl);
-
-    int si = it.s0, ri = it.r0;
-    int srow = (si < it.s1) ? P.srcs[si].row : INT_MAX;
-    int rrow = (ri < it.r1) ? P.recs[ri].row : INT_MAX;
-
-    int slot = 0;
-    for (int y = it.y0; y < it.y1; ++y) {
-        cp_wait<MAIN_DEPTH - 1>();
-        const float4* st = ring + slot * ST_SIZE;
-        const size_t ro = (size_t)y * pitch + xl;
-        q[2 * R] = st[ST_P + lane];
-        float pm1[4], cc[4], pc[4];
-        to_arr(st[ST_P1 + lane], pm1);
-        to_arr(st[ST_C2 + lane], cc);
-        to_arr(q[R], pc);
-        const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
-        const float4 hl = has_hl ? st[ST_HL] : z4, hr = has_hr ? st[ST_HR] : z4;
-        float ph[4] = {0.f, 0.f, 0.f, 0.f}, ch[4] = {0.f, 0.f, 0.f, 0.f};
-        if (lane_strip) {
-            to_arr(st[ST_PH + lane], ph);
-            to_arr(st[ST_CH + lane], ch);
-        }
-        float w[12];
-        window(q[R], hl, hr, lane, w);
-        float d2x[4], dx[4], d2y[4];
-        xderivs<R>(w, P, d2x, dx);
-        yderiv2<R>(q, P, d2y);
-
-        // source injection: source(nys,nxs) = S(k-1,j), interior cells only
-        float sv[4] = {0.f, 0.f, 0.f, 0.f};
-        while (srow == y) {
-            const SrcEnt s = P.srcs[si];
-            if ((s.col >> 2) == (xl >> 2)) {
-                const float val = __ldg(S.srcv + (size_t)s.vidx * S.nt + P.t);
-                const int el = s.col & 3;
-                sv[0] = el == 0 ? val : sv[0];
-                sv[1] = el == 1 ? val : sv[1];
-                sv[2] = el == 2 ? val : sv[2];
-                sv[3] = el == 3 ? val : sv[3];
-            }
-            ++si;
-            srow = (si < it.s1) ? P.srcs[si].row : INT_MAX;
-        }
-
-        float p3[4];
-        if (!edge) {
-#pragma unroll
-            for (int e = 0; e < 4; ++e)
-                p3[e] = ((-pm1[e]) + 2.f * pc[e]) + (((d2x[e] + d2y[e]) + sv[e]) * cc[e]);
-        } else {
-            xclamp<R>(S, x0, c0, first, last, d2x, dx);
-            float dph[4];
-            phi_xderiv<R>(S, P, from_arr(ph), lane, x0, c0, first, last, dph);
-#pragma unroll
-            for (int e = 0; e < 4; ++e) {
-                const int c = c0 + e;
-                if (c < 0 || c >= nxt) {
-                    p3[e] = 0.f;
-                } else if (c >= dn && c < dn + nx) {
-                    p3[e] = ((-pm1[e]) + 2.f * pc[e]) + (((d2x[e] + d2y[e]) + sv[e]) * cc[e]);
-                } else {
-                    // xl strip: factor(dn-i+1); xr strip: factor(i)  (solver_PML_matrices.f90:296-312)
-                    const int fi = (c < dn) ? (dn - 1 - c) : (c - dn - nx);
-                    const float A = __ldg(P.fA + fi), B = __ldg(P.fB + fi);
-                    const float phn = A * ph[e] + B * dx[e];
-                    const float chn = A * ch[e] + B * (d2x[e] + dph[e]);
-                    const float prop = dph[e] + chn;
-                    ph[e] = phn;
-                    ch[e] = chn;
-                    p3[e] = ((-pm1[e]) + 2.f * pc[e]) + cc[e] * ((d2x[e] + d2y[e]) + prop);
-                }
-            }
-            if (lane_strip) {
-                st4(S.phx + ro, from_arr(ph));
-                st4(S.chx + ro, from_arr(ch));
-            }
-        }
-
-        if (MODE == 0 && P.snap >= 0) store_snapshot(P, S, y - dn, lane, x0, xl, c0, p3, pm1, it.tile);
-        if (MODE == 1 && P.snap >= 0) image_row(P, S, y - dn, xl, c0, p3, pm1, it.tile);
-        st4(P1 + ro, from_arr(p3));
-        if (MODE == 0 && P.record) record_row(P, S, y, xl, ri, it.r1, rrow, p3);
-
-#pragma unroll
-        for (int i = 0; i < 2 * R; ++i) q[i] = q[i + 1];
-        // refill this slot (its values are consumed above) with row y + depth
-        if (y + MAIN_DEPTH < it.y1) issue(y + MAIN_DEPTH, slot);
-        cp_commit();
-        slot = (slot + 1 == MAIN_DEPTH) ? 0 : slot + 1;
-    }
-    cp_wait<0>();
-}
 
 // One prefetch stage of the bottom kernel: p(y+R), p_1(y), c2(y), y-phi(y),
 // y-chi(y), x-phi(y), x-chi(y), the y-phi row the derivative queue needs
@@ -679,8 +463,50 @@ __device__ __forceinline__ void bottom_rows(const StepParams& P, const WorkItem&
     cp_wait<0>();
 }
 
-// Model rows of the middle tiles: interior cells only (no CPML, no clamp),
-// so only second derivatives are needed.  This is the kernel that moves
+// Interior update of one row on packed FP32 pairs (Blackwell f32x2
+// add/fma: two independently rounded FP32 operations per instruction).
+// Products are formed as fma(a, b, +0): ptxas contracts a packed multiply
+// feeding a packed add into a fused multiply-add (even with --fmad=false),
+// which would change the rounding; fma with a +0 addend is the correctly
+// rounded product, and it is not fused with the following add.  (It can only
+// differ from a*b in the sign of a zero product, and every sum it enters
+// starts from +0, so no value changes.)  Lane columns (0,1) and (2,3) form
+// the two pairs; x-neighbour pairs at odd offsets are re-paired.
+__device__ __forceinline__ float2 pr(const float4& v, int k) { return k == 0 ? make_float2(v.x, v.y) : make_float2(v.z, v.w); }
+__device__ __forceinline__ float2 mul0(float2 a, float2 b) { return __ffma2_rn(a, b, make_float2(0.f, 0.f)); }
+
+template <int R>
+__device__ __forceinline__ void interior_update2(const float4* q, float4 L, float4 Rt, float4 pm1, float4 cc,
+                                                 const float* sv, const float2* cp, float* p3) {
+    const float4 C = q[R];
+    const float w[12] = {L.x, L.y, L.z, L.w, C.x, C.y, C.z, C.w, Rt.x, Rt.y, Rt.z, Rt.w};
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+        // space_deriv2x: s = s + coef(i)*(p(j+i) + p(j-i))
+        float2 ax = make_float2(0.f, 0.f);
+#pragma unroll
+        for (int i = 0; i <= R; ++i) {
+            const int a = 4 + 2 * k + i, b = 4 + 2 * k - i;
+            ax = __fadd2_rn(ax, mul0(cp[i], __fadd2_rn(make_float2(w[a], w[a + 1]), make_float2(w[b], w[b + 1]))));
+        }
+        // space_deriv2y: s = s + (p(j+i) + p(j-i))*coef(i)
+        float2 ay = make_float2(0.f, 0.f);
+#pragma unroll
+        for (int i = 0; i <= R; ++i) ay = __fadd2_rn(ay, mul0(__fadd2_rn(pr(q[R + i], k), pr(q[R - i], k)), cp[i]));
+        // p_3 = -p_1 + 2p + (d2x + d2y + source)*c2
+        const float2 pc = pr(C, k), pm = pr(pm1, k);
+        const float2 t = __fadd2_rn(make_float2(-pm.x, -pm.y), __fadd2_rn(pc, pc));
+        const float2 u = mul0(__fadd2_rn(__fadd2_rn(ax, ay), make_float2(sv[2 * k], sv[2 * k + 1])), pr(cc, k));
+        const float2 r = __fadd2_rn(t, u);
+        p3[2 * k] = r.x;
+        p3[2 * k + 1] = r.y;
+    }
+}
+
+// Model rows, interior columns [sl, sr): no CPML and no clamp, so only
+// second derivatives are needed.  The first and last tile of the range may
+// be partial; their lanes outside it compute but store nothing (those cells
+// belong to the strip warps).  This is the kernel that moves
 // almost all of the bytes.  SNAP selects the variant for the time steps
 // that store a snapshot (forward) or apply the imaging condition (adjoint);
 // the adjoint variant also prefetches the snapshot row and the imaging
@@ -718,6 +544,9 @@ __global__ void __launch_bounds__(128, (MODE == 1 && SNAP) ? 3 : 5) k_step_inter
     const bool has_h = (lane == 0) || (lane == 31);
     float4* hslot = ring + (lane == 0 ? IN_HL : IN_HR);
     const size_t snap_base = IMG ? (size_t)P.snap * (size_t)S.snap_stride : 0;
+    // this lane stores its elements [lo, hi): the interior columns [sl, sr)
+    const int lo = S.off + S.sl - xl, hi = S.off + S.sr - xl;
+    const bool full = lo <= 0 && hi >= 4;
 
     auto issue = [&](int y, int slot) {
         float4* st = ring + slot * SZ;
@@ -733,7 +562,7 @@ __global__ void __launch_bounds__(128, (MODE == 1 && SNAP) ? 3 : 5) k_step_inter
             } else {
                 if (lane < 16) cp16(st + IN_F + lane, reinterpret_cast<const unsigned short*>(S.snaps) + fo + 8 * lane);
                 if (lane == 16)
-                    cp4(st + IN_FS, S.sscale + ((size_t)P.snap * S.ny + (y - S.dn)) * S.ntiles + it.tile);
+                    cp4(st + IN_FS, S.sscale + ((size_t)P.snap * S.ny + (y - S.dn)) * (S.ntiles + 2) + it.tile);
             }
             const size_t ko = (size_t)(y - S.dn) * pitch + xl;
             if (P.grad_form == 0) {
@@ -757,6 +586,9 @@ __global__ void __launch_bounds__(128, (MODE == 1 && SNAP) ? 3 : 5) k_step_inter
     int srow = (si < it.s1) ? P.srcs[si].row : INT_MAX;
     int rrow = (ri < it.r1) ? P.recs[ri].row : INT_MAX;
     const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
+    float2 cp[R + 1];
+#pragma unroll
+    for (int i = 0; i <= R; ++i) cp[i] = make_float2(P.c2[i], P.c2[i]);
 
     int slot = 0;
     for (int y = it.y0; y < it.y1; ++y) {
@@ -768,11 +600,9 @@ __global__ void __launch_bounds__(128, (MODE == 1 && SNAP) ? 3 : 5) k_step_inter
         to_arr(st[IN_C2 + lane], cc);
         to_arr(q[R], pc);
         const float4 h = has_h ? st[lane == 0 ? IN_HL : IN_HR] : z4;
-        float w[12];
-        window(q[R], h, h, lane, w);
-        float d2x[4], d2y[4];
-        xderiv2<R>(w, P, d2x);
-        yderiv2<R>(q, P, d2y);
+        float4 Lf = shfl_up4(q[R]), Rf = shfl_dn4(q[R]);
+        if (lane == 0) Lf = h;
+        if (lane == 31) Rf = h;
 
         // source injection: source(nys,nxs) = S(k-1,j)  (solver_acoustic_SS.f90:319-330)
         float sv[4] = {0.f, 0.f, 0.f, 0.f};
@@ -791,12 +621,11 @@ __global__ void __launch_bounds__(128, (MODE == 1 && SNAP) ? 3 : 5) k_step_inter
         }
         // p_3 = -p_1 + 2p + (d2x + d2y + source)*c2  (:433-434)
         float p3[4];
-#pragma unroll
-        for (int e = 0; e < 4; ++e) p3[e] = ((-pm1[e]) + 2.f * pc[e]) + (((d2x[e] + d2y[e]) + sv[e]) * cc[e]);
+        interior_update2<R>(q, Lf, Rf, from_arr(pm1), from_arr(cc), sv, cp, p3);
 
-        if (MODE == 0 && SNAP) store_snapshot(P, S, y - S.dn, lane, x0, xl, xl - S.off, p3, pm1, it.tile);
+        if (MODE == 0 && SNAP) store_snapshot(P, S, y - S.dn, lane, xl, lo, hi, p3, pm1, it.tile);
         if (IMG) {
-            // kernel += -0.5*(p_3-p_1)*Fields(snap)*store_snap  (:465-466); all columns interior
+            // kernel += -0.5*(p_3-p_1)*Fields(snap)*store_snap  (:465-466)
             float F[4];
             if (P.snap_form == 0) {
                 to_arr(st[IN_F + lane], F);
@@ -820,17 +649,38 @@ __global__ void __launch_bounds__(128, (MODE == 1 && SNAP) ? 3 : 5) k_step_inter
             if (P.grad_form == 0) {
                 float4 k = st[IN_K + lane];
                 k.x = k.x + k2[0]; k.y = k.y + k2[1]; k.z = k.z + k2[2]; k.w = k.w + k2[3];
-                st4(S.k32 + ko, k);
+                if (full) {
+                    st4(S.k32 + ko, k);
+                } else {
+                    float kv[4];
+                    to_arr(k, kv);
+#pragma unroll
+                    for (int e = 0; e < 4; ++e)
+                        if (e >= lo && e < hi) S.k32[ko + e] = kv[e];
+                }
             } else {
                 const double2* kk = reinterpret_cast<const double2*>(st + IN_K) + 2 * lane;
                 double2 a = kk[0], b = kk[1];
                 a.x += (double)k2[0]; a.y += (double)k2[1]; b.x += (double)k2[2]; b.y += (double)k2[3];
-                double2* K2 = reinterpret_cast<double2*>(S.k64 + ko);
-                K2[0] = a;
-                K2[1] = b;
+                if (full) {
+                    double2* K2 = reinterpret_cast<double2*>(S.k64 + ko);
+                    K2[0] = a;
+                    K2[1] = b;
+                } else {
+                    const double kv[4] = {a.x, a.y, b.x, b.y};
+#pragma unroll
+                    for (int e = 0; e < 4; ++e)
+                        if (e >= lo && e < hi) S.k64[ko + e] = kv[e];
+                }
             }
         }
-        st4(P1 + (size_t)y * pitch, from_arr(p3));
+        if (full) {
+            st4(P1 + (size_t)y * pitch, from_arr(p3));
+        } else {
+#pragma unroll
+            for (int e = 0; e < 4; ++e)
+                if (e >= lo && e < hi) P1[(size_t)y * pitch + e] = p3[e];
+        }
         if (MODE == 0 && P.record) record_row(P, S, y, xl, ri, it.r1, rrow, p3);
 
 #pragma unroll
@@ -842,26 +692,318 @@ __global__ void __launch_bounds__(128, (MODE == 1 && SNAP) ? 3 : 5) k_step_inter
     cp_wait<0>();
 }
 
-// Everything next to a boundary: model rows of the first/last tile (kind 0)
-// and the bottom pad rows of every tile (kind 1).  Runs on a second stream,
-// concurrently with k_step_interior.
-constexpr int BND_WARP_F4 = (MAIN_DEPTH * ST_SIZE > BOT_DEPTH * SB_SIZE) ? MAIN_DEPTH * ST_SIZE : BOT_DEPTH * SB_SIZE;
-constexpr int BND_SMEM = 4 * BND_WARP_F4 * 16;
+// ---------------------------------------------------------------------------
+// Side strips of the model rows: the left strip [0, sl) and the right strip
+// [sr, nxt) of the logical columns, each at most 32*K columns wide.  One
+// warp per band of rows; lane l holds strip-local columns l, 32+l, ... (one
+// float per chunk), so the CPML arithmetic runs once per strip column.
+// ---------------------------------------------------------------------------
 
-template <int R, int MODE>
-__global__ void __launch_bounds__(128) k_step_boundary(const __grid_constant__ StepParams P) {
-    extern __shared__ float4 smem[];
+// Prefetch stage of the strip kernel (floats): p(y+R), p_1(y), c2(y),
+// x-phi(y), x-chi(y) per strip column, then the p(y) halo columns left of the
+// strip (lanes 32-R..31) and right of it (lanes 0..R-1).
+template <int K>
+struct StripSlot {
+    static constexpr int P = 0, P1 = 32 * K, C2 = 64 * K, PH = 96 * K, CH = 128 * K, HL = 160 * K,
+                         HR = 160 * K + 32, SIZE = 160 * K + 64;
+};
+constexpr int STRIP_DEPTH = 8;  // rows in flight per warp
+template <int K>
+constexpr int strip_smem() {
+    return 4 * STRIP_DEPTH * StripSlot<K>::SIZE * 4;
+}
+
+// Value at strip-local column 32k + lane + d of a row held one column per
+// lane; columns left of the strip come from hl (lane 32+t holds column t,
+// -R <= t < 0), columns right of it from hr (lane j holds column 32K + j).
+// k and d are compile-time constants after unrolling.
+template <int K>
+__device__ __forceinline__ float nbr(const float (&v)[K], float hl, float hr, int k, int d, int lane) {
+    if (d == 0) return v[k];
+    const int t = lane + d;
+    const float a = __shfl_sync(FULL, v[k], t & 31);
+    const float o = (d > 0) ? ((k + 1 < K) ? v[k + 1 < K ? k + 1 : k] : hr) : ((k > 0) ? v[k > 0 ? k - 1 : 0] : hl);
+    const float b = __shfl_sync(FULL, o, t & 31);
+    if (d > 0) return t < 32 ? a : b;
+    return t >= 0 ? a : b;
+}
+
+// Value at the warp-uniform strip-local column j.
+template <int K>
+__device__ __forceinline__ float bcast(const float (&v)[K], int j) {
+    const float src = (K > 1 && j >= 32) ? v[K - 1] : v[0];
+    return __shfl_sync(FULL, src, j & 31);
+}
+
+template <int R, int MODE, int K>
+__global__ void __launch_bounds__(128) k_step_strip(const __grid_constant__ StepParams P) {
+    using SL = StripSlot<K>;
+    extern __shared__ float sfl[];
     const int lane = threadIdx.x & 31;
     const int wid = blockIdx.x * 4 + (threadIdx.x >> 5);
-    if (wid >= P.nitems) return;
-    float4* ring = smem + (threadIdx.x >> 5) * BND_WARP_F4;
+    if (wid >= P.nstrip) return;
+    float* ring = sfl + (threadIdx.x >> 5) * (STRIP_DEPTH * SL::SIZE);
     const WorkItem it = P.items[wid];
-    if (it.kind == 0) edge_rows<R, MODE>(P, it, ring, lane);
-    else bottom_rows<R, MODE>(P, it, ring, lane);
+    const ShotDev& S = P.shots[it.shot];
+    const int pitch = S.pitch, dn = S.dn, nx = S.nx, nxt = S.nxt;
+    const bool right = it.tile != 0;
+    const int cs = right ? S.sr : 0, ce = right ? nxt : S.sl;  // logical strip columns [cs, ce)
+    const float* PC = P.parity ? S.pa : S.pb;  // p
+    float* P1 = P.parity ? S.pb : S.pa;        // p_1, overwritten with p_3
+
+    int col[K];
+    bool valid[K], act[K], cpml[K];
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+        col[k] = cs + 32 * k + lane;
+        valid[k] = col[k] < nxt;  // inside the grid (x-neighbour source)
+        act[k] = col[k] < ce;     // updated by this warp
+        cpml[k] = act[k] && (col[k] < dn || col[k] >= dn + nx);
+    }
+    const int hlc = cs - 32 + lane, hrc = cs + 32 * K + lane;  // halo columns
+    const bool has_hl = lane >= 32 - R && hlc >= 0, has_hr = lane < R && hrc < nxt;
+    const size_t xs = (size_t)S.off + cs + lane;  // physical column of chunk 0
+
+    auto issue = [&](int y, int slot) {
+        float* st = ring + slot * SL::SIZE;
+        const size_t ro = (size_t)y * pitch + xs;
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+            const size_t o = ro + 32 * k;
+            if (valid[k]) cp4(st + SL::P + 32 * k + lane, PC + o + (size_t)R * pitch);
+            if (act[k]) {
+                cp4(st + SL::P1 + 32 * k + lane, P1 + o);
+                cp4(st + SL::C2 + 32 * k + lane, S.c2 + o);
+            }
+            if (cpml[k]) {
+                cp4(st + SL::PH + 32 * k + lane, S.phx + o);
+                cp4(st + SL::CH + 32 * k + lane, S.chx + o);
+            }
+        }
+        if (has_hl) cp4(st + SL::HL + lane, PC + (size_t)y * pitch + S.off + hlc);
+        if (has_hr) cp4(st + SL::HR + lane, PC + (size_t)y * pitch + S.off + hrc);
+    };
+#pragma unroll
+    for (int i = 0; i < STRIP_DEPTH; ++i) {
+        if (it.y0 + i < it.y1) issue(it.y0 + i, i);
+        cp_commit();
+    }
+    float q[K][2 * R + 1];
+#pragma unroll
+    for (int k = 0; k < K; ++k)
+#pragma unroll
+        for (int i = 0; i < 2 * R; ++i)
+            q[k][i] = valid[k] ? __ldg(PC + (size_t)(it.y0 - R + i) * pitch + xs + 32 * k) : 0.f;
+
+    // clamp sources (warp-uniform strip-local columns): the p derivatives of
+    // columns < R copy column R, of columns > nxt-1-R column nxt-1-R
+    // (solver_space_derivs.f90:18-23, :84-94); the strip-local derivative of
+    // the old phi copies its value at strip index R / dn-1-R
+    // (solver_PML_matrices.f90:15, :97 on the dn-wide strip array).
+    const int jc = right ? (nxt - 1 - R - cs) : R;
+    const int jlo = right ? (dn + nx + R - cs) : R;
+    const int jhi = right ? (nxt - 1 - R - cs) : (dn - 1 - R);
+
+    int si = it.s0, ri = it.r0;
+    int srow = (si < it.s1) ? P.srcs[si].row : INT_MAX;
+    int rrow = (ri < it.r1) ? P.recs[ri].row : INT_MAX;
+    const size_t seg = (size_t)S.ntiles + (right ? 1 : 0);
+
+    int slot = 0;
+    for (int y = it.y0; y < it.y1; ++y) {
+        cp_wait<STRIP_DEPTH - 1>();
+        const float* st = ring + slot * SL::SIZE;
+        float pc[K], pm1[K], cc[K], ph[K], ch[K];
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+            q[k][2 * R] = valid[k] ? st[SL::P + 32 * k + lane] : 0.f;
+            pc[k] = q[k][R];
+            pm1[k] = act[k] ? st[SL::P1 + 32 * k + lane] : 0.f;
+            cc[k] = act[k] ? st[SL::C2 + 32 * k + lane] : 0.f;
+            ph[k] = cpml[k] ? st[SL::PH + 32 * k + lane] : 0.f;
+            ch[k] = cpml[k] ? st[SL::CH + 32 * k + lane] : 0.f;
+        }
+        const float hl = has_hl ? st[SL::HL + lane] : 0.f, hr = has_hr ? st[SL::HR + lane] : 0.f;
+
+        // space_deriv2x / space_derivx, space_deriv2y, and the strip-local
+        // derivative of the old x-phi (pml_matrices_x :15)
+        float d2x[K], dx[K], d2y[K], dph[K];
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+            float s2 = 0.f, s1 = 0.f, sy = 0.f, sp = 0.f;
+#pragma unroll
+            for (int i = 0; i <= R; ++i) {
+                const float r = nbr<K>(pc, hl, hr, k, i, lane), l = nbr<K>(pc, hl, hr, k, -i, lane);
+                s2 = s2 + P.c2[i] * (r + l);
+                s1 = s1 + (r - l) * P.c1[i];
+                sy = sy + (q[k][R + i] + q[k][R - i]) * P.c2[i];
+                const float pr_ = nbr<K>(ph, 0.f, 0.f, k, i, lane), pl_ = nbr<K>(ph, 0.f, 0.f, k, -i, lane);
+                sp = sp + (pr_ - pl_) * P.c1[i];
+            }
+            d2x[k] = s2;
+            dx[k] = s1;
+            d2y[k] = sy;
+            dph[k] = sp;
+        }
+        {
+            const float c2v = bcast<K>(d2x, jc), c1v = bcast<K>(dx, jc);
+            const float plo = bcast<K>(dph, jlo), phi_ = bcast<K>(dph, jhi);
+#pragma unroll
+            for (int k = 0; k < K; ++k) {
+                const int c = col[k];
+                if (right ? (c > nxt - 1 - R) : (c < R)) {
+                    d2x[k] = c2v;
+                    dx[k] = c1v;
+                }
+                const int il = right ? c - dn - nx : c;  // index inside the dn-wide CPML strip
+                if (il < R) dph[k] = plo;
+                else if (il > dn - 1 - R) dph[k] = phi_;
+            }
+        }
+
+        // source injection: source(nys,nxs) = S(k-1,j), interior cells only
+        float sv[K];
+#pragma unroll
+        for (int k = 0; k < K; ++k) sv[k] = 0.f;
+        while (srow == y) {
+            const SrcEnt e = P.srcs[si];
+            const float val = __ldg(S.srcv + (size_t)e.vidx * S.nt + P.t);
+#pragma unroll
+            for (int k = 0; k < K; ++k)
+                if (e.col == (int)xs + 32 * k) sv[k] = val;
+            ++si;
+            srow = (si < it.s1) ? P.srcs[si].row : INT_MAX;
+        }
+
+        float p3[K];
+        const size_t ro = (size_t)y * pitch + xs;
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+            const int c = col[k];
+            if (cpml[k]) {
+                // xl strip: factor(dn-i+1); xr strip: factor(i)  (solver_PML_matrices.f90:296-312)
+                const int fi = (c < dn) ? (dn - 1 - c) : (c - dn - nx);
+                const float A = __ldg(P.fA + fi), B = __ldg(P.fB + fi);
+                const float phn = A * ph[k] + B * dx[k];
+                const float chn = A * ch[k] + B * (d2x[k] + dph[k]);
+                const float prop = dph[k] + chn;
+                p3[k] = ((-pm1[k]) + 2.f * pc[k]) + cc[k] * ((d2x[k] + d2y[k]) + prop);
+                S.phx[ro + 32 * k] = phn;
+                S.chx[ro + 32 * k] = chn;
+            } else {
+                p3[k] = ((-pm1[k]) + 2.f * pc[k]) + (((d2x[k] + d2y[k]) + sv[k]) * cc[k]);
+            }
+        }
+
+        if (P.snap >= 0) {
+            const int yrow = y - dn;
+            const size_t fb = (size_t)P.snap * (size_t)S.snap_stride + (size_t)yrow * pitch + xs;
+            float v[K];
+            bool in[K];
+#pragma unroll
+            for (int k = 0; k < K; ++k) in[k] = act[k] && !cpml[k];
+            if (MODE == 0) {
+                // Fields(j, snap*nx+i) = (p_3 - p_1)*0.5/dt  (:447)
+#pragma unroll
+                for (int k = 0; k < K; ++k) v[k] = in[k] ? ((p3[k] - pm1[k]) * 0.5f) / P.dt : 0.f;
+                if (P.snap_form == 0) {
+#pragma unroll
+                    for (int k = 0; k < K; ++k)
+                        if (in[k]) reinterpret_cast<float*>(S.snaps)[fb + 32 * k] = v[k];
+                } else {
+                    float m = fabsf(v[0]);
+#pragma unroll
+                    for (int k = 1; k < K; ++k) m = fmaxf(m, fabsf(v[k]));
+#pragma unroll
+                    for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(FULL, m, o));
+                    int ex = 0;
+                    if (m > 0.f) frexpf(m, &ex);
+                    const int sh = 14 - ex;
+#pragma unroll
+                    for (int k = 0; k < K; ++k) {
+                        if (!in[k]) continue;
+                        const float scaled = ldexpf(v[k], sh);
+                        unsigned short h;
+                        if (P.snap_form == 1) {
+                            __nv_bfloat16 b = __float2bfloat16_rn(scaled);
+                            h = *reinterpret_cast<unsigned short*>(&b);
+                        } else {
+                            __half b = __float2half_rn(scaled);
+                            h = *reinterpret_cast<unsigned short*>(&b);
+                        }
+                        reinterpret_cast<unsigned short*>(S.snaps)[fb + 32 * k] = h;
+                    }
+                    if (lane == 0) S.sscale[((size_t)P.snap * S.ny + yrow) * (S.ntiles + 2) + seg] = ldexpf(1.f, -sh);
+                }
+            } else {
+                // kernel += -0.5*(p_3-p_1)*Fields(snap)*store_snap  (:465-466)
+                const float sc = (P.snap_form == 0)
+                                     ? 1.f
+                                     : __ldg(S.sscale + ((size_t)P.snap * S.ny + yrow) * (S.ntiles + 2) + seg);
+                const size_t ko = (size_t)yrow * pitch + xs;
+#pragma unroll
+                for (int k = 0; k < K; ++k) {
+                    if (!in[k]) continue;
+                    float F;
+                    if (P.snap_form == 0) {
+                        F = __ldg(reinterpret_cast<const float*>(S.snaps) + fb + 32 * k);
+                    } else {
+                        const unsigned short h = __ldg(reinterpret_cast<const unsigned short*>(S.snaps) + fb + 32 * k);
+                        float f;
+                        if (P.snap_form == 1) f = __bfloat162float(*reinterpret_cast<const __nv_bfloat16*>(&h));
+                        else f = __half2float(*reinterpret_cast<const __half*>(&h));
+                        F = f * sc;
+                    }
+                    const float k2 = -(((0.5f * (p3[k] - pm1[k])) * F) * P.ss);
+                    if (P.grad_form == 0) S.k32[ko + 32 * k] = S.k32[ko + 32 * k] + k2;
+                    else S.k64[ko + 32 * k] += (double)k2;
+                }
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < K; ++k)
+            if (act[k]) P1[ro + 32 * k] = p3[k];
+        // receivers: every receiver in this cell gets p_3 (:553)
+        if (MODE == 0 && P.record) {
+            while (rrow == y) {
+                const RecEnt r = P.recs[ri];
+#pragma unroll
+                for (int k = 0; k < K; ++k)
+                    if (r.col == (int)xs + 32 * k) S.rec[(size_t)r.ridx * S.nt + P.t] = p3[k];
+                ++ri;
+                rrow = (ri < it.r1) ? P.recs[ri].row : INT_MAX;
+            }
+        }
+
+#pragma unroll
+        for (int k = 0; k < K; ++k)
+#pragma unroll
+            for (int i = 0; i < 2 * R; ++i) q[k][i] = q[k][i + 1];
+        if (y + STRIP_DEPTH < it.y1) issue(y + STRIP_DEPTH, slot);
+        cp_commit();
+        slot = (slot + 1 == STRIP_DEPTH) ? 0 : slot + 1;
+    }
+    cp_wait<0>();
+}
+
+// Bottom pad rows of every tile (the boundary list after its nstrip side
+// strip items).  Runs on its own stream, concurrently with k_step_interior
+// and k_step_strip.
+constexpr int BND_SMEM = 4 * BOT_DEPTH * SB_SIZE * 16;
+
+template <int R, int MODE>
+__global__ void __launch_bounds__(128) k_step_bottom(const __grid_constant__ StepParams P) {
+    extern __shared__ float4 smem[];
+    const int lane = threadIdx.x & 31;
+    const int wid = P.nstrip + blockIdx.x * 4 + (threadIdx.x >> 5);
+    if (wid >= P.nitems) return;
+    float4* ring = smem + (threadIdx.x >> 5) * (BOT_DEPTH * SB_SIZE);
+    const WorkItem it = P.items[wid];
+    bottom_rows<R, MODE>(P, it, ring, lane);
 }
 
 // Opt the step kernels into the dynamic shared memory they use (the
-// boundary kernel's prefetch rings are above the 48 KB default).
+// bottom kernel's prefetch rings are above the 48 KB default).
 cudaError_t configure_step_kernels() {
     cudaError_t e = cudaSuccess;
 #define FWI_CFG(R_, M_)                                                                                           \
@@ -872,7 +1014,13 @@ cudaError_t configure_step_kernels() {
         e = cudaFuncSetAttribute(k_step_interior<R_, M_, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,       \
                                  M_ == 1 ? IN_SMEM_IMG : IN_SMEM);                                                 \
     if (e == cudaSuccess)                                                                                         \
-        e = cudaFuncSetAttribute(k_step_boundary<R_, M_>, cudaFuncAttributeMaxDynamicSharedMemorySize, BND_SMEM);
+        e = cudaFuncSetAttribute(k_step_bottom<R_, M_>, cudaFuncAttributeMaxDynamicSharedMemorySize, BND_SMEM);    \
+    if (e == cudaSuccess)                                                                                         \
+        e = cudaFuncSetAttribute(k_step_strip<R_, M_, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,             \
+                                 strip_smem<1>());                                                                 \
+    if (e == cudaSuccess)                                                                                         \
+        e = cudaFuncSetAttribute(k_step_strip<R_, M_, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize,             \
+                                 strip_smem<2>());
     FWI_CFG(3, 0)
     FWI_CFG(3, 1)
     FWI_CFG(4, 0)
@@ -881,20 +1029,26 @@ cudaError_t configure_step_kernels() {
     return e;
 }
 
-// Interior kernel on stream sm and boundary kernel on stream sb (the caller
-// orders the two streams around each time step).
-cudaError_t launch_step(int acc, int mode, const StepParams& pm, const StepParams& pb, cudaStream_t sm,
-                        cudaStream_t sb) {
-    const int bm = (pm.nitems + 3) / 4, bb = (pb.nitems + 3) / 4;
-#define FWI_LAUNCH(R_, M_)                                                          \
-    do {                                                                           \
-        if (bb) k_step_boundary<R_, M_><<<bb, 128, BND_SMEM, sb>>>(pb);             \
-        if (bm) {                                                                  \
-            if (pm.snap >= 0)                                                      \
-                k_step_interior<R_, M_, true><<<bm, 128, M_ == 1 ? IN_SMEM_IMG : IN_SMEM, sm>>>(pm); \
-            else                                                                   \
-                k_step_interior<R_, M_, false><<<bm, 128, IN_SMEM, sm>>>(pm);      \
-        }                                                                          \
+// Interior kernel on stream sm, bottom kernel on sb, strip kernel on ss (the
+// caller orders the streams around each time step).  kstrip = columns per
+// lane of the strip kernel (ceil(strip width / 32)).
+cudaError_t launch_step(int acc, int mode, int kstrip, const StepParams& pm, const StepParams& pb, cudaStream_t sm,
+                        cudaStream_t sb, cudaStream_t ss) {
+    const int bm = (pm.nitems + 3) / 4, bs = (pb.nstrip + 3) / 4, bb = (pb.nitems - pb.nstrip + 3) / 4;
+    if (kstrip != 1 && kstrip != 2) return cudaErrorInvalidValue;
+#define FWI_LAUNCH(R_, M_)                                                                                  \
+    do {                                                                                                   \
+        if (bs) {                                                                                          \
+            if (kstrip == 1) k_step_strip<R_, M_, 1><<<bs, 128, strip_smem<1>(), ss>>>(pb);                 \
+            else k_step_strip<R_, M_, 2><<<bs, 128, strip_smem<2>(), ss>>>(pb);                            \
+        }                                                                                                  \
+        if (bb) k_step_bottom<R_, M_><<<bb, 128, BND_SMEM, sb>>>(pb);                                      \
+        if (bm) {                                                                                          \
+            if (pm.snap >= 0)                                                                              \
+                k_step_interior<R_, M_, true><<<bm, 128, M_ == 1 ? IN_SMEM_IMG : IN_SMEM, sm>>>(pm);       \
+            else                                                                                           \
+                k_step_interior<R_, M_, false><<<bm, 128, IN_SMEM, sm>>>(pm);                              \
+        }                                                                                                  \
     } while (0)
     if (acc == 3) {
         if (mode == 0) FWI_LAUNCH(3, 0);

@@ -270,8 +270,9 @@ int validate_geometry(const ShotGeom& g, const Layout& l, int shot) {
 // inject the sources and record the receivers, adjoint lists inject the
 // adjoint sources at the receivers.
 struct Lists {
-    std::vector<WorkItem> int_fwd, int_adj, bnd_fwd, bnd_adj;  // boundary lists: nstrip strips, then bottom tiles
-    int nstrip = 0, kstrip = 1;
+    // boundary lists: nstrip strips, nbot bottom tiles without corners, the corner tiles
+    std::vector<WorkItem> int_fwd, int_adj, bnd_fwd, bnd_adj;
+    int nstrip = 0, nbot = 0, kstrip = 1;
     std::vector<SrcEnt> src_fwd, src_adj;
     std::vector<RecEnt> recs;
 };
@@ -328,7 +329,7 @@ constexpr int STRIP_BAND = 16;  // rows per side-strip work item
 // All shots share dn (one acc / dpml per launch), hence one kstrip.
 Lists build_lists(const std::vector<ShotGeom>& geoms, const std::vector<Layout>& lays, int band_rows) {
     Lists out;
-    std::vector<WorkItem> strip_f, strip_a, bot_f, bot_a;
+    std::vector<WorkItem> strip_f, strip_a, bot_f, bot_a, cor_f, cor_a;
     if (!lays.empty()) out.kstrip = lays[0].kstrip;
     auto bands = [](int n, int rows, auto&& fn) {
         const int nb = std::max(1, (n + rows - 1) / rows);
@@ -377,18 +378,22 @@ Lists build_lists(const std::vector<ShotGeom>& geoms, const std::vector<Layout>&
         std::vector<SrcEnt> none;
         bands(l.dn, BOTTOM_BAND, [&](int j0, int j1) {
             for (int t = 0; t < l.ntiles; ++t) {
-                append_item(out, bot_f, out.src_fwd, none, recs, (int)s, t, l.nyt - l.dn + j0, l.nyt - l.dn + j1, 1,
-                            true, t * TILE, (t + 1) * TILE);
-                append_item(out, bot_a, out.src_adj, none, recs, (int)s, t, l.nyt - l.dn + j0, l.nyt - l.dn + j1, 1,
-                            false, t * TILE, (t + 1) * TILE);
+                const bool corner = t == 0 || t == l.ntiles - 1;
+                append_item(out, corner ? cor_f : bot_f, out.src_fwd, none, recs, (int)s, t, l.nyt - l.dn + j0,
+                            l.nyt - l.dn + j1, 1, true, t * TILE, (t + 1) * TILE);
+                append_item(out, corner ? cor_a : bot_a, out.src_adj, none, recs, (int)s, t, l.nyt - l.dn + j0,
+                            l.nyt - l.dn + j1, 1, false, t * TILE, (t + 1) * TILE);
             }
         });
     }
     out.nstrip = (int)strip_f.size();
+    out.nbot = (int)bot_f.size();
     out.bnd_fwd = strip_f;
     out.bnd_fwd.insert(out.bnd_fwd.end(), bot_f.begin(), bot_f.end());
+    out.bnd_fwd.insert(out.bnd_fwd.end(), cor_f.begin(), cor_f.end());
     out.bnd_adj = strip_a;
     out.bnd_adj.insert(out.bnd_adj.end(), bot_a.begin(), bot_a.end());
+    out.bnd_adj.insert(out.bnd_adj.end(), cor_a.begin(), cor_a.end());
     return out;
 }
 
@@ -521,7 +526,7 @@ struct StepSet {
 };
 
 int step_kernels(const StepSet& ps) {
-    return (ps.pm.nitems > 0) + (ps.pb.nstrip > 0) + (ps.pb.nitems > ps.pb.nstrip);
+    return (ps.pm.nitems > 0) + (ps.pb.nstrip > 0) + (ps.pb.nbot > 0) + (ps.pb.nitems > ps.pb.nstrip + ps.pb.nbot);
 }
 
 // One time step: interior tiles on st, bottom tiles on st2, side strips on
@@ -530,7 +535,8 @@ int step_kernels(const StepSet& ps) {
 // wait on an event with no new node on st in between would accumulate
 // dependencies under stream capture).
 int step_fork_join(int acc, int mode, const StepSet& ps, cudaStream_t st, cudaStream_t st2) {
-    const bool has_m = ps.pm.nitems > 0, has_s = ps.pb.nstrip > 0, has_b = ps.pb.nitems > ps.pb.nstrip;
+    const bool has_m = ps.pm.nitems > 0, has_b = ps.pb.nbot > 0;
+    const bool has_s = ps.pb.nstrip > 0 || ps.pb.nitems > ps.pb.nstrip + ps.pb.nbot;
     L().launches += step_kernels(ps);
     if (!has_m || (!has_s && !has_b)) {
         CK(launch_step(acc, mode, ps.kstrip, ps.pm, ps.pb, st, st, st));
@@ -783,6 +789,7 @@ int fwi_solver_acoustic_ss(const int* rank, const int* iprop_, const int* NumSou
     ps.pb.items = sg.d_items_b.as<WorkItem>();
     ps.pb.nitems = (int)(adj ? lists.bnd_adj.size() : lists.bnd_fwd.size());
     ps.pb.nstrip = lists.nstrip;
+    ps.pb.nbot = lists.nbot;
     ps.kstrip = lists.kstrip;
     TRY(run_time_loop(acc, adj ? 1 : 0, nt, store_snap, nt_store, iprop == 1, ps, st, L().aux));
 
@@ -946,7 +953,7 @@ struct fwi_survey {
     // per-wave lists
     struct WaveDev {
         DBuf items_if, items_ia, items_bf, items_ba, src_f, src_a, recs, shots_f, shots_a, stack;
-        int n_if = 0, n_ia = 0, n_bf = 0, n_ba = 0, n_strip = 0, kstrip = 1;
+        int n_if = 0, n_ia = 0, n_bf = 0, n_ba = 0, n_strip = 0, n_bot = 0, kstrip = 1;
         cudaGraphExec_t graph[3] = {nullptr, nullptr, nullptr};
         long long graph_kernels[3] = {0, 0, 0};  // kernel nodes per graph
         DBuf save_jobs, restore_jobs;  // checkpoint copies: [ckpt][shot][field]
@@ -1042,6 +1049,7 @@ int survey_prepare_waves(fwi_survey* s) {
         wd->n_bf = (int)lists.bnd_fwd.size();
         wd->n_ba = (int)lists.bnd_adj.size();
         wd->n_strip = lists.nstrip;
+        wd->n_bot = lists.nbot;
         wd->kstrip = lists.kstrip;
         s->wdev.push_back(std::move(wd));
     }
@@ -1247,6 +1255,7 @@ int rc_adjoint(fwi_survey* s, size_t wi, StepSet ps, cudaStream_t st, cudaStream
     psf.pb.items = wd.items_bf.as<WorkItem>();
     psf.pb.nitems = wd.n_bf;
     psf.pb.nstrip = wd.n_strip;
+    psf.pb.nbot = wd.n_bot;
     psf.kstrip = wd.kstrip;
     ps.pm.items = wd.items_ia.as<WorkItem>();
     ps.pm.nitems = wd.n_ia;
@@ -1257,6 +1266,7 @@ int rc_adjoint(fwi_survey* s, size_t wi, StepSet ps, cudaStream_t st, cudaStream
     ps.pb.items = wd.items_ba.as<WorkItem>();
     ps.pb.nitems = wd.n_ba;
     ps.pb.nstrip = wd.n_strip;
+    ps.pb.nbot = wd.n_bot;
     ps.kstrip = wd.kstrip;
     int cur = s->rc_J - 1;
     size_t evi = 0;
@@ -1324,6 +1334,7 @@ int issue_wave(fwi_survey* s, size_t wi, int step, cudaStream_t st, cudaStream_t
     ps.pb.items = wd.items_bf.as<WorkItem>();
     ps.pb.nitems = wd.n_bf;
     ps.pb.nstrip = wd.n_strip;
+    ps.pb.nbot = wd.n_bot;
     ps.kstrip = wd.kstrip;
     if (s->rc_C) {
         TRY(rc_forward(s, wi, step, ps, st, st2));
@@ -1366,6 +1377,7 @@ int issue_wave(fwi_survey* s, size_t wi, int step, cudaStream_t st, cudaStream_t
     ps.pb.items = wd.items_ba.as<WorkItem>();
     ps.pb.nitems = wd.n_ba;
     ps.pb.nstrip = wd.n_strip;
+    ps.pb.nbot = wd.n_bot;
     ps.kstrip = wd.kstrip;
     TRY(run_time_loop(D.acc, 1, D.nt, D.store_snap, s->nt_store, true, ps, st, st2));
     LK(launch_stack(s->d_G.as<double>(), D.ny, D.nx_model, wd.stack.p, (int)w.size(), D.grad_form, st));
@@ -1676,6 +1688,7 @@ int time_wave0_steps(fwi_survey* s, int steps, float* ms) {
     ps.pb.items = wd.items_bf.as<WorkItem>();
     ps.pb.nitems = wd.n_bf;
     ps.pb.nstrip = wd.n_strip;
+    ps.pb.nbot = wd.n_bot;
     ps.kstrip = wd.kstrip;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     if (ms) {
@@ -1892,6 +1905,7 @@ extern "C" int fwi_solver_forward_noalloc(int NumSou, int NumRec, const int* nxS
     ps.pb.items = reinterpret_cast<WorkItem*>(sb + o_bm);
     ps.pb.nitems = (int)lists.bnd_fwd.size();
     ps.pb.nstrip = lists.nstrip;
+    ps.pb.nbot = lists.nbot;
     ps.kstrip = lists.kstrip;
     TRY(run_time_loop(acc, 0, nt, nt + 1, 0, false, ps, st, L().aux));
     LK(launch_rec_last(Rec_point_dev, nt, NumRec, st));

@@ -75,7 +75,8 @@ struct StepParams {
     const float* fA;            // CPML factors (dn entries, 0-based)
     const float* fB;
     int nitems;
-    int nstrip;                 // boundary list: the first nstrip items are side strips (kind 2)
+    int nstrip;                 // boundary list: the first nstrip items are side strips (kind 2),
+    int nbot;                   // then nbot bottom tiles without corners, then the corner tiles
     int t;                      // k-2: source column / receiver row this step
     int parity;                 // k & 1: which buffer holds p_1 (written as p_3)
     int snap;                   // snapshot block this step, -1 if none

@@ -286,12 +286,14 @@ constexpr int BOT_SMEM = 4 * BOT_DEPTH * SB_SIZE * 16;
 // corners.  The y-direction phi is ping-ponged between two buffers (old read
 // from one, new written to the other), so the strip-local derivative of the
 // old phi can be taken in any band of the bottom pad.
-template <int R, int MODE>
+// EDGE: the first or last tile, which holds the bottom corners (x- and
+// y-CPML); the other tiles have the y-CPML only and skip the x-CPML terms.
+template <int R, int MODE, bool EDGE>
 __device__ __forceinline__ void bottom_rows(const StepParams& P, const WorkItem& it, float4* ring, int lane) {
     const ShotDev& S = P.shots[it.shot];
     const int pitch = S.pitch, dn = S.dn, nx = S.nx, nxt = S.nxt, nyt = S.nyt;
     const int x0 = it.tile * TILE, xl = x0 + 4 * lane, c0 = xl - S.off;
-    const bool first = it.tile == 0, last = it.tile == S.ntiles - 1, edge = first || last;
+    const bool first = it.tile == 0, last = it.tile == S.ntiles - 1, edge = EDGE;
     const float* PC = P.parity ? S.pa : S.pb;
     float* P1 = P.parity ? S.pb : S.pa;
     const float* PHO = P.parity ? S.phy2 : S.phy;  // old y-phi
@@ -383,8 +385,20 @@ __device__ __forceinline__ void bottom_rows(const StepParams& P, const WorkItem&
         float w[12];
         window(q[R], hl, hr, lane, w);
         float d2x[4], dx[4];
-        xderivs<R>(w, P, d2x, dx);
-        if (edge) xclamp<R>(S, x0, c0, first, last, d2x, dx);
+        if (EDGE) {
+            xderivs<R>(w, P, d2x, dx);
+            xclamp<R>(S, x0, c0, first, last, d2x, dx);
+        } else {
+            // space_deriv2x only: no first x derivative outside the corners
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+                float s2 = 0.f;
+#pragma unroll
+                for (int i = 0; i <= R; ++i) s2 = s2 + P.c2[i] * (w[4 + e + i] + w[4 + e - i]);
+                d2x[e] = s2;
+                dx[e] = 0.f;
+            }
+        }
 
         // strip-local y derivative of the old y-direction phi (pml_matrices_y :335)
         float dphy[4];
@@ -405,7 +419,7 @@ __device__ __forceinline__ void bottom_rows(const StepParams& P, const WorkItem&
         to_arr(st[SB_PY + lane], phy);
         to_arr(st[SB_CY + lane], chy);
         float phx[4] = {0.f, 0.f, 0.f, 0.f}, chx[4] = {0.f, 0.f, 0.f, 0.f}, dphx[4] = {0.f, 0.f, 0.f, 0.f};
-        if (edge) {
+        if (EDGE) {
             if (lane_corner) {
                 to_arr(st[SB_PX + lane], phx);
                 to_arr(st[SB_CX + lane], chx);
@@ -421,7 +435,7 @@ __device__ __forceinline__ void bottom_rows(const StepParams& P, const WorkItem&
                 p3[e] = 0.f;
                 continue;
             }
-            const bool left = c < dn, right = c >= dn + nx;
+            const bool left = EDGE && c < dn, right = EDGE && c >= dn + nx;
             // factor index: strip factor(j); corners factor(max(i,j)) with the
             // ld/rd orientation (solver_PML_coeffs.f90:240-267)
             int fi = jl;
@@ -986,20 +1000,22 @@ __global__ void __launch_bounds__(128) k_step_strip(const __grid_constant__ Step
     cp_wait<0>();
 }
 
-// Bottom pad rows of every tile (the boundary list after its nstrip side
-// strip items).  Runs on its own stream, concurrently with k_step_interior
-// and k_step_strip.
+// Bottom pad rows: the tiles without corners are the nbot items after the
+// nstrip side strips of the boundary list, the two corner tiles follow.
+// Each runs on its own stream, concurrently with k_step_interior.
 constexpr int BND_SMEM = 4 * BOT_DEPTH * SB_SIZE * 16;
 
-template <int R, int MODE>
-__global__ void __launch_bounds__(128) k_step_bottom(const __grid_constant__ StepParams P) {
+template <int R, int MODE, bool EDGE>
+__global__ void __launch_bounds__(128, EDGE ? 2 : 3) k_step_bottom(const __grid_constant__ StepParams P) {
     extern __shared__ float4 smem[];
     const int lane = threadIdx.x & 31;
-    const int wid = P.nstrip + blockIdx.x * 4 + (threadIdx.x >> 5);
-    if (wid >= P.nitems) return;
+    const int base = EDGE ? P.nstrip + P.nbot : P.nstrip;
+    const int end = EDGE ? P.nitems : P.nstrip + P.nbot;
+    const int wid = base + blockIdx.x * 4 + (threadIdx.x >> 5);
+    if (wid >= end) return;
     float4* ring = smem + (threadIdx.x >> 5) * (BOT_DEPTH * SB_SIZE);
     const WorkItem it = P.items[wid];
-    bottom_rows<R, MODE>(P, it, ring, lane);
+    bottom_rows<R, MODE, EDGE>(P, it, ring, lane);
 }
 
 // Opt the step kernels into the dynamic shared memory they use (the
@@ -1014,7 +1030,11 @@ cudaError_t configure_step_kernels() {
         e = cudaFuncSetAttribute(k_step_interior<R_, M_, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,       \
                                  M_ == 1 ? IN_SMEM_IMG : IN_SMEM);                                                 \
     if (e == cudaSuccess)                                                                                         \
-        e = cudaFuncSetAttribute(k_step_bottom<R_, M_>, cudaFuncAttributeMaxDynamicSharedMemorySize, BND_SMEM);    \
+        e = cudaFuncSetAttribute(k_step_bottom<R_, M_, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,        \
+                                 BND_SMEM);                                                                        \
+    if (e == cudaSuccess)                                                                                         \
+        e = cudaFuncSetAttribute(k_step_bottom<R_, M_, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,         \
+                                 BND_SMEM);                                                                        \
     if (e == cudaSuccess)                                                                                         \
         e = cudaFuncSetAttribute(k_step_strip<R_, M_, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,             \
                                  strip_smem<1>());                                                                 \
@@ -1026,15 +1046,35 @@ cudaError_t configure_step_kernels() {
     FWI_CFG(4, 0)
     FWI_CFG(4, 1)
 #undef FWI_CFG
+    // The step kernels share SMs; with the largest shared-memory carveout
+    // every one of them reaches its register-limited occupancy.
+#define FWI_CO(K_)                                                                                             \
+    if (e == cudaSuccess)                                                                                      \
+        e = cudaFuncSetAttribute(K_, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
+#define FWI_CO_ALL(R_, M_)                     \
+    FWI_CO((k_step_interior<R_, M_, false>))   \
+    FWI_CO((k_step_interior<R_, M_, true>))    \
+    FWI_CO((k_step_bottom<R_, M_, false>))     \
+    FWI_CO((k_step_bottom<R_, M_, true>))      \
+    FWI_CO((k_step_strip<R_, M_, 1>))          \
+    FWI_CO((k_step_strip<R_, M_, 2>))
+    FWI_CO_ALL(3, 0)
+    FWI_CO_ALL(3, 1)
+    FWI_CO_ALL(4, 0)
+    FWI_CO_ALL(4, 1)
+#undef FWI_CO_ALL
+#undef FWI_CO
     return e;
 }
 
-// Interior kernel on stream sm, bottom kernel on sb, strip kernel on ss (the
-// caller orders the streams around each time step).  kstrip = columns per
+// Interior kernel on stream sm, bottom tiles without corners on sb, side
+// strips and the corner tiles on ss (the caller orders the streams around
+// each time step).  kstrip = columns per
 // lane of the strip kernel (ceil(strip width / 32)).
 cudaError_t launch_step(int acc, int mode, int kstrip, const StepParams& pm, const StepParams& pb, cudaStream_t sm,
                         cudaStream_t sb, cudaStream_t ss) {
-    const int bm = (pm.nitems + 3) / 4, bs = (pb.nstrip + 3) / 4, bb = (pb.nitems - pb.nstrip + 3) / 4;
+    const int bm = (pm.nitems + 3) / 4, bs = (pb.nstrip + 3) / 4, bb = (pb.nbot + 3) / 4,
+              be = (pb.nitems - pb.nstrip - pb.nbot + 3) / 4;
     if (kstrip != 1 && kstrip != 2) return cudaErrorInvalidValue;
 #define FWI_LAUNCH(R_, M_)                                                                                  \
     do {                                                                                                   \
@@ -1042,7 +1082,8 @@ cudaError_t launch_step(int acc, int mode, int kstrip, const StepParams& pm, con
             if (kstrip == 1) k_step_strip<R_, M_, 1><<<bs, 128, strip_smem<1>(), ss>>>(pb);                 \
             else k_step_strip<R_, M_, 2><<<bs, 128, strip_smem<2>(), ss>>>(pb);                            \
         }                                                                                                  \
-        if (bb) k_step_bottom<R_, M_><<<bb, 128, BND_SMEM, sb>>>(pb);                                      \
+        if (be) k_step_bottom<R_, M_, true><<<be, 128, BND_SMEM, ss>>>(pb);                                \
+        if (bb) k_step_bottom<R_, M_, false><<<bb, 128, BND_SMEM, sb>>>(pb);                               \
         if (bm) {                                                                                          \
             if (pm.snap >= 0)                                                                              \
                 k_step_interior<R_, M_, true><<<bm, 128, M_ == 1 ? IN_SMEM_IMG : IN_SMEM, sm>>>(pm);       \

@@ -270,9 +270,9 @@ int validate_geometry(const ShotGeom& g, const Layout& l, int shot) {
 // inject the sources and record the receivers, adjoint lists inject the
 // adjoint sources at the receivers.
 struct Lists {
-    // boundary lists: nstrip strips, nbot bottom tiles without corners, the corner tiles
+    // boundary lists: nstrip side-strip items (bottom rows first), then the bottom tiles
     std::vector<WorkItem> int_fwd, int_adj, bnd_fwd, bnd_adj;
-    int nstrip = 0, nbot = 0, kstrip = 1;
+    int nstrip = 0, kstrip = 1;
     std::vector<SrcEnt> src_fwd, src_adj;
     std::vector<RecEnt> recs;
 };
@@ -322,14 +322,15 @@ void append_item(Lists& L_, std::vector<WorkItem>& items, std::vector<SrcEnt>& s
     items.push_back(it);
 }
 
-constexpr int BOTTOM_BAND = 9;  // rows per bottom-pad work item
-constexpr int STRIP_BAND = 16;  // rows per side-strip work item
+constexpr int BOTTOM_BAND = 9;        // rows per bottom-tile work item
+constexpr int STRIP_BAND = 16;        // rows per side-strip work item (model rows)
+constexpr int STRIP_BOTTOM_BAND = 5;  // rows per side-strip work item (bottom pad rows)
 
 // Work lists for a set of shots (local shot index = position in `geoms`).
 // All shots share dn (one acc / dpml per launch), hence one kstrip.
 Lists build_lists(const std::vector<ShotGeom>& geoms, const std::vector<Layout>& lays, int band_rows) {
     Lists out;
-    std::vector<WorkItem> strip_f, strip_a, bot_f, bot_a, cor_f, cor_a;
+    std::vector<WorkItem> sbot_f, sbot_a, strip_f, strip_a, bot_f, bot_a;
     if (!lays.empty()) out.kstrip = lays[0].kstrip;
     auto bands = [](int n, int rows, auto&& fn) {
         const int nb = std::max(1, (n + rows - 1) / rows);
@@ -349,8 +350,12 @@ Lists build_lists(const std::vector<ShotGeom>& geoms, const std::vector<Layout>&
             if (pr < l.dn) continue;  // top pad: identically zero, never recorded
             recs.push_back(RecEnt{pr, l.off + pc, (int)i});
         }
-        // interior columns [sl, sr): 128-column tiles in bands of band_rows
-        const int xa = l.off + l.sl, xb = l.off + l.sr;
+        std::vector<SrcEnt> none;
+        const int xa = l.off + l.sl, xb = l.off + l.sr;  // interior columns, physical
+        const int yb0 = l.nyt - l.dn;                    // first bottom pad row
+        // interior columns: 128-column tiles, model rows in bands of band_rows,
+        // bottom pad rows in bands of about BOTTOM_BAND (the y-phi is
+        // ping-ponged, so bands are independent)
         if (xa < xb) {
             bands(l.ny, band_rows, [&](int y0, int y1) {
                 for (int t = xa / TILE; t <= (xb - 1) / TILE; ++t) {
@@ -361,39 +366,35 @@ Lists build_lists(const std::vector<ShotGeom>& geoms, const std::vector<Layout>&
                                 false, c0, c1);
                 }
             });
+            bands(l.dn, BOTTOM_BAND, [&](int j0, int j1) {
+                for (int t = xa / TILE; t <= (xb - 1) / TILE; ++t) {
+                    const int c0 = std::max(t * TILE, xa), c1 = std::min((t + 1) * TILE, xb);
+                    append_item(out, bot_f, out.src_fwd, none, recs, (int)s, t, yb0 + j0, yb0 + j1, 1, true, c0, c1);
+                    append_item(out, bot_a, out.src_adj, none, recs, (int)s, t, yb0 + j0, yb0 + j1, 1, false, c0, c1);
+                }
+            });
         }
-        // side strips of the model rows
-        bands(l.ny, STRIP_BAND, [&](int y0, int y1) {
-            for (int side = 0; side < 2; ++side) {
-                const int c0 = l.off + (side ? l.sr : 0), c1 = l.off + (side ? l.nxt : l.sl);
-                if (c1 <= c0) continue;
+        // side strips: model rows and bottom pad rows
+        for (int side = 0; side < 2; ++side) {
+            const int c0 = l.off + (side ? l.sr : 0), c1 = l.off + (side ? l.nxt : l.sl);
+            if (c1 <= c0) continue;
+            bands(l.ny, STRIP_BAND, [&](int y0, int y1) {
                 append_item(out, strip_f, out.src_fwd, cells_f, recs, (int)s, side, l.dn + y0, l.dn + y1, 2, true,
                             c0, c1);
                 append_item(out, strip_a, out.src_adj, cells_a, recs, (int)s, side, l.dn + y0, l.dn + y1, 2, false,
                             c0, c1);
-            }
-        });
-        // bottom pad in bands of about BOTTOM_BAND rows (the y-phi is ping-ponged,
-        // so bands are independent)
-        std::vector<SrcEnt> none;
-        bands(l.dn, BOTTOM_BAND, [&](int j0, int j1) {
-            for (int t = 0; t < l.ntiles; ++t) {
-                const bool corner = t == 0 || t == l.ntiles - 1;
-                append_item(out, corner ? cor_f : bot_f, out.src_fwd, none, recs, (int)s, t, l.nyt - l.dn + j0,
-                            l.nyt - l.dn + j1, 1, true, t * TILE, (t + 1) * TILE);
-                append_item(out, corner ? cor_a : bot_a, out.src_adj, none, recs, (int)s, t, l.nyt - l.dn + j0,
-                            l.nyt - l.dn + j1, 1, false, t * TILE, (t + 1) * TILE);
-            }
-        });
+            });
+            bands(l.dn, STRIP_BOTTOM_BAND, [&](int j0, int j1) {
+                append_item(out, sbot_f, out.src_fwd, none, recs, (int)s, side, yb0 + j0, yb0 + j1, 3, true, c0, c1);
+                append_item(out, sbot_a, out.src_adj, none, recs, (int)s, side, yb0 + j0, yb0 + j1, 3, false, c0,
+                            c1);
+            });
+        }
     }
-    out.nstrip = (int)strip_f.size();
-    out.nbot = (int)bot_f.size();
-    out.bnd_fwd = strip_f;
-    out.bnd_fwd.insert(out.bnd_fwd.end(), bot_f.begin(), bot_f.end());
-    out.bnd_fwd.insert(out.bnd_fwd.end(), cor_f.begin(), cor_f.end());
-    out.bnd_adj = strip_a;
-    out.bnd_adj.insert(out.bnd_adj.end(), bot_a.begin(), bot_a.end());
-    out.bnd_adj.insert(out.bnd_adj.end(), cor_a.begin(), cor_a.end());
+    // boundary lists: the strip warps (the short bottom-row bands first), then the bottom tiles
+    out.nstrip = (int)(sbot_f.size() + strip_f.size());
+    for (auto* v : {&sbot_f, &strip_f, &bot_f}) out.bnd_fwd.insert(out.bnd_fwd.end(), v->begin(), v->end());
+    for (auto* v : {&sbot_a, &strip_a, &bot_a}) out.bnd_adj.insert(out.bnd_adj.end(), v->begin(), v->end());
     return out;
 }
 
@@ -526,7 +527,7 @@ struct StepSet {
 };
 
 int step_kernels(const StepSet& ps) {
-    return (ps.pm.nitems > 0) + (ps.pb.nstrip > 0) + (ps.pb.nbot > 0) + (ps.pb.nitems > ps.pb.nstrip + ps.pb.nbot);
+    return (ps.pm.nitems > 0) + (ps.pb.nstrip > 0) + (ps.pb.nitems > ps.pb.nstrip);
 }
 
 // One time step: interior tiles on st, bottom tiles on st2, side strips on
@@ -535,8 +536,7 @@ int step_kernels(const StepSet& ps) {
 // wait on an event with no new node on st in between would accumulate
 // dependencies under stream capture).
 int step_fork_join(int acc, int mode, const StepSet& ps, cudaStream_t st, cudaStream_t st2) {
-    const bool has_m = ps.pm.nitems > 0, has_b = ps.pb.nbot > 0;
-    const bool has_s = ps.pb.nstrip > 0 || ps.pb.nitems > ps.pb.nstrip + ps.pb.nbot;
+    const bool has_m = ps.pm.nitems > 0, has_b = ps.pb.nitems > ps.pb.nstrip, has_s = ps.pb.nstrip > 0;
     L().launches += step_kernels(ps);
     if (!has_m || (!has_s && !has_b)) {
         CK(launch_step(acc, mode, ps.kstrip, ps.pm, ps.pb, st, st, st));
@@ -789,7 +789,6 @@ int fwi_solver_acoustic_ss(const int* rank, const int* iprop_, const int* NumSou
     ps.pb.items = sg.d_items_b.as<WorkItem>();
     ps.pb.nitems = (int)(adj ? lists.bnd_adj.size() : lists.bnd_fwd.size());
     ps.pb.nstrip = lists.nstrip;
-    ps.pb.nbot = lists.nbot;
     ps.kstrip = lists.kstrip;
     TRY(run_time_loop(acc, adj ? 1 : 0, nt, store_snap, nt_store, iprop == 1, ps, st, L().aux));
 
@@ -953,7 +952,7 @@ struct fwi_survey {
     // per-wave lists
     struct WaveDev {
         DBuf items_if, items_ia, items_bf, items_ba, src_f, src_a, recs, shots_f, shots_a, stack;
-        int n_if = 0, n_ia = 0, n_bf = 0, n_ba = 0, n_strip = 0, n_bot = 0, kstrip = 1;
+        int n_if = 0, n_ia = 0, n_bf = 0, n_ba = 0, n_strip = 0, kstrip = 1;
         cudaGraphExec_t graph[3] = {nullptr, nullptr, nullptr};
         long long graph_kernels[3] = {0, 0, 0};  // kernel nodes per graph
         DBuf save_jobs, restore_jobs;  // checkpoint copies: [ckpt][shot][field]
@@ -1049,7 +1048,6 @@ int survey_prepare_waves(fwi_survey* s) {
         wd->n_bf = (int)lists.bnd_fwd.size();
         wd->n_ba = (int)lists.bnd_adj.size();
         wd->n_strip = lists.nstrip;
-        wd->n_bot = lists.nbot;
         wd->kstrip = lists.kstrip;
         s->wdev.push_back(std::move(wd));
     }
@@ -1255,7 +1253,6 @@ int rc_adjoint(fwi_survey* s, size_t wi, StepSet ps, cudaStream_t st, cudaStream
     psf.pb.items = wd.items_bf.as<WorkItem>();
     psf.pb.nitems = wd.n_bf;
     psf.pb.nstrip = wd.n_strip;
-    psf.pb.nbot = wd.n_bot;
     psf.kstrip = wd.kstrip;
     ps.pm.items = wd.items_ia.as<WorkItem>();
     ps.pm.nitems = wd.n_ia;
@@ -1266,7 +1263,6 @@ int rc_adjoint(fwi_survey* s, size_t wi, StepSet ps, cudaStream_t st, cudaStream
     ps.pb.items = wd.items_ba.as<WorkItem>();
     ps.pb.nitems = wd.n_ba;
     ps.pb.nstrip = wd.n_strip;
-    ps.pb.nbot = wd.n_bot;
     ps.kstrip = wd.kstrip;
     int cur = s->rc_J - 1;
     size_t evi = 0;
@@ -1334,7 +1330,6 @@ int issue_wave(fwi_survey* s, size_t wi, int step, cudaStream_t st, cudaStream_t
     ps.pb.items = wd.items_bf.as<WorkItem>();
     ps.pb.nitems = wd.n_bf;
     ps.pb.nstrip = wd.n_strip;
-    ps.pb.nbot = wd.n_bot;
     ps.kstrip = wd.kstrip;
     if (s->rc_C) {
         TRY(rc_forward(s, wi, step, ps, st, st2));
@@ -1377,7 +1372,6 @@ int issue_wave(fwi_survey* s, size_t wi, int step, cudaStream_t st, cudaStream_t
     ps.pb.items = wd.items_ba.as<WorkItem>();
     ps.pb.nitems = wd.n_ba;
     ps.pb.nstrip = wd.n_strip;
-    ps.pb.nbot = wd.n_bot;
     ps.kstrip = wd.kstrip;
     TRY(run_time_loop(D.acc, 1, D.nt, D.store_snap, s->nt_store, true, ps, st, st2));
     LK(launch_stack(s->d_G.as<double>(), D.ny, D.nx_model, wd.stack.p, (int)w.size(), D.grad_form, st));
@@ -1688,7 +1682,6 @@ int time_wave0_steps(fwi_survey* s, int steps, float* ms) {
     ps.pb.items = wd.items_bf.as<WorkItem>();
     ps.pb.nitems = wd.n_bf;
     ps.pb.nstrip = wd.n_strip;
-    ps.pb.nbot = wd.n_bot;
     ps.kstrip = wd.kstrip;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     if (ms) {
@@ -1905,7 +1898,6 @@ extern "C" int fwi_solver_forward_noalloc(int NumSou, int NumRec, const int* nxS
     ps.pb.items = reinterpret_cast<WorkItem*>(sb + o_bm);
     ps.pb.nitems = (int)lists.bnd_fwd.size();
     ps.pb.nstrip = lists.nstrip;
-    ps.pb.nbot = lists.nbot;
     ps.kstrip = lists.kstrip;
     TRY(run_time_loop(acc, 0, nt, nt + 1, 0, false, ps, st, L().aux));
     LK(launch_rec_last(Rec_point_dev, nt, NumRec, st));

@@ -11,7 +11,8 @@
 //   go to one warp per band with one column per lane; the interior columns
 //   [sl, sr) go to 128-column tiles, one warp per tile and band (4 columns
 //   per lane, float4), with stores masked to [sl, sr) in the two partial
-//   tiles.  Bottom pad rows go to 128-column tiles of the whole width.
+//   tiles.  Bottom pad rows are split the same way (strip warps for the
+//   corners and the columns next to them, 128-column tiles for [sl, sr)).
 //   Every warp marches down its band with a register queue of 2*acc+1 rows.
 #pragma once
 #include <cstdint>
@@ -37,7 +38,8 @@ struct WorkItem {               // one warp's work in a step launch
     int shot;
     int tile;                   // tile index (x0 = tile*TILE physical); side strip: 0 left, 1 right
     int y0, y1;                 // padded rows [y0, y1)
-    int kind;                   // 0 = interior model rows, 1 = bottom pad rows, 2 = side strip
+    int kind;                   // 0 = interior model rows, 1 = bottom pad rows (interior columns),
+                                // 2 = side strip, model rows; 3 = side strip, bottom pad rows
     int s0, s1;                 // SrcEnt range (sorted by row)
     int r0, r1;                 // RecEnt range (sorted by row)
     int pad_;
@@ -75,8 +77,8 @@ struct StepParams {
     const float* fA;            // CPML factors (dn entries, 0-based)
     const float* fB;
     int nitems;
-    int nstrip;                 // boundary list: the first nstrip items are side strips (kind 2),
-    int nbot;                   // then nbot bottom tiles without corners, then the corner tiles
+    int nstrip;                 // boundary list: the first nstrip items are side strips (kinds 2, 3),
+                                // the bottom tiles follow
     int t;                      // k-2: source column / receiver row this step
     int parity;                 // k & 1: which buffer holds p_1 (written as p_3)
     int snap;                   // snapshot block this step, -1 if none

@@ -275,25 +275,25 @@ template <int N>
 __device__ __forceinline__ void cp_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
 
 // One prefetch stage of the bottom kernel: p(y+R), p_1(y), c2(y), y-phi(y),
-// y-chi(y), x-phi(y), x-chi(y), the y-phi row the derivative queue needs
-// next (jl+1+R), and the halo float4 of p(y).
-constexpr int SB_P = 0, SB_P1 = 32, SB_C2 = 64, SB_PY = 96, SB_CY = 128, SB_PX = 160, SB_CX = 192, SB_FA = 224,
-              SB_HL = 256, SB_HR = 257, SB_SIZE = 258;
+// y-chi(y), the y-phi row the derivative queue needs next (jl+1+R), and the
+// halo float4 of p(y).
+constexpr int SB_P = 0, SB_P1 = 32, SB_C2 = 64, SB_PY = 96, SB_CY = 128, SB_FA = 160, SB_HL = 192, SB_HR = 193,
+              SB_SIZE = 194;
 constexpr int BOT_DEPTH = 3;
 constexpr int BOT_SMEM = 4 * BOT_DEPTH * SB_SIZE * 16;
 
-// Bottom pad rows [it.y0, it.y1) of one tile: bottom strip and bottom
-// corners.  The y-direction phi is ping-ponged between two buffers (old read
-// from one, new written to the other), so the strip-local derivative of the
-// old phi can be taken in any band of the bottom pad.
-// EDGE: the first or last tile, which holds the bottom corners (x- and
-// y-CPML); the other tiles have the y-CPML only and skip the x-CPML terms.
-template <int R, int MODE, bool EDGE>
+// Bottom pad rows [it.y0, it.y1) of one tile, interior columns [sl, sr)
+// only: the bottom CPML strip (pml_matrices_y, solver_PML_matrices.f90:42-81);
+// the corners lie in the side strips.  The first and last tile of the range
+// may be partial: lanes outside it compute but store nothing.  The
+// y-direction phi is ping-ponged between two buffers (old read from one, new
+// written to the other), so the strip-local derivative of the old phi can be
+// taken in any band of the bottom pad.
+template <int R, int MODE>
 __device__ __forceinline__ void bottom_rows(const StepParams& P, const WorkItem& it, float4* ring, int lane) {
     const ShotDev& S = P.shots[it.shot];
-    const int pitch = S.pitch, dn = S.dn, nx = S.nx, nxt = S.nxt, nyt = S.nyt;
-    const int x0 = it.tile * TILE, xl = x0 + 4 * lane, c0 = xl - S.off;
-    const bool first = it.tile == 0, last = it.tile == S.ntiles - 1, edge = EDGE;
+    const int pitch = S.pitch, dn = S.dn, nyt = S.nyt;
+    const int x0 = it.tile * TILE, xl = x0 + 4 * lane;
     const float* PC = P.parity ? S.pa : S.pb;
     float* P1 = P.parity ? S.pb : S.pa;
     const float* PHO = P.parity ? S.phy2 : S.phy;  // old y-phi
@@ -301,9 +301,10 @@ __device__ __forceinline__ void bottom_rows(const StepParams& P, const WorkItem&
     const int yb0 = nyt - dn;
     const int j0 = it.y0 - yb0, j1 = it.y1 - yb0;
     const int jA = max(j0, R), jB = min(j1 - 1, dn - 1 - R);  // rows with an unclamped phi derivative
-    bool lane_corner = false;
-    if (edge) lane_corner = (c0 < dn) || (c0 + 3 >= dn + nx);
     const bool has_hl = (lane == 0) && (x0 > 0), has_hr = (lane == 31) && (x0 + TILE < pitch);
+    // this lane stores its elements [lo, hi): the interior columns [sl, sr)
+    const int lo = S.off + S.sl - xl, hi = S.off + S.sr - xl;
+    const bool full = lo <= 0 && hi >= 4;
 
     auto issue = [&](int jl, int slot) {
         float4* st = ring + slot * SB_SIZE;
@@ -314,10 +315,6 @@ __device__ __forceinline__ void bottom_rows(const StepParams& P, const WorkItem&
         cp16(st + SB_C2 + lane, S.c2 + ro);
         cp16(st + SB_PY + lane, PHO + ro);
         cp16(st + SB_CY + lane, S.chy + ro);
-        if (lane_corner) {
-            cp16(st + SB_PX + lane, S.phx + ro);
-            cp16(st + SB_CX + lane, S.chx + ro);
-        }
         if (jl >= jA && jl <= jB) cp16(st + SB_FA + lane, PHO + (size_t)(yb0 + jl + R) * pitch + xl);
         if (has_hl) cp16(st + SB_HL, PC + (size_t)y * pitch + x0 - 4);
         if (has_hr) cp16(st + SB_HR, PC + (size_t)y * pitch + x0 + TILE);
@@ -384,20 +381,14 @@ __device__ __forceinline__ void bottom_rows(const StepParams& P, const WorkItem&
         const float4 hl = has_hl ? st[SB_HL] : z4, hr = has_hr ? st[SB_HR] : z4;
         float w[12];
         window(q[R], hl, hr, lane, w);
-        float d2x[4], dx[4];
-        if (EDGE) {
-            xderivs<R>(w, P, d2x, dx);
-            xclamp<R>(S, x0, c0, first, last, d2x, dx);
-        } else {
-            // space_deriv2x only: no first x derivative outside the corners
+        // space_deriv2x (no clamp and no first x derivative: interior columns)
+        float d2x[4];
 #pragma unroll
-            for (int e = 0; e < 4; ++e) {
-                float s2 = 0.f;
+        for (int e = 0; e < 4; ++e) {
+            float s2 = 0.f;
 #pragma unroll
-                for (int i = 0; i <= R; ++i) s2 = s2 + P.c2[i] * (w[4 + e + i] + w[4 + e - i]);
-                d2x[e] = s2;
-                dx[e] = 0.f;
-            }
+            for (int i = 0; i <= R; ++i) s2 = s2 + P.c2[i] * (w[4 + e + i] + w[4 + e - i]);
+            d2x[e] = s2;
         }
 
         // strip-local y derivative of the old y-direction phi (pml_matrices_y :335)
@@ -415,57 +406,33 @@ __device__ __forceinline__ void bottom_rows(const StepParams& P, const WorkItem&
             for (int e = 0; e < 4; ++e) dphy[e] = dphyBot[e];
         }
 
-        float phy[4], chy[4];
+        float phy[4], chy[4], p3[4];
         to_arr(st[SB_PY + lane], phy);
         to_arr(st[SB_CY + lane], chy);
-        float phx[4] = {0.f, 0.f, 0.f, 0.f}, chx[4] = {0.f, 0.f, 0.f, 0.f}, dphx[4] = {0.f, 0.f, 0.f, 0.f};
-        if (EDGE) {
-            if (lane_corner) {
-                to_arr(st[SB_PX + lane], phx);
-                to_arr(st[SB_CX + lane], chx);
-            }
-            phi_xderiv<R>(S, P, from_arr(phx), lane, x0, c0, first, last, dphx);
-        }
-
-        float p3[4];
+        // bottom strip: factor(j)  (solver_PML_coeffs.f90, pml_matrices_y)
+        const float A = __ldg(P.fA + jl), B = __ldg(P.fB + jl);
 #pragma unroll
         for (int e = 0; e < 4; ++e) {
-            const int c = c0 + e;
-            if (c < 0 || c >= nxt) {
-                p3[e] = 0.f;
-                continue;
-            }
-            const bool left = EDGE && c < dn, right = EDGE && c >= dn + nx;
-            // factor index: strip factor(j); corners factor(max(i,j)) with the
-            // ld/rd orientation (solver_PML_coeffs.f90:240-267)
-            int fi = jl;
-            if (left) fi = max(jl, dn - 1 - c);
-            if (right) fi = max(jl, c - dn - nx);
-            const float A = __ldg(P.fA + fi), B = __ldg(P.fB + fi);
             const float phyn = A * phy[e] + B * dy[e];
             const float chyn = A * chy[e] + B * (d2y[e] + dphy[e]);
             const float propy = dphy[e] + chyn;
             phy[e] = phyn;
             chy[e] = chyn;
-            if (!left && !right) {
-                p3[e] = ((-pm1[e]) + 2.f * pc[e]) + cc[e] * ((d2x[e] + d2y[e]) + propy);
-            } else {
-                const float phxn = A * phx[e] + B * dx[e];
-                const float chxn = A * chx[e] + B * (d2x[e] + dphx[e]);
-                const float propx = dphx[e] + chxn;
-                phx[e] = phxn;
-                chx[e] = chxn;
-                const float tt = ((-pm1[e]) + 2.f * pc[e]) + cc[e] * ((d2x[e] + d2y[e]) + propx);
-                p3[e] = tt + cc[e] * propy;
-            }
+            p3[e] = ((-pm1[e]) + 2.f * pc[e]) + cc[e] * ((d2x[e] + d2y[e]) + propy);
         }
-        st4(PHN + ro, from_arr(phy));
-        st4(S.chy + ro, from_arr(chy));
-        if (lane_corner) {
-            st4(S.phx + ro, from_arr(phx));
-            st4(S.chx + ro, from_arr(chx));
+        if (full) {
+            st4(PHN + ro, from_arr(phy));
+            st4(S.chy + ro, from_arr(chy));
+            st4(P1 + ro, from_arr(p3));
+        } else {
+#pragma unroll
+            for (int e = 0; e < 4; ++e)
+                if (e >= lo && e < hi) {
+                    PHN[ro + e] = phy[e];
+                    S.chy[ro + e] = chy[e];
+                    P1[ro + e] = p3[e];
+                }
         }
-        st4(P1 + ro, from_arr(p3));
         if (MODE == 0 && P.record) record_row(P, S, y, xl, ri, it.r1, rrow, p3);
 
 #pragma unroll
@@ -707,161 +674,220 @@ __global__ void __launch_bounds__(128, (MODE == 1 && SNAP) ? 3 : 5) k_step_inter
 }
 
 // ---------------------------------------------------------------------------
-// Side strips of the model rows: the left strip [0, sl) and the right strip
-// [sr, nxt) of the logical columns, each at most 32*K columns wide.  One
-// warp per band of rows; lane l holds strip-local columns l, 32+l, ... (one
-// float per chunk), so the CPML arithmetic runs once per strip column.
+// Side strips: the logical columns [0, sl) and [sr, nxt), in the model rows
+// (x-CPML strips, kind 2) and in the bottom pad rows (the corners and the
+// y-CPML columns next to them, kind 3).  One warp per band of rows; lane l
+// holds the strip-local columns j = 32k + l (k < K), so the CPML arithmetic
+// runs once per strip column.  Rows live in shared-memory lines of 32K
+// columns plus M margin columns on either side, and every neighbour of a
+// cell, in x or y, is a plain shared load:
+//   p ring     QN lines, p row r in line r mod QN, with its halo columns;
+//   y-phi ring QN lines, the old y-phi row r (bottom rows);
+//   row slots  NA slots of NS lines: p_1, c2, x-phi, x-chi, y-chi of row y
+//              in slot y mod NA.
+// At step y the rings hold rows y-R..y+R and the slot of row y; LA rows
+// ahead are in flight (cp.async, 4 bytes per lane and column; every lane
+// waits for its own copies, then the warp synchronises before it reads the
+// other lanes' columns).
 // ---------------------------------------------------------------------------
-
-// Prefetch stage of the strip kernel (floats): p(y+R), p_1(y), c2(y),
-// x-phi(y), x-chi(y) per strip column, then the p(y) halo columns left of the
-// strip (lanes 32-R..31) and right of it (lanes 0..R-1).
-template <int K>
-struct StripSlot {
-    static constexpr int P = 0, P1 = 32 * K, C2 = 64 * K, PH = 96 * K, CH = 128 * K, HL = 160 * K,
-                         HR = 160 * K + 32, SIZE = 160 * K + 64;
+template <int R, int K>
+struct StripLayout {
+    static constexpr int M = 4;  // margin columns (>= R; keeps lines 16-byte multiples)
+    static constexpr int LINE = 32 * K + 2 * M;
+    static constexpr int LA = 4;  // rows of lookahead
+    static constexpr int QN = 2 * R + 1 + LA;
+    static constexpr int NA = LA + 1;
+    static constexpr int S_P1 = 0, S_C2 = 1, S_PX = 2, S_CX = 3, S_CY = 4, NS = 5;
+    static constexpr int P_RING = 0, Y_RING = QN * LINE, SLOTS = 2 * QN * LINE;
+    static constexpr int WARP = SLOTS + NA * NS * LINE;  // floats per warp
 };
-constexpr int STRIP_DEPTH = 8;  // rows in flight per warp
-template <int K>
+template <int R, int K>
 constexpr int strip_smem() {
-    return 4 * STRIP_DEPTH * StripSlot<K>::SIZE * 4;
+    return 4 * StripLayout<R, K>::WARP * 4;
 }
 
-// Value at strip-local column 32k + lane + d of a row held one column per
-// lane; columns left of the strip come from hl (lane 32+t holds column t,
-// -R <= t < 0), columns right of it from hr (lane j holds column 32K + j).
-// k and d are compile-time constants after unrolling.
-template <int K>
-__device__ __forceinline__ float nbr(const float (&v)[K], float hl, float hr, int k, int d, int lane) {
-    if (d == 0) return v[k];
-    const int t = lane + d;
-    const float a = __shfl_sync(FULL, v[k], t & 31);
-    const float o = (d > 0) ? ((k + 1 < K) ? v[k + 1 < K ? k + 1 : k] : hr) : ((k > 0) ? v[k > 0 ? k - 1 : 0] : hl);
-    const float b = __shfl_sync(FULL, o, t & 31);
-    if (d > 0) return t < 32 ? a : b;
-    return t >= 0 ? a : b;
-}
-
-// Value at the warp-uniform strip-local column j.
+// Value at the warp-uniform strip-local column j of a per-lane array.
 template <int K>
 __device__ __forceinline__ float bcast(const float (&v)[K], int j) {
     const float src = (K > 1 && j >= 32) ? v[K - 1] : v[0];
     return __shfl_sync(FULL, src, j & 31);
 }
 
-template <int R, int MODE, int K>
-__global__ void __launch_bounds__(128) k_step_strip(const __grid_constant__ StepParams P) {
-    using SL = StripSlot<K>;
-    extern __shared__ float sfl[];
-    const int lane = threadIdx.x & 31;
-    const int wid = blockIdx.x * 4 + (threadIdx.x >> 5);
-    if (wid >= P.nstrip) return;
-    float* ring = sfl + (threadIdx.x >> 5) * (STRIP_DEPTH * SL::SIZE);
-    const WorkItem it = P.items[wid];
+template <int R, int MODE, int K, bool BOT>
+__device__ __forceinline__ void strip_rows(const StepParams& P, const WorkItem& it, float* sw, int lane) {
+    using L = StripLayout<R, K>;
     const ShotDev& S = P.shots[it.shot];
-    const int pitch = S.pitch, dn = S.dn, nx = S.nx, nxt = S.nxt;
+    const int pitch = S.pitch, dn = S.dn, nx = S.nx, nxt = S.nxt, nyt = S.nyt;
     const bool right = it.tile != 0;
     const int cs = right ? S.sr : 0, ce = right ? nxt : S.sl;  // logical strip columns [cs, ce)
     const float* PC = P.parity ? S.pa : S.pb;  // p
     float* P1 = P.parity ? S.pb : S.pa;        // p_1, overwritten with p_3
+    const float* PHO = P.parity ? S.phy2 : S.phy;  // old y-phi (bottom rows)
+    float* PHN = P.parity ? S.phy : S.phy2;        // new y-phi
+    const int yb0 = nyt - dn;
+    const size_t xs = (size_t)S.off + cs;  // physical column of strip column 0
 
     int col[K];
-    bool valid[K], act[K], cpml[K];
+    bool valid[K], act[K], xc[K];
 #pragma unroll
     for (int k = 0; k < K; ++k) {
         col[k] = cs + 32 * k + lane;
-        valid[k] = col[k] < nxt;  // inside the grid (x-neighbour source)
+        valid[k] = col[k] < nxt;  // inside the grid (a neighbour of some cell)
         act[k] = col[k] < ce;     // updated by this warp
-        cpml[k] = act[k] && (col[k] < dn || col[k] >= dn + nx);
+        xc[k] = act[k] && (col[k] < dn || col[k] >= dn + nx);  // x-CPML column
     }
-    const int hlc = cs - 32 + lane, hrc = cs + 32 * K + lane;  // halo columns
-    const bool has_hl = lane >= 32 - R && hlc >= 0, has_hr = lane < R && hrc < nxt;
-    const size_t xs = (size_t)S.off + cs + lane;  // physical column of chunk 0
+    // halo columns, copied by lanes 0..R-1: left j = lane-R, right j = 32K+lane
+    const int jhl = lane - R, jhr = 32 * K + lane;
+    const bool has_hl = lane < R && cs + jhl >= 0, has_hr = lane < R && cs + jhr < nxt;
 
-    auto issue = [&](int y, int slot) {
-        float* st = ring + slot * SL::SIZE;
+    float* pring = sw + L::P_RING;
+    float* yring = sw + L::Y_RING;
+    float* slots = sw + L::SLOTS;
+    auto pline = [&](int r) { return pring + (r % L::QN) * L::LINE + L::M; };
+    auto yline = [&](int r) { return yring + (r % L::QN) * L::LINE + L::M; };
+    auto sline = [&](int y, int f) { return slots + ((y % L::NA) * L::NS + f) * L::LINE + L::M; };
+
+    // p row r (and the old y-phi row r) into the rings; rows past the grid
+    // are never read
+    auto issue_row = [&](int r) {
+        if (r > nyt - 1) return;
+        float* d = pline(r);
+        const float* src = PC + (size_t)r * pitch + xs;
+#pragma unroll
+        for (int k = 0; k < K; ++k)
+            if (valid[k]) cp4(d + 32 * k + lane, src + 32 * k + lane);
+        if (has_hl) cp4(d + jhl, src + jhl);
+        if (has_hr) cp4(d + jhr, src + jhr);
+        if (BOT && r >= yb0) {
+            float* e = yline(r);
+            const float* ysrc = PHO + (size_t)r * pitch + xs;
+#pragma unroll
+            for (int k = 0; k < K; ++k)
+                if (valid[k]) cp4(e + 32 * k + lane, ysrc + 32 * k + lane);
+        }
+    };
+    auto issue_slot = [&](int y) {
         const size_t ro = (size_t)y * pitch + xs;
 #pragma unroll
         for (int k = 0; k < K; ++k) {
-            const size_t o = ro + 32 * k;
-            if (valid[k]) cp4(st + SL::P + 32 * k + lane, PC + o + (size_t)R * pitch);
+            const int j = 32 * k + lane;
             if (act[k]) {
-                cp4(st + SL::P1 + 32 * k + lane, P1 + o);
-                cp4(st + SL::C2 + 32 * k + lane, S.c2 + o);
+                cp4(sline(y, L::S_P1) + j, P1 + ro + j);
+                cp4(sline(y, L::S_C2) + j, S.c2 + ro + j);
+                if (BOT) cp4(sline(y, L::S_CY) + j, S.chy + ro + j);
             }
-            if (cpml[k]) {
-                cp4(st + SL::PH + 32 * k + lane, S.phx + o);
-                cp4(st + SL::CH + 32 * k + lane, S.chx + o);
+            if (xc[k]) {
+                cp4(sline(y, L::S_PX) + j, S.phx + ro + j);
+                cp4(sline(y, L::S_CX) + j, S.chx + ro + j);
             }
         }
-        if (has_hl) cp4(st + SL::HL + lane, PC + (size_t)y * pitch + S.off + hlc);
-        if (has_hr) cp4(st + SL::HR + lane, PC + (size_t)y * pitch + S.off + hrc);
     };
-#pragma unroll
-    for (int i = 0; i < STRIP_DEPTH; ++i) {
-        if (it.y0 + i < it.y1) issue(it.y0 + i, i);
+    const int y0 = it.y0, y1 = it.y1;
+#pragma unroll 1
+    for (int i = 0; i < 2 * R; ++i) issue_row(y0 - R + i);
+    cp_commit();
+#pragma unroll 1
+    for (int i = 0; i < L::LA; ++i) {
+        if (y0 + i < y1) {
+            issue_row(y0 + i + R);
+            issue_slot(y0 + i);
+        }
         cp_commit();
     }
-    float q[K][2 * R + 1];
-#pragma unroll
-    for (int k = 0; k < K; ++k)
-#pragma unroll
-        for (int i = 0; i < 2 * R; ++i)
-            q[k][i] = valid[k] ? __ldg(PC + (size_t)(it.y0 - R + i) * pitch + xs + 32 * k) : 0.f;
 
     // clamp sources (warp-uniform strip-local columns): the p derivatives of
     // columns < R copy column R, of columns > nxt-1-R column nxt-1-R
     // (solver_space_derivs.f90:18-23, :84-94); the strip-local derivative of
-    // the old phi copies its value at strip index R / dn-1-R
+    // the old x-phi copies its value at strip index R / dn-1-R
     // (solver_PML_matrices.f90:15, :97 on the dn-wide strip array).
     const int jc = right ? (nxt - 1 - R - cs) : R;
     const int jlo = right ? (dn + nx + R - cs) : R;
     const int jhi = right ? (nxt - 1 - R - cs) : (dn - 1 - R);
+
+    // bottom rows: the y-phi derivative of rows jl < R is that of row R, of
+    // rows jl > dn-1-R that of row dn-1-R; rows below nyt-1-R take the p
+    // derivatives of row nyt-1-R (solver_space_derivs.f90:38-53, :109-128)
+    float dphyTop[K], dphyBot[K], d2yBot[K], dyBot[K];
+#pragma unroll
+    for (int k = 0; k < K; ++k) dphyTop[k] = dphyBot[k] = d2yBot[k] = dyBot[k] = 0.f;
+    if (BOT) {
+        const int j0 = y0 - yb0, j1 = y1 - yb0;
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+            if (!valid[k]) continue;
+            const size_t cx = xs + 32 * k + lane;
+            if (j0 < R) {
+                float s1 = 0.f;
+#pragma unroll
+                for (int i = 0; i <= R; ++i)
+                    s1 = s1 + (PHO[(size_t)(yb0 + R + i) * pitch + cx] - PHO[(size_t)(yb0 + R - i) * pitch + cx]) * P.c1[i];
+                dphyTop[k] = s1;
+            }
+            if (j1 - 1 > dn - 1 - R) {
+                const int yc = nyt - 1 - R;
+                float s1 = 0.f, s2 = 0.f, t1 = 0.f;
+#pragma unroll
+                for (int i = 0; i <= R; ++i) {
+                    s1 = s1 + (PHO[(size_t)(yc + i) * pitch + cx] - PHO[(size_t)(yc - i) * pitch + cx]) * P.c1[i];
+                    const float a = __ldg(PC + (size_t)(yc + i) * pitch + cx), b = __ldg(PC + (size_t)(yc - i) * pitch + cx);
+                    s2 = s2 + (a + b) * P.c2[i];
+                    t1 = t1 + (a - b) * P.c1[i];
+                }
+                dphyBot[k] = s1;
+                d2yBot[k] = s2;
+                dyBot[k] = t1;
+            }
+        }
+    }
+    float2 c1p[R + 1], c2p[R + 1];
+#pragma unroll
+    for (int i = 0; i <= R; ++i) {
+        c1p[i] = make_float2(P.c1[i], P.c1[i]);
+        c2p[i] = make_float2(P.c2[i], P.c2[i]);
+    }
 
     int si = it.s0, ri = it.r0;
     int srow = (si < it.s1) ? P.srcs[si].row : INT_MAX;
     int rrow = (ri < it.r1) ? P.recs[ri].row : INT_MAX;
     const size_t seg = (size_t)S.ntiles + (right ? 1 : 0);
 
-    int slot = 0;
-    for (int y = it.y0; y < it.y1; ++y) {
-        cp_wait<STRIP_DEPTH - 1>();
-        const float* st = ring + slot * SL::SIZE;
-        float pc[K], pm1[K], cc[K], ph[K], ch[K];
+#pragma unroll 1
+    for (int y = y0; y < y1; ++y) {
+        cp_wait<L::LA - 1>();
+        __syncwarp();
+        const int jl = y - yb0;  // bottom rows: index inside the bottom strip
+        const float* pl = pline(y);
+        const float* px = sline(y, L::S_PX);
+        float pc[K], d2x[K], dx[K], d2y[K], dy[K], dphx[K], dphy[K];
 #pragma unroll
         for (int k = 0; k < K; ++k) {
-            q[k][2 * R] = valid[k] ? st[SL::P + 32 * k + lane] : 0.f;
-            pc[k] = q[k][R];
-            pm1[k] = act[k] ? st[SL::P1 + 32 * k + lane] : 0.f;
-            cc[k] = act[k] ? st[SL::C2 + 32 * k + lane] : 0.f;
-            ph[k] = cpml[k] ? st[SL::PH + 32 * k + lane] : 0.f;
-            ch[k] = cpml[k] ? st[SL::CH + 32 * k + lane] : 0.f;
-        }
-        const float hl = has_hl ? st[SL::HL + lane] : 0.f, hr = has_hr ? st[SL::HR + lane] : 0.f;
-
-        // space_deriv2x / space_derivx, space_deriv2y, and the strip-local
-        // derivative of the old x-phi (pml_matrices_x :15)
-        float d2x[K], dx[K], d2y[K], dph[K];
-#pragma unroll
-        for (int k = 0; k < K; ++k) {
-            float s2 = 0.f, s1 = 0.f, sy = 0.f, sp = 0.f;
+            const int j = 32 * k + lane;
+            pc[k] = pl[j];
+            // (d2x, d2y): s2 = s2 + c2(i)*(p(j+i)+p(j-i)), s2 = s2 + (p(j+i)+p(j-i))*c2(i)
+            // (dx, dy):   s1 = s1 + (p(j+i)-p(j-i))*c1(i)
+            // (dphx, dphy): the same on the old phi
+            // space_deriv2x/2y, space_derivx/y (solver_space_derivs.f90:11-16, :38-45, :70-82, :109-116)
+            float2 a2 = make_float2(0.f, 0.f), a1 = make_float2(0.f, 0.f), ap = make_float2(0.f, 0.f);
 #pragma unroll
             for (int i = 0; i <= R; ++i) {
-                const float r = nbr<K>(pc, hl, hr, k, i, lane), l = nbr<K>(pc, hl, hr, k, -i, lane);
-                s2 = s2 + P.c2[i] * (r + l);
-                s1 = s1 + (r - l) * P.c1[i];
-                sy = sy + (q[k][R + i] + q[k][R - i]) * P.c2[i];
-                const float pr_ = nbr<K>(ph, 0.f, 0.f, k, i, lane), pl_ = nbr<K>(ph, 0.f, 0.f, k, -i, lane);
-                sp = sp + (pr_ - pl_) * P.c1[i];
+                const float2 hi_ = make_float2(pl[j + i], pline(y + i)[j]);
+                const float2 lo_ = make_float2(pl[j - i], pline(y - i)[j]);
+                a2 = __fadd2_rn(a2, mul0(__fadd2_rn(hi_, lo_), c2p[i]));
+                a1 = __fadd2_rn(a1, mul0(__fadd2_rn(hi_, make_float2(-lo_.x, -lo_.y)), c1p[i]));
+                const float2 fh = make_float2(px[j + i], BOT ? yline(y + i)[j] : 0.f);
+                const float2 fl = make_float2(px[j - i], BOT ? yline(y - i)[j] : 0.f);
+                ap = __fadd2_rn(ap, mul0(__fadd2_rn(fh, make_float2(-fl.x, -fl.y)), c1p[i]));
             }
-            d2x[k] = s2;
-            dx[k] = s1;
-            d2y[k] = sy;
-            dph[k] = sp;
+            d2x[k] = a2.x;
+            d2y[k] = a2.y;
+            dx[k] = a1.x;
+            dy[k] = a1.y;
+            dphx[k] = ap.x;
+            dphy[k] = ap.y;
         }
         {
             const float c2v = bcast<K>(d2x, jc), c1v = bcast<K>(dx, jc);
-            const float plo = bcast<K>(dph, jlo), phi_ = bcast<K>(dph, jhi);
+            const float plo = bcast<K>(dphx, jlo), phi_ = bcast<K>(dphx, jhi);
 #pragma unroll
             for (int k = 0; k < K; ++k) {
                 const int c = col[k];
@@ -869,9 +895,17 @@ __global__ void __launch_bounds__(128) k_step_strip(const __grid_constant__ Step
                     d2x[k] = c2v;
                     dx[k] = c1v;
                 }
-                const int il = right ? c - dn - nx : c;  // index inside the dn-wide CPML strip
-                if (il < R) dph[k] = plo;
-                else if (il > dn - 1 - R) dph[k] = phi_;
+                const int il = right ? c - dn - nx : c;  // index inside the dn-wide x-CPML strip
+                if (il < R) dphx[k] = plo;
+                else if (il > dn - 1 - R) dphx[k] = phi_;
+                if (BOT) {
+                    if (y > nyt - 1 - R) {
+                        d2y[k] = d2yBot[k];
+                        dy[k] = dyBot[k];
+                    }
+                    if (jl < R) dphy[k] = dphyTop[k];
+                    else if (jl > dn - 1 - R) dphy[k] = dphyBot[k];
+                }
             }
         }
 
@@ -879,45 +913,76 @@ __global__ void __launch_bounds__(128) k_step_strip(const __grid_constant__ Step
         float sv[K];
 #pragma unroll
         for (int k = 0; k < K; ++k) sv[k] = 0.f;
-        while (srow == y) {
+        while (!BOT && srow == y) {
             const SrcEnt e = P.srcs[si];
             const float val = __ldg(S.srcv + (size_t)e.vidx * S.nt + P.t);
 #pragma unroll
             for (int k = 0; k < K; ++k)
-                if (e.col == (int)xs + 32 * k) sv[k] = val;
+                if (e.col == (int)xs + 32 * k + lane) sv[k] = val;
             ++si;
             srow = (si < it.s1) ? P.srcs[si].row : INT_MAX;
         }
 
-        float p3[K];
-        const size_t ro = (size_t)y * pitch + xs;
+        float p3[K], pm1[K];
+        const size_t ro = (size_t)y * pitch + xs + lane;
 #pragma unroll
         for (int k = 0; k < K; ++k) {
-            const int c = col[k];
-            if (cpml[k]) {
-                // xl strip: factor(dn-i+1); xr strip: factor(i)  (solver_PML_matrices.f90:296-312)
-                const int fi = (c < dn) ? (dn - 1 - c) : (c - dn - nx);
-                const float A = __ldg(P.fA + fi), B = __ldg(P.fB + fi);
-                const float phn = A * ph[k] + B * dx[k];
-                const float chn = A * ch[k] + B * (d2x[k] + dph[k]);
-                const float prop = dph[k] + chn;
-                p3[k] = ((-pm1[k]) + 2.f * pc[k]) + cc[k] * ((d2x[k] + d2y[k]) + prop);
-                S.phx[ro + 32 * k] = phn;
-                S.chx[ro + 32 * k] = chn;
+            const int j = 32 * k + lane, c = col[k];
+            pm1[k] = sline(y, L::S_P1)[j];
+            const float cc = sline(y, L::S_C2)[j];
+            const float base = (-pm1[k]) + 2.f * pc[k];
+            if (!BOT) {
+                if (xc[k]) {
+                    // xl strip: factor(dn-i+1); xr strip: factor(i)  (solver_PML_matrices.f90:296-312)
+                    const int fi = (c < dn) ? (dn - 1 - c) : (c - dn - nx);
+                    const float A = __ldg(P.fA + fi), B = __ldg(P.fB + fi);
+                    const float phn = A * px[j] + B * dx[k];
+                    const float chn = A * sline(y, L::S_CX)[j] + B * (d2x[k] + dphx[k]);
+                    const float prop = dphx[k] + chn;
+                    p3[k] = base + cc * ((d2x[k] + d2y[k]) + prop);
+                    S.phx[ro + 32 * k] = phn;
+                    S.chx[ro + 32 * k] = chn;
+                } else {
+                    p3[k] = base + (((d2x[k] + d2y[k]) + sv[k]) * cc);
+                }
             } else {
-                p3[k] = ((-pm1[k]) + 2.f * pc[k]) + (((d2x[k] + d2y[k]) + sv[k]) * cc[k]);
+                // bottom strip factor(j); corners factor(max(i,j)) with the
+                // ld/rd orientation (solver_PML_coeffs.f90:240-267)
+                int fi = jl;
+                if (xc[k]) fi = max(jl, (c < dn) ? (dn - 1 - c) : (c - dn - nx));
+                if (!act[k]) fi = 0;
+                const float A = __ldg(P.fA + fi), B = __ldg(P.fB + fi);
+                const float phyn = A * yline(y)[j] + B * dy[k];
+                const float chyn = A * sline(y, L::S_CY)[j] + B * (d2y[k] + dphy[k]);
+                const float propy = dphy[k] + chyn;
+                if (xc[k]) {
+                    // corner, two stages (solver_acoustic_SS.f90:395-411)
+                    const float phxn = A * px[j] + B * dx[k];
+                    const float chxn = A * sline(y, L::S_CX)[j] + B * (d2x[k] + dphx[k]);
+                    const float propx = dphx[k] + chxn;
+                    const float tt = base + cc * ((d2x[k] + d2y[k]) + propx);
+                    p3[k] = tt + cc * propy;
+                    S.phx[ro + 32 * k] = phxn;
+                    S.chx[ro + 32 * k] = chxn;
+                } else {
+                    p3[k] = base + cc * ((d2x[k] + d2y[k]) + propy);
+                }
+                if (act[k]) {
+                    PHN[ro + 32 * k] = phyn;
+                    S.chy[ro + 32 * k] = chyn;
+                }
             }
         }
 
-        if (P.snap >= 0) {
+        if (!BOT && P.snap >= 0) {
             const int yrow = y - dn;
-            const size_t fb = (size_t)P.snap * (size_t)S.snap_stride + (size_t)yrow * pitch + xs;
-            float v[K];
+            const size_t fb = (size_t)P.snap * (size_t)S.snap_stride + (size_t)yrow * pitch + xs + lane;
             bool in[K];
 #pragma unroll
-            for (int k = 0; k < K; ++k) in[k] = act[k] && !cpml[k];
+            for (int k = 0; k < K; ++k) in[k] = act[k] && !xc[k];
             if (MODE == 0) {
                 // Fields(j, snap*nx+i) = (p_3 - p_1)*0.5/dt  (:447)
+                float v[K];
 #pragma unroll
                 for (int k = 0; k < K; ++k) v[k] = in[k] ? ((p3[k] - pm1[k]) * 0.5f) / P.dt : 0.f;
                 if (P.snap_form == 0) {
@@ -954,7 +1019,7 @@ __global__ void __launch_bounds__(128) k_step_strip(const __grid_constant__ Step
                 const float sc = (P.snap_form == 0)
                                      ? 1.f
                                      : __ldg(S.sscale + ((size_t)P.snap * S.ny + yrow) * (S.ntiles + 2) + seg);
-                const size_t ko = (size_t)yrow * pitch + xs;
+                const size_t ko = (size_t)yrow * pitch + xs + lane;
 #pragma unroll
                 for (int k = 0; k < K; ++k) {
                     if (!in[k]) continue;
@@ -983,124 +1048,111 @@ __global__ void __launch_bounds__(128) k_step_strip(const __grid_constant__ Step
                 const RecEnt r = P.recs[ri];
 #pragma unroll
                 for (int k = 0; k < K; ++k)
-                    if (r.col == (int)xs + 32 * k) S.rec[(size_t)r.ridx * S.nt + P.t] = p3[k];
+                    if (r.col == (int)xs + 32 * k + lane) S.rec[(size_t)r.ridx * S.nt + P.t] = p3[k];
                 ++ri;
                 rrow = (ri < it.r1) ? P.recs[ri].row : INT_MAX;
             }
         }
 
-#pragma unroll
-        for (int k = 0; k < K; ++k)
-#pragma unroll
-            for (int i = 0; i < 2 * R; ++i) q[k][i] = q[k][i + 1];
-        if (y + STRIP_DEPTH < it.y1) issue(y + STRIP_DEPTH, slot);
+        if (y + L::LA < y1) {
+            issue_row(y + L::LA + R);
+            issue_slot(y + L::LA);
+        }
         cp_commit();
-        slot = (slot + 1 == STRIP_DEPTH) ? 0 : slot + 1;
     }
     cp_wait<0>();
 }
 
-// Bottom pad rows: the tiles without corners are the nbot items after the
-// nstrip side strips of the boundary list, the two corner tiles follow.
-// Each runs on its own stream, concurrently with k_step_interior.
-constexpr int BND_SMEM = 4 * BOT_DEPTH * SB_SIZE * 16;
-
-template <int R, int MODE, bool EDGE>
-__global__ void __launch_bounds__(128, EDGE ? 2 : 3) k_step_bottom(const __grid_constant__ StepParams P) {
-    extern __shared__ float4 smem[];
+template <int R, int MODE, int K>
+__global__ void __launch_bounds__(128) k_step_strip(const __grid_constant__ StepParams P) {
+    extern __shared__ float sfl[];
     const int lane = threadIdx.x & 31;
-    const int base = EDGE ? P.nstrip + P.nbot : P.nstrip;
-    const int end = EDGE ? P.nitems : P.nstrip + P.nbot;
-    const int wid = base + blockIdx.x * 4 + (threadIdx.x >> 5);
-    if (wid >= end) return;
-    float4* ring = smem + (threadIdx.x >> 5) * (BOT_DEPTH * SB_SIZE);
+    const int wid = blockIdx.x * 4 + (threadIdx.x >> 5);
+    if (wid >= P.nstrip) return;
+    float* sw = sfl + (threadIdx.x >> 5) * StripLayout<R, K>::WARP;
     const WorkItem it = P.items[wid];
-    bottom_rows<R, MODE, EDGE>(P, it, ring, lane);
+    if (it.kind == 3) strip_rows<R, MODE, K, true>(P, it, sw, lane);
+    else strip_rows<R, MODE, K, false>(P, it, sw, lane);
 }
 
-// Opt the step kernels into the dynamic shared memory they use (the
-// bottom kernel's prefetch rings are above the 48 KB default).
-cudaError_t configure_step_kernels() {
-    cudaError_t e = cudaSuccess;
-#define FWI_CFG(R_, M_)                                                                                           \
-    if (e == cudaSuccess)                                                                                         \
-        e = cudaFuncSetAttribute(k_step_interior<R_, M_, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,      \
-                                 IN_SMEM);                                                                         \
-    if (e == cudaSuccess)                                                                                         \
-        e = cudaFuncSetAttribute(k_step_interior<R_, M_, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,       \
-                                 M_ == 1 ? IN_SMEM_IMG : IN_SMEM);                                                 \
-    if (e == cudaSuccess)                                                                                         \
-        e = cudaFuncSetAttribute(k_step_bottom<R_, M_, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,        \
-                                 BND_SMEM);                                                                        \
-    if (e == cudaSuccess)                                                                                         \
-        e = cudaFuncSetAttribute(k_step_bottom<R_, M_, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,         \
-                                 BND_SMEM);                                                                        \
-    if (e == cudaSuccess)                                                                                         \
-        e = cudaFuncSetAttribute(k_step_strip<R_, M_, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,             \
-                                 strip_smem<1>());                                                                 \
-    if (e == cudaSuccess)                                                                                         \
-        e = cudaFuncSetAttribute(k_step_strip<R_, M_, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize,             \
-                                 strip_smem<2>());
-    FWI_CFG(3, 0)
-    FWI_CFG(3, 1)
-    FWI_CFG(4, 0)
-    FWI_CFG(4, 1)
-#undef FWI_CFG
-    // The step kernels share SMs; with the largest shared-memory carveout
-    // every one of them reaches its register-limited occupancy.
-#define FWI_CO(K_)                                                                                             \
-    if (e == cudaSuccess)                                                                                      \
-        e = cudaFuncSetAttribute(K_, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
-#define FWI_CO_ALL(R_, M_)                     \
-    FWI_CO((k_step_interior<R_, M_, false>))   \
-    FWI_CO((k_step_interior<R_, M_, true>))    \
-    FWI_CO((k_step_bottom<R_, M_, false>))     \
-    FWI_CO((k_step_bottom<R_, M_, true>))      \
-    FWI_CO((k_step_strip<R_, M_, 1>))          \
-    FWI_CO((k_step_strip<R_, M_, 2>))
-    FWI_CO_ALL(3, 0)
-    FWI_CO_ALL(3, 1)
-    FWI_CO_ALL(4, 0)
-    FWI_CO_ALL(4, 1)
-#undef FWI_CO_ALL
-#undef FWI_CO
+// Bottom pad rows, interior columns: the boundary list after its nstrip
+// side-strip items.  Runs on its own stream, concurrently with
+// k_step_interior and k_step_strip.
+constexpr int BND_SMEM = 4 * BOT_DEPTH * SB_SIZE * 16;
+
+template <int R, int MODE>
+__global__ void __launch_bounds__(128, 3) k_step_bottom(const __grid_constant__ StepParams P) {
+    extern __shared__ float4 smem[];
+    const int lane = threadIdx.x & 31;
+    const int wid = P.nstrip + blockIdx.x * 4 + (threadIdx.x >> 5);
+    if (wid >= P.nitems) return;
+    float4* ring = smem + (threadIdx.x >> 5) * (BOT_DEPTH * SB_SIZE);
+    const WorkItem it = P.items[wid];
+    bottom_rows<R, MODE>(P, it, ring, lane);
+}
+
+// Opt the step kernels into the dynamic shared memory they use (above the
+// 48 KB default) and into the largest shared-memory carveout: the step
+// kernels share SMs, and with it every one of them reaches its
+// register-limited occupancy.
+template <typename KernelT>
+cudaError_t kernel_smem(KernelT* k, int bytes) {
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
     return e;
 }
 
-// Interior kernel on stream sm, bottom tiles without corners on sb, side
-// strips and the corner tiles on ss (the caller orders the streams around
-// each time step).  kstrip = columns per
-// lane of the strip kernel (ceil(strip width / 32)).
+template <int R, int MODE>
+cudaError_t configure_variant() {
+    cudaError_t e = kernel_smem(k_step_interior<R, MODE, false>, IN_SMEM);
+    if (e == cudaSuccess) e = kernel_smem(k_step_interior<R, MODE, true>, MODE == 1 ? IN_SMEM_IMG : IN_SMEM);
+    if (e == cudaSuccess) e = kernel_smem(k_step_bottom<R, MODE>, BND_SMEM);
+    if (e == cudaSuccess) e = kernel_smem(k_step_strip<R, MODE, 1>, strip_smem<R, 1>());
+    if (e == cudaSuccess) e = kernel_smem(k_step_strip<R, MODE, 2>, strip_smem<R, 2>());
+    return e;
+}
+
+cudaError_t configure_step_kernels() {
+    cudaError_t e = configure_variant<3, 0>();
+    if (e == cudaSuccess) e = configure_variant<3, 1>();
+    if (e == cudaSuccess) e = configure_variant<4, 0>();
+    if (e == cudaSuccess) e = configure_variant<4, 1>();
+    return e;
+}
+
+template <int R, int MODE>
+void launch_variant(int kstrip, const StepParams& pm, const StepParams& pb, cudaStream_t sm, cudaStream_t sb,
+                    cudaStream_t ss) {
+    const int bm = (pm.nitems + 3) / 4, bs = (pb.nstrip + 3) / 4, bb = (pb.nitems - pb.nstrip + 3) / 4;
+    if (bs) {
+        if (kstrip == 1) k_step_strip<R, MODE, 1><<<bs, 128, strip_smem<R, 1>(), ss>>>(pb);
+        else k_step_strip<R, MODE, 2><<<bs, 128, strip_smem<R, 2>(), ss>>>(pb);
+    }
+    if (bb) k_step_bottom<R, MODE><<<bb, 128, BND_SMEM, sb>>>(pb);
+    if (bm) {
+        if (pm.snap >= 0)
+            k_step_interior<R, MODE, true><<<bm, 128, MODE == 1 ? IN_SMEM_IMG : IN_SMEM, sm>>>(pm);
+        else
+            k_step_interior<R, MODE, false><<<bm, 128, IN_SMEM, sm>>>(pm);
+    }
+}
+
+// Interior kernel on stream sm, bottom tiles on sb, side strips (model and
+// bottom rows) on ss; the caller orders the streams around each time step.
+// kstrip = columns per lane of the strip kernel (ceil(strip width / 32)).
 cudaError_t launch_step(int acc, int mode, int kstrip, const StepParams& pm, const StepParams& pb, cudaStream_t sm,
                         cudaStream_t sb, cudaStream_t ss) {
-    const int bm = (pm.nitems + 3) / 4, bs = (pb.nstrip + 3) / 4, bb = (pb.nbot + 3) / 4,
-              be = (pb.nitems - pb.nstrip - pb.nbot + 3) / 4;
     if (kstrip != 1 && kstrip != 2) return cudaErrorInvalidValue;
-#define FWI_LAUNCH(R_, M_)                                                                                  \
-    do {                                                                                                   \
-        if (bs) {                                                                                          \
-            if (kstrip == 1) k_step_strip<R_, M_, 1><<<bs, 128, strip_smem<1>(), ss>>>(pb);                 \
-            else k_step_strip<R_, M_, 2><<<bs, 128, strip_smem<2>(), ss>>>(pb);                            \
-        }                                                                                                  \
-        if (be) k_step_bottom<R_, M_, true><<<be, 128, BND_SMEM, ss>>>(pb);                                \
-        if (bb) k_step_bottom<R_, M_, false><<<bb, 128, BND_SMEM, sb>>>(pb);                               \
-        if (bm) {                                                                                          \
-            if (pm.snap >= 0)                                                                              \
-                k_step_interior<R_, M_, true><<<bm, 128, M_ == 1 ? IN_SMEM_IMG : IN_SMEM, sm>>>(pm);       \
-            else                                                                                           \
-                k_step_interior<R_, M_, false><<<bm, 128, IN_SMEM, sm>>>(pm);                              \
-        }                                                                                                  \
-    } while (0)
     if (acc == 3) {
-        if (mode == 0) FWI_LAUNCH(3, 0);
-        else FWI_LAUNCH(3, 1);
+        if (mode == 0) launch_variant<3, 0>(kstrip, pm, pb, sm, sb, ss);
+        else launch_variant<3, 1>(kstrip, pm, pb, sm, sb, ss);
     } else if (acc == 4) {
-        if (mode == 0) FWI_LAUNCH(4, 0);
-        else FWI_LAUNCH(4, 1);
+        if (mode == 0) launch_variant<4, 0>(kstrip, pm, pb, sm, sb, ss);
+        else launch_variant<4, 1>(kstrip, pm, pb, sm, sb, ss);
     } else {
         return cudaErrorInvalidValue;
     }
-#undef FWI_LAUNCH
     return cudaGetLastError();
 }
 

@@ -296,7 +296,7 @@ def main():
     tr = traffic_from_profile()
     roof = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
             "traffic": tr * wave if (tr and a.config == 2) else None,
-            "kernel": "k_step_interior + k_step_boundary (one time step of all shots, concurrent streams)",
+            "kernel": "k_step_interior + k_step_strip + k_step_bottom (one time step of all shots, three concurrent streams)",
             "algorithmic_bytes_per_launch": bytes_step, "avg_launch_ms": step_s * 1e3,
             "peak_kind": f"{peak_kind} copy bandwidth (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured"
             else "fallback 6.8 TB/s"}

@@ -16,10 +16,13 @@ from .api import (  # noqa: E402,F401
     Survey,
     calculate_misfit_gradient,
     init,
+    interpolation_akima,
     kernel_launch_count,
     mcs_geometry,
+    set_filter_order,
     set_solver_options,
     set_stream,
     solver_acoustic_SS,
+    time_filter,
     time_rules,
 )

@@ -29,7 +29,8 @@ EXPORTS = [
     "fwi_mcs_geometry", "fwi_ricker", "fwi_time_rules", "fwi_survey_create", "fwi_survey_destroy",
     "fwi_survey_set_lambda", "fwi_survey_set_observed", "fwi_survey_set_sources", "fwi_survey_run",
     "fwi_survey_grad_device", "fwi_survey_get_synthetic", "fwi_survey_step_bytes", "fwi_survey_tuning",
-    "fwi_survey_recompute",
+    "fwi_survey_recompute", "fwi_survey_set_time", "fwi_time_filter", "fwi_set_filter_order",
+    "fwi_interpolation_akima",
     "fwi_survey_time_steps", "fwi_misfit_gradient_batch", "fwi_solver_forward_noalloc",
 ]
 
@@ -84,6 +85,10 @@ def load():
     lib.fwi_survey_set_lambda.argtypes = [P, P]
     lib.fwi_survey_set_observed.argtypes = [P, P]
     lib.fwi_survey_set_sources.argtypes = [P, P]
+    lib.fwi_survey_set_time.argtypes = [P, F, I, P, P]
+    lib.fwi_time_filter.argtypes = [P] * 7
+    lib.fwi_set_filter_order.argtypes = [I]
+    lib.fwi_interpolation_akima.argtypes = [P] * 7
     lib.fwi_survey_run.argtypes = [P, I, P, P]
     lib.fwi_survey_grad_device.argtypes = [P, C.POINTER(C.c_void_p)]
     lib.fwi_survey_get_synthetic.argtypes = [P, I, P]

@@ -125,6 +125,40 @@ def time_rules(lam, dmodel, tfin, store_snap=10):
     return np.float32(dt.value), nt.value, nts.value
 
 
+def set_filter_order(order: int = 6):
+    """Butterworth order of time_filter (the reference's filters.f90 uses 6)."""
+    N.check(N.load().fwi_set_filter_order(int(order)))
+
+
+def time_filter(Data_trace, nt, dt, Num, typef, f1, fc):
+    """time_filter (time_filter.f90:1): filters Data_trace(nt, Num) in place on
+    the device.  Data_trace: float32 Fortran array (host) or an integer device
+    address."""
+    if isinstance(Data_trace, int):
+        ptr = C.c_void_p(Data_trace)
+    else:
+        if Data_trace.dtype != np.float32 or not Data_trace.flags.f_contiguous:
+            raise TypeError("Data_trace must be a float32 Fortran-ordered array")
+        ptr = _p(Data_trace)
+    N.check(N.load().fwi_time_filter(ptr, _ri(nt), _rf(dt), _ri(Num), _ri(typef), _rf(f1), _rf(fc)))
+    return Data_trace
+
+
+def interpolation_akima(Data_tmp, dt_Data, nt_Data, NumRec, dt, nt, out=None):
+    """interpolation_akima (interpolation_akima.f90:1): resamples Data_tmp
+    (nt_Data, NumRec) to (nt, NumRec) at step dt.  Host arrays, or integer
+    device addresses for Data_tmp and `out` (then `out` is required)."""
+    src = C.c_void_p(Data_tmp) if isinstance(Data_tmp, int) else None
+    if src is None:
+        Data_tmp = _f32(Data_tmp)
+        src = _p(Data_tmp)
+    if out is None:
+        out = np.zeros((nt, NumRec), np.float32, order="F")
+    dst = C.c_void_p(out) if isinstance(out, int) else _p(out)
+    N.check(N.load().fwi_interpolation_akima(src, _rf(dt_Data), _ri(nt_Data), dst, _ri(NumRec), _rf(dt), _ri(nt)))
+    return out
+
+
 class _DescHolder:
     """Keeps the numpy arrays behind a FwiSurveyDesc alive."""
 
@@ -160,6 +194,7 @@ class Survey:
         handle = C.c_void_p()
         N.check(N.load().fwi_survey_create(C.byref(self._h.desc), C.byref(handle)))
         self.handle = handle
+        self.nt, self.dt = spec.nt, spec.dt
 
     def close(self):
         if getattr(self, "handle", None) and self.handle.value:
@@ -187,6 +222,22 @@ class Survey:
             self._obs = np.ascontiguousarray(obs_packed, dtype=np.float32)
             N.check(N.load().fwi_survey_set_observed(self.handle, _p(self._obs)))
 
+    def set_time(self, dt, nt, src_packed=None, obs_packed=None):
+        """New time axis (dt, nt) with the sources and observed traces resampled
+        to it, packed in shot order ((nt, n) column-major blocks): numpy arrays
+        or integer device addresses; None = zeros (fwi_survey_set_time)."""
+        def arg(a, keep):
+            if a is None:
+                return None
+            if isinstance(a, int):
+                return C.c_void_p(a)
+            arr = np.ascontiguousarray(a, dtype=np.float32)
+            setattr(self, keep, arr)
+            return _p(arr)
+        N.check(N.load().fwi_survey_set_time(self.handle, C.c_float(dt), int(nt), arg(src_packed, "_src_t"),
+                                             arg(obs_packed, "_obs_t")))
+        self.nt, self.dt = int(nt), float(dt)
+
     def run(self, step=1, grad=None, misfit=0.0):
         """Returns (misfit + this run's misfit, grad) where grad (ny, nx_model)
         float32 Fortran array is updated in place if given."""
@@ -204,7 +255,7 @@ class Survey:
 
     def synthetic(self, shot):
         nrec = len(self.spec.shots[shot].nxRec)
-        out = np.zeros((self.spec.nt, nrec), np.float32, order="F")
+        out = np.zeros((self.nt, nrec), np.float32, order="F")
         N.check(N.load().fwi_survey_get_synthetic(self.handle, shot, _p(out)))
         return out
 

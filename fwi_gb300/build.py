@@ -21,8 +21,9 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_lib")
 LIB = os.path.join(OUT_DIR, "libfwi_gb300.so")
-SOURCES = ["fwi_step.cu", "fwi_aux.cu", "fwi_host.cu"]
+SOURCES = ["fwi_step.cu", "fwi_aux.cu", "fwi_host.cu", "fwi_prep.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+CUDA_LIB = "/usr/local/cuda/lib64"  # cuFFT (the trace filter) is linked dynamically from the toolkit
 
 
 def nvcc() -> str:
@@ -64,7 +65,8 @@ def build(verbose: bool = False, force: bool = False) -> str:
             if r.returncode:
                 raise RuntimeError(f"nvcc failed for {cmd[-3]}")
     if force or jobs or _stale(LIB, objs):
-        cmd = [nvcc()] + ARCH + ["-shared", "-o", LIB] + objs + ["-cudart", "static"]
+        cmd = [nvcc()] + ARCH + ["-shared", "-o", LIB] + objs + ["-cudart", "static", "-lcufft",
+                                                                 "-Xlinker", "-rpath," + CUDA_LIB]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if verbose or r.returncode:
             sys.stderr.write(" ".join(cmd) + "\n" + r.stdout + r.stderr)

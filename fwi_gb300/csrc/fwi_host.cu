@@ -435,6 +435,11 @@ struct ShotState {
         DBuf* a[7] = {&pa, &pb, &phx, &chx, &phy, &phy2, &chy};
         return a[i]->p;
     }
+    size_t bytes() const {
+        size_t n = pa.n + pb.n + c2.n + phx.n + chx.n + phy.n + phy2.n + chy.n + snaps.n + sscale.n + k.n + ckpt.n;
+        for (auto& b : bst) n += b.n;
+        return n;
+    }
     int alloc_rc(int nckpt) {
         for (auto& b : bst) TRY(b.ensure(field_bytes));
         TRY(ckpt.ensure(std::max<size_t>(16, (size_t)nckpt * 7 * field_bytes)));
@@ -611,6 +616,17 @@ int check_nonfinite(const float* dptr, size_t n, DBuf& flag, cudaStream_t st, co
 }
 
 }  // namespace
+
+// Library services for the pre-processing entry points (fwi_prep.cu).
+namespace fwi {
+int prep_fail(int code, const std::string& msg) { return fail(code, msg); }
+cudaStream_t prep_stream() { return stream(); }
+bool prep_is_device_ptr(const void* p) { return is_device_ptr(p); }
+int prep_ensure_init() {
+    std::lock_guard<std::recursive_mutex> g(L().mu);
+    return ensure_init();
+}
+}  // namespace fwi
 
 // ===========================================================================
 // C ABI
@@ -995,8 +1011,9 @@ int survey_prepare_slots(fwi_survey* s) {
         std::vector<int> w(order.begin() + i, order.begin() + std::min(D.nshots, i + s->wave));
         s->waves.push_back(w);
     }
-    s->slots.clear();
-    for (int k = 0; k < s->wave; ++k) s->slots.emplace_back(new ShotState());
+    // slots persist across re-plans (their buffers only grow)
+    if ((int)s->slots.size() > s->wave) s->slots.resize(s->wave);
+    while ((int)s->slots.size() < s->wave) s->slots.emplace_back(new ShotState());
     for (int k = 0; k < s->wave; ++k) {
         Layout big = s->lays[s->waves[0][0]];
         size_t best = 0;
@@ -1380,6 +1397,69 @@ int issue_wave(fwi_survey* s, size_t wi, int step, cudaStream_t st, cudaStream_t
 
 }  // namespace
 
+// Time-axis plan of a survey: the wave size from the HBM budget (the memory
+// the survey's slots already hold counts as available), checkpointed
+// recomputation when waves would get too small, the slots (reused; their
+// buffers only grow), the band height and the work lists of every wave.
+int survey_plan(fwi_survey* s, bool tune) {
+    const auto& D = s->desc;
+    s->rc_C = 0;
+    size_t held = 0;
+    for (auto& sl : s->slots) held += sl->bytes();
+    // wave size from the HBM budget
+    size_t per = 0;
+    for (auto& l : s->lays) per = std::max(per, shot_wave_bytes(l, s->nt_store, D.snap_form, D.grad_form));
+    size_t freeb = 0, totb = 0;
+    CK(cudaMemGetInfo(&freeb, &totb));
+    size_t budget = (size_t)(0.92 * (double)(freeb + held));
+    if (s->desc.hbm_budget) {
+        size_t used_resident = s->d_obs.n + s->d_synth.n + s->d_adj.n + s->d_src.n + s->d_G.n + s->d_lambda.n;
+        if (s->desc.hbm_budget <= used_resident) return fail(FWI_ERR_NOMEM, "HBM budget smaller than the resident data");
+        budget = std::min(budget, s->desc.hbm_budget - used_resident);
+    }
+    int wave = (int)std::min<size_t>((size_t)D.nshots, budget / std::max<size_t>(per, 1));
+    // Checkpointed recomputation keeps a forward-state checkpoint every C steps
+    // and a ring of C/store_snap snapshots instead of all of them, for one more
+    // forward pass.  It is used when asked for, or when the budget would leave
+    // waves so small (< 8 shots) that the extra pass is cheaper than the lost
+    // batching.
+    {
+        size_t fb = 0, bb = 0, kb = 0;
+        for (auto& l : s->lays) {
+            fb = std::max(fb, (size_t)l.nyt * l.pitch * 4);
+            bb = std::max(bb, (size_t)l.ny * l.pitch * (D.snap_form == FWI_SNAP_F32 ? 4 : 2) + (size_t)l.ny * (l.ntiles + 2) * 4);
+            kb = std::max(kb, (size_t)l.ny * l.pitch * (D.grad_form == FWI_GRAD_F64 ? 8 : 4));
+        }
+        const int ss = D.store_snap;
+        int C = (int)std::lround(std::sqrt(7.0 * fb * D.nt * ss / (double)std::max<size_t>(bb, 1)));
+        C = std::max(ss, std::min(D.nt, (C + ss - 1) / ss * ss));
+        const int J = (D.nt - 1) / C + 1;
+        const size_t per_rc = 15 * fb + (size_t)(J - 1) * 7 * fb + (size_t)(C / ss + 2) * bb + kb;
+        const int wave_rc = (int)std::min<size_t>((size_t)D.nshots, budget / std::max<size_t>(per_rc, 1));
+        const bool force = (D.flags & FWI_SURVEY_RECOMPUTE) != 0;
+        if (force || (wave < std::min(D.nshots, 8) && wave_rc > wave)) {
+            if (wave_rc < 1)
+                return fail(FWI_ERR_NOMEM, "one shot's checkpoints and snapshot ring (" + std::to_string(per_rc) +
+                                               " bytes) exceed the device budget");
+            TRY(rc_plan(s, C));
+            wave = wave_rc;
+        }
+    }
+    if (wave < 1)
+        return fail(FWI_ERR_NOMEM, "one shot's wavefields and snapshots (" + std::to_string(per) +
+                                       " bytes) exceed the device budget");
+    if (D.wave_shots > 0) wave = std::min(wave, D.wave_shots);
+    // balance the waves: same number of shots in each
+    const int nw = (D.nshots + wave - 1) / wave;
+    wave = (D.nshots + nw - 1) / nw;
+    s->wave = wave;
+    TRY(survey_prepare_slots(s));
+    if (D.band_rows > 0) s->band = D.band_rows;
+    else if (tune) TRY(tune_band(s));
+    TRY(survey_prepare_waves(s));
+    return FWI_OK;
+}
+
 extern "C" {
 
 int fwi_survey_create(const fwi_survey_desc* desc, fwi_survey** out) {
@@ -1462,58 +1542,56 @@ int fwi_survey_create(const fwi_survey_desc* desc, fwi_survey** out) {
     }
     CK(cudaStreamSynchronize(st));
     s->desc.shots = nullptr;  // host pointers are not kept
-    // wave size from the HBM budget
-    size_t per = 0;
-    for (auto& l : s->lays) per = std::max(per, shot_wave_bytes(l, s->nt_store, D.snap_form, D.grad_form));
-    size_t freeb = 0, totb = 0;
-    CK(cudaMemGetInfo(&freeb, &totb));
-    size_t budget = (size_t)(0.92 * (double)freeb);
-    if (D.hbm_budget) {
-        size_t used_resident = s->d_obs.n + s->d_synth.n + s->d_adj.n + s->d_src.n + s->d_G.n + s->d_lambda.n;
-        if (D.hbm_budget <= used_resident) return fail(FWI_ERR_NOMEM, "HBM budget smaller than the resident data");
-        budget = std::min(budget, D.hbm_budget - used_resident);
-    }
-    int wave = (int)std::min<size_t>((size_t)D.nshots, budget / std::max<size_t>(per, 1));
-    // Checkpointed recomputation keeps a forward-state checkpoint every C steps
-    // and a ring of C/store_snap snapshots instead of all of them, for one more
-    // forward pass.  It is used when asked for, or when the budget would leave
-    // waves so small (< 8 shots) that the extra pass is cheaper than the lost
-    // batching.
-    {
-        size_t fb = 0, bb = 0, kb = 0;
-        for (auto& l : s->lays) {
-            fb = std::max(fb, (size_t)l.nyt * l.pitch * 4);
-            bb = std::max(bb, (size_t)l.ny * l.pitch * (D.snap_form == FWI_SNAP_F32 ? 4 : 2) + (size_t)l.ny * (l.ntiles + 2) * 4);
-            kb = std::max(kb, (size_t)l.ny * l.pitch * (D.grad_form == FWI_GRAD_F64 ? 8 : 4));
-        }
-        const int ss = D.store_snap;
-        int C = (int)std::lround(std::sqrt(7.0 * fb * D.nt * ss / (double)std::max<size_t>(bb, 1)));
-        C = std::max(ss, std::min(D.nt, (C + ss - 1) / ss * ss));
-        const int J = (D.nt - 1) / C + 1;
-        const size_t per_rc = 15 * fb + (size_t)(J - 1) * 7 * fb + (size_t)(C / ss + 2) * bb + kb;
-        const int wave_rc = (int)std::min<size_t>((size_t)D.nshots, budget / std::max<size_t>(per_rc, 1));
-        const bool force = (D.flags & FWI_SURVEY_RECOMPUTE) != 0;
-        if (force || (wave < std::min(D.nshots, 8) && wave_rc > wave)) {
-            if (wave_rc < 1)
-                return fail(FWI_ERR_NOMEM, "one shot's checkpoints and snapshot ring (" + std::to_string(per_rc) +
-                                               " bytes) exceed the device budget");
-            TRY(rc_plan(s.get(), C));
-            wave = wave_rc;
-        }
-    }
-    if (wave < 1)
-        return fail(FWI_ERR_NOMEM, "one shot's wavefields and snapshots (" + std::to_string(per) +
-                                       " bytes) exceed the device budget");
-    if (D.wave_shots > 0) wave = std::min(wave, D.wave_shots);
-    // balance the waves: same number of shots in each
-    const int nw = (D.nshots + wave - 1) / wave;
-    wave = (D.nshots + nw - 1) / nw;
-    s->wave = wave;
-    TRY(survey_prepare_slots(s.get()));
-    if (D.band_rows > 0) s->band = D.band_rows;
-    else TRY(tune_band(s.get()));
-    TRY(survey_prepare_waves(s.get()));
+    TRY(survey_plan(s.get(), D.band_rows <= 0));
     *out = s.release();
+    return FWI_OK;
+}
+
+int fwi_survey_set_time(fwi_survey* s, float dt, int nt, const float* src, const float* obs) {
+    std::lock_guard<std::recursive_mutex> g(L().mu);
+    if (!s) return fail(FWI_ERR_STATE, "null survey");
+    auto& D = s->desc;
+    TRY(validate_common(D.ny, D.nx_model, D.acc, D.dpml, nt, D.store_snap));
+    if (!(dt > 0.f)) return fail(FWI_ERR_ARG, "dt must be positive");
+    if ((int)snapshot_steps(nt, D.store_snap).size() > nt / D.store_snap)
+        return fail(FWI_ERR_ARG, "nt/store_snap snapshots exceed nt_Store");
+    cudaStream_t st = stream();
+    CK(cudaStreamSynchronize(st));
+    const bool nt_changed = nt != D.nt;
+    size_t nsou_tot = 0;
+    for (auto& gm : s->geoms) nsou_tot += gm.nxS.size();
+    D.nt = nt;
+    D.dt = dt;
+    s->nt_store = nt / D.store_snap;
+    const size_t nsrc = (size_t)nt * nsou_tot, ntrc = (size_t)nt * s->ntr;
+    TRY(s->d_src.ensure(std::max<size_t>(nsrc * 4, 16)));
+    TRY(s->d_obs.ensure(std::max<size_t>(ntrc * 4, 16)));
+    TRY(s->d_synth.ensure(std::max<size_t>(ntrc * 4, 16)));
+    TRY(s->d_adj.ensure(std::max<size_t>(ntrc * 4, 16)));
+    // CPML factors depend on dt (solver_PML_coeffs.f90)
+    pml_factors(D.acc, D.dpml, D.dt, D.d, s->h_fA, s->h_fB);
+    TRY(upload(s->d_fA, s->h_fA, st));
+    TRY(upload(s->d_fB, s->h_fB, st));
+    auto put = [&](DBuf& dst, const float* p, size_t n) -> int {
+        if (!n) return FWI_OK;
+        if (p) CK(cudaMemcpyAsync(dst.p, p, n * 4, is_device_ptr(p) ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, st));
+        else CK(cudaMemsetAsync(dst.p, 0, n * 4, st));
+        return FWI_OK;
+    };
+    TRY(put(s->d_src, src, nsrc));
+    TRY(put(s->d_obs, obs, ntrc));
+    if (nt_changed) {
+        TRY(survey_plan(s, false));
+    } else {
+        // dt is baked into the captured graphs (c2, the snapshot scaling)
+        for (auto& w : s->wdev)
+            for (auto& gexec : w->graph)
+                if (gexec) {
+                    cudaGraphExecDestroy(gexec);
+                    gexec = nullptr;
+                }
+    }
+    CK(cudaStreamSynchronize(st));
     return FWI_OK;
 }
 

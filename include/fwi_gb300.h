@@ -19,6 +19,8 @@
  *   fwi_mcs_geometry          src/get_mcs_data.f90:113-114,147-155,503-512
  *   fwi_ricker                src/get_mcs_data.f90:331 (Ricker_mcs)
  *   fwi_time_rules            src/calculate_misfit_gradient.f90:198-203
+ *   fwi_time_filter           src/time_filter.f90:1 (time_filter), src/filters.f90:1 (filters_function1D)
+ *   fwi_interpolation_akima   src/interpolation_akima.f90:1 (interpolation_akima, INTRPL of akima433.f90:6)
  */
 #ifndef FWI_GB300_H
 #define FWI_GB300_H
@@ -111,6 +113,27 @@ int fwi_ricker(float freq, float dt, int nt, float* out);
 int fwi_time_rules(const float* lambda, int ny, int nx, float dmodel, float tfin, int store_snap,
                    float* dt, int* nt, int* nt_Store);
 
+/* ---- trace pre-processing on the device ----------------------------------- */
+
+/* time_filter(Data_trace,nt,dt,Num,typef,f1,fc): every trace of
+ * Data_trace(nt,Num) (column-major, host or device pointer, filtered in
+ * place) is placed at the end of a 24x zero-padded buffer, transformed,
+ * multiplied by the Butterworth response of filters_function1D (typef 1
+ * low-pass at fc, 2 high-pass at 40 Hz, 3 band-pass f1..fc; order 6 unless
+ * fwi_set_filter_order) and transformed back.  The FFT is cuFFT in FP32. */
+int fwi_time_filter(float* Data_trace, const int* nt, const float* dt, const int* Num, const int* typef,
+                    const float* f1, const float* fc);
+/* Butterworth order of fwi_time_filter (the reference hard-codes n = 6,
+ * filters.f90:21); 1..32. */
+int fwi_set_filter_order(int order);
+/* interpolation_akima(Data_tmp,dt_Data,nt_Data,Data_trace,NumRec,dt,nt):
+ * Akima resampling (ACM Algorithm 433, as INTRPL) of every trace of
+ * Data_tmp(nt_Data,NumRec) from the axis (i-1)*dt_Data to (i-1)*dt,
+ * i = 1..nt, into Data_trace(nt,NumRec); host or device pointers.  FP32 in
+ * the reference's evaluation order: bit-identical results. */
+int fwi_interpolation_akima(const float* Data_tmp, const float* dt_Data, const int* nt_Data, float* Data_trace,
+                            const int* NumRec, const float* dt, const int* nt);
+
 /* ---- batched misfit + gradient over shots ------------------------------ */
 
 typedef struct fwi_shot {
@@ -162,6 +185,15 @@ typedef struct fwi_survey fwi_survey;
 /* Plan a survey: validate the geometry, upload sources and observed data,
  * size the shot waves to the HBM budget and allocate device buffers. */
 int fwi_survey_create(const fwi_survey_desc* desc, fwi_survey** out);
+/* New time axis for an existing survey (the line search of FWI.f90:225-230
+ * recomputes dt from the CFL rule and nt = 1+ceiling(tfin/dt) for every trial
+ * model; calculate_misfit_gradient.f90:198-203 truncates nt to whole
+ * snapshot blocks).  src: all shots' sources resampled to (dt, nt), shot after
+ * shot, each (nt, num_sou) column-major; obs: all shots' observed traces,
+ * (nt, num_rec) each, in shot order.  Host or device pointers; NULL = zeros.
+ * The survey keeps its model, buffers (grown if nt grew) and band height; the
+ * wave plan is redone when nt changes and the graphs are re-captured. */
+int fwi_survey_set_time(fwi_survey* s, float dt, int nt, const float* src, const float* obs);
 int fwi_survey_destroy(fwi_survey* s);
 /* Model parameter: lambda(ny,nx_model) bulk modulus (rho = 1000), host or
  * device pointer (the call detects which).  Vp = sqrt(lambda/1000.) as in

@@ -168,7 +168,7 @@ class _DescHolder:
         shots = (N.FwiShot * len(spec.shots))()
         for i, sh in enumerate(spec.shots):
             arrs = [_i32(sh.nxSou), _i32(sh.nySou), _i32(sh.nxRec), _i32(sh.nyRec),
-                    _f32(np.asarray(sh.src).reshape(spec.nt, -1, order="F")),
+                    _f32(np.asarray(sh.src).reshape(spec.nt, -1, order="F")) if sh.src is not None else None,
                     _f32(np.asarray(sh.obs).reshape(spec.nt, -1, order="F")) if sh.obs is not None else None]
             self.keep.extend(a for a in arrs if a is not None)
             shots[i] = N.FwiShot(sh.x0, sh.nx, len(sh.nxSou), len(sh.nxRec), _p(arrs[0]), _p(arrs[1]), _p(arrs[2]),

@@ -21,7 +21,7 @@ class ShotSpec:
     nySou: np.ndarray
     nxRec: np.ndarray
     nyRec: np.ndarray
-    src: np.ndarray             # S(nt, num_sou) float32, Fortran order
+    src: Optional[np.ndarray]   # S(nt, num_sou) float32, Fortran order (None: zeros)
     obs: Optional[np.ndarray] = None   # Data_target(nt, num_rec)
     grad_weight: float = 1.0
     misfit_weight: float = 1.0

@@ -377,6 +377,15 @@ def parse_stmt(no, s):
                     "double" if base in ("real*8", "doubleprecision") else (
                         "logical" if base == "logical" else "character")))
             alloc = "allocatable" in attrs
+            # a DIMENSION(...) attribute gives every entity without its own
+            # bounds that shape
+            attr_dims = None
+            md = re.search(r"dimension\s*\(", attrs)
+            if md:
+                start = md.end() - 1
+                end = _match_paren(attrs, start)
+                attr_dims = [d.strip() for d in _split_top(attrs[start + 1:end])]
+                attr_dims = [None if d == ":" else parse_expr(d) for d in attr_dims]
             entities = []
             for ent in _split_top(ents):
                 ent = ent.strip()
@@ -389,7 +398,7 @@ def parse_stmt(no, s):
                 mm = re.match(r"^([a-z_][a-z0-9_]*)\s*(\((.*)\))?\s*(\*\s*\d+)?$", ent)
                 if not mm:
                     raise SyntaxError(f"bad declaration entity {ent!r}")
-                dims = None
+                dims = attr_dims
                 if mm.group(2):
                     dims = [d.strip() for d in _split_top(mm.group(3))]
                     dims = [None if d == ":" else parse_expr(d) for d in dims]
@@ -753,7 +762,12 @@ class Interp:
     # -- calls --------------------------------------------------------------
     def do_call(self, ctx, name, args):
         if name.startswith("mpi_"):
-            raise RuntimeError("MPI call in interpreted code")
+            # single-process stubs: rank 0 of 1; other MPI calls are no-ops
+            if not getattr(self, "mpi_stub", False):
+                raise RuntimeError("MPI call in interpreted code")
+            if name in ("mpi_comm_size", "mpi_comm_rank"):
+                self.lookup(ctx, args[1][1]).value = 1 if name == "mpi_comm_size" else 0
+            return
         actuals, writeback = [], []
         for a in args:
             if a[0] == "name" and self.has_var(ctx, a[1]):
@@ -1027,12 +1041,13 @@ class _MeshIndex(tuple):
 class Program:
     """All subroutines of a set of Fortran source files."""
 
-    def __init__(self, paths, globals_=None, overrides=None):
+    def __init__(self, paths, globals_=None, overrides=None, mpi_stub=False):
         self.units = {}
         for p in paths:
             with open(p, encoding="latin-1") as f:
                 self.units.update(parse_units(f.read()))
         self.interp = Interp(self.units, globals_, overrides)
+        self.interp.mpi_stub = mpi_stub
 
     def call(self, name, *actuals):
         return self.interp.call(name, list(actuals))

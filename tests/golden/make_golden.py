@@ -10,7 +10,7 @@ precision, on small seeded inputs, and stores inputs and outputs.
 
 The fixtures are committed; tests read them and never need the reference.
 
-    python tests/golden/make_golden.py [/path/to/reference]
+    python tests/golden/make_golden.py [/path/to/reference [case ...]]
 """
 from __future__ import annotations
 
@@ -202,11 +202,43 @@ def case_geometry(src):
     print("geometry/ricker/time rules: done")
 
 
+def case_polyfit(src):
+    """polyfit.f90 (line-search step from three trials), single process."""
+    prog = fe.Program([os.path.join(src, "polyfit.f90")], mpi_stub=True,
+                      globals_={"mpi_comm_world": V(0, "integer"), "mpi_status_size": V(1, "integer")})
+    rng = np.random.default_rng(11)
+    cases = [(0.3, 10.0, 8.0, 9.0, 2), (0.7, 7.0, 6.5, 6.9, 3), (1e-3, 5.0, 4.0, 4.5, 2),
+             (2.5e-4, 1.0, 0.9, 0.95, 4), (0.01, 3.0, 3.0, 3.0, 2),      # flat: ties, the last sample wins
+             (0.05, 3.0, 2.0, 1.0, 2), (0.05, 1.0, 2.0, 3.0, 3),        # monotone fits: an end of the range
+             (0.2, 4.0, 5.0, 4.0, 2)]                                   # concave
+    for _ in range(24):
+        nut = float(F32(10.0 ** rng.uniform(-5, 1)))
+        m = np.sort(rng.uniform(0.5, 2.0, 3))[::-1] if rng.random() < 0.5 else rng.uniform(0.5, 2.0, 3)
+        cases.append((nut, float(m[0]), float(m[1]), float(m[2]), int(rng.integers(2, 6))))
+    inp = np.array(cases, dtype=np.float64)
+    out = np.zeros(len(cases), np.float32)
+    for i, (nut, m0, m1, m2, li) in enumerate(cases):
+        end = V(F32(0))
+        prog.call("polyfit", V(F32(nut)), V(F32(m0)), V(F32(m1)), V(F32(m2)), V(int(li), "integer"), end)
+        out[i] = F32(end.value)
+    np.savez_compressed(os.path.join(HERE, "polyfit.npz"), cases=inp, endstep=out)
+    print("polyfit: done")
+
+
 def main():
     src = os.path.join(sys.argv[1] if len(sys.argv) > 1 else "/root/reference", "src")
-    case_coeffs(src)
-    case_misfit(src)
-    case_geometry(src)
+    only = set(sys.argv[2:])  # optional case names: coeffs misfit geometry polyfit akima solver
+    if only:
+        for name in ("coeffs", "misfit", "geometry", "polyfit", "akima"):
+            if name in only:
+                globals()["case_" + name](src)
+        if "solver" not in only:
+            return
+    else:
+        case_coeffs(src)
+        case_misfit(src)
+        case_geometry(src)
+        case_polyfit(src)
     # acc=3 (the reference's hard-coded order), snapshots every 10 steps;
     # sources incl. one outside the interior; receivers with duplicates,
     # in the left pad, in the bottom strip and in a bottom corner.

@@ -67,7 +67,10 @@ def random_case(seed, ny, nx, nt, acc, dpml, store_snap, nsou, nrec):
 
 @pytest.mark.parametrize("acc,dpml,ny,nx,store", [(3, 20, 37, 301, 10), (4, 20, 50, 130, 4), (3, 5, 23, 77, 7),
                                                    (4, 11, 64, 250, 10), (3, 20, 40, 1, 10),
-                                                   (3, 20, 20, 2000, 10), (4, 20, 16, 1100, 10)])
+                                                   (3, 20, 20, 2000, 10), (4, 20, 16, 1100, 10),
+                                                   # dn > 32: side strips of two columns per lane
+                                                   (3, 30, 30, 200, 10), (4, 40, 24, 90, 7), (3, 50, 20, 60, 10),
+                                                   (3, 30, 12, 5, 10)])
 def test_random_geometry_bit_exact_vs_oracle(acc, dpml, ny, nx, store):
     """Random sources and receivers anywhere in the padded grid (pads, top
     pad, corners, duplicates), odd widths that exercise the tile edges."""

@@ -78,6 +78,22 @@ module fwi_gpu_iface
        integer(c_int), value :: step
      end function fwi_misfit_gradient_batch
 
+     !! time_filter (src/time_filter.f90:1): Butterworth filter of Data_trace(nt,Num) in place
+     integer(c_int) function fwi_time_filter(Data_trace, nt, dt, Num, typef, f1, fc) &
+          bind(C, name="fwi_time_filter")
+       import :: c_int, c_float
+       real(c_float)  :: Data_trace(*), dt, f1, fc
+       integer(c_int) :: nt, Num, typef
+     end function fwi_time_filter
+
+     !! interpolation_akima (src/interpolation_akima.f90:1)
+     integer(c_int) function fwi_interpolation_akima(Data_tmp, dt_Data, nt_Data, Data_trace, NumRec, dt, nt) &
+          bind(C, name="fwi_interpolation_akima")
+       import :: c_int, c_float
+       real(c_float)  :: Data_tmp(*), Data_trace(*), dt_Data, dt
+       integer(c_int) :: nt_Data, NumRec, nt
+     end function fwi_interpolation_akima
+
      type(c_ptr) function fwi_last_error() bind(C, name="fwi_last_error")
        import :: c_ptr
      end function fwi_last_error

@@ -128,6 +128,34 @@ def config2(seed=2, nshots=64, nt=6000, store_snap=10):
     return spec, vp_true, smooth(vp_true, 8)
 
 
+def config5(seed=5, nshots=128, nt=8000, store_snap=10, window_margin=2000.0):
+    """Full-inversion workload (BASELINE config 5): 600 x 3000 at 12.5 m, a
+    layered model with two Gaussian low-velocity lenses, 128 MCS shots of 480
+    channels at 12.5 m, 8 s records at dt = 1 ms, 10 Hz Ricker.  Each shot
+    propagates on its own window: from window_margin metres behind the last
+    channel to window_margin metres ahead of the source.  Returns (spec,
+    vp_true, vp_start) with the start model = the smoothed model without the
+    lenses."""
+    rng = np.random.default_rng(seed)
+    ny, nx, d = 600, 3000, 12.5
+    lenses = [(float(rng.uniform(9000, 16000)), float(rng.uniform(2200, 3500)), 700.0, -450.0),
+              (float(rng.uniform(22000, 30000)), float(rng.uniform(3000, 4800)), 900.0, -400.0)]
+    vp_true, wrows = model_layered(ny, nx, d, seed, lenses=lenses)
+    vp_bg, _ = model_layered(ny, nx, d, seed)
+    nrec, drec, near = 480, 12.5, 150.0
+    x_first = near + nrec * drec + window_margin + 500.0
+    x_last = nx * d - window_margin - 500.0
+    xs = [x_first + (x_last - x_first) * i / max(nshots - 1, 1) for i in range(nshots)]
+    windows = []
+    for x in xs:
+        lo = max(0, int((x - near - nrec * drec - window_margin) / d))
+        hi = min(nx, int(np.ceil((x + window_margin) / d)))
+        windows.append((lo, hi - lo))
+    spec = mcs_survey(vp_true, d, 0.001, nt, xs, nrec, drec, near=near, freq=10.0, acc=3, dpml=20,
+                      store_snap=store_snap, seed=seed, water_rows=wrows, windows=windows)
+    return spec, vp_true, smooth(vp_bg, 8)
+
+
 def smooth(vp, r):
     """Box-smoothed copy of vp (r cells each way) for starting models."""
     v = np.asarray(vp, np.float64)

@@ -19,10 +19,14 @@ from .api import (  # noqa: E402,F401
     interpolation_akima,
     kernel_launch_count,
     mcs_geometry,
+    read_nav,
     set_filter_order,
     set_solver_options,
     set_stream,
     solver_acoustic_SS,
+    su_info,
+    su_read,
+    su_write,
     time_filter,
     time_rules,
 )

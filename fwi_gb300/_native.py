@@ -30,7 +30,7 @@ EXPORTS = [
     "fwi_survey_set_lambda", "fwi_survey_set_observed", "fwi_survey_set_sources", "fwi_survey_run",
     "fwi_survey_grad_device", "fwi_survey_get_synthetic", "fwi_survey_step_bytes", "fwi_survey_tuning",
     "fwi_survey_recompute", "fwi_survey_set_time", "fwi_time_filter", "fwi_set_filter_order",
-    "fwi_interpolation_akima",
+    "fwi_interpolation_akima", "fwi_su_info", "fwi_su_read", "fwi_su_write", "fwi_read_nav",
     "fwi_survey_time_steps", "fwi_misfit_gradient_batch", "fwi_solver_forward_noalloc",
 ]
 
@@ -89,6 +89,10 @@ def load():
     lib.fwi_time_filter.argtypes = [P] * 7
     lib.fwi_set_filter_order.argtypes = [I]
     lib.fwi_interpolation_akima.argtypes = [P] * 7
+    lib.fwi_su_info.argtypes = [C.c_char_p, I, P, P, P]
+    lib.fwi_su_read.argtypes = [C.c_char_p, I, I, I, P]
+    lib.fwi_su_write.argtypes = [C.c_char_p, P, I, I, F, I]
+    lib.fwi_read_nav.argtypes = [C.c_char_p, I, P, P, P, P]
     lib.fwi_survey_run.argtypes = [P, I, P, P]
     lib.fwi_survey_grad_device.argtypes = [P, C.POINTER(C.c_void_p)]
     lib.fwi_survey_get_synthetic.argtypes = [P, I, P]

@@ -159,6 +159,38 @@ def interpolation_akima(Data_tmp, dt_Data, nt_Data, NumRec, dt, nt, out=None):
     return out
 
 
+def su_info(path, big_endian=False):
+    """(ns, dt, ntraces) of an SU file."""
+    ns, dt, n = C.c_int(0), C.c_float(0), C.c_int(0)
+    N.check(N.load().fwi_su_info(str(path).encode(), int(bool(big_endian)), C.byref(ns), C.byref(dt), C.byref(n)))
+    return ns.value, np.float32(dt.value), n.value
+
+
+def su_read(path, nt, ntr, big_endian=False):
+    """The first ntr traces (nt samples each) of an SU file: (nt, ntr) float32,
+    Fortran order, as get_shot_data reads a shot gather."""
+    out = np.zeros((nt, ntr), np.float32, order="F")
+    N.check(N.load().fwi_su_read(str(path).encode(), int(nt), int(ntr), int(bool(big_endian)), _p(out)))
+    return out
+
+
+def su_write(path, data, dt, big_endian=False):
+    """data (nt, ntr) as an SU file (tracl, ns, dt headers), as write_new_data."""
+    d = _f32(data)
+    nt, ntr = d.shape
+    N.check(N.load().fwi_su_write(str(path).encode(), _p(d), nt, ntr, C.c_float(dt), int(bool(big_endian))))
+
+
+def read_nav(path):
+    """Navigation list of MCS shots: (shot numbers int32, x float32, water
+    depth float32), as read_nav_shot_mcs reads it."""
+    n = C.c_int(0)
+    N.check(N.load().fwi_read_nav(str(path).encode(), 0, None, None, None, C.byref(n)))
+    ids, xs, bat = np.zeros(n.value, np.int32), np.zeros(n.value, np.float32), np.zeros(n.value, np.float32)
+    N.check(N.load().fwi_read_nav(str(path).encode(), n.value, _p(ids), _p(xs), _p(bat), C.byref(n)))
+    return ids, xs, bat
+
+
 class _DescHolder:
     """Keeps the numpy arrays behind a FwiSurveyDesc alive."""
 

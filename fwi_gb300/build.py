@@ -21,7 +21,7 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_lib")
 LIB = os.path.join(OUT_DIR, "libfwi_gb300.so")
-SOURCES = ["fwi_step.cu", "fwi_aux.cu", "fwi_host.cu", "fwi_prep.cu"]
+SOURCES = ["fwi_step.cu", "fwi_aux.cu", "fwi_host.cu", "fwi_prep.cu", "fwi_io.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CUDA_LIB = "/usr/local/cuda/lib64"  # cuFFT (the trace filter) is linked dynamically from the toolkit
 
@@ -52,7 +52,7 @@ def build(verbose: bool = False, force: bool = False) -> str:
     objs, jobs = [], []
     for src in SOURCES:
         s = os.path.join(CSRC, src)
-        o = os.path.join(OUT_DIR, src.replace(".cu", ".o"))
+        o = os.path.join(OUT_DIR, os.path.splitext(src)[0] + ".o")
         objs.append(o)
         if force or _stale(o, [s] + headers):
             jobs.append([nvcc()] + _flags() + ["-c", s, "-o", o])

@@ -21,6 +21,9 @@
  *   fwi_time_rules            src/calculate_misfit_gradient.f90:198-203
  *   fwi_time_filter           src/time_filter.f90:1 (time_filter), src/filters.f90:1 (filters_function1D)
  *   fwi_interpolation_akima   src/interpolation_akima.f90:1 (interpolation_akima, INTRPL of akima433.f90:6)
+ *   fwi_su_read / fwi_su_info src/get_mcs_data.f90:167 (get_shot_data), src/get_was_data.f90:241 (get_obs_data)
+ *   fwi_su_write              src/auxiliar.f90:433 (write_new_data: the suaddhead/sushw pipeline)
+ *   fwi_read_nav              src/get_mcs_data.f90:88 (read_nav_shot_mcs)
  */
 #ifndef FWI_GB300_H
 #define FWI_GB300_H
@@ -133,6 +136,24 @@ int fwi_set_filter_order(int order);
  * the reference's evaluation order: bit-identical results. */
 int fwi_interpolation_akima(const float* Data_tmp, const float* dt_Data, const int* nt_Data, float* Data_trace,
                             const int* NumRec, const float* dt, const int* nt);
+
+/* ---- Seismic Unix trace files (host) -------------------------------------- */
+
+/* ns, dt (s) from the first 240-byte SU header of `path` and the number of
+ * traces from the file size; big_endian = byte order of the file. */
+int fwi_su_info(const char* path, int big_endian, int* ns, float* dt, int* ntraces);
+/* The first ntr traces of nt samples of an SU file into out(nt, ntr)
+ * (column-major), skipping the headers, as get_shot_data reads a shot. */
+int fwi_su_read(const char* path, int nt, int ntr, int big_endian, float* out);
+/* data(nt, ntr) as an SU file: tracl (1-based trace number), ns = nt and
+ * dt = int(dt*1e6) microseconds in each header, every other word 0 (what
+ * `suaddhead ns= | sushw key=dt a=` writes in write_new_data). */
+int fwi_su_write(const char* path, const float* data, int nt, int ntr, float dt, int big_endian);
+/* Navigation list of MCS shots (read_nav_shot_mcs, get_mcs_data.f90:88-117):
+ * one record per line -- shot number, shot x (m), water depth (m) -- blanks
+ * or commas between values.  Fills up to max_records entries and returns the
+ * number of records in the file in *nrecords. */
+int fwi_read_nav(const char* path, int max_records, int* shot_id, float* xs, float* bat, int* nrecords);
 
 /* ---- batched misfit + gradient over shots ------------------------------ */
 

@@ -170,6 +170,13 @@ class DeviceGradient:
         self.band_id = 0
         self.calls = 0
 
+    def set_source(self, wavelet):
+        """Replace the source wavelet S0(nt_data) (source estimation); the
+        next set_band filters it."""
+        w = np.asarray(wavelet, np.float32).reshape(1, -1)
+        self.src_raw = self.torch.from_numpy(np.ascontiguousarray(w)).to(self.dev)
+        self.src_band = self.src_raw.clone()
+
     def set_band(self, f1, f2):
         torch = self.torch
         self.obs_band.copy_(self.obs_raw)
@@ -328,14 +335,19 @@ def fwi_band(lam: np.ndarray, gradient: Callable, f1: float, f2: float, n_iter: 
     return lam, it
 
 
-def invert(lam0: np.ndarray, gradient, bands: List[Tuple[float, float]], n_iter: int, **kw):
+def invert(lam0: np.ndarray, gradient, bands: List[Tuple[float, float]], n_iter: int,
+           estimate_source: Optional[Callable] = None, **kw):
     """Frequency continuation (00-main_Inversion.f90:83-98): fwi_band for every
     (f1, f2) band in turn, the model and the global iteration count carried
     over.  ``gradient.set_band(f1, f2)`` (when present) re-filters the data.
+    ``estimate_source(lam, f1, f2)`` (inv_source = 1, FWI.f90:103-107) gives
+    the band's wavelet, handed to ``gradient.set_source`` before filtering.
     Returns (final model, list of IterationLog)."""
     log: List[IterationLog] = []
     lam, it = np.asfortranarray(lam0, dtype=np.float32), 1
     for f1, f2 in bands:
+        if estimate_source is not None:
+            gradient.set_source(estimate_source(lam, f1, f2))
         if hasattr(gradient, "set_band"):
             gradient.set_band(f1, f2)
         lam, it = fwi_band(lam, gradient, f1, f2, n_iter, iter0=it, log=log, **kw)

@@ -39,15 +39,19 @@ def parse():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--config", type=int, choices=[2, 3, 5], default=2,
+    ap.add_argument("--config", type=int, choices=[2, 3, 4, 5], default=2,
                     help="2: batched MCS survey (the metric's workload); 3: uneven-window WAS batch; "
-                         "5: NLCG inversion with frequency continuation")
+                         "4: config 2 in the precision form (snapshots every 4 steps in 16 bits, checkpointed "
+                         "recomputation under a 120 GB budget); 5: NLCG inversion with frequency continuation")
+    ap.add_argument("--budget", type=float, default=0.0, help="HBM budget in GB (0: all; config 4: 120)")
+    ap.add_argument("--recompute", action="store_true", help="checkpointed recomputation (config 4: on)")
     ap.add_argument("--iters", type=int, default=10, help="config 5: NLCG iterations per band")
     ap.add_argument("--bands", default="3,5,7", help="config 5: low-pass corner frequencies (Hz), one band each")
     ap.add_argument("--order", type=int, default=4, help="config 5: Butterworth order")
     ap.add_argument("--shots", type=int, default=0, help="shots (0 = the config's: 64 or 30)")
     ap.add_argument("--nt", type=int, default=0, help="time steps (0 = the config's: 6000 or 12800)")
-    ap.add_argument("--snap", choices=["f32", "bf16", "f16"], default="f32")
+    ap.add_argument("--snap", choices=["f32", "bf16", "f16"], default=None,
+                    help="snapshot form (default f32; config 4: f16)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg")
     ap.add_argument("--no-plain", action="store_true", help="skip the plain-path leg")
@@ -55,7 +59,13 @@ def parse():
                     help="only build the survey and run this many forward time steps (for ncu captures)")
     ap.add_argument("--wave", type=int, default=0, help="shots per wave (0 = tuner)")
     ap.add_argument("--band", type=int, default=0, help="rows per warp work item (0 = tuner)")
-    return ap.parse_args()
+    a = ap.parse_args()
+    if a.config == 4:
+        a.snap = a.snap or "f16"
+        a.budget = a.budget or 120.0
+        a.recompute = True
+    a.snap = a.snap or "f32"
+    return a
 
 
 def workload_name(a):
@@ -63,6 +73,10 @@ def workload_name(a):
         return (f"uneven-window WAS batch: 600x6000 cells @25 m crustal model, {a.shots} OBS sources on 30-100 km "
                 f"windows, 1200 receivers @125 m, nt={a.nt} (dt=1.5625 ms, the CFL rule; 2.5 ms is unstable), "
                 f"acc=3, dPML=20, store_snap=10, {a.snap} snapshots, FP64 gradient stack")
+    if a.config == 4:
+        return (f"precision form of the batched MCS survey: 400x2000 cells @12.5 m, {a.shots} shots x 480 ch, "
+                f"nt={a.nt} (dt=1 ms), acc=3, dPML=20, store_snap=4, {a.snap} snapshots with a power-of-two scale "
+                f"per row segment, checkpointed recomputation under a {a.budget:g} GB HBM budget, FP64 stack")
     return (f"batched MCS survey: 400x2000 cells @12.5 m, {a.shots} shots x 480 ch, nt={a.nt} (dt=1 ms), "
             f"acc=3 (6th order), dPML=20, store_snap=10, {a.snap} snapshots, FP64 gradient stack")
 
@@ -76,7 +90,8 @@ def make_workload(a, seed_offset=0):
     else:
         a.shots = a.shots or 64
         a.nt = a.nt or 6000
-        spec, vp_true, vp0 = synth.config2(seed=2 + seed_offset, nshots=a.shots, nt=a.nt)
+        spec, vp_true, vp0 = synth.config2(seed=2 + seed_offset, nshots=a.shots, nt=a.nt,
+                                           store_snap=4 if a.config == 4 else 10)
     return spec, vp_true, vp0
 
 
@@ -181,7 +196,7 @@ def run_reference(a):
         return 0
     spec, vp_true, vp0 = make_workload(a)
     nthreads = os.cpu_count() or 1
-    nt_sample = 100 if a.config == 2 else 40
+    nt_sample = 100 if a.config in (2, 4) else 40
     for _ in range(a.warmup):
         cpu_sample(spec, vp0, nthreads, nt_sample)
     times = []
@@ -294,11 +309,13 @@ def main():
     stream = torch.cuda.Stream()
     F.set_stream(stream.cuda_stream)
     snap_form = {"f32": F.SNAP_F32, "bf16": F.SNAP_BF16, "f16": F.SNAP_F16}[a.snap]
+    budget = int(a.budget * 1e9)
     spec, vp_true, vp0 = make_workload(a, rank)
     lam_true, lam0 = lam_from_vp(vp_true), lam_from_vp(vp0)
 
     if a.profile:
-        sv = F.Survey(spec, snap_form=snap_form, wave_shots=a.wave, band_rows=a.band)
+        sv = F.Survey(spec, snap_form=snap_form, wave_shots=a.wave, band_rows=a.band, hbm_budget=budget,
+                      recompute=a.recompute)
         sv.set_lambda(lam0)
         torch.cuda.synchronize()
         p0, p1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -311,7 +328,8 @@ def main():
                           "GBps": sv.step_bytes() / ms / 1e6, "tuning": sv.tuning()}))
         return 0
     # observed data from the true model (untimed setup)
-    sv = F.Survey(spec, snap_form=snap_form, wave_shots=a.wave, band_rows=a.band)
+    sv = F.Survey(spec, snap_form=snap_form, wave_shots=a.wave, band_rows=a.band, hbm_budget=budget,
+                  recompute=a.recompute)
     sv.set_lambda(lam_true)
     sv.run(2)
     for i, sh in enumerate(spec.shots):
@@ -363,10 +381,11 @@ def main():
     step_s = r0.elapsed_time(r1) / 1e3 / nsteps
     bytes_step = sv.step_bytes()  # the shots of the first wave, which time_steps advances
     wave, band = sv.tuning()
+    rc_plan = sv.recompute_plan()
     achieved = bytes_step / step_s / 1e9
     tr = traffic_from_profile()
     roof = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
-            "traffic": tr * wave if (tr and a.config == 2) else None,
+            "traffic": tr * wave if (tr and a.config in (2, 4)) else None,
             "kernel": "k_step_interior + k_step_strip + k_step_bottom (one time step of all shots, three concurrent streams)",
             "algorithmic_bytes_per_launch": bytes_step, "avg_launch_ms": step_s * 1e3,
             "peak_kind": f"{peak_kind} copy bandwidth (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured"
@@ -381,7 +400,8 @@ def main():
         from fwi_gb300.survey import SurveySpec
         one = SurveySpec(ny=spec.ny, nx_model=spec.nx_model, d=spec.d, dt=spec.dt, nt=spec.nt, shots=[spec.shots[0]],
                          store_snap=spec.store_snap, acc=spec.acc, dpml=spec.dpml, water_rows=spec.water_rows)
-        pv = F.Survey(one, snap_form=snap_form, graph=False)
+        # config 4 compares with the FP32-snapshot plain path
+        pv = F.Survey(one, snap_form=F.SNAP_F32 if a.config == 4 else snap_form, graph=False)
         pv.set_lambda(lam0_dev.data_ptr())
         pv.run_device_grad(1, grad_dev.data_ptr())
         torch.cuda.synchronize()
@@ -412,7 +432,8 @@ def main():
         nsrc = sum(np.asarray(s.src).size for s in spec.shots)
         h_src = pin(nsrc)
         h_src[:] = np.concatenate([np.asarray(s.src, np.float32).reshape(-1, order="F") for s in spec.shots])
-        dh = _DescHolder(spec, snap_form, F.GRAD_F64)
+        dh = _DescHolder(spec, snap_form, F.GRAD_F64, hbm_budget=budget,
+                         flags=F.SURVEY_RECOMPUTE if a.recompute else 0)
         so = oo = 0
         for i, s in enumerate(spec.shots):
             ns, nr = s.src.size, len(s.nxRec) * spec.nt
@@ -451,7 +472,7 @@ def main():
     cpu = None
     if rank == 0 and world == 1 and not a.no_cpu:
         nthreads = os.cpu_count() or 1
-        rate, tcpu, desc = cpu_sample(spec, vp0, nthreads, 600 if a.config == 2 else 150)
+        rate, tcpu, desc = cpu_sample(spec, vp0, nthreads, 600 if a.config in (2, 4) else 150)
         cpu = {"value": rate, "unit": METRIC, "cores": nthreads, "kind": "port", "sample": desc,
                "seconds": tcpu}
 
@@ -461,7 +482,7 @@ def main():
                 "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded layered model, Ricker sources, "
                 "observed data synthesised on the true model)",
                 "config": {"workload": workload_name(a), "shots_per_gpu": len(spec.shots), "wave_shots": wave,
-                           "band_rows": band,
+                           "band_rows": band, "recompute_segment_steps": rc_plan[0], "recompute_segments": rc_plan[1],
                            "l2": "inputs larger than L2 (wavefields of all shots of a wave and their snapshots: "
                                  "tens to hundreds of GB)"},
                 "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "plain": plain, "gpu_launches": int(launches),

@@ -6,7 +6,17 @@ Every entry point loads fwi_gb300/_lib/libfwi_gb300.so and raises if it is
 missing (build it with ``python -m fwi_gb300.build``): there is no CPU
 fallback.
 """
-from ._native import FwiError, GRAD_F32, GRAD_F64, SNAP_BF16, SNAP_F16, SNAP_F32, load  # noqa: F401
+from ._native import (  # noqa: F401
+    GRAD_F32,
+    GRAD_F64,
+    SNAP_BF16,
+    SNAP_F16,
+    SNAP_F32,
+    SURVEY_NO_GRAPH,
+    SURVEY_RECOMPUTE,
+    FwiError,
+    load,
+)
 from .survey import ShotSpec, SurveySpec  # noqa: F401
 
 from .api import (  # noqa: E402,F401

@@ -71,22 +71,6 @@ __device__ __forceinline__ void window(float4 c, float4 hl, float4 hr, int lane,
     to_arr(r, w + 8);
 }
 
-// space_deriv2x / space_derivx at this lane's columns (solver_space_derivs.f90:11-16, :70-82)
-template <int R>
-__device__ __forceinline__ void xderivs(const float* w, const StepParams& P, float* d2, float* d1) {
-#pragma unroll
-    for (int e = 0; e < 4; ++e) {
-        float s2 = 0.f, s1 = 0.f;
-#pragma unroll
-        for (int i = 0; i <= R; ++i) {
-            s2 = s2 + P.c2[i] * (w[4 + e + i] + w[4 + e - i]);
-            s1 = s1 + (w[4 + e + i] - w[4 + e - i]) * P.c1[i];
-        }
-        d2[e] = s2;
-        d1[e] = s1;
-    }
-}
-
 // space_deriv2y / space_derivy at the centre row of the queue (:38-45, :109-116)
 template <int R>
 __device__ __forceinline__ void yderivs(const float4* q, const StepParams& P, float* d2, float* d1) {
@@ -118,74 +102,6 @@ __device__ __forceinline__ void yderiv1(const float4* f, const StepParams& P, fl
 #pragma unroll
         for (int i = 0; i <= R; ++i) s1 = s1 + (a[R + i][e] - a[R - i][e]) * P.c1[i];
         d1[e] = s1;
-    }
-}
-
-// Fetch element `col` (physical, inside this tile) of a per-lane 4-array.
-__device__ __forceinline__ float fetch(const float* a, int col_in_tile) {
-    const int ln = col_in_tile >> 2, el = col_in_tile & 3;
-    return __shfl_sync(FULL, sel(a, el), ln);
-}
-
-// Grid-edge clamp of the x derivatives: columns < R copy column R, columns
-// > nxt-1-R copy column nxt-1-R (solver_space_derivs.f90:18-23, :84-94).
-template <int R>
-__device__ __forceinline__ void xclamp(const ShotDev& S, int x0, int c0, bool first, bool last, float* d2, float* d1) {
-    if (first) {
-        const int ct = S.off + R - x0;
-        const float v2 = fetch(d2, ct), v1 = fetch(d1, ct);
-#pragma unroll
-        for (int e = 0; e < 4; ++e)
-            if (c0 + e < R) { d2[e] = v2; d1[e] = v1; }
-    }
-    if (last) {
-        const int ct = S.off + S.nxt - 1 - R - x0;
-        const float v2 = fetch(d2, ct), v1 = fetch(d1, ct);
-#pragma unroll
-        for (int e = 0; e < 4; ++e)
-            if (c0 + e > S.nxt - 1 - R) { d2[e] = v2; d1[e] = v1; }
-    }
-}
-
-// Strip-local x derivative of the old x-direction phi with the strip-edge
-// clamp (pml_matrices_x / _xycorner call space_derivx on the dn-wide strip
-// array, solver_PML_matrices.f90:15, :97).  Valid for columns of the side
-// strips / corners only.
-template <int R>
-__device__ __forceinline__ void phi_xderiv(const ShotDev& S, const StepParams& P, float4 ph, int lane, int x0, int c0,
-                                           bool first, bool last, float* dph) {
-    float w[12];
-    window(ph, ph, ph, lane, w);
-#pragma unroll
-    for (int e = 0; e < 4; ++e) {
-        float s1 = 0.f;
-#pragma unroll
-        for (int i = 0; i <= R; ++i) s1 = s1 + (w[4 + e + i] - w[4 + e - i]) * P.c1[i];
-        dph[e] = s1;
-    }
-    const int dn = S.dn, nx = S.nx;
-    if (first) {
-        const float lo = fetch(dph, S.off + R - x0), hi = fetch(dph, S.off + dn - 1 - R - x0);
-#pragma unroll
-        for (int e = 0; e < 4; ++e) {
-            const int c = c0 + e;
-            if (c < dn) {
-                if (c < R) dph[e] = lo;
-                else if (c > dn - 1 - R) dph[e] = hi;
-            }
-        }
-    }
-    if (last) {
-        const int base = dn + nx;
-        const float lo = fetch(dph, S.off + base + R - x0), hi = fetch(dph, S.off + base + dn - 1 - R - x0);
-#pragma unroll
-        for (int e = 0; e < 4; ++e) {
-            const int il = c0 + e - base;
-            if (il >= 0) {
-                if (il < R) dph[e] = lo;
-                else if (il > dn - 1 - R) dph[e] = hi;
-            }
-        }
     }
 }
 
@@ -520,7 +436,9 @@ __global__ void __launch_bounds__(128, (MODE == 1 && SNAP) ? 3 : 5) k_step_inter
     const float* PC = (P.parity ? S.pa : S.pb) + xl;  // p at this lane's columns
     float* P1 = (P.parity ? S.pb : S.pa) + xl;        // p_1, overwritten with p_3
     const float* C2 = S.c2 + xl;
-    // every middle tile has both neighbours; lanes 0 and 31 fetch the halos
+    // lanes 0 and 31 fetch the halo float4 left and right of the tile (in the
+    // first and last tile of a row these are the ends of the neighbouring
+    // rows: in bounds, and read only by lanes whose columns are outside [sl, sr))
     const int hoff = (lane == 0) ? -4 - 4 * lane : TILE - 4 * lane;
     const bool has_h = (lane == 0) || (lane == 31);
     float4* hslot = ring + (lane == 0 ? IN_HL : IN_HR);

@@ -88,3 +88,15 @@ def test_time_filter_device_pointer_and_batches():
     assert np.array_equal(dev.cpu().numpy().T, host)
     ref = O.time_filter(data, dt, 1, 0.0, 7.0)
     assert _rel(host, ref) <= 2e-5
+
+
+def test_akima_device_vs_reference_golden():
+    """The device resampler against INTRPL executed from akima433.f90."""
+    import os
+    import fwi_gb300 as F
+    z = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "akima.npz"))
+    for k in range(int(z["ncases"])):
+        d, out = z[f"c{k}_data"], z[f"c{k}_out"]
+        got = F.interpolation_akima(np.asfortranarray(d), float(z[f"c{k}_dt_in"]), d.shape[0], d.shape[1],
+                                    float(z[f"c{k}_dt_out"]), out.shape[0])
+        assert np.array_equal(got, out), k

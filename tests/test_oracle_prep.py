@@ -25,3 +25,13 @@ def test_butterworth_lowpass_gain():
     f10 = int(round(10.0 / (500.0 / 1000)))
     assert abs(abs(H[f10]) - 2 ** -0.5) < 1e-3              # -3 dB at the cut-off
     assert not np.any(P.time_filter(np.zeros((50, 2)), dt, 1, 0.0, 10.0))
+
+
+def test_akima_oracle_vs_reference_golden():
+    """oracle/prep.akima against INTRPL executed from akima433.f90."""
+    import os
+    z = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "akima.npz"))
+    for k in range(int(z["ncases"])):
+        d, out = z[f"c{k}_data"], z[f"c{k}_out"]
+        got = P.akima(d, z[f"c{k}_dt_in"], z[f"c{k}_dt_out"], out.shape[0])
+        assert np.array_equal(got, out), k

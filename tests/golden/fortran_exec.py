@@ -113,9 +113,10 @@ def _split_semis(line: str):
     return [p.strip() for p in parts if p.strip()]
 
 
-def logical_lines(text: str):
-    """Yield (lineno, statement) pairs with comments, continuations and
-    statement labels removed, lower-cased."""
+def logical_lines(text: str, with_labels: bool = False):
+    """Yield (lineno, statement) pairs -- (lineno, statement, label) with
+    with_labels -- with comments, continuations and statement labels removed,
+    lower-cased."""
     raw = text.split("\n")
     buf, start = "", None
     for no, line in enumerate(raw, 1):
@@ -136,9 +137,15 @@ def logical_lines(text: str):
             continue
         full = buf
         buf = ""
-        full = re.sub(r"^\d+\s+", "", full)  # statement label
+        ml = re.match(r"^(\d+)\s+", full)  # statement label
+        label = int(ml.group(1)) if ml else None
+        full = full[ml.end():] if ml else full
         for stmt in _split_semis(full):
-            yield start, stmt.lower()
+            if with_labels:
+                yield start, stmt.lower(), label
+            else:
+                yield start, stmt.lower()
+            label = None
 
 
 _TOKEN = re.compile(
@@ -360,7 +367,16 @@ def parse_stmt(no, s):
         return ("skip", no)
     if s.startswith("read") and re.match(r"^read\s*\(", s):
         return ("read", no)
-    if re.match(r"^(implicit|use|include|save|intrinsic|external|continue)\b", s):
+    if s == "continue":
+        return ("continue", no)
+    m = re.match(r"^go\s*to\s+(\d+)$", s)
+    if m:
+        return ("goto", no, int(m.group(1)))
+    m = re.match(r"^equivalence\s*(\(.*\))$", s)
+    if m:
+        groups = [[n.strip() for n in g.split(",")] for g in re.findall(r"\(([^()]*)\)", m.group(1))]
+        return ("equiv", no, groups)
+    if re.match(r"^(implicit|use|include|save|intrinsic|external)\b", s):
         return ("skip", no)
     m = _DECL.match(s)
     if m:
@@ -440,6 +456,10 @@ def parse_stmt(no, s):
     m = re.match(r"^do\s+while\s*\((.*)\)$", s)
     if m:
         return ("dowhile", no, parse_expr(m.group(1)))
+    m = re.match(r"^do\s+(\d+)\s*,?\s*([a-z_][a-z0-9_]*)\s*=\s*(.*)$", s)
+    if m:  # DO <label> var = ...: the loop ends at the labelled statement
+        parts = _split_top(m.group(3))
+        return ("dolab", no, int(m.group(1)), m.group(2), [parse_expr(p) for p in parts])
     m = re.match(r"^do\s+([a-z_][a-z0-9_]*)\s*=\s*(.*)$", s)
     if m:
         parts = _split_top(m.group(2))
@@ -522,12 +542,14 @@ def parse_units(text: str):
     units = {}
     cur = None
     stmts = []
-    for no, s in logical_lines(text):
+    labels = []
+    for no, s, label in logical_lines(text, with_labels=True):
         m = re.match(r"^(?:(?:integer|real|logical)\s+)?(subroutine|function)\s+([a-z_][a-z0-9_]*)\s*(\((.*)\))?", s)
         if m and cur is None:
             args = [a.strip() for a in (m.group(4) or "").split(",") if a.strip()]
             cur = (m.group(1), m.group(2), args)
             stmts = []
+            labels = []
             implicit_none = False
             continue
         if cur is None:
@@ -540,12 +562,19 @@ def parse_units(text: str):
             st = ("bad", no, s)
         if st[0] == "end" and not _open_blocks(stmts):
             decls = [x for x in stmts if x[0] == "decl"]
-            body = build_blocks([x for x in stmts if x[0] != "decl"])
-            units[cur[1]] = Unit(cur[0], cur[1], cur[2], body, decls)
-            units[cur[1]].implicit = not implicit_none
+            equivs = [g for x in stmts if x[0] == "equiv" for g in x[2]]
+            rest = [(x, lab) for x, lab in zip(stmts, labels) if x[0] not in ("decl", "equiv")]
+            flat = any(x[0] in ("goto", "dolab") or (x[0] == "if1" and x[3][0] == "goto") for x, _ in rest)
+            body = [] if flat else build_blocks([x for x, _ in rest])
+            u = Unit(cur[0], cur[1], cur[2], body, decls)
+            u.implicit = not implicit_none
+            u.equivs = equivs
+            u.flat = rest if flat else None  # statements with labels, run by a program counter
+            units[cur[1]] = u
             cur = None
             continue
         stmts.append(st)
+        labels.append(label)
     return units
 
 
@@ -647,8 +676,22 @@ class Interp:
                     env[nm] = Var(self._zero(ftype) if init is None else self.eval(ctx, init), ftype)
         if u.kind == "function" and name not in env:
             env[name] = Var(F32(0), "real")
+        # EQUIVALENCE: names of one group and of the same type share storage
+        # (members of another type keep their own: they are only aliased in
+        # memory, which these sources never read across types)
+        for group in getattr(u, "equivs", []):
+            first = {}
+            for nm in group:
+                v = self.lookup(ctx, nm)
+                if v.ftype in first:
+                    env[nm] = first[v.ftype]
+                else:
+                    first[v.ftype] = v
         try:
-            self.run(ctx, u.body)
+            if getattr(u, "flat", None) is not None:
+                self.run_flat(ctx, u.flat)
+            else:
+                self.run(ctx, u.body)
         except Return:
             pass
         if u.kind == "function":
@@ -669,6 +712,52 @@ class Interp:
         return {"integer": 0, "real": F32(0), "double": np.float64(0), "logical": False}.get(ftype, None)
 
     # -- statements ---------------------------------------------------------
+    def run_flat(self, ctx, flat):
+        """Statements with labels, GO TO and labelled DO loops, run by a
+        program counter (no block structure in these units)."""
+        where = {lab: i for i, (_, lab) in enumerate(flat) if lab is not None}
+        loops = []  # [var, iterations left, step, first body index, end index]
+        pc = 0
+        while pc < len(flat):
+            st, _ = flat[pc]
+            kind = st[0]
+            nxt = pc + 1
+            if kind == "dolab":
+                _, no, endlab, var, parts = st
+                lo = int(self.eval(ctx, parts[0]))
+                hi = int(self.eval(ctx, parts[1]))
+                step = int(self.eval(ctx, parts[2])) if len(parts) > 2 else 1
+                count = max((hi - lo + step) // step, 0)
+                v = self.lookup(ctx, var)
+                v.value = lo
+                if count == 0:
+                    nxt = where[endlab] + 1
+                else:
+                    loops.append([v, count, step, pc + 1, where[endlab]])
+            elif kind == "goto":
+                nxt = where[st[2]]
+            elif kind == "if1" and st[3][0] == "goto":
+                if self.truth(self.eval(ctx, st[2])):
+                    nxt = where[st[3][2]]
+            elif kind in ("continue", "skip"):
+                pass
+            else:
+                self.exec(ctx, st)
+            if nxt == pc + 1:
+                # the statement that ends a loop: next iteration or leave it
+                while loops and loops[-1][4] == pc:
+                    lp = loops[-1]
+                    lp[1] -= 1
+                    lp[0].value = lp[0].value + lp[2]
+                    if lp[1] > 0:
+                        nxt = lp[3]
+                        break
+                    loops.pop()
+            else:
+                while loops and not (loops[-1][3] <= nxt <= loops[-1][4]):
+                    loops.pop()  # a jump out of the loop
+            pc = nxt
+
     def run(self, ctx, body):
         for st in body:
             self.exec(ctx, st)
@@ -729,7 +818,7 @@ class Interp:
             raise Exit()
         elif kind == "cycle":
             raise Cycle()
-        elif kind == "skip":
+        elif kind in ("skip", "continue"):
             pass
         elif kind == "bad":
             raise RuntimeError(f"line {st[1]}: statement not supported: {st[2]!r}")

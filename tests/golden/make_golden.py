@@ -3,10 +3,11 @@
 Run in a container where the reference checkout exists (its path is the
 first argument, default /root/reference).  Each case executes the
 reference's own Fortran routines -- solver_acoustic_SS and the files it
-calls, Misfit_function/Misfit_L2, Beta_calculous, Ricker_mcs, and the
-geometry and time-step statements of get_mcs_data.f90 and
-calculate_misfit_gradient.f90 -- through fortran_exec.py in IEEE single
-precision, on small seeded inputs, and stores inputs and outputs.
+calls, Misfit_function/Misfit_L2, Beta_calculous, Ricker_mcs, polyfit,
+interpolation_akima/INTRPL, and the geometry and time-step statements of
+get_mcs_data.f90 and calculate_misfit_gradient.f90 -- through fortran_exec.py
+in IEEE single precision, on small seeded inputs, and stores inputs and
+outputs.
 
 The fixtures are committed; tests read them and never need the reference.
 
@@ -225,6 +226,31 @@ def case_polyfit(src):
     print("polyfit: done")
 
 
+def case_akima(src):
+    """interpolation_akima.f90 + INTRPL (akima433.f90): resampling of traces
+    between time axes, incl. two/three/four input samples, flat and linear
+    traces and output times past the last input sample."""
+    prog = fe.Program([os.path.join(src, "interpolation_akima.f90"), os.path.join(src, "akima433.f90")])
+    rng = np.random.default_rng(13)
+    out = {}
+    cases = [(60, 0.004, 190, 0.0013), (2, 0.01, 7, 0.004), (3, 0.01, 9, 0.003), (4, 0.01, 11, 0.004),
+             (5, 0.002, 1, 0.001), (90, 0.001, 40, 0.0025), (48, 0.0025, 96, 0.00125)]
+    for k, (L, dti, nto, dto) in enumerate(cases):
+        ntr = 5
+        data = farr(rng.standard_normal((L, ntr)))
+        data[:, 1] = F32(0.25) * np.arange(L, dtype=np.float32)
+        data[:, 2] = 0.0
+        if L > 6:
+            data[L // 2:L // 2 + 3, 3] = 1.0
+        res = farr(np.zeros((nto, ntr)))
+        prog.call("interpolation_akima", V(data), V(F32(dti)), V(L, "integer"), V(res), V(ntr, "integer"),
+                  V(F32(dto)), V(nto, "integer"))
+        out.update({f"c{k}_data": data, f"c{k}_dt_in": F32(dti), f"c{k}_dt_out": F32(dto), f"c{k}_out": res})
+    out["ncases"] = len(cases)
+    np.savez_compressed(os.path.join(HERE, "akima.npz"), **out)
+    print("akima: done")
+
+
 def main():
     src = os.path.join(sys.argv[1] if len(sys.argv) > 1 else "/root/reference", "src")
     only = set(sys.argv[2:])  # optional case names: coeffs misfit geometry polyfit akima solver
@@ -239,6 +265,7 @@ def main():
         case_misfit(src)
         case_geometry(src)
         case_polyfit(src)
+        case_akima(src)
     # acc=3 (the reference's hard-coded order), snapshots every 10 steps;
     # sources incl. one outside the interior; receivers with duplicates,
     # in the left pad, in the bottom strip and in a bottom corner.

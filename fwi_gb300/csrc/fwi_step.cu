@@ -49,6 +49,20 @@ __device__ __forceinline__ void st4(float* p, float4 v) { *reinterpret_cast<floa
 
 __device__ __forceinline__ void to_arr(float4 v, float* a) { a[0] = v.x; a[1] = v.y; a[2] = v.z; a[3] = v.w; }
 __device__ __forceinline__ float4 from_arr(const float* a) { return make_float4(a[0], a[1], a[2], a[3]); }
+// Packed FP32 pairs (Blackwell f32x2 add/fma: two independently rounded FP32
+// operations per instruction), used by the interior and bottom updates.
+// Products are formed as fma(a, b, +0): ptxas contracts a packed multiply
+// feeding a packed add into a fused multiply-add (even with --fmad=false),
+// which would change the rounding.  fma with a +0 addend is the correctly
+// rounded product and is not contracted; it differs from a*b only in the
+// sign of a zero product, which changes no nonzero value downstream (these
+// updates only add and multiply).  An addend of -0 would keep the sign too,
+// but then fma(a, b, -0) is a plain product to ptxas and is contracted
+// again.  Lane columns (0,1) and (2,3) form the two pairs; x-neighbour pairs
+// at odd offsets are re-paired.
+__device__ __forceinline__ float2 pr(const float4& v, int k) { return k == 0 ? make_float2(v.x, v.y) : make_float2(v.z, v.w); }
+__device__ __forceinline__ float2 mul0(float2 a, float2 b) { return __ffma2_rn(a, b, make_float2(0.f, 0.f)); }
+
 __device__ __forceinline__ float sel(const float* a, int e) {
     return e == 0 ? a[0] : (e == 1 ? a[1] : (e == 2 ? a[2] : a[3]));
 }
@@ -274,6 +288,12 @@ __device__ __forceinline__ void bottom_rows(const StepParams& P, const WorkItem&
 
     int ri = it.r0;
     int rrow = (ri < it.r1) ? P.recs[ri].row : INT_MAX;
+    float2 c1p[R + 1], c2p[R + 1];
+#pragma unroll
+    for (int i = 0; i <= R; ++i) {
+        c1p[i] = make_float2(P.c1[i], P.c1[i]);
+        c2p[i] = make_float2(P.c2[i], P.c2[i]);
+    }
 
     int slot = 0;
     for (int jl = j0; jl < j1; ++jl) {
@@ -282,59 +302,78 @@ __device__ __forceinline__ void bottom_rows(const StepParams& P, const WorkItem&
         const float4* st = ring + slot * SB_SIZE;
         if (y + R <= nyt - 1) q[2 * R] = st[SB_P + lane];
         const size_t ro = (size_t)y * pitch + xl;
-        float pm1[4], cc[4], pc[4];
-        to_arr(st[SB_P1 + lane], pm1);
-        to_arr(st[SB_C2 + lane], cc);
-        to_arr(q[R], pc);
-        float d2y[4], dy[4];
-        if (y <= nyt - 1 - R) {
-            yderivs<R>(q, P, d2y, dy);
-        } else {
-#pragma unroll
-            for (int e = 0; e < 4; ++e) { d2y[e] = d2yBot[e]; dy[e] = dyBot[e]; }
-        }
+        const float4 PM1 = st[SB_P1 + lane], CC = st[SB_C2 + lane], PHY = st[SB_PY + lane], CHY = st[SB_CY + lane];
         const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
         const float4 hl = has_hl ? st[SB_HL] : z4, hr = has_hr ? st[SB_HR] : z4;
         float w[12];
         window(q[R], hl, hr, lane, w);
-        // space_deriv2x (no clamp and no first x derivative: interior columns)
-        float d2x[4];
-#pragma unroll
-        for (int e = 0; e < 4; ++e) {
-            float s2 = 0.f;
-#pragma unroll
-            for (int i = 0; i <= R; ++i) s2 = s2 + P.c2[i] * (w[4 + e + i] + w[4 + e - i]);
-            d2x[e] = s2;
-        }
-
-        // strip-local y derivative of the old y-direction phi (pml_matrices_y :335)
-        float dphy[4];
-        if (jl < R) {
-#pragma unroll
-            for (int e = 0; e < 4; ++e) dphy[e] = dphyTop[e];
-        } else if (jl <= dn - 1 - R) {
-            f[2 * R] = st[SB_FA + lane];
-            yderiv1<R>(f, P, dphy);
-#pragma unroll
-            for (int i = 0; i < 2 * R; ++i) f[i] = f[i + 1];
-        } else {
-#pragma unroll
-            for (int e = 0; e < 4; ++e) dphy[e] = dphyBot[e];
-        }
-
-        float phy[4], chy[4], p3[4];
-        to_arr(st[SB_PY + lane], phy);
-        to_arr(st[SB_CY + lane], chy);
+        // strip-local y derivative of the old y-direction phi (pml_matrices_y
+        // :335): clamped to local rows R and dn-1-R at the strip's ends
+        const int dmode = (jl < R) ? 0 : ((jl <= dn - 1 - R) ? 1 : 2);
+        if (dmode == 1) f[2 * R] = st[SB_FA + lane];
+        const bool yclamp = y > nyt - 1 - R;
         // bottom strip: factor(j)  (solver_PML_coeffs.f90, pml_matrices_y)
         const float A = __ldg(P.fA + jl), B = __ldg(P.fB + jl);
+        const float2 Ap = make_float2(A, A), Bp = make_float2(B, B);
+        float phy[4], chy[4], p3[4];
 #pragma unroll
-        for (int e = 0; e < 4; ++e) {
-            const float phyn = A * phy[e] + B * dy[e];
-            const float chyn = A * chy[e] + B * (d2y[e] + dphy[e]);
-            const float propy = dphy[e] + chyn;
-            phy[e] = phyn;
-            chy[e] = chyn;
-            p3[e] = ((-pm1[e]) + 2.f * pc[e]) + cc[e] * ((d2x[e] + d2y[e]) + propy);
+        for (int k = 0; k < 2; ++k) {
+            // space_deriv2y / space_derivy: s2 = s2 + (p(j+i)+p(j-i))*c2(i),
+            // s1 = s1 + (p(j+i)-p(j-i))*c1(i); rows below nyt-1-R take row nyt-1-R's
+            float2 d2y, dy;
+            if (!yclamp) {
+                float2 s2 = make_float2(0.f, 0.f), s1 = make_float2(0.f, 0.f);
+#pragma unroll
+                for (int i = 0; i <= R; ++i) {
+                    const float2 up = pr(q[R + i], k), dn2 = pr(q[R - i], k);
+                    s2 = __fadd2_rn(s2, mul0(__fadd2_rn(up, dn2), c2p[i]));
+                    s1 = __fadd2_rn(s1, mul0(__fadd2_rn(up, make_float2(-dn2.x, -dn2.y)), c1p[i]));
+                }
+                d2y = s2;
+                dy = s1;
+            } else {
+                d2y = make_float2(d2yBot[2 * k], d2yBot[2 * k + 1]);
+                dy = make_float2(dyBot[2 * k], dyBot[2 * k + 1]);
+            }
+            // space_deriv2x: s2 = s2 + c2(i)*(p(j+i)+p(j-i)) (interior columns: no clamp)
+            float2 d2x = make_float2(0.f, 0.f);
+#pragma unroll
+            for (int i = 0; i <= R; ++i) {
+                const int ia = 4 + 2 * k + i, ib = 4 + 2 * k - i;
+                d2x = __fadd2_rn(d2x, mul0(c2p[i], __fadd2_rn(make_float2(w[ia], w[ia + 1]), make_float2(w[ib], w[ib + 1]))));
+            }
+            float2 dph;
+            if (dmode == 0) {
+                dph = make_float2(dphyTop[2 * k], dphyTop[2 * k + 1]);
+            } else if (dmode == 1) {
+                float2 s1 = make_float2(0.f, 0.f);
+#pragma unroll
+                for (int i = 0; i <= R; ++i) {
+                    const float2 up = pr(f[R + i], k), dn2 = pr(f[R - i], k);
+                    s1 = __fadd2_rn(s1, mul0(__fadd2_rn(up, make_float2(-dn2.x, -dn2.y)), c1p[i]));
+                }
+                dph = s1;
+            } else {
+                dph = make_float2(dphyBot[2 * k], dphyBot[2 * k + 1]);
+            }
+            // phi' = A phi + B dy, chi' = A chi + B (d2y + dphi), prop = dphi + chi',
+            // p_3 = (-p_1 + 2p) + c2 ((d2x + d2y) + prop)
+            const float2 phyn = __fadd2_rn(mul0(Ap, pr(PHY, k)), mul0(Bp, dy));
+            const float2 chyn = __fadd2_rn(mul0(Ap, pr(CHY, k)), mul0(Bp, __fadd2_rn(d2y, dph)));
+            const float2 propy = __fadd2_rn(dph, chyn);
+            const float2 pc = pr(q[R], k), pm = pr(PM1, k);
+            const float2 base = __fadd2_rn(make_float2(-pm.x, -pm.y), __fadd2_rn(pc, pc));
+            const float2 r = __fadd2_rn(base, mul0(pr(CC, k), __fadd2_rn(__fadd2_rn(d2x, d2y), propy)));
+            phy[2 * k] = phyn.x;
+            phy[2 * k + 1] = phyn.y;
+            chy[2 * k] = chyn.x;
+            chy[2 * k + 1] = chyn.y;
+            p3[2 * k] = r.x;
+            p3[2 * k + 1] = r.y;
+        }
+        if (dmode == 1) {
+#pragma unroll
+            for (int i = 0; i < 2 * R; ++i) f[i] = f[i + 1];
         }
         if (full) {
             st4(PHN + ro, from_arr(phy));
@@ -359,18 +398,6 @@ __device__ __forceinline__ void bottom_rows(const StepParams& P, const WorkItem&
     }
     cp_wait<0>();
 }
-
-// Interior update of one row on packed FP32 pairs (Blackwell f32x2
-// add/fma: two independently rounded FP32 operations per instruction).
-// Products are formed as fma(a, b, +0): ptxas contracts a packed multiply
-// feeding a packed add into a fused multiply-add (even with --fmad=false),
-// which would change the rounding; fma with a +0 addend is the correctly
-// rounded product, and it is not fused with the following add.  (It can only
-// differ from a*b in the sign of a zero product, and every sum it enters
-// starts from +0, so no value changes.)  Lane columns (0,1) and (2,3) form
-// the two pairs; x-neighbour pairs at odd offsets are re-paired.
-__device__ __forceinline__ float2 pr(const float4& v, int k) { return k == 0 ? make_float2(v.x, v.y) : make_float2(v.z, v.w); }
-__device__ __forceinline__ float2 mul0(float2 a, float2 b) { return __ffma2_rn(a, b, make_float2(0.f, 0.f)); }
 
 template <int R>
 __device__ __forceinline__ void interior_update2(const float4* q, float4 L, float4 Rt, float4 pm1, float4 cc,
@@ -661,15 +688,19 @@ __device__ __forceinline__ void strip_rows(const StepParams& P, const WorkItem& 
     float* pring = sw + L::P_RING;
     float* yring = sw + L::Y_RING;
     float* slots = sw + L::SLOTS;
-    auto pline = [&](int r) { return pring + (r % L::QN) * L::LINE + L::M; };
-    auto yline = [&](int r) { return yring + (r % L::QN) * L::LINE + L::M; };
-    auto sline = [&](int y, int f) { return slots + ((y % L::NA) * L::NS + f) * L::LINE + L::M; };
+    // ring positions: padded row r lives in line r % QN of the p / y-phi
+    // rings and row y's per-cell inputs in slot y % NA; the row loop keeps
+    // both positions incrementally (rows are >= 0: every item starts at or
+    // below row dn >= R)
+    auto pline = [&](int q) { return pring + q * L::LINE + L::M; };
+    auto yline = [&](int q) { return yring + q * L::LINE + L::M; };
+    auto sline = [&](int q, int f) { return slots + (q * L::NS + f) * L::LINE + L::M; };
 
-    // p row r (and the old y-phi row r) into the rings; rows past the grid
+    // p row r (and the old y-phi row r) into ring line q; rows past the grid
     // are never read
-    auto issue_row = [&](int r) {
+    auto issue_row = [&](int r, int q) {
         if (r > nyt - 1) return;
-        float* d = pline(r);
+        float* d = pline(q);
         const float* src = PC + (size_t)r * pitch + xs;
 #pragma unroll
         for (int k = 0; k < K; ++k)
@@ -677,38 +708,38 @@ __device__ __forceinline__ void strip_rows(const StepParams& P, const WorkItem& 
         if (has_hl) cp4(d + jhl, src + jhl);
         if (has_hr) cp4(d + jhr, src + jhr);
         if (BOT && r >= yb0) {
-            float* e = yline(r);
+            float* e = yline(q);
             const float* ysrc = PHO + (size_t)r * pitch + xs;
 #pragma unroll
             for (int k = 0; k < K; ++k)
                 if (valid[k]) cp4(e + 32 * k + lane, ysrc + 32 * k + lane);
         }
     };
-    auto issue_slot = [&](int y) {
+    auto issue_slot = [&](int y, int q) {
         const size_t ro = (size_t)y * pitch + xs;
 #pragma unroll
         for (int k = 0; k < K; ++k) {
             const int j = 32 * k + lane;
             if (act[k]) {
-                cp4(sline(y, L::S_P1) + j, P1 + ro + j);
-                cp4(sline(y, L::S_C2) + j, S.c2 + ro + j);
-                if (BOT) cp4(sline(y, L::S_CY) + j, S.chy + ro + j);
+                cp4(sline(q, L::S_P1) + j, P1 + ro + j);
+                cp4(sline(q, L::S_C2) + j, S.c2 + ro + j);
+                if (BOT) cp4(sline(q, L::S_CY) + j, S.chy + ro + j);
             }
             if (xc[k]) {
-                cp4(sline(y, L::S_PX) + j, S.phx + ro + j);
-                cp4(sline(y, L::S_CX) + j, S.chx + ro + j);
+                cp4(sline(q, L::S_PX) + j, S.phx + ro + j);
+                cp4(sline(q, L::S_CX) + j, S.chx + ro + j);
             }
         }
     };
     const int y0 = it.y0, y1 = it.y1;
 #pragma unroll 1
-    for (int i = 0; i < 2 * R; ++i) issue_row(y0 - R + i);
+    for (int i = 0; i < 2 * R; ++i) issue_row(y0 - R + i, (y0 - R + i) % L::QN);
     cp_commit();
 #pragma unroll 1
     for (int i = 0; i < L::LA; ++i) {
         if (y0 + i < y1) {
-            issue_row(y0 + i + R);
-            issue_slot(y0 + i);
+            issue_row(y0 + i + R, (y0 + i + R) % L::QN);
+            issue_slot(y0 + i, (y0 + i) % L::NA);
         }
         cp_commit();
     }
@@ -769,13 +800,21 @@ __device__ __forceinline__ void strip_rows(const StepParams& P, const WorkItem& 
     int rrow = (ri < it.r1) ? P.recs[ri].row : INT_MAX;
     const size_t seg = (size_t)S.ntiles + (right ? 1 : 0);
 
+    int qy = y0 % L::QN, sy = y0 % L::NA;  // ring line of row y, slot of row y
+    // ring line of row y + i for a compile-time i in [-QN, QN]
+    auto qat = [&](int i) {
+        int q = qy + i;
+        if (i > 0) q = (q >= L::QN) ? q - L::QN : q;
+        if (i < 0) q = (q < 0) ? q + L::QN : q;
+        return q;
+    };
 #pragma unroll 1
     for (int y = y0; y < y1; ++y) {
         cp_wait<L::LA - 1>();
         __syncwarp();
         const int jl = y - yb0;  // bottom rows: index inside the bottom strip
-        const float* pl = pline(y);
-        const float* px = sline(y, L::S_PX);
+        const float* pl = pline(qy);
+        const float* px = sline(sy, L::S_PX);
         float pc[K], d2x[K], dx[K], d2y[K], dy[K], dphx[K], dphy[K];
 #pragma unroll
         for (int k = 0; k < K; ++k) {
@@ -788,12 +827,12 @@ __device__ __forceinline__ void strip_rows(const StepParams& P, const WorkItem& 
             float2 a2 = make_float2(0.f, 0.f), a1 = make_float2(0.f, 0.f), ap = make_float2(0.f, 0.f);
 #pragma unroll
             for (int i = 0; i <= R; ++i) {
-                const float2 hi_ = make_float2(pl[j + i], pline(y + i)[j]);
-                const float2 lo_ = make_float2(pl[j - i], pline(y - i)[j]);
+                const float2 hi_ = make_float2(pl[j + i], pline(qat(i))[j]);
+                const float2 lo_ = make_float2(pl[j - i], pline(qat(-i))[j]);
                 a2 = __fadd2_rn(a2, mul0(__fadd2_rn(hi_, lo_), c2p[i]));
                 a1 = __fadd2_rn(a1, mul0(__fadd2_rn(hi_, make_float2(-lo_.x, -lo_.y)), c1p[i]));
-                const float2 fh = make_float2(px[j + i], BOT ? yline(y + i)[j] : 0.f);
-                const float2 fl = make_float2(px[j - i], BOT ? yline(y - i)[j] : 0.f);
+                const float2 fh = make_float2(px[j + i], BOT ? yline(qat(i))[j] : 0.f);
+                const float2 fl = make_float2(px[j - i], BOT ? yline(qat(-i))[j] : 0.f);
                 ap = __fadd2_rn(ap, mul0(__fadd2_rn(fh, make_float2(-fl.x, -fl.y)), c1p[i]));
             }
             d2x[k] = a2.x;
@@ -846,8 +885,8 @@ __device__ __forceinline__ void strip_rows(const StepParams& P, const WorkItem& 
 #pragma unroll
         for (int k = 0; k < K; ++k) {
             const int j = 32 * k + lane, c = col[k];
-            pm1[k] = sline(y, L::S_P1)[j];
-            const float cc = sline(y, L::S_C2)[j];
+            pm1[k] = sline(sy, L::S_P1)[j];
+            const float cc = sline(sy, L::S_C2)[j];
             const float base = (-pm1[k]) + 2.f * pc[k];
             if (!BOT) {
                 if (xc[k]) {
@@ -855,7 +894,7 @@ __device__ __forceinline__ void strip_rows(const StepParams& P, const WorkItem& 
                     const int fi = (c < dn) ? (dn - 1 - c) : (c - dn - nx);
                     const float A = __ldg(P.fA + fi), B = __ldg(P.fB + fi);
                     const float phn = A * px[j] + B * dx[k];
-                    const float chn = A * sline(y, L::S_CX)[j] + B * (d2x[k] + dphx[k]);
+                    const float chn = A * sline(sy, L::S_CX)[j] + B * (d2x[k] + dphx[k]);
                     const float prop = dphx[k] + chn;
                     p3[k] = base + cc * ((d2x[k] + d2y[k]) + prop);
                     S.phx[ro + 32 * k] = phn;
@@ -870,13 +909,13 @@ __device__ __forceinline__ void strip_rows(const StepParams& P, const WorkItem& 
                 if (xc[k]) fi = max(jl, (c < dn) ? (dn - 1 - c) : (c - dn - nx));
                 if (!act[k]) fi = 0;
                 const float A = __ldg(P.fA + fi), B = __ldg(P.fB + fi);
-                const float phyn = A * yline(y)[j] + B * dy[k];
-                const float chyn = A * sline(y, L::S_CY)[j] + B * (d2y[k] + dphy[k]);
+                const float phyn = A * yline(qy)[j] + B * dy[k];
+                const float chyn = A * sline(sy, L::S_CY)[j] + B * (d2y[k] + dphy[k]);
                 const float propy = dphy[k] + chyn;
                 if (xc[k]) {
                     // corner, two stages (solver_acoustic_SS.f90:395-411)
                     const float phxn = A * px[j] + B * dx[k];
-                    const float chxn = A * sline(y, L::S_CX)[j] + B * (d2x[k] + dphx[k]);
+                    const float chxn = A * sline(sy, L::S_CX)[j] + B * (d2x[k] + dphx[k]);
                     const float propx = dphx[k] + chxn;
                     const float tt = base + cc * ((d2x[k] + d2y[k]) + propx);
                     p3[k] = tt + cc * propy;
@@ -973,10 +1012,12 @@ __device__ __forceinline__ void strip_rows(const StepParams& P, const WorkItem& 
         }
 
         if (y + L::LA < y1) {
-            issue_row(y + L::LA + R);
-            issue_slot(y + L::LA);
+            issue_row(y + L::LA + R, qat(L::LA + R));
+            issue_slot(y + L::LA, (sy + L::LA >= L::NA) ? sy + L::LA - L::NA : sy + L::LA);
         }
         cp_commit();
+        qy = (qy + 1 == L::QN) ? 0 : qy + 1;
+        sy = (sy + 1 == L::NA) ? 0 : sy + 1;
     }
     cp_wait<0>();
 }

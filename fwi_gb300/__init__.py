@@ -14,6 +14,7 @@ from ._native import (  # noqa: F401
     SNAP_F32,
     SURVEY_NO_GRAPH,
     SURVEY_RECOMPUTE,
+    SURVEY_SINGLE_STEP,
     FwiError,
     load,
 )

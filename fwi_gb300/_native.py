@@ -21,6 +21,7 @@ FWI_ERR_STATE = -5
 SNAP_F32, SNAP_BF16, SNAP_F16 = 0, 1, 2
 SURVEY_NO_GRAPH = 1
 SURVEY_RECOMPUTE = 2
+SURVEY_SINGLE_STEP = 4
 GRAD_F32, GRAD_F64 = 0, 1
 
 EXPORTS = [

@@ -219,9 +219,10 @@ class Survey:
     """Device-resident batched survey (fwi_survey_create & co)."""
 
     def __init__(self, spec: SurveySpec, snap_form=N.SNAP_F32, grad_form=N.GRAD_F64, hbm_budget=0, wave_shots=0,
-                 band_rows=0, graph=True, recompute=False):
+                 band_rows=0, graph=True, recompute=False, two_step=True):
         self.spec = spec
-        flags = (0 if graph else N.SURVEY_NO_GRAPH) | (N.SURVEY_RECOMPUTE if recompute else 0)
+        flags = ((0 if graph else N.SURVEY_NO_GRAPH) | (N.SURVEY_RECOMPUTE if recompute else 0)
+                 | (0 if two_step else N.SURVEY_SINGLE_STEP))
         self._h = _DescHolder(spec, snap_form, grad_form, hbm_budget, wave_shots, band_rows, flags)
         handle = C.c_void_p()
         N.check(N.load().fwi_survey_create(C.byref(self._h.desc), C.byref(handle)))

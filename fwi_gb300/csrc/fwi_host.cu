@@ -22,6 +22,7 @@
 #include "fwi_internal.cuh"
 
 namespace fwi {
+cudaError_t launch_step2(int acc, int mode, const StepParams& pf, cudaStream_t st);
 cudaError_t launch_step(int acc, int mode, int kstrip, const StepParams& pm, const StepParams& pb, cudaStream_t sm,
                         cudaStream_t sb, cudaStream_t ss);
 cudaError_t configure_step_kernels();
@@ -93,6 +94,7 @@ struct LibState {
     cudaStream_t aux = nullptr;      // bottom-row kernels run here, concurrently
     cudaStream_t aux3 = nullptr;     // side-strip kernels run here, concurrently
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_join2 = nullptr;
+    cudaEvent_t ev2[10] = {};  // two-step pipeline (two sets of five)
     int prio_hi = 0;
     int acc = 3, dpml = 20;
     long long launches = 0;
@@ -190,6 +192,7 @@ struct Layout {
     int ny, nx, dn, nyt, nxt, off, pitch, ntiles;
     int sl, sr;   // side strips [0, sl) and [sr, nxt), interior columns [sl, sr)
     int kstrip;   // columns per lane of a strip warp: strips are at most 32*kstrip wide
+    int acc;      // stencil half-width R
 };
 
 Layout make_layout(int ny, int nx, int acc, int dpml) {
@@ -197,6 +200,7 @@ Layout make_layout(int ny, int nx, int acc, int dpml) {
     l.ny = ny;
     l.nx = nx;
     l.dn = dpml + 2 * acc;
+    l.acc = acc;
     l.nyt = 2 * l.dn + ny;
     l.nxt = nx + 2 * l.dn;
     const int r0 = (l.nxt - 1) % TILE;
@@ -272,6 +276,10 @@ int validate_geometry(const ShotGeom& g, const Layout& l, int shot) {
 struct Lists {
     // boundary lists: nstrip side-strip items (bottom rows first), then the bottom tiles
     std::vector<WorkItem> int_fwd, int_adj, bnd_fwd, bnd_adj;
+    // two-step passes: two-step tiles (kind 4; the first ncore of them core tiles, which read
+    // no cell of the single-step lists) and the interior items outside them (kind 0)
+    std::vector<WorkItem> fus_fwd, fus_adj, lft_fwd, lft_adj;
+    int ncore = 0;
     int nstrip = 0, kstrip = 1;
     std::vector<SrcEnt> src_fwd, src_adj;
     std::vector<RecEnt> recs;
@@ -322,6 +330,49 @@ void append_item(Lists& L_, std::vector<WorkItem>& items, std::vector<SrcEnt>& s
     items.push_back(it);
 }
 
+// One two-step tile: output columns [x0, x0 + 120) (stored within [c0, c1))
+// of rows [y0, y1); its sources are the cells of its whole first-step region,
+// rows [y0 - R, y1 + R) and columns [x0 - 4, x0 + 124); its receivers the
+// cells it stores.
+void append_two_step(Lists& L_, std::vector<WorkItem>& items, std::vector<SrcEnt>& srcs,
+                     const std::vector<SrcEnt>& cells, const std::vector<RecEnt>& recs_shot, int shot, int x0, int y0,
+                     int y1, int R, bool with_recs, int c0, int c1) {
+    WorkItem it{};
+    it.shot = shot;
+    it.tile = x0;
+    it.y0 = y0;
+    it.y1 = y1;
+    it.kind = 4;
+    std::vector<SrcEnt> sel;
+    for (auto& c : cells)
+        if (c.row >= y0 - R && c.row < y1 + R && c.col >= x0 - 4 && c.col < x0 + 124) sel.push_back(c);
+    std::stable_sort(sel.begin(), sel.end(), [](const SrcEnt& a, const SrcEnt& b) { return a.row < b.row; });
+    it.s0 = (int)srcs.size();
+    srcs.insert(srcs.end(), sel.begin(), sel.end());
+    it.s1 = (int)srcs.size();
+    it.r0 = it.r1 = (int)L_.recs.size();
+    if (with_recs) {
+        std::vector<RecEnt> rs;
+        for (auto& r : recs_shot)
+            if (r.row >= y0 && r.row < y1 && r.col >= std::max(c0, x0) && r.col < std::min(c1, x0 + 120))
+                rs.push_back(r);
+        std::stable_sort(rs.begin(), rs.end(), [](const RecEnt& a, const RecEnt& b) { return a.row < b.row; });
+        L_.recs.insert(L_.recs.end(), rs.begin(), rs.end());
+        it.r1 = (int)L_.recs.size();
+    }
+    items.push_back(it);
+}
+
+// A shot gets two-step tiles when the first-step cells around its interior
+// columns are plain interior cells: R model columns on either side of
+// [sl, sr) (no CPML column, no clamp) and at least one model row above the
+// last R (which border the bottom pad and stay single-step).
+bool two_step_ok(const Layout& l) {
+    const int R = l.acc;
+    return l.sl < l.sr && l.sl - R >= l.dn && l.sr + R <= l.dn + l.nx && l.ny > R;
+}
+
+constexpr int TWO_STEP_BAND = 48;     // rows per two-step tile
 constexpr int BOTTOM_BAND = 9;        // rows per bottom-tile work item
 constexpr int STRIP_BAND = 16;        // rows per side-strip work item (model rows)
 constexpr int STRIP_BOTTOM_BAND = 5;  // rows per side-strip work item (bottom pad rows)
@@ -329,11 +380,13 @@ constexpr int STRIP_BOTTOM_BAND = 5;  // rows per side-strip work item (bottom p
 
 // Work lists for a set of shots (local shot index = position in `geoms`).
 // All shots share dn (one acc / dpml per launch), hence one kstrip.
-Lists build_lists(const std::vector<ShotGeom>& geoms, const std::vector<Layout>& lays, int band_rows) {
+// fband > 0 also builds the two-step lists (two-step tiles in bands of fband
+// rows).
+Lists build_lists(const std::vector<ShotGeom>& geoms, const std::vector<Layout>& lays, int band_rows, int fband = 0) {
     Lists out;
     std::vector<WorkItem> sbot_f, sbot_a, strip_f, strip_a, bot_f, bot_a;
     // interior items grouped [shot][band] (a band = the tiles of one row band)
-    std::vector<std::vector<std::vector<WorkItem>>> main_f, main_a;
+    std::vector<std::vector<std::vector<WorkItem>>> main_f, main_a, fus_f, fus_a, edge_f, edge_a;
     if (!lays.empty()) out.kstrip = lays[0].kstrip;
     auto bands = [](int n, int rows, auto&& fn) {
         const int nb = std::max(1, (n + rows - 1) / rows);
@@ -376,6 +429,43 @@ Lists build_lists(const std::vector<ShotGeom>& geoms, const std::vector<Layout>&
             main_f.emplace_back();
             main_a.emplace_back();
             bands(l.ny, band_rows, [&](int y0, int y1) { interior(main_f.back(), main_a.back(), y0, y1); });
+            if (fband > 0) {
+                if (two_step_ok(l)) {
+                    // model rows but the last R in two-step tiles of 120 columns; the last R rows
+                    // as single-step tiles
+                    const int R = l.acc, nr = l.ny - R;
+                    fus_f.emplace_back();
+                    fus_a.emplace_back();
+                    edge_f.emplace_back();
+                    edge_a.emplace_back();
+                    bands(nr, fband, [&](int y0, int y1) {
+                        std::vector<WorkItem> vf, va, ef, ea;
+                        for (int x0 = xa & ~3; x0 < xb; x0 += 120) {
+                            // core: the wavefield cells it reads, rows [y0-2R-1, y1+2R] and columns
+                            // [x0-8, x0+128), are two-step cells or the top pad
+                            const bool core = x0 - 8 >= xa && x0 + 128 <= xb && l.dn + y1 + 2 * R < l.dn + nr;
+                            append_two_step(out, core ? vf : ef, out.src_fwd, cells_f, recs, (int)s, x0, l.dn + y0,
+                                            l.dn + y1, R, true, xa, xb);
+                            append_two_step(out, core ? va : ea, out.src_adj, cells_a, recs, (int)s, x0, l.dn + y0,
+                                            l.dn + y1, R, false, xa, xb);
+                        }
+                        fus_f.back().push_back(vf);
+                        fus_a.back().push_back(va);
+                        edge_f.back().push_back(ef);
+                        edge_a.back().push_back(ea);
+                    });
+                    for (int t = xa / TILE; t <= (xb - 1) / TILE; ++t) {
+                        const int c0 = std::max(t * TILE, xa), c1 = std::min((t + 1) * TILE, xb);
+                        append_item(out, out.lft_fwd, out.src_fwd, cells_f, recs, (int)s, t, l.dn + nr, l.dn + l.ny,
+                                    0, true, c0, c1);
+                        append_item(out, out.lft_adj, out.src_adj, cells_a, recs, (int)s, t, l.dn + nr, l.dn + l.ny,
+                                    0, false, c0, c1);
+                    }
+                } else {
+                    for (auto& b : main_f.back()) out.lft_fwd.insert(out.lft_fwd.end(), b.begin(), b.end());
+                    for (auto& b : main_a.back()) out.lft_adj.insert(out.lft_adj.end(), b.begin(), b.end());
+                }
+            }
             bands(l.dn, BOTTOM_BAND, [&](int j0, int j1) {
                 for (int t = xa / TILE; t <= (xb - 1) / TILE; ++t) {
                     const int c0 = std::max(t * TILE, xa), c1 = std::min((t + 1) * TILE, xb);
@@ -413,6 +503,11 @@ Lists build_lists(const std::vector<ShotGeom>& geoms, const std::vector<Layout>&
     };
     flatten(main_f, out.int_fwd);
     flatten(main_a, out.int_adj);
+    flatten(fus_f, out.fus_fwd);
+    flatten(fus_a, out.fus_adj);
+    out.ncore = (int)out.fus_fwd.size();
+    flatten(edge_f, out.fus_fwd);
+    flatten(edge_a, out.fus_adj);
     // boundary lists: the strip warps (the short bottom-row bands first), then the bottom tiles
     out.nstrip = (int)(sbot_f.size() + strip_f.size());
     for (auto* v : {&sbot_f, &strip_f, &bot_f}) out.bnd_fwd.insert(out.bnd_fwd.end(), v->begin(), v->end());
@@ -447,7 +542,7 @@ double step_bytes_shot(int ny, int nx, int dn) {
 // ---------------------------------------------------------------------------
 
 struct ShotState {
-    DBuf pa, pb, c2, phx, chx, phy, phy2, chy, snaps, sscale, k;
+    DBuf pa, pb, pc, pd, c2, phx, chx, phy, phy2, chy, snaps, sscale, k;  // pc, pd: second wavefield pair
     DBuf bst[7];   // second wavefield state (adjoint) when recomputing
     DBuf ckpt;     // forward-state checkpoints when recomputing
     Layout lay{};
@@ -458,7 +553,7 @@ struct ShotState {
         return a[i]->p;
     }
     size_t bytes() const {
-        size_t n = pa.n + pb.n + c2.n + phx.n + chx.n + phy.n + phy2.n + chy.n + snaps.n + sscale.n + k.n + ckpt.n;
+        size_t n = pa.n + pb.n + pc.n + pd.n + c2.n + phx.n + chx.n + phy.n + phy2.n + chy.n + snaps.n + sscale.n + k.n + ckpt.n;
         for (auto& b : bst) n += b.n;
         return n;
     }
@@ -474,6 +569,8 @@ struct ShotState {
         snap_bytes = (size_t)nsnap_blocks * l.ny * l.pitch * esz;
         TRY(pa.ensure(field_bytes));
         TRY(pb.ensure(field_bytes));
+        TRY(pc.ensure(field_bytes));
+        TRY(pd.ensure(field_bytes));
         TRY(c2.ensure(field_bytes));
         TRY(phx.ensure(field_bytes));
         TRY(chx.ensure(field_bytes));
@@ -488,6 +585,8 @@ struct ShotState {
     int zero_state(cudaStream_t st) {
         CK(cudaMemsetAsync(pa.p, 0, field_bytes, st));
         CK(cudaMemsetAsync(pb.p, 0, field_bytes, st));
+        CK(cudaMemsetAsync(pc.p, 0, field_bytes, st));
+        CK(cudaMemsetAsync(pd.p, 0, field_bytes, st));
         CK(cudaMemsetAsync(phx.p, 0, field_bytes, st));
         CK(cudaMemsetAsync(chx.p, 0, field_bytes, st));
         CK(cudaMemsetAsync(phy.p, 0, field_bytes, st));
@@ -497,8 +596,10 @@ struct ShotState {
     }
     ShotDev dev(int nt, int nrec, int x0, const float* srcv, float* rec) const {
         ShotDev d{};
-        d.pa = pa.as<float>();
-        d.pb = pb.as<float>();
+        d.pf[0] = pa.as<float>();
+        d.pf[1] = pb.as<float>();
+        d.pf[2] = pc.as<float>();
+        d.pf[3] = pd.as<float>();
         d.c2 = c2.as<float>();
         d.phx = phx.as<float>();
         d.chx = chx.as<float>();
@@ -553,6 +654,37 @@ struct StepSet {
     int kstrip = 1;
 };
 
+// Wavefield buffers of step k.  A shot's state (p, p_1) lives in pair 0
+// (pf[0], pf[1]) or pair 1 (pf[2], pf[3]); within a pair, step k reads p from
+// the first buffer for odd k and from the second for even k, and writes p_3
+// over p_1 (the reference's two-array rotation of p and p_1).
+inline int cur_buf(int k, int pair) { return 2 * pair + ((k & 1) ? 0 : 1); }
+inline int prev_buf(int k, int pair) { return 2 * pair + ((k & 1) ? 1 : 0); }
+
+// Parameters of the single step k with the state in `pair` (sn: snapshot
+// block or -1).
+void set_step(StepSet& ps, int k, int sn, int pair = 0) {
+    for (StepParams* p : {&ps.pm, &ps.pb}) {
+        p->t = k - 2;
+        p->parity = k & 1;
+        p->snap = sn;
+        p->rp = cur_buf(k, pair);
+        p->rp1 = p->wo = p->wo2 = prev_buf(k, pair);
+    }
+}
+
+// Two-step passes.  Steps k and k+1 run as: the single-step lists `lo` (the
+// interior items outside the two-step tiles and the boundary list) for step
+// k, concurrently with the two-step tiles `pf` (steps k and k+1), then `lo`
+// for step k+1.  Inputs are read from the state pair X and both steps are
+// written to the other pair Y, so no warp overwrites a p_n or p_{n-1} that a
+// neighbour still reads; the state moves to pair Y (two_step_run).
+struct TwoStep {
+    StepParams pf;  // the first ncore items are core tiles
+    StepSet lo;
+    int ncore = 0;
+};
+
 int step_kernels(const StepSet& ps) {
     return (ps.pm.nitems > 0) + (ps.pb.nstrip > 0) + (ps.pb.nitems > ps.pb.nstrip);
 }
@@ -585,14 +717,142 @@ int step_fork_join(int acc, int mode, const StepSet& ps, cudaStream_t st, cudaSt
     return FWI_OK;
 }
 
+// npass consecutive two-step passes from step k, state in pair X.  Pass j
+// (steps k, k+1; inputs in pair X, outputs in pair Y) is
+//   C(j)  the core tiles (both steps), on st;
+//   E(j)  the edge tiles (both steps), on st2;
+//   A(j)  step k of the single-step lists: interior items and bottom tiles
+//         on st2 (A2), side strips on aux3 (A3);
+//   B(j)  step k+1 of the single-step lists (B2 on st2, B3 on aux3).
+// Core tiles read only two-step cells and the top pad; the cells next to the
+// single-step cells belong to edge tiles.  So
+//   C(j) waits for C(j-1) and E(j-1);  E(j) for C(j-1) and B(j-1);
+//   A(j) for B(j-1) and E(j-1);        B(j) for A(j) and E(j),
+// and the single-step chain A, B runs beside the core tiles.  Kernels in
+// flight together never write a cell another one reads: every kernel writes
+// only its own cells, the tiles write pair Y while the core tiles of the next
+// pass read it only where the finished tiles wrote, and the single-step
+// kernels read the pair they do not write only at their own cells.
+int two_step_run(int acc, int mode, const TwoStep& tw, int k, int npass, int X, cudaStream_t st, cudaStream_t st2) {
+    cudaStream_t st3 = L().aux3;
+    cudaEvent_t* ev = L().ev2;  // [set][C, E, A3, B2, B3]
+    auto C = [&](int p) { return ev[5 * p + 0]; };
+    auto E = [&](int p) { return ev[5 * p + 1]; };
+    auto A3 = [&](int p) { return ev[5 * p + 2]; };
+    auto B2 = [&](int p) { return ev[5 * p + 3]; };
+    auto B3 = [&](int p) { return ev[5 * p + 4]; };
+    // entry: everything so far is on st; set 1 stands for "pass -1"
+    CK(cudaEventRecord(C(1), st));
+    CK(cudaEventRecord(E(1), st));
+    CK(cudaStreamWaitEvent(st2, C(1), 0));
+    CK(cudaStreamWaitEvent(st3, C(1), 0));
+    CK(cudaEventRecord(B2(1), st2));
+    CK(cudaEventRecord(B3(1), st3));
+    StepParams fc = tw.pf, fe = tw.pf;
+    fc.nitems = tw.ncore;
+    fe.items = tw.pf.items + tw.ncore;
+    fe.nitems = tw.pf.nitems - tw.ncore;
+    int p = 0;
+    for (int j = 0; j < npass; ++j, k += 2, X ^= 1, p ^= 1) {
+        const int Y = X ^ 1, q = p ^ 1;
+        StepSet a = tw.lo, b = tw.lo;
+        for (StepParams* sp : {&a.pm, &a.pb, &fc, &fe}) {
+            sp->t = k - 2;
+            sp->parity = k & 1;
+            sp->snap = -1;
+            sp->rp = cur_buf(k, X);
+            sp->rp1 = prev_buf(k, X);
+            sp->wo = sp->wo2 = prev_buf(k, Y);
+        }
+        fc.wo2 = fe.wo2 = prev_buf(k + 1, Y);
+        for (StepParams* sp : {&b.pm, &b.pb}) {
+            sp->t = k - 1;
+            sp->parity = (k + 1) & 1;
+            sp->snap = -1;
+            sp->rp = cur_buf(k + 1, Y);  // step k's output
+            sp->rp1 = cur_buf(k, X);     // p_n
+            sp->wo = sp->wo2 = prev_buf(k + 1, Y);
+        }
+        StepSet a2 = a, a3 = a, b2 = b, b3 = b;  // the st2 part (no strips) and the strip part
+        a2.pb.nstrip = b2.pb.nstrip = 0;
+        a2.pb.items = a.pb.items + a.pb.nstrip;
+        a2.pb.nitems = a.pb.nitems - a.pb.nstrip;
+        b2.pb.items = a2.pb.items;
+        b2.pb.nitems = a2.pb.nitems;
+        a3.pm.nitems = b3.pm.nitems = 0;
+        a3.pb.nitems = b3.pb.nitems = a.pb.nstrip;
+        L().launches += 2 * step_kernels(a) + (fc.nitems > 0) + (fe.nitems > 0);
+        // C(j)
+        CK(cudaStreamWaitEvent(st, E(q), 0));
+        CK(launch_step2(acc, mode, fc, st));
+        CK(cudaEventRecord(C(p), st));
+        // A3(j)
+        CK(cudaStreamWaitEvent(st3, B2(q), 0));
+        CK(launch_step(acc, mode, a3.kstrip, a3.pm, a3.pb, st3, st3, st3));
+        CK(cudaEventRecord(A3(p), st3));
+        // A2(j), then E(j)
+        CK(cudaStreamWaitEvent(st2, B3(q), 0));
+        CK(launch_step(acc, mode, a2.kstrip, a2.pm, a2.pb, st2, st2, st2));
+        CK(cudaStreamWaitEvent(st2, C(q), 0));
+        CK(launch_step2(acc, mode, fe, st2));
+        CK(cudaEventRecord(E(p), st2));
+        // B3(j) after A2(j) and E(j); B2(j) after A3(j)
+        CK(cudaStreamWaitEvent(st3, E(p), 0));
+        CK(launch_step(acc, mode, b3.kstrip, b3.pm, b3.pb, st3, st3, st3));
+        CK(cudaEventRecord(B3(p), st3));
+        CK(cudaStreamWaitEvent(st2, A3(p), 0));
+        CK(launch_step(acc, mode, b2.kstrip, b2.pm, b2.pb, st2, st2, st2));
+        CK(cudaEventRecord(B2(p), st2));
+    }
+    // exit: everything joins st
+    CK(cudaStreamWaitEvent(st, B2(p ^ 1), 0));
+    CK(cudaStreamWaitEvent(st, B3(p ^ 1), 0));
+    return FWI_OK;
+}
+
+// Which steps of k0..k1 start a two-step pass: pairs (k, k+1) with no
+// event step in them, an even number of them, so that the state ends in
+// the pair it started in.
+std::vector<char> two_step_plan(int k0, int k1, const std::vector<int>& events) {
+    std::vector<char> ev(k1 + 2, 0), start(k1 + 2, 0);
+    for (int e : events)
+        if (e >= k0 && e <= k1) ev[e] = 1;
+    int n = 0, last = -1;
+    for (int k = k0; k + 1 <= k1;) {
+        if (!ev[k] && !ev[k + 1]) {
+            start[k] = 1;
+            ++n;
+            last = k;
+            k += 2;
+        } else {
+            ++k;
+        }
+    }
+    if (n & 1) start[last] = 0;
+    return start;
+}
+
 // One pass over the time loop k = 2..nt for a set of shots.
 // mode 0: forward (snapshots if store, receivers recorded); mode 1: adjoint.
+// tw: two-step passes for the pairs of steps between snapshot events (null:
+// single steps only).
 int run_time_loop(int acc, int mode, int nt, int store_snap, int nt_store, bool store, StepSet ps, cudaStream_t st,
-                  cudaStream_t st2) {
+                  cudaStream_t st2, const TwoStep* tw = nullptr) {
     std::vector<int> ev = snapshot_steps(nt, store_snap);
+    std::vector<char> plan;
+    if (tw) plan = two_step_plan(2, nt, ev);
     size_t evi = 0;
     int snap = (mode == 0) ? 0 : nt_store;
+    int pair = 0;
     for (int k = 2; k <= nt; ++k) {
+        if (tw && plan[k]) {
+            int n = 0;
+            while (k + 2 * n <= nt && plan[k + 2 * n]) ++n;
+            TRY(two_step_run(acc, mode, *tw, k, n, pair, st, st2));
+            pair ^= n & 1;
+            k += 2 * n - 1;
+            continue;
+        }
         int sn = -1;
         if (evi < ev.size() && ev[evi] == k) {
             ++evi;
@@ -604,9 +864,7 @@ int run_time_loop(int acc, int mode, int nt, int store_snap, int nt_store, bool 
                 sn = snap;
             }
         }
-        ps.pm.t = ps.pb.t = k - 2;
-        ps.pm.parity = ps.pb.parity = k & 1;
-        ps.pm.snap = ps.pb.snap = sn;
+        set_step(ps, k, sn, pair);
         TRY(step_fork_join(acc, mode, ps, st, st2));
     }
     return FWI_OK;
@@ -680,6 +938,8 @@ int fwi_init(int device) {
     if (!L().ev_fork) CK(cudaEventCreateWithFlags(&L().ev_fork, cudaEventDisableTiming));
     if (!L().ev_join) CK(cudaEventCreateWithFlags(&L().ev_join, cudaEventDisableTiming));
     if (!L().ev_join2) CK(cudaEventCreateWithFlags(&L().ev_join2, cudaEventDisableTiming));
+    for (auto& e : L().ev2)
+        if (!e) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
     CK(configure_step_kernels());
     L().device = device;
     L().init = true;
@@ -699,6 +959,10 @@ int fwi_finalize(void) {
     if (L().ev_fork) cudaEventDestroy(L().ev_fork);
     if (L().ev_join) cudaEventDestroy(L().ev_join);
     if (L().ev_join2) cudaEventDestroy(L().ev_join2);
+    for (auto& e : L().ev2) {
+        if (e) cudaEventDestroy(e);
+        e = nullptr;
+    }
     L().own = L().aux = L().aux3 = nullptr;
     L().ev_fork = L().ev_join = L().ev_join2 = nullptr;
     L().user = nullptr;
@@ -990,7 +1254,9 @@ struct fwi_survey {
     // per-wave lists
     struct WaveDev {
         DBuf items_if, items_ia, items_bf, items_ba, src_f, src_a, recs, shots_f, shots_a, stack;
+        DBuf items_ff, items_fa, items_lf, items_la;  // two-step tiles; single-step interior items beside them
         int n_if = 0, n_ia = 0, n_bf = 0, n_ba = 0, n_strip = 0, kstrip = 1;
+        int n_ff = 0, n_fa = 0, n_lf = 0, n_la = 0, n_core = 0;
         cudaGraphExec_t graph[3] = {nullptr, nullptr, nullptr};
         long long graph_kernels[3] = {0, 0, 0};  // kernel nodes per graph
         DBuf save_jobs, restore_jobs;  // checkpoint copies: [ckpt][shot][field]
@@ -1016,7 +1282,7 @@ size_t shot_wave_bytes(const Layout& l, int nt_store, int snap_form, int grad_fo
     const size_t esz = snap_form == FWI_SNAP_F32 ? 4 : 2;
     const size_t sb = (size_t)(nt_store + 1) * l.ny * l.pitch * esz + (size_t)(nt_store + 1) * l.ny * (l.ntiles + 2) * 4;
     const size_t kb = (size_t)l.ny * l.pitch * (grad_form == FWI_GRAD_F64 ? 8 : 4);
-    return 8 * fb + sb + kb;
+    return 10 * fb + sb + kb;
 }
 
 // Shot packing: shots sorted by window width (widest first, stable) and cut
@@ -1073,12 +1339,21 @@ int survey_prepare_waves(fwi_survey* s) {
             g.push_back(s->geoms[sh]);
             l.push_back(s->lays[sh]);
         }
-        Lists lists = build_lists(g, l, s->band);
+        Lists lists = build_lists(g, l, s->band, (D.flags & FWI_SURVEY_SINGLE_STEP) ? 0 : TWO_STEP_BAND);
         std::unique_ptr<fwi_survey::WaveDev> wd(new fwi_survey::WaveDev());
         TRY(upload(wd->items_if, lists.int_fwd, st));
         TRY(upload(wd->items_ia, lists.int_adj, st));
         TRY(upload(wd->items_bf, lists.bnd_fwd, st));
         TRY(upload(wd->items_ba, lists.bnd_adj, st));
+        TRY(upload(wd->items_ff, lists.fus_fwd, st));
+        TRY(upload(wd->items_fa, lists.fus_adj, st));
+        TRY(upload(wd->items_lf, lists.lft_fwd, st));
+        TRY(upload(wd->items_la, lists.lft_adj, st));
+        wd->n_ff = (int)lists.fus_fwd.size();
+        wd->n_fa = (int)lists.fus_adj.size();
+        wd->n_lf = (int)lists.lft_fwd.size();
+        wd->n_la = (int)lists.lft_adj.size();
+        wd->n_core = lists.ncore;
         TRY(upload(wd->src_f, lists.src_fwd, st));
         TRY(upload(wd->src_a, lists.src_adj, st));
         TRY(upload(wd->recs, lists.recs, st));
@@ -1111,8 +1386,9 @@ int survey_prepare_waves(fwi_survey* s) {
             f.push_back(dv);
             dv.srcv = s->d_adj.as<float>() + (size_t)s->tr_off[sh] * D.nt;
             if (s->rc_C) {  // the adjoint runs on the second state while the forward is recomputed
-                dv.pa = ss.bst[0].as<float>();
-                dv.pb = ss.bst[1].as<float>();
+                dv.pf[0] = ss.bst[0].as<float>();
+                dv.pf[1] = ss.bst[1].as<float>();
+                dv.pf[2] = dv.pf[3] = nullptr;  // the adjoint of a recomputing survey runs single steps
                 dv.phx = ss.bst[2].as<float>();
                 dv.chx = ss.bst[3].as<float>();
                 dv.phy = ss.bst[4].as<float>();
@@ -1244,9 +1520,7 @@ int rc_steps(fwi_survey* s, int k0, int k1, int keep_seg, bool save_ckpt, size_t
             if (s->blk_seg[b] == keep_seg) sn = s->blk_slot[b];
             ++evi;
         }
-        ps.pm.t = ps.pb.t = k - 2;
-        ps.pm.parity = ps.pb.parity = k & 1;
-        ps.pm.snap = ps.pb.snap = sn;
+        set_step(ps, k, sn);
         TRY(step_fork_join(D.acc, 0, ps, st, st2));
         if (save_ckpt && k % s->rc_C == 0 && k / s->rc_C <= s->rc_J - 1) {
             const int c = k / s->rc_C - 1;
@@ -1318,12 +1592,24 @@ int rc_adjoint(fwi_survey* s, size_t wi, StepSet ps, cudaStream_t st, cudaStream
             }
             sn = snap == 0 ? 0 : s->blk_slot[snap];
         }
-        ps.pm.t = ps.pb.t = k - 2;
-        ps.pm.parity = ps.pb.parity = k & 1;
-        ps.pm.snap = ps.pb.snap = sn;
+        set_step(ps, k, sn);
         TRY(step_fork_join(D.acc, 1, ps, st, st2));
     }
     return FWI_OK;
+}
+
+// Two-step lists of a wave from its single-step set: the two-step tiles,
+// and the single-step interior items outside them beside the boundary list.
+TwoStep two_step_set(const StepSet& ps, const DBuf& fus, int nfus, int ncore, const DBuf& lft, int nlft) {
+    TwoStep tw;
+    tw.ncore = ncore;
+    tw.pf = ps.pm;
+    tw.pf.items = fus.as<WorkItem>();
+    tw.pf.nitems = nfus;
+    tw.lo = ps;
+    tw.lo.pm.items = lft.as<WorkItem>();
+    tw.lo.pm.nitems = nlft;
+    return tw;
 }
 
 // Issue one wave's work: forward (+ misfit) and, for step 1, adjoint + stack.
@@ -1338,6 +1624,8 @@ int issue_wave(fwi_survey* s, size_t wi, int step, cudaStream_t st, cudaStream_t
         // the slot may be larger than this shot: zero the whole allocation
         CK(cudaMemsetAsync(ss.pa.p, 0, ss.pa.n, st));
         CK(cudaMemsetAsync(ss.pb.p, 0, ss.pb.n, st));
+        CK(cudaMemsetAsync(ss.pc.p, 0, ss.pc.n, st));
+        CK(cudaMemsetAsync(ss.pd.p, 0, ss.pd.n, st));
         CK(cudaMemsetAsync(ss.phx.p, 0, ss.phx.n, st));
         CK(cudaMemsetAsync(ss.chx.p, 0, ss.chx.n, st));
         CK(cudaMemsetAsync(ss.phy.p, 0, ss.phy.n, st));
@@ -1373,7 +1661,9 @@ int issue_wave(fwi_survey* s, size_t wi, int step, cudaStream_t st, cudaStream_t
     if (s->rc_C) {
         TRY(rc_forward(s, wi, step, ps, st, st2));
     } else {
-        TRY(run_time_loop(D.acc, 0, D.nt, D.store_snap, s->nt_store, step == 1, ps, st, st2));
+        TwoStep tw = two_step_set(ps, wd.items_ff, wd.n_ff, wd.n_core, wd.items_lf, wd.n_lf);
+        TRY(run_time_loop(D.acc, 0, D.nt, D.store_snap, s->nt_store, step == 1, ps, st, st2,
+                          wd.n_ff ? &tw : nullptr));
     }
     for (size_t k = 0; k < w.size(); ++k) {
         const int sh = w[k];
@@ -1412,7 +1702,8 @@ int issue_wave(fwi_survey* s, size_t wi, int step, cudaStream_t st, cudaStream_t
     ps.pb.nitems = wd.n_ba;
     ps.pb.nstrip = wd.n_strip;
     ps.kstrip = wd.kstrip;
-    TRY(run_time_loop(D.acc, 1, D.nt, D.store_snap, s->nt_store, true, ps, st, st2));
+    TwoStep tw = two_step_set(ps, wd.items_fa, wd.n_fa, wd.n_core, wd.items_la, wd.n_la);
+    TRY(run_time_loop(D.acc, 1, D.nt, D.store_snap, s->nt_store, true, ps, st, st2, wd.n_fa ? &tw : nullptr));
     LK(launch_stack(s->d_G.as<double>(), D.ny, D.nx_model, wd.stack.p, (int)w.size(), D.grad_form, st));
     return FWI_OK;
 }
@@ -1789,10 +2080,20 @@ int time_wave0_steps(fwi_survey* s, int steps, float* ms) {
         CK(cudaEventCreate(&e1));
         CK(cudaEventRecord(e0, stream()));
     }
-    for (int i = 0; i < steps; ++i) {
+    // pairs of steps as two-step passes when the wave has two-step tiles
+    // (an even number of them, so that the state stays in pair 0)
+    const TwoStep tw = two_step_set(ps, wd.items_ff, wd.n_ff, wd.n_core, wd.items_lf, wd.n_lf);
+    const int npass = (wd.n_ff && D.nt >= 3) ? (steps / 4) * 2 : 0;
+    // (in runs that stay inside the time axis: steps 2..nt)
+    for (int done = 0, pair = 0; done < npass;) {
+        const int n = std::min(npass - done, (D.nt - 1) / 2);
+        TRY(two_step_run(D.acc, 0, tw, 2, n, pair, stream(), L().aux));
+        pair ^= n & 1;
+        done += n;
+    }
+    for (int i = 2 * npass; i < steps; ++i) {
         const int k = 2 + (i % (D.nt - 1));
-        ps.pm.t = ps.pb.t = k - 2;
-        ps.pm.parity = ps.pb.parity = k & 1;
+        set_step(ps, k, -1);
         TRY(step_fork_join(D.acc, 0, ps, stream(), L().aux));
     }
     if (ms) {
@@ -1961,8 +2262,8 @@ extern "C" int fwi_solver_forward_noalloc(int NumSou, int NumRec, const int* nxS
     if (NumRec > 0) CK(cudaMemsetAsync(Rec_point_dev, 0, (size_t)nt * NumRec * sizeof(float), st));
 
     ShotDev sd{};
-    sd.pa = fld[0];
-    sd.pb = fld[1];
+    sd.pf[0] = fld[0];
+    sd.pf[1] = fld[1];
     sd.c2 = fld[2];
     sd.phx = fld[3];
     sd.chx = fld[4];

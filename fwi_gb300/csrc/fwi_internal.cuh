@@ -36,18 +36,20 @@ struct RecEnt {                 // one recorded receiver
 
 struct WorkItem {               // one warp's work in a step launch
     int shot;
-    int tile;                   // tile index (x0 = tile*TILE physical); side strip: 0 left, 1 right
+    int tile;                   // tile index (x0 = tile*TILE physical); side strip: 0 left, 1 right;
+                                // two-step tile: its first physical column
     int y0, y1;                 // padded rows [y0, y1)
     int kind;                   // 0 = interior model rows, 1 = bottom pad rows (interior columns),
-                                // 2 = side strip, model rows; 3 = side strip, bottom pad rows
+                                // 2 = side strip, model rows; 3 = side strip, bottom pad rows;
+                                // 4 = two-step interior tile
     int s0, s1;                 // SrcEnt range (sorted by row)
     int r0, r1;                 // RecEnt range (sorted by row)
     int pad_;
 };
 
 struct ShotDev {
-    float* pa;                  // wavefield ping-pong buffers
-    float* pb;
+    float* pf[4];               // wavefield buffers: pair 0 (pf[0], pf[1]) and pair 1 (pf[2], pf[3]);
+                                // StepParams::rp/rp1/wo/wo2 select them per launch
     const float* c2;            // c^2 dt^2 / d^2
     float* phx;                 // x-direction CPML phi (side strips and corners)
     float* chx;                 // x-direction chi
@@ -80,7 +82,9 @@ struct StepParams {
     int nstrip;                 // boundary list: the first nstrip items are side strips (kinds 2, 3),
                                 // the bottom tiles follow
     int t;                      // k-2: source column / receiver row this step
-    int parity;                 // k & 1: which buffer holds p_1 (written as p_3)
+    int parity;                 // k & 1: which y-phi buffer is current
+    int rp, rp1, wo;            // wavefield buffers (ShotDev::pf): p, p_1 read; p_3 written (wo may be rp1)
+    int wo2;                    // two-step tiles: buffer of the second step's p_3
     int snap;                   // snapshot block this step, -1 if none
     int snap_form;              // FWI_SNAP_*
     int grad_form;              // FWI_GRAD_*

@@ -224,8 +224,9 @@ __device__ __forceinline__ void bottom_rows(const StepParams& P, const WorkItem&
     const ShotDev& S = P.shots[it.shot];
     const int pitch = S.pitch, dn = S.dn, nyt = S.nyt;
     const int x0 = it.tile * TILE, xl = x0 + 4 * lane;
-    const float* PC = P.parity ? S.pa : S.pb;
-    float* P1 = P.parity ? S.pb : S.pa;
+    const float* PC = S.pf[P.rp];
+    const float* P1 = S.pf[P.rp1];
+    float* PO = S.pf[P.wo];
     const float* PHO = P.parity ? S.phy2 : S.phy;  // old y-phi
     float* PHN = P.parity ? S.phy : S.phy2;        // new y-phi
     const int yb0 = nyt - dn;
@@ -378,14 +379,14 @@ __device__ __forceinline__ void bottom_rows(const StepParams& P, const WorkItem&
         if (full) {
             st4(PHN + ro, from_arr(phy));
             st4(S.chy + ro, from_arr(chy));
-            st4(P1 + ro, from_arr(p3));
+            st4(PO + ro, from_arr(p3));
         } else {
 #pragma unroll
             for (int e = 0; e < 4; ++e)
                 if (e >= lo && e < hi) {
                     PHN[ro + e] = phy[e];
                     S.chy[ro + e] = chy[e];
-                    P1[ro + e] = p3[e];
+                    PO[ro + e] = p3[e];
                 }
         }
         if (MODE == 0 && P.record) record_row(P, S, y, xl, ri, it.r1, rrow, p3);
@@ -401,8 +402,13 @@ __device__ __forceinline__ void bottom_rows(const StepParams& P, const WorkItem&
 
 template <int R>
 __device__ __forceinline__ void interior_update2(const float4* q, float4 L, float4 Rt, float4 pm1, float4 cc,
-                                                 const float* sv, const float2* cp, float* p3) {
-    const float4 C = q[R];
+                                                 const float* sv, const float2* cp, float* p3);
+
+// The same update with the 2R+1 rows given by an accessor: q(i) is row y-R+i.
+template <int R, typename QF>
+__device__ __forceinline__ void interior_update2f(QF q, float4 L, float4 Rt, float4 pm1, float4 cc, const float* sv,
+                                                  const float2* cp, float* p3) {
+    const float4 C = q(R);
     const float w[12] = {L.x, L.y, L.z, L.w, C.x, C.y, C.z, C.w, Rt.x, Rt.y, Rt.z, Rt.w};
 #pragma unroll
     for (int k = 0; k < 2; ++k) {
@@ -416,7 +422,7 @@ __device__ __forceinline__ void interior_update2(const float4* q, float4 L, floa
         // space_deriv2y: s = s + (p(j+i) + p(j-i))*coef(i)
         float2 ay = make_float2(0.f, 0.f);
 #pragma unroll
-        for (int i = 0; i <= R; ++i) ay = __fadd2_rn(ay, mul0(__fadd2_rn(pr(q[R + i], k), pr(q[R - i], k)), cp[i]));
+        for (int i = 0; i <= R; ++i) ay = __fadd2_rn(ay, mul0(__fadd2_rn(pr(q(R + i), k), pr(q(R - i), k)), cp[i]));
         // p_3 = -p_1 + 2p + (d2x + d2y + source)*c2
         const float2 pc = pr(C, k), pm = pr(pm1, k);
         const float2 t = __fadd2_rn(make_float2(-pm.x, -pm.y), __fadd2_rn(pc, pc));
@@ -425,6 +431,12 @@ __device__ __forceinline__ void interior_update2(const float4* q, float4 L, floa
         p3[2 * k] = r.x;
         p3[2 * k + 1] = r.y;
     }
+}
+
+template <int R>
+__device__ __forceinline__ void interior_update2(const float4* q, float4 L, float4 Rt, float4 pm1, float4 cc,
+                                                 const float* sv, const float2* cp, float* p3) {
+    interior_update2f<R>([&](int i) { return q[i]; }, L, Rt, pm1, cc, sv, cp, p3);
 }
 
 // Model rows, interior columns [sl, sr): no CPML and no clamp, so only
@@ -460,8 +472,9 @@ __global__ void __launch_bounds__(128, (MODE == 1 && SNAP) ? 3 : 5) k_step_inter
     const ShotDev& S = P.shots[it.shot];
     const int pitch = S.pitch;
     const int x0 = it.tile * TILE, xl = x0 + 4 * lane;
-    const float* PC = (P.parity ? S.pa : S.pb) + xl;  // p at this lane's columns
-    float* P1 = (P.parity ? S.pb : S.pa) + xl;        // p_1, overwritten with p_3
+    const float* PC = S.pf[P.rp] + xl;   // p at this lane's columns
+    const float* P1 = S.pf[P.rp1] + xl;  // p_1
+    float* PO = S.pf[P.wo] + xl;         // p_3 (may be the p_1 buffer: each cell reads only its own p_1)
     const float* C2 = S.c2 + xl;
     // lanes 0 and 31 fetch the halo float4 left and right of the tile (in the
     // first and last tile of a row these are the ends of the neighbouring
@@ -601,11 +614,11 @@ __global__ void __launch_bounds__(128, (MODE == 1 && SNAP) ? 3 : 5) k_step_inter
             }
         }
         if (full) {
-            st4(P1 + (size_t)y * pitch, from_arr(p3));
+            st4(PO + (size_t)y * pitch, from_arr(p3));
         } else {
 #pragma unroll
             for (int e = 0; e < 4; ++e)
-                if (e >= lo && e < hi) P1[(size_t)y * pitch + e] = p3[e];
+                if (e >= lo && e < hi) PO[(size_t)y * pitch + e] = p3[e];
         }
         if (MODE == 0 && P.record) record_row(P, S, y, xl, ri, it.r1, rrow, p3);
 
@@ -665,8 +678,9 @@ __device__ __forceinline__ void strip_rows(const StepParams& P, const WorkItem& 
     const int pitch = S.pitch, dn = S.dn, nx = S.nx, nxt = S.nxt, nyt = S.nyt;
     const bool right = it.tile != 0;
     const int cs = right ? S.sr : 0, ce = right ? nxt : S.sl;  // logical strip columns [cs, ce)
-    const float* PC = P.parity ? S.pa : S.pb;  // p
-    float* P1 = P.parity ? S.pb : S.pa;        // p_1, overwritten with p_3
+    const float* PC = S.pf[P.rp];   // p
+    const float* P1 = S.pf[P.rp1];  // p_1
+    float* PO = S.pf[P.wo];         // p_3
     const float* PHO = P.parity ? S.phy2 : S.phy;  // old y-phi (bottom rows)
     float* PHN = P.parity ? S.phy : S.phy2;        // new y-phi
     const int yb0 = nyt - dn;
@@ -998,7 +1012,7 @@ __device__ __forceinline__ void strip_rows(const StepParams& P, const WorkItem& 
         }
 #pragma unroll
         for (int k = 0; k < K; ++k)
-            if (act[k]) P1[ro + 32 * k] = p3[k];
+            if (act[k]) PO[ro + 32 * k] = p3[k];
         // receivers: every receiver in this cell gets p_3 (:553)
         if (MODE == 0 && P.record) {
             while (rrow == y) {
@@ -1032,6 +1046,207 @@ __global__ void __launch_bounds__(128) k_step_strip(const __grid_constant__ Step
     const WorkItem it = P.items[wid];
     if (it.kind == 3) strip_rows<R, MODE, K, true>(P, it, sw, lane);
     else strip_rows<R, MODE, K, false>(P, it, sw, lane);
+}
+
+// ---------------------------------------------------------------------------
+// Two time steps of the model-row interior in one pass (temporal blocking).
+//
+// A two-step tile owns the output columns [x0, x0 + F2_W) of rows [y0, y1).
+// Lane l holds the four columns x0 - 4 + 4l, so the warp spans [x0 - 4,
+// x0 + 124): the first step (p_{n+1}) is computed on all 128 columns, the
+// second (p_{n+2}) on the 120 columns of lanes 1..30, whose x-neighbours
+// (R <= 4 columns) are all on the warp.  The first step runs over rows
+// [y0 - R, y1 + R) (rows above the model rows are the free-surface pad:
+// zero), the second R rows behind it.  p_n comes through a register queue of
+// 2R+1 rows, p_{n+1} through a second one; p_{n-1}, c2 and the halo float4s
+// of p_n through a cp.async ring whose slots are kept R rows longer, for the
+// second step's c2.  Both results go to buffers other than the inputs (the
+// warp reads its neighbours' p_n and p_{n-1}), and the cells a warp computes
+// outside its own columns and rows are bit-identical to their owners' (same
+// arithmetic, same source injection; the host only makes tiles whose halo
+// cells are plain interior cells).
+// ---------------------------------------------------------------------------
+constexpr int F2_W = 120;
+// ring slot of row y: p_n row y+R with its halo float4s [HL | 32 lanes | HR],
+// p_{n-1} row y, c2 row y
+constexpr int F2_HL = 0, F2_P = 1, F2_HR = 33, F2_P1 = 34, F2_C2 = 66, F2_SIZE = 98;
+constexpr int F2_DEPTH = 4;  // rows in flight
+constexpr int F2_LINE = 34;  // p_{n+1} line: [garbage | 32 lanes | garbage]
+template <int R>
+struct F2Ring {
+    static constexpr int SLOTS = F2_DEPTH + R + 1;
+    static constexpr int Q1 = R + 2;  // p_{n+1} lines: rows y-R-1 .. y
+    static constexpr int WARP = SLOTS * F2_SIZE + Q1 * F2_LINE;  // float4 per warp
+    static constexpr int SMEM = 4 * WARP * 16;
+};
+
+// Injected values of row y for this lane's four columns (entries sorted by
+// row, the cursor at the first entry of row y or below; sv starts at zero).
+__device__ __forceinline__ void gather_sources(const StepParams& P, const ShotDev& S, int y, int xl, int t, int& si,
+                                               int s1, int& srow, float* sv) {
+    while (srow == y) {
+        const SrcEnt e = P.srcs[si];
+        if ((e.col >> 2) == (xl >> 2)) {
+            const float val = __ldg(S.srcv + (size_t)e.vidx * S.nt + t);
+            const int el = e.col & 3;
+            sv[0] = el == 0 ? val : sv[0];
+            sv[1] = el == 1 ? val : sv[1];
+            sv[2] = el == 2 ? val : sv[2];
+            sv[3] = el == 3 ? val : sv[3];
+        }
+        ++si;
+        srow = (si < s1) ? P.srcs[si].row : INT_MAX;
+    }
+}
+
+__device__ __forceinline__ void record_row_t(const StepParams& P, const ShotDev& S, int y, int xl, int t, int& ri,
+                                             int r1, int& rrow, const float* p3) {
+    while (rrow == y) {
+        const RecEnt r = P.recs[ri];
+        if ((r.col >> 2) == (xl >> 2)) S.rec[(size_t)r.ridx * S.nt + t] = sel(p3, r.col & 3);
+        ++ri;
+        rrow = (ri < r1) ? P.recs[ri].row : INT_MAX;
+    }
+}
+
+template <int R, int MODE>
+__global__ void __launch_bounds__(128, 3) k_step2_interior(const __grid_constant__ StepParams P) {
+    using RG = F2Ring<R>;
+    extern __shared__ float4 smem[];
+    const int lane = threadIdx.x & 31;
+    const int wid = blockIdx.x * 4 + (threadIdx.x >> 5);
+    if (wid >= P.nitems) return;
+    float4* ring = smem + (threadIdx.x >> 5) * RG::WARP;
+    float4* q1l = ring + RG::SLOTS * F2_SIZE;  // p_{n+1} lines
+    const WorkItem it = P.items[wid];
+    const ShotDev& S = P.shots[it.shot];
+    const int pitch = S.pitch, dn = S.dn;
+    const int x0 = it.tile, xl = x0 - 4 + 4 * lane;
+    const float* PN = S.pf[P.rp] + xl;    // p_n
+    const float* PM = S.pf[P.rp1] + xl;   // p_{n-1}
+    float* O1 = S.pf[P.wo] + xl;          // p_{n+1}
+    float* O2 = S.pf[P.wo2] + xl;         // p_{n+2}
+    const float* C2 = S.c2 + xl;
+    // lanes 0 and 31 also fetch the halo float4 beyond the warp's columns
+    const bool has_h = (lane == 0) || (lane == 31);
+    const int hslot = (lane == 0) ? F2_HL : F2_HR, hoff = (lane == 0) ? -4 : 4;
+    // lanes 1..30 store their elements [lo, hi): the interior columns [sl, sr)
+    const int lo = S.off + S.sl - xl, hi = S.off + S.sr - xl;
+    const bool mine = lane >= 1 && lane <= 30;
+    const bool full = mine && lo <= 0 && hi >= 4, part = mine && !full && lo < 4 && hi > 0;
+    // first step over rows [ya, yb) (one row past the R halo rows below, so
+    // that the second step, R+1 rows behind, ends at row y1 - 1)
+    const int y0 = it.y0, y1 = it.y1, ya = y0 - R, yb = y1 + R + 1;
+
+    auto issue = [&](int y, int slot) {
+        float4* st = ring + slot * F2_SIZE;
+        const size_t ro = (size_t)y * pitch;
+        cp16(st + F2_P + lane, PN + ro + (size_t)R * pitch);
+        if (has_h) cp16(st + hslot, PN + ro + (size_t)R * pitch + hoff);
+        cp16(st + F2_P1 + lane, PM + ro);
+        cp16(st + F2_C2 + lane, C2 + ro);
+    };
+    // the x-neighbours of row y's p_n sit in the slot of row y - R, which
+    // holds p_n row y (with its halos); for the first R rows these are slots
+    // SLOTS-R .. SLOTS-1 (rows ya-R .. ya-1), filled here
+    float4* pre = ring + (RG::SLOTS - R) * F2_SIZE;
+#pragma unroll
+    for (int i = 0; i < R; ++i) {
+        const size_t ro = (size_t)(ya + i) * pitch;
+        cp16(pre + i * F2_SIZE + F2_P + lane, PN + ro);
+        if (has_h) cp16(pre + i * F2_SIZE + hslot, PN + ro + hoff);
+    }
+    cp_commit();
+#pragma unroll
+    for (int i = 0; i < F2_DEPTH; ++i) {
+        issue(ya + i, i);
+        cp_commit();
+    }
+    // qn: p_n rows y-R-1 .. y+R; q1: p_{n+1} rows y-2R-1 .. y-1 (before row y's first step)
+    float4 qn[2 * R + 2], q1[2 * R + 1];
+#pragma unroll
+    for (int i = 0; i < 2 * R + 1; ++i) qn[i] = ldg4(PN + (size_t)(ya - R - 1 + i) * pitch);
+    const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+    for (int i = 0; i <= 2 * R; ++i) q1[i] = z4;
+
+    // source cursors: first step from the list start, second step from row y0
+    int si1 = it.s0, si2 = it.s0, ri1 = it.r0, ri2 = it.r0;
+    while (si2 < it.s1 && P.srcs[si2].row < y0) ++si2;
+    int srow1 = (si1 < it.s1) ? P.srcs[si1].row : INT_MAX, srow2 = (si2 < it.s1) ? P.srcs[si2].row : INT_MAX;
+    int rrow1 = (ri1 < it.r1) ? P.recs[ri1].row : INT_MAX, rrow2 = rrow1;
+    float2 cp[R + 1];
+#pragma unroll
+    for (int i = 0; i <= R; ++i) cp[i] = make_float2(P.c2[i], P.c2[i]);
+
+    // slot of row y, of row y - R (x-neighbours of p_n row y), of row y - R - 1 (c2 of the second step);
+    // p_{n+1} line of row y and of row y - R - 1
+    int slot = 0, slotx = RG::SLOTS - R, slot2 = RG::SLOTS - R - 1, l1 = 0, l2 = 1;
+    for (int y = ya; y < yb; ++y) {
+        // every lane has its own copies of row y (and of the pre slots); the
+        // warp synchronises before it reads the other lanes' copies and the
+        // p_{n+1} line written R+1 iterations ago
+        cp_wait<F2_DEPTH - 1>();
+        __syncwarp();
+        const float4* st = ring + slot * F2_SIZE;
+        const float4* sx = ring + slotx * F2_SIZE;
+        qn[2 * R + 1] = st[F2_P + lane];
+        // first step, row y: p_{n+1} = -p_{n-1} + 2p_n + (d2x + d2y + source)*c2
+        float np1[4] = {0.f, 0.f, 0.f, 0.f};
+        {
+            const float4 Lf = sx[F2_HL + lane], Rf = sx[F2_P + 1 + lane];
+            float sv[4] = {0.f, 0.f, 0.f, 0.f};
+            if (srow1 == y) gather_sources(P, S, y, xl, P.t, si1, it.s1, srow1, sv);
+            if (y >= dn) interior_update2<R>(qn + 1, Lf, Rf, st[F2_P1 + lane], st[F2_C2 + lane], sv, cp, np1);
+        }
+        q1l[l1 * F2_LINE + 1 + lane] = from_arr(np1);
+        // second step, row y - R - 1, from the p_{n+1} rows of earlier iterations
+        // (independent of this iteration's first step)
+        const int y2 = y - R - 1;
+        if (y2 >= y0) {
+            const float4* st2 = ring + slot2 * F2_SIZE;
+            const float4* ln = q1l + l2 * F2_LINE;
+            const float4 Lf = ln[lane], Rf = ln[lane + 2];
+            float sv[4] = {0.f, 0.f, 0.f, 0.f};
+            if (srow2 == y2) gather_sources(P, S, y2, xl, P.t + 1, si2, it.s1, srow2, sv);
+            float np2[4];
+            interior_update2<R>(q1, Lf, Rf, qn[0], st2[F2_C2 + lane], sv, cp, np2);
+            if (full) {
+                st4(O2 + (size_t)y2 * pitch, from_arr(np2));
+            } else if (part) {
+#pragma unroll
+                for (int e = 0; e < 4; ++e)
+                    if (e >= lo && e < hi) O2[(size_t)y2 * pitch + e] = np2[e];
+            }
+            if (MODE == 0 && P.record && rrow2 == y2) record_row_t(P, S, y2, xl, P.t + 1, ri2, it.r1, rrow2, np2);
+        }
+        if (y >= y0 && y < y1) {
+            if (full) {
+                st4(O1 + (size_t)y * pitch, from_arr(np1));
+            } else if (part) {
+#pragma unroll
+                for (int e = 0; e < 4; ++e)
+                    if (e >= lo && e < hi) O1[(size_t)y * pitch + e] = np1[e];
+            }
+            if (MODE == 0 && P.record && rrow1 == y) record_row_t(P, S, y, xl, P.t, ri1, it.r1, rrow1, np1);
+        }
+#pragma unroll
+        for (int i = 0; i < 2 * R + 1; ++i) qn[i] = qn[i + 1];
+#pragma unroll
+        for (int i = 0; i < 2 * R; ++i) q1[i] = q1[i + 1];
+        q1[2 * R] = from_arr(np1);
+        // the slot of row y - R - 1 is free now: it takes row y + DEPTH (the
+        // other lanes read it last in the previous iteration, before this
+        // iteration's sync)
+        if (y + F2_DEPTH < yb) issue(y + F2_DEPTH, slot2);
+        cp_commit();
+        slot = (slot + 1 == RG::SLOTS) ? 0 : slot + 1;
+        slotx = (slotx + 1 == RG::SLOTS) ? 0 : slotx + 1;
+        slot2 = (slot2 + 1 == RG::SLOTS) ? 0 : slot2 + 1;
+        l1 = (l1 + 1 == RG::Q1) ? 0 : l1 + 1;
+        l2 = (l2 + 1 == RG::Q1) ? 0 : l2 + 1;
+    }
+    cp_wait<0>();
 }
 
 // Bottom pad rows, interior columns: the boundary list after its nstrip
@@ -1069,6 +1284,7 @@ cudaError_t configure_variant() {
     if (e == cudaSuccess) e = kernel_smem(k_step_bottom<R, MODE>, BND_SMEM);
     if (e == cudaSuccess) e = kernel_smem(k_step_strip<R, MODE, 1>, strip_smem<R, 1>());
     if (e == cudaSuccess) e = kernel_smem(k_step_strip<R, MODE, 2>, strip_smem<R, 2>());
+    if (e == cudaSuccess) e = kernel_smem(k_step2_interior<R, MODE>, F2Ring<R>::SMEM);
     return e;
 }
 
@@ -1109,6 +1325,22 @@ cudaError_t launch_step(int acc, int mode, int kstrip, const StepParams& pm, con
     } else if (acc == 4) {
         if (mode == 0) launch_variant<4, 0>(kstrip, pm, pb, sm, sb, ss);
         else launch_variant<4, 1>(kstrip, pm, pb, sm, sb, ss);
+    } else {
+        return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+}
+
+// Two-step interior tiles (kind 4) of list pf on stream st.
+cudaError_t launch_step2(int acc, int mode, const StepParams& pf, cudaStream_t st) {
+    const int nb = (pf.nitems + 3) / 4;
+    if (!nb) return cudaSuccess;
+    if (acc == 3) {
+        if (mode == 0) k_step2_interior<3, 0><<<nb, 128, F2Ring<3>::SMEM, st>>>(pf);
+        else k_step2_interior<3, 1><<<nb, 128, F2Ring<3>::SMEM, st>>>(pf);
+    } else if (acc == 4) {
+        if (mode == 0) k_step2_interior<4, 0><<<nb, 128, F2Ring<4>::SMEM, st>>>(pf);
+        else k_step2_interior<4, 1><<<nb, 128, F2Ring<4>::SMEM, st>>>(pf);
     } else {
         return cudaErrorInvalidValue;
     }

@@ -200,6 +200,11 @@ typedef struct fwi_survey_desc {
  * pass, far less memory).  Chosen automatically when the HBM budget would
  * otherwise leave waves of fewer than 8 shots. */
 #define FWI_SURVEY_RECOMPUTE 2
+/* fwi_survey_desc.flags: advance every time step with the single-step
+ * kernels.  By default, pairs of steps with no snapshot or imaging in them
+ * run as two-step passes (the model-row interior advanced twice per sweep
+ * over the wavefields); the results are bit-identical either way. */
+#define FWI_SURVEY_SINGLE_STEP 4
 
 typedef struct fwi_survey fwi_survey;
 

@@ -379,15 +379,22 @@ def main():
     r1.record(stream)
     torch.cuda.synchronize()
     step_s = r0.elapsed_time(r1) / 1e3 / nsteps
-    bytes_step = sv.step_bytes()  # the shots of the first wave, which time_steps advances
+    # the shots of the first wave, which time_steps advances: single-step
+    # algorithmic bytes, and those of the two-step passes it runs
+    bytes_single = sv.step_bytes()
+    bytes_step, tile_bytes_pass = sv.two_step_bytes()
     wave, band = sv.tuning()
     rc_plan = sv.recompute_plan()
     achieved = bytes_step / step_s / 1e9
     tr = traffic_from_profile()
     roof = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
             "traffic": tr * wave if (tr and a.config in (2, 4)) else None,
-            "kernel": "k_step_interior + k_step_strip + k_step_bottom (one time step of all shots, three concurrent streams)",
+            "kernel": "one time step of all shots of a wave, run as two-step passes: k_step2_interior (model-row "
+                      "interior, two steps per sweep) beside k_step_strip + k_step_bottom + k_step_interior "
+                      "(single-step lists, twice per pass)",
             "algorithmic_bytes_per_launch": bytes_step, "avg_launch_ms": step_s * 1e3,
+            "single_step_bytes": bytes_single, "single_step_equivalent_GBps": bytes_single / step_s / 1e9,
+            "two_step_tile_bytes_per_pass": tile_bytes_pass,
             "peak_kind": f"{peak_kind} copy bandwidth (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured"
             else "fallback 6.8 TB/s"}
     sv.close()

@@ -302,6 +302,12 @@ class Survey:
         N.check(N.load().fwi_survey_step_bytes(self.handle, C.byref(b)))
         return b.value
 
+    def two_step_bytes(self):
+        """(algorithmic bytes per time step with two-step passes, two-step tiles' bytes per pass)."""
+        a, t = C.c_double(0), C.c_double(0)
+        N.check(N.load().fwi_survey_two_step_bytes(self.handle, C.byref(a), C.byref(t)))
+        return a.value, t.value
+
     def tuning(self):
         w, b = C.c_int(0), C.c_int(0)
         N.check(N.load().fwi_survey_tuning(self.handle, C.byref(w), C.byref(b)))

@@ -280,6 +280,7 @@ struct Lists {
     // no cell of the single-step lists) and the interior items outside them (kind 0)
     std::vector<WorkItem> fus_fwd, fus_adj, lft_fwd, lft_adj;
     int ncore = 0;
+    double fus_cells = 0.0;  // cells the two-step tiles store (per step)
     int nstrip = 0, kstrip = 1;
     std::vector<SrcEnt> src_fwd, src_adj;
     std::vector<RecEnt> recs;
@@ -372,7 +373,7 @@ bool two_step_ok(const Layout& l) {
     return l.sl < l.sr && l.sl - R >= l.dn && l.sr + R <= l.dn + l.nx && l.ny > R;
 }
 
-constexpr int TWO_STEP_BAND = 48;     // rows per two-step tile
+constexpr int TWO_STEP_BAND = 64;     // rows per two-step tile
 constexpr int BOTTOM_BAND = 9;        // rows per bottom-tile work item
 constexpr int STRIP_BAND = 16;        // rows per side-strip work item (model rows)
 constexpr int STRIP_BOTTOM_BAND = 5;  // rows per side-strip work item (bottom pad rows)
@@ -446,6 +447,7 @@ Lists build_lists(const std::vector<ShotGeom>& geoms, const std::vector<Layout>&
                             const bool core = x0 - 8 >= xa && x0 + 128 <= xb && l.dn + y1 + 2 * R < l.dn + nr;
                             append_two_step(out, core ? vf : ef, out.src_fwd, cells_f, recs, (int)s, x0, l.dn + y0,
                                             l.dn + y1, R, true, xa, xb);
+                            out.fus_cells += (double)(y1 - y0) * (std::min(x0 + 120, xb) - std::max(x0, xa));
                             append_two_step(out, core ? va : ea, out.src_adj, cells_a, recs, (int)s, x0, l.dn + y0,
                                             l.dn + y1, R, false, xa, xb);
                         }
@@ -543,7 +545,7 @@ double step_bytes_shot(int ny, int nx, int dn) {
 
 struct ShotState {
     DBuf pa, pb, pc, pd, c2, phx, chx, phy, phy2, chy, snaps, sscale, k;  // pc, pd: second wavefield pair
-    DBuf bst[7];   // second wavefield state (adjoint) when recomputing
+    DBuf bst[9];   // second state (adjoint) when recomputing: the seven fields, then its second wavefield pair
     DBuf ckpt;     // forward-state checkpoints when recomputing
     Layout lay{};
     size_t field_bytes = 0, snap_bytes = 0;
@@ -683,7 +685,26 @@ struct TwoStep {
     StepParams pf;  // the first ncore items are core tiles
     StepSet lo;
     int ncore = 0;
+    bool snap_ok = false;  // a pass's first step may store a snapshot / image
 };
+
+// Two-step lists of a wave from its single-step set: the two-step tiles,
+// and the single-step interior items outside them beside the boundary list.
+TwoStep two_step_set(const StepSet& ps, int mode, const DBuf& fus, int nfus, int ncore, const DBuf& lft, int nlft) {
+    TwoStep tw;
+    tw.ncore = ncore;
+    tw.pf = ps.pm;
+    tw.pf.items = fus.as<WorkItem>();
+    tw.pf.nitems = nfus;
+    tw.lo = ps;
+    tw.lo.pm.items = lft.as<WorkItem>();
+    tw.lo.pm.nitems = nlft;
+    // the two-step kernel stores FP32 snapshots (a 16-bit snapshot's scale is
+    // the maximum over a 128-column segment, which the single-step kernel
+    // reduces within one warp) and images with any form
+    tw.snap_ok = mode == 1 || ps.pm.snap_form == FWI_SNAP_F32;
+    return tw;
+}
 
 int step_kernels(const StepSet& ps) {
     return (ps.pm.nitems > 0) + (ps.pb.nstrip > 0) + (ps.pb.nitems > ps.pb.nstrip);
@@ -733,7 +754,9 @@ int step_fork_join(int acc, int mode, const StepSet& ps, cudaStream_t st, cudaSt
 // only its own cells, the tiles write pair Y while the core tiles of the next
 // pass read it only where the finished tiles wrote, and the single-step
 // kernels read the pair they do not write only at their own cells.
-int two_step_run(int acc, int mode, const TwoStep& tw, int k, int npass, int X, cudaStream_t st, cudaStream_t st2) {
+// sn[j]: snapshot block that pass j's first step stores / images with (-1: none).
+int two_step_run(int acc, int mode, const TwoStep& tw, int k, int npass, const int* sn, int X, cudaStream_t st,
+                 cudaStream_t st2) {
     cudaStream_t st3 = L().aux3;
     cudaEvent_t* ev = L().ev2;  // [set][C, E, A3, B2, B3]
     auto C = [&](int p) { return ev[5 * p + 0]; };
@@ -759,7 +782,7 @@ int two_step_run(int acc, int mode, const TwoStep& tw, int k, int npass, int X, 
         for (StepParams* sp : {&a.pm, &a.pb, &fc, &fe}) {
             sp->t = k - 2;
             sp->parity = k & 1;
-            sp->snap = -1;
+            sp->snap = sn ? sn[j] : -1;
             sp->rp = cur_buf(k, X);
             sp->rp1 = prev_buf(k, X);
             sp->wo = sp->wo2 = prev_buf(k, Y);
@@ -810,64 +833,82 @@ int two_step_run(int acc, int mode, const TwoStep& tw, int k, int npass, int X, 
     return FWI_OK;
 }
 
-// Which steps of k0..k1 start a two-step pass: pairs (k, k+1) with no
-// event step in them, an even number of them, so that the state ends in
-// the pair it started in.
-std::vector<char> two_step_plan(int k0, int k1, const std::vector<int>& events) {
-    std::vector<char> ev(k1 + 2, 0), start(k1 + 2, 0);
-    for (int e : events)
-        if (e >= k0 && e <= k1) ev[e] = 1;
-    int n = 0, last = -1;
-    for (int k = k0; k + 1 <= k1;) {
-        if (!ev[k] && !ev[k + 1]) {
-            start[k] = 1;
-            ++n;
-            last = k;
+// Steps k0..k1; sn_of(k) is the snapshot block step k stores (forward) or
+// images with (adjoint), -1 for none.  Pairs of steps run as two-step passes
+// (when tw is given) where the second step has no snapshot and the first has
+// none or tw allows it; the rest run as single steps.  The state is in pair 0
+// before and after (an even number of passes).
+template <typename SnOf>
+int run_range(int acc, int mode, int k0, int k1, SnOf sn_of, StepSet& ps, const TwoStep* tw, cudaStream_t st,
+              cudaStream_t st2) {
+    struct Unit {
+        int k, sn;
+        bool pass;
+    };
+    std::vector<Unit> units;
+    int npass = 0;
+    for (int k = k0; k <= k1;) {
+        const int s0 = sn_of(k);
+        if (tw && k + 1 <= k1 && sn_of(k + 1) < 0 && (s0 < 0 || tw->snap_ok)) {
+            units.push_back({k, s0, true});
+            ++npass;
             k += 2;
         } else {
-            ++k;
+            units.push_back({k, s0, false});
+            k += 1;
         }
     }
-    if (n & 1) start[last] = 0;
-    return start;
+    if (npass & 1) {  // the last pass becomes two single steps
+        for (size_t i = units.size(); i-- > 0;)
+            if (units[i].pass) {
+                const Unit u = units[i];
+                units[i] = {u.k, u.sn, false};
+                units.insert(units.begin() + i + 1, Unit{u.k + 1, -1, false});
+                break;
+            }
+    }
+    int pair = 0;
+    std::vector<int> sns;
+    for (size_t i = 0; i < units.size();) {
+        if (units[i].pass) {
+            size_t j = i;
+            sns.clear();
+            while (j < units.size() && units[j].pass) sns.push_back(units[j++].sn);
+            TRY(two_step_run(acc, mode, *tw, units[i].k, (int)sns.size(), sns.data(), pair, st, st2));
+            pair ^= (int)(sns.size() & 1);
+            i = j;
+            continue;
+        }
+        set_step(ps, units[i].k, units[i].sn, pair);
+        TRY(step_fork_join(acc, mode, ps, st, st2));
+        ++i;
+    }
+    return FWI_OK;
+}
+
+int run_plain_range(int acc, int mode, int k0, int k1, StepSet& ps, const TwoStep* tw, cudaStream_t st,
+                    cudaStream_t st2) {
+    return run_range(acc, mode, k0, k1, [](int) { return -1; }, ps, tw, st, st2);
 }
 
 // One pass over the time loop k = 2..nt for a set of shots.
 // mode 0: forward (snapshots if store, receivers recorded); mode 1: adjoint.
-// tw: two-step passes for the pairs of steps between snapshot events (null:
-// single steps only).
+// tw: two-step passes (null: single steps only).
 int run_time_loop(int acc, int mode, int nt, int store_snap, int nt_store, bool store, StepSet ps, cudaStream_t st,
                   cudaStream_t st2, const TwoStep* tw = nullptr) {
-    std::vector<int> ev = snapshot_steps(nt, store_snap);
-    std::vector<char> plan;
-    if (tw) plan = two_step_plan(2, nt, ev);
-    size_t evi = 0;
+    const std::vector<int> ev = snapshot_steps(nt, store_snap);
+    std::vector<int> sn(nt + 2, -1);
     int snap = (mode == 0) ? 0 : nt_store;
-    int pair = 0;
-    for (int k = 2; k <= nt; ++k) {
-        if (tw && plan[k]) {
-            int n = 0;
-            while (k + 2 * n <= nt && plan[k + 2 * n]) ++n;
-            TRY(two_step_run(acc, mode, *tw, k, n, pair, st, st2));
-            pair ^= n & 1;
-            k += 2 * n - 1;
-            continue;
+    for (int e : ev) {
+        if (mode == 0) {
+            ++snap;
+            sn[e] = store ? snap : -1;
+        } else {
+            --snap;
+            sn[e] = snap;
         }
-        int sn = -1;
-        if (evi < ev.size() && ev[evi] == k) {
-            ++evi;
-            if (mode == 0) {
-                ++snap;
-                if (store) sn = snap;
-            } else {
-                --snap;
-                sn = snap;
-            }
-        }
-        set_step(ps, k, sn, pair);
-        TRY(step_fork_join(acc, mode, ps, st, st2));
     }
-    return FWI_OK;
+    return run_range(acc, mode, 2, nt, [&](int k) { return sn[k]; }, ps, tw, st, st2);
 }
 
 // ---------------------------------------------------------------------------
@@ -1257,6 +1298,7 @@ struct fwi_survey {
         DBuf items_ff, items_fa, items_lf, items_la;  // two-step tiles; single-step interior items beside them
         int n_if = 0, n_ia = 0, n_bf = 0, n_ba = 0, n_strip = 0, kstrip = 1;
         int n_ff = 0, n_fa = 0, n_lf = 0, n_la = 0, n_core = 0;
+        double fus_cells = 0.0;
         cudaGraphExec_t graph[3] = {nullptr, nullptr, nullptr};
         long long graph_kernels[3] = {0, 0, 0};  // kernel nodes per graph
         DBuf save_jobs, restore_jobs;  // checkpoint copies: [ckpt][shot][field]
@@ -1354,6 +1396,7 @@ int survey_prepare_waves(fwi_survey* s) {
         wd->n_lf = (int)lists.lft_fwd.size();
         wd->n_la = (int)lists.lft_adj.size();
         wd->n_core = lists.ncore;
+        wd->fus_cells = lists.fus_cells;
         TRY(upload(wd->src_f, lists.src_fwd, st));
         TRY(upload(wd->src_a, lists.src_adj, st));
         TRY(upload(wd->recs, lists.recs, st));
@@ -1388,7 +1431,8 @@ int survey_prepare_waves(fwi_survey* s) {
             if (s->rc_C) {  // the adjoint runs on the second state while the forward is recomputed
                 dv.pf[0] = ss.bst[0].as<float>();
                 dv.pf[1] = ss.bst[1].as<float>();
-                dv.pf[2] = dv.pf[3] = nullptr;  // the adjoint of a recomputing survey runs single steps
+                dv.pf[2] = ss.bst[7].as<float>();
+                dv.pf[3] = ss.bst[8].as<float>();
                 dv.phx = ss.bst[2].as<float>();
                 dv.chx = ss.bst[3].as<float>();
                 dv.phy = ss.bst[4].as<float>();
@@ -1506,37 +1550,51 @@ int zero_slot0(fwi_survey* s, size_t wi, cudaStream_t st) {
 }
 
 // Forward steps k0..k1 on state A; snapshots of blocks whose segment is
-// `keep_seg` go to their ring slots (keep_seg < 0: none).
-int rc_steps(fwi_survey* s, int k0, int k1, int keep_seg, bool save_ckpt, size_t wi, StepSet ps, cudaStream_t st,
-             cudaStream_t st2) {
+// `keep_seg` go to their ring slots (keep_seg < 0: none).  With save_ckpt the
+// state is saved after every checkpoint step (a multiple of C); the steps in
+// between run as two-step passes and single steps (run_range), so the state
+// is in pair 0 at every save.
+int rc_steps(fwi_survey* s, int k0, int k1, int keep_seg, bool save_ckpt, size_t wi, StepSet ps, const TwoStep* tw,
+             cudaStream_t st, cudaStream_t st2) {
     const auto& D = s->desc;
     auto& wd = *s->wdev[wi];
     const int per = (int)s->waves[wi].size() * 7;
-    size_t evi = std::lower_bound(s->ev.begin(), s->ev.end(), k0) - s->ev.begin();
-    for (int k = k0; k <= k1; ++k) {
-        int sn = -1;
-        if (evi < s->ev.size() && s->ev[evi] == k) {
-            const int b = (int)evi + 1;
-            if (s->blk_seg[b] == keep_seg) sn = s->blk_slot[b];
-            ++evi;
+    std::vector<int> sn(k1 + 2, -1);
+    for (size_t i = 0; i < s->ev.size(); ++i) {
+        const int e = s->ev[i], b = (int)i + 1;
+        if (e >= k0 && e <= k1 && s->blk_seg[b] == keep_seg) sn[e] = s->blk_slot[b];
+    }
+    auto sn_of = [&](int k) { return sn[k]; };
+    int k = k0;
+    while (k <= k1) {
+        int e = k1;
+        bool save = false;
+        if (save_ckpt) {
+            const int c = (k + s->rc_C - 1) / s->rc_C * s->rc_C;  // first multiple of C at or after k
+            if (c <= k1 && c / s->rc_C <= s->rc_J - 1) {
+                e = c;
+                save = true;
+            }
         }
-        set_step(ps, k, sn);
-        TRY(step_fork_join(D.acc, 0, ps, st, st2));
-        if (save_ckpt && k % s->rc_C == 0 && k / s->rc_C <= s->rc_J - 1) {
-            const int c = k / s->rc_C - 1;
+        TRY(run_range(D.acc, 0, k, e, sn_of, ps, tw, st, st2));
+        if (save) {
+            const int c = e / s->rc_C - 1;
             LK(launch_copy_jobs(wd.save_jobs.as<unsigned char>() + (size_t)c * per * copy_job_size(), per, st));
         }
+        k = e + 1;
     }
     return FWI_OK;
 }
 
-int rc_forward(fwi_survey* s, size_t wi, int step, StepSet ps, cudaStream_t st, cudaStream_t st2) {
+int rc_forward(fwi_survey* s, size_t wi, int step, StepSet ps, const TwoStep* tw, cudaStream_t st,
+               cudaStream_t st2) {
     // keep the last segment's snapshots (the adjoint needs them first)
     if (step == 1 && s->rc_J == 1) TRY(zero_slot0(s, wi, st));
-    return rc_steps(s, 2, s->desc.nt, step == 1 ? s->rc_J - 1 : -1, step == 1, wi, ps, st, st2);
+    return rc_steps(s, 2, s->desc.nt, step == 1 ? s->rc_J - 1 : -1, step == 1, wi, ps, tw, st, st2);
 }
 
-int rc_recompute(fwi_survey* s, size_t wi, int j, StepSet psf, cudaStream_t st, cudaStream_t st2) {
+int rc_recompute(fwi_survey* s, size_t wi, int j, StepSet psf, const TwoStep* twf, cudaStream_t st,
+                 cudaStream_t st2) {
     auto& wd = *s->wdev[wi];
     const int per = (int)s->waves[wi].size() * 7;
     if (j == 0) {
@@ -1549,7 +1607,7 @@ int rc_recompute(fwi_survey* s, size_t wi, int j, StepSet psf, cudaStream_t st, 
         LK(launch_copy_jobs(wd.restore_jobs.as<unsigned char>() + (size_t)(j - 1) * per * copy_job_size(), per, st));
     }
     const int k0 = std::max(2, s->rc_C * j + 1), k1 = std::min(s->desc.nt, s->rc_C * (j + 1));
-    return rc_steps(s, k0, k1, j, false, wi, psf, st, st2);
+    return rc_steps(s, k0, k1, j, false, wi, psf, twf, st, st2);
 }
 
 int rc_adjoint(fwi_survey* s, size_t wi, StepSet ps, cudaStream_t st, cudaStream_t st2) {
@@ -1577,39 +1635,31 @@ int rc_adjoint(fwi_survey* s, size_t wi, StepSet ps, cudaStream_t st, cudaStream
     ps.pb.nitems = wd.n_ba;
     ps.pb.nstrip = wd.n_strip;
     ps.kstrip = wd.kstrip;
-    int cur = s->rc_J - 1;
-    size_t evi = 0;
+    const TwoStep twf = two_step_set(psf, 0, wd.items_ff, wd.n_ff, wd.n_core, wd.items_lf, wd.n_lf);
+    const TwoStep twa = two_step_set(ps, 1, wd.items_fa, wd.n_fa, wd.n_core, wd.items_la, wd.n_la);
+    const TwoStep* pf = wd.n_ff ? &twf : nullptr;
+    const TwoStep* pa = wd.n_fa ? &twa : nullptr;
+    // imaging steps: the block each uses (solver_acoustic_SS.f90:460) and its
+    // slot in the snapshot ring; a block of another segment than the ring
+    // holds is recomputed first, so the adjoint runs in ranges between those
+    std::vector<int> sn(D.nt + 2, -1), need(D.nt + 2, -1);
     int snap = s->nt_store;
-    for (int k = 2; k <= D.nt; ++k) {
-        int sn = -1;
-        if (evi < s->ev.size() && s->ev[evi] == k) {
-            ++evi;
-            --snap;  // block used by this imaging step (solver_acoustic_SS.f90:460)
-            const int need = snap == 0 ? 0 : s->blk_seg[snap];
-            if (need != cur) {
-                TRY(rc_recompute(s, wi, need, psf, st, st2));
-                cur = need;
-            }
-            sn = snap == 0 ? 0 : s->blk_slot[snap];
-        }
-        set_step(ps, k, sn);
-        TRY(step_fork_join(D.acc, 1, ps, st, st2));
+    for (int e : s->ev) {
+        --snap;
+        sn[e] = snap == 0 ? 0 : s->blk_slot[snap];
+        need[e] = snap == 0 ? 0 : s->blk_seg[snap];
     }
-    return FWI_OK;
-}
-
-// Two-step lists of a wave from its single-step set: the two-step tiles,
-// and the single-step interior items outside them beside the boundary list.
-TwoStep two_step_set(const StepSet& ps, const DBuf& fus, int nfus, int ncore, const DBuf& lft, int nlft) {
-    TwoStep tw;
-    tw.ncore = ncore;
-    tw.pf = ps.pm;
-    tw.pf.items = fus.as<WorkItem>();
-    tw.pf.nitems = nfus;
-    tw.lo = ps;
-    tw.lo.pm.items = lft.as<WorkItem>();
-    tw.lo.pm.nitems = nlft;
-    return tw;
+    auto sn_of = [&](int k) { return sn[k]; };
+    int cur = s->rc_J - 1;
+    int k = 2;
+    for (int e : s->ev) {
+        if (need[e] == cur) continue;
+        TRY(run_range(D.acc, 1, k, e - 1, sn_of, ps, pa, st, st2));
+        TRY(rc_recompute(s, wi, need[e], psf, pf, st, st2));
+        cur = need[e];
+        k = e;
+    }
+    return run_range(D.acc, 1, k, D.nt, sn_of, ps, pa, st, st2);
 }
 
 // Issue one wave's work: forward (+ misfit) and, for step 1, adjoint + stack.
@@ -1658,12 +1708,11 @@ int issue_wave(fwi_survey* s, size_t wi, int step, cudaStream_t st, cudaStream_t
     ps.pb.nitems = wd.n_bf;
     ps.pb.nstrip = wd.n_strip;
     ps.kstrip = wd.kstrip;
-    if (s->rc_C) {
-        TRY(rc_forward(s, wi, step, ps, st, st2));
-    } else {
-        TwoStep tw = two_step_set(ps, wd.items_ff, wd.n_ff, wd.n_core, wd.items_lf, wd.n_lf);
-        TRY(run_time_loop(D.acc, 0, D.nt, D.store_snap, s->nt_store, step == 1, ps, st, st2,
-                          wd.n_ff ? &tw : nullptr));
+    {
+        const TwoStep tw = two_step_set(ps, 0, wd.items_ff, wd.n_ff, wd.n_core, wd.items_lf, wd.n_lf);
+        const TwoStep* ptw = wd.n_ff ? &tw : nullptr;
+        if (s->rc_C) TRY(rc_forward(s, wi, step, ps, ptw, st, st2));
+        else TRY(run_time_loop(D.acc, 0, D.nt, D.store_snap, s->nt_store, step == 1, ps, st, st2, ptw));
     }
     for (size_t k = 0; k < w.size(); ++k) {
         const int sh = w[k];
@@ -1685,6 +1734,10 @@ int issue_wave(fwi_survey* s, size_t wi, int step, cudaStream_t st, cudaStream_t
             void* f = s->rc_C ? ss.bst[fi].p : ss.state(fi);
             CK(cudaMemsetAsync(f, 0, ss.field_bytes, st));
         }
+        if (s->rc_C) {  // the adjoint's second wavefield pair (its top pad must read zero)
+            CK(cudaMemsetAsync(ss.bst[7].p, 0, ss.field_bytes, st));
+            CK(cudaMemsetAsync(ss.bst[8].p, 0, ss.field_bytes, st));
+        }
         CK(cudaMemsetAsync(ss.k.p, 0, ss.k.n, st));
     }
     if (s->rc_C) {
@@ -1702,7 +1755,7 @@ int issue_wave(fwi_survey* s, size_t wi, int step, cudaStream_t st, cudaStream_t
     ps.pb.nitems = wd.n_ba;
     ps.pb.nstrip = wd.n_strip;
     ps.kstrip = wd.kstrip;
-    TwoStep tw = two_step_set(ps, wd.items_fa, wd.n_fa, wd.n_core, wd.items_la, wd.n_la);
+    TwoStep tw = two_step_set(ps, 1, wd.items_fa, wd.n_fa, wd.n_core, wd.items_la, wd.n_la);
     TRY(run_time_loop(D.acc, 1, D.nt, D.store_snap, s->nt_store, true, ps, st, st2, wd.n_fa ? &tw : nullptr));
     LK(launch_stack(s->d_G.as<double>(), D.ny, D.nx_model, wd.stack.p, (int)w.size(), D.grad_form, st));
     return FWI_OK;
@@ -1747,7 +1800,7 @@ int survey_plan(fwi_survey* s, bool tune) {
         int C = (int)std::lround(std::sqrt(7.0 * fb * D.nt * ss / (double)std::max<size_t>(bb, 1)));
         C = std::max(ss, std::min(D.nt, (C + ss - 1) / ss * ss));
         const int J = (D.nt - 1) / C + 1;
-        const size_t per_rc = 15 * fb + (size_t)(J - 1) * 7 * fb + (size_t)(C / ss + 2) * bb + kb;
+        const size_t per_rc = 19 * fb + (size_t)(J - 1) * 7 * fb + (size_t)(C / ss + 2) * bb + kb;
         const int wave_rc = (int)std::min<size_t>((size_t)D.nshots, budget / std::max<size_t>(per_rc, 1));
         const bool force = (D.flags & FWI_SURVEY_RECOMPUTE) != 0;
         if (force || (wave < std::min(D.nshots, 8) && wave_rc > wave)) {
@@ -2035,6 +2088,18 @@ int fwi_survey_step_bytes(fwi_survey* s, double* bytes) {
     return FWI_OK;
 }
 
+int fwi_survey_two_step_bytes(fwi_survey* s, double* per_step, double* tiles_per_pass) {
+    if (!s || s->wdev.empty()) return fail(FWI_ERR_STATE, "survey not prepared");
+    double b = 0.0;
+    for (int sh : s->waves[0]) b += step_bytes_shot(s->lays[sh].ny, s->lays[sh].nx, s->lays[sh].dn);
+    // a two-step tile reads p_n, p_{n-1}, c2 and writes p_{n+1}, p_{n+2} once
+    // per cell and pass: 20 B for two steps instead of 2 x 16 B
+    const double cells = s->wdev[0]->n_ff ? s->wdev[0]->fus_cells : 0.0;
+    if (per_step) *per_step = b - 6.0 * cells;
+    if (tiles_per_pass) *tiles_per_pass = 20.0 * cells;
+    return FWI_OK;
+}
+
 int fwi_survey_tuning(fwi_survey* s, int* wave_shots, int* band_rows) {
     if (!s) return fail(FWI_ERR_STATE, "null survey");
     if (wave_shots) *wave_shots = s->wave;
@@ -2082,12 +2147,12 @@ int time_wave0_steps(fwi_survey* s, int steps, float* ms) {
     }
     // pairs of steps as two-step passes when the wave has two-step tiles
     // (an even number of them, so that the state stays in pair 0)
-    const TwoStep tw = two_step_set(ps, wd.items_ff, wd.n_ff, wd.n_core, wd.items_lf, wd.n_lf);
+    const TwoStep tw = two_step_set(ps, 0, wd.items_ff, wd.n_ff, wd.n_core, wd.items_lf, wd.n_lf);
     const int npass = (wd.n_ff && D.nt >= 3) ? (steps / 4) * 2 : 0;
     // (in runs that stay inside the time axis: steps 2..nt)
     for (int done = 0, pair = 0; done < npass;) {
         const int n = std::min(npass - done, (D.nt - 1) / 2);
-        TRY(two_step_run(D.acc, 0, tw, 2, n, pair, stream(), L().aux));
+        TRY(two_step_run(D.acc, 0, tw, 2, n, nullptr, pair, stream(), L().aux));
         pair ^= n & 1;
         done += n;
     }

@@ -457,6 +457,10 @@ __device__ __forceinline__ void cp4(void* smem_dst, const void* gmem_src) {
     const unsigned d = (unsigned)__cvta_generic_to_shared(smem_dst);
     asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(d), "l"(gmem_src) : "memory");
 }
+__device__ __forceinline__ void cp8(void* smem_dst, const void* gmem_src) {
+    const unsigned d = (unsigned)__cvta_generic_to_shared(smem_dst);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(d), "l"(gmem_src) : "memory");
+}
 
 template <int R, int MODE, bool SNAP>
 __global__ void __launch_bounds__(128, (MODE == 1 && SNAP) ? 3 : 5) k_step_interior(const __grid_constant__ StepParams P) {
@@ -1072,31 +1076,41 @@ constexpr int F2_W = 120;
 constexpr int F2_HL = 0, F2_P = 1, F2_HR = 33, F2_P1 = 34, F2_C2 = 66, F2_SIZE = 98;
 constexpr int F2_DEPTH = 4;  // rows in flight
 constexpr int F2_LINE = 34;  // p_{n+1} line: [garbage | 32 lanes | garbage]
-template <int R>
+// imaging passes: per row in flight the snapshot row (FP32: 32 float4;
+// 16-bit: 16 float4 and one scale per lane) and the accumulator row (FP32: 32
+// float4; FP64: 64 float4)
+constexpr int F2_IF = 0, F2_IS = 32, F2_IK = 40, F2_ISIZE = 104;
+template <int R, bool IMG = false>
 struct F2Ring {
     static constexpr int SLOTS = F2_DEPTH + R + 1;
     static constexpr int Q1 = R + 2;  // p_{n+1} lines: rows y-R-1 .. y
-    static constexpr int WARP = SLOTS * F2_SIZE + Q1 * F2_LINE;  // float4 per warp
+    static constexpr int WARP = SLOTS * F2_SIZE + (Q1 + 1) * F2_LINE + (IMG ? F2_DEPTH * F2_ISIZE : 0);  // float4 per warp
     static constexpr int SMEM = 4 * WARP * 16;
 };
 
-// Injected values of row y for this lane's four columns (entries sorted by
-// row, the cursor at the first entry of row y or below; sv starts at zero).
-__device__ __forceinline__ void gather_sources(const StepParams& P, const ShotDev& S, int y, int xl, int t, int& si,
-                                               int s1, int& srow, float* sv) {
+// Injected values of row y for the warp's 128 columns starting at physical
+// column c0 (entries sorted by row, one per cell, all inside those columns;
+// the cursor si at the first entry of row y).  The lanes take the row's
+// entries 32 at a time and scatter their values into the warp's line `inj`
+// (a float4 per lane, entry [1 + lane] for lane l's columns c0 + 4l ..);
+// each lane then reads its own float4.  Called by the whole warp when srow == y.
+__device__ __forceinline__ float4 gather_sources(const StepParams& P, const ShotDev& S, int y, int c0, int t, int& si,
+                                                 int s1, int& srow, float4* inj, int lane) {
+    inj[1 + lane] = make_float4(0.f, 0.f, 0.f, 0.f);
+    __syncwarp();
     while (srow == y) {
-        const SrcEnt e = P.srcs[si];
-        if ((e.col >> 2) == (xl >> 2)) {
-            const float val = __ldg(S.srcv + (size_t)e.vidx * S.nt + t);
-            const int el = e.col & 3;
-            sv[0] = el == 0 ? val : sv[0];
-            sv[1] = el == 1 ? val : sv[1];
-            sv[2] = el == 2 ? val : sv[2];
-            sv[3] = el == 3 ? val : sv[3];
+        const int i = si + lane;
+        bool mine = false;
+        if (i < s1) {
+            const SrcEnt e = P.srcs[i];
+            mine = e.row == y;
+            if (mine) reinterpret_cast<float*>(inj + 1)[e.col - c0] = __ldg(S.srcv + (size_t)e.vidx * S.nt + t);
         }
-        ++si;
+        si += __popc(__ballot_sync(FULL, mine));  // the row's entries are consecutive
         srow = (si < s1) ? P.srcs[si].row : INT_MAX;
     }
+    __syncwarp();
+    return inj[1 + lane];
 }
 
 __device__ __forceinline__ void record_row_t(const StepParams& P, const ShotDev& S, int y, int xl, int t, int& ri,
@@ -1109,15 +1123,100 @@ __device__ __forceinline__ void record_row_t(const StepParams& P, const ShotDev&
     }
 }
 
-template <int R, int MODE>
-__global__ void __launch_bounds__(128, 3) k_step2_interior(const __grid_constant__ StepParams P) {
-    using RG = F2Ring<R>;
+// SNAP: the first of the two steps stores a snapshot (MODE 0, FP32 form) or
+// applies the imaging condition (MODE 1) at the tile's own cells, as
+// k_step_interior does at a snapshot step (P.snap = the block).
+// Snapshot store (MODE 0: Fields = (p_3 - p_1)*0.5/dt, FP32 form) or imaging
+// condition (MODE 1: kernel += -0.5*(p_3-p_1)*Fields*store_snap) for the
+// elements [lo, hi) of this lane's four cells in snapshot row yrow, the same
+// arithmetic as k_step_interior's snapshot steps (solver_acoustic_SS.f90:447,
+// :465-466).  The scale of a 16-bit snapshot is that of the cell's 128-column
+// segment.
+template <int MODE>
+__device__ __forceinline__ void snap_or_image(const StepParams& P, const ShotDev& S, int yrow, int xl, int lo, int hi,
+                                              bool full, const float* p3, float4 pm1v, const float4* isl, int lane) {
+    float pm1[4];
+    to_arr(pm1v, pm1);
+    const size_t fo = (size_t)P.snap * (size_t)S.snap_stride + (size_t)yrow * S.pitch + xl;
+    if (MODE == 0) {
+        float v[4];
+#pragma unroll
+        for (int e = 0; e < 4; ++e) v[e] = ((p3[e] - pm1[e]) * 0.5f) / P.dt;
+        float* F = reinterpret_cast<float*>(S.snaps) + fo;
+        if (full) {
+            st4(F, from_arr(v));
+        } else {
+#pragma unroll
+            for (int e = 0; e < 4; ++e)
+                if (e >= lo && e < hi) F[e] = v[e];
+        }
+        return;
+    }
+    // the snapshot and accumulator rows were prefetched into the slot isl
+    float F[4];
+    if (P.snap_form == 0) {
+        to_arr(isl[F2_IF + lane], F);
+    } else {
+        const uint2 pk = reinterpret_cast<const uint2*>(isl + F2_IF)[lane];
+        const float sc = reinterpret_cast<const float*>(isl + F2_IS)[lane];
+        const unsigned short hv[4] = {(unsigned short)(pk.x & 0xffffu), (unsigned short)(pk.x >> 16),
+                                      (unsigned short)(pk.y & 0xffffu), (unsigned short)(pk.y >> 16)};
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+            float f;
+            if (P.snap_form == 1) f = __bfloat162float(*reinterpret_cast<const __nv_bfloat16*>(&hv[e]));
+            else f = __half2float(*reinterpret_cast<const __half*>(&hv[e]));
+            F[e] = f * sc;
+        }
+    }
+    float k2[4];
+#pragma unroll
+    for (int e = 0; e < 4; ++e) k2[e] = -(((0.5f * (p3[e] - pm1[e])) * F[e]) * P.ss);
+    const size_t ko = (size_t)yrow * S.pitch + xl;
+    if (P.grad_form == 0) {
+        float kv[4];
+        to_arr(isl[F2_IK + lane], kv);
+#pragma unroll
+        for (int e = 0; e < 4; ++e) kv[e] = kv[e] + k2[e];
+        if (full) {
+            st4(S.k32 + ko, from_arr(kv));
+        } else {
+#pragma unroll
+            for (int e = 0; e < 4; ++e)
+                if (e >= lo && e < hi) S.k32[ko + e] = kv[e];
+        }
+    } else {
+        const double2* kk = reinterpret_cast<const double2*>(isl + F2_IK) + 2 * lane;
+        double2 a = kk[0], b = kk[1];
+        a.x += (double)k2[0];
+        a.y += (double)k2[1];
+        b.x += (double)k2[2];
+        b.y += (double)k2[3];
+        if (full) {
+            double2* K2 = reinterpret_cast<double2*>(S.k64 + ko);
+            K2[0] = a;
+            K2[1] = b;
+        } else {
+            const double kv[4] = {a.x, a.y, b.x, b.y};
+#pragma unroll
+            for (int e = 0; e < 4; ++e)
+                if (e >= lo && e < hi) S.k64[ko + e] = kv[e];
+        }
+    }
+}
+
+template <int R, int MODE, bool SNAP>
+__global__ void __launch_bounds__(128, (MODE == 1 && SNAP) ? 2 : 3) k_step2_interior(const __grid_constant__ StepParams P) {
+    constexpr bool IMG = MODE == 1 && SNAP;
+    using RG = F2Ring<R, IMG>;
     extern __shared__ float4 smem[];
     const int lane = threadIdx.x & 31;
     const int wid = blockIdx.x * 4 + (threadIdx.x >> 5);
     if (wid >= P.nitems) return;
     float4* ring = smem + (threadIdx.x >> 5) * RG::WARP;
     float4* q1l = ring + RG::SLOTS * F2_SIZE;  // p_{n+1} lines
+    float4* inj = q1l + RG::Q1 * F2_LINE;       // injected values of a row
+    float4* iring = inj + F2_LINE;              // imaging rows (IMG)
     const WorkItem it = P.items[wid];
     const ShotDev& S = P.shots[it.shot];
     const int pitch = S.pitch, dn = S.dn;
@@ -1146,6 +1245,28 @@ __global__ void __launch_bounds__(128, 3) k_step2_interior(const __grid_constant
         cp16(st + F2_P1 + lane, PM + ro);
         cp16(st + F2_C2 + lane, C2 + ro);
     };
+    // imaging passes: the snapshot and accumulator rows of the own rows, into
+    // slot (y - ya) mod DEPTH, with the row's other copies
+    auto issue_img = [&](int y, int islot) {
+        if (!IMG || y < y0 || y >= y1) return;
+        float4* isl = iring + islot * F2_ISIZE;
+        const int yrow = y - dn;
+        const size_t fo = (size_t)P.snap * (size_t)S.snap_stride + (size_t)yrow * pitch + xl;
+        if (P.snap_form == 0) {
+            cp16(isl + F2_IF + lane, reinterpret_cast<const float*>(S.snaps) + fo);
+        } else {
+            cp8(reinterpret_cast<uint2*>(isl + F2_IF) + lane, reinterpret_cast<const unsigned short*>(S.snaps) + fo);
+            cp4(reinterpret_cast<float*>(isl + F2_IS) + lane,
+                S.sscale + ((size_t)P.snap * S.ny + yrow) * (S.ntiles + 2) + (xl >> 7));
+        }
+        const size_t ko = (size_t)yrow * pitch + xl;
+        if (P.grad_form == 0) {
+            cp16(isl + F2_IK + lane, S.k32 + ko);
+        } else {
+            cp16(isl + F2_IK + 2 * lane, S.k64 + ko);
+            cp16(isl + F2_IK + 2 * lane + 1, S.k64 + ko + 2);
+        }
+    };
     // the x-neighbours of row y's p_n sit in the slot of row y - R, which
     // holds p_n row y (with its halos); for the first R rows these are slots
     // SLOTS-R .. SLOTS-1 (rows ya-R .. ya-1), filled here
@@ -1160,6 +1281,7 @@ __global__ void __launch_bounds__(128, 3) k_step2_interior(const __grid_constant
 #pragma unroll
     for (int i = 0; i < F2_DEPTH; ++i) {
         issue(ya + i, i);
+        issue_img(ya + i, i);
         cp_commit();
     }
     // qn: p_n rows y-R-1 .. y+R; q1: p_{n+1} rows y-2R-1 .. y-1 (before row y's first step)
@@ -1181,7 +1303,7 @@ __global__ void __launch_bounds__(128, 3) k_step2_interior(const __grid_constant
 
     // slot of row y, of row y - R (x-neighbours of p_n row y), of row y - R - 1 (c2 of the second step);
     // p_{n+1} line of row y and of row y - R - 1
-    int slot = 0, slotx = RG::SLOTS - R, slot2 = RG::SLOTS - R - 1, l1 = 0, l2 = 1;
+    int slot = 0, slotx = RG::SLOTS - R, slot2 = RG::SLOTS - R - 1, l1 = 0, l2 = 1, islot = 0;
     for (int y = ya; y < yb; ++y) {
         // every lane has its own copies of row y (and of the pre slots); the
         // warp synchronises before it reads the other lanes' copies and the
@@ -1196,7 +1318,7 @@ __global__ void __launch_bounds__(128, 3) k_step2_interior(const __grid_constant
         {
             const float4 Lf = sx[F2_HL + lane], Rf = sx[F2_P + 1 + lane];
             float sv[4] = {0.f, 0.f, 0.f, 0.f};
-            if (srow1 == y) gather_sources(P, S, y, xl, P.t, si1, it.s1, srow1, sv);
+            if (srow1 == y) to_arr(gather_sources(P, S, y, x0 - 4, P.t, si1, it.s1, srow1, inj, lane), sv);
             if (y >= dn) interior_update2<R>(qn + 1, Lf, Rf, st[F2_P1 + lane], st[F2_C2 + lane], sv, cp, np1);
         }
         q1l[l1 * F2_LINE + 1 + lane] = from_arr(np1);
@@ -1208,7 +1330,7 @@ __global__ void __launch_bounds__(128, 3) k_step2_interior(const __grid_constant
             const float4* ln = q1l + l2 * F2_LINE;
             const float4 Lf = ln[lane], Rf = ln[lane + 2];
             float sv[4] = {0.f, 0.f, 0.f, 0.f};
-            if (srow2 == y2) gather_sources(P, S, y2, xl, P.t + 1, si2, it.s1, srow2, sv);
+            if (srow2 == y2) to_arr(gather_sources(P, S, y2, x0 - 4, P.t + 1, si2, it.s1, srow2, inj, lane), sv);
             float np2[4];
             interior_update2<R>(q1, Lf, Rf, qn[0], st2[F2_C2 + lane], sv, cp, np2);
             if (full) {
@@ -1229,6 +1351,9 @@ __global__ void __launch_bounds__(128, 3) k_step2_interior(const __grid_constant
                     if (e >= lo && e < hi) O1[(size_t)y * pitch + e] = np1[e];
             }
             if (MODE == 0 && P.record && rrow1 == y) record_row_t(P, S, y, xl, P.t, ri1, it.r1, rrow1, np1);
+            if (SNAP && (full || part))
+                snap_or_image<MODE>(P, S, y - dn, xl, lo, hi, full, np1, st[F2_P1 + lane], iring + islot * F2_ISIZE,
+                                    lane);
         }
 #pragma unroll
         for (int i = 0; i < 2 * R + 1; ++i) qn[i] = qn[i + 1];
@@ -1238,8 +1363,12 @@ __global__ void __launch_bounds__(128, 3) k_step2_interior(const __grid_constant
         // the slot of row y - R - 1 is free now: it takes row y + DEPTH (the
         // other lanes read it last in the previous iteration, before this
         // iteration's sync)
-        if (y + F2_DEPTH < yb) issue(y + F2_DEPTH, slot2);
+        if (y + F2_DEPTH < yb) {
+            issue(y + F2_DEPTH, slot2);
+            issue_img(y + F2_DEPTH, islot);
+        }
         cp_commit();
+        islot = (islot + 1 == F2_DEPTH) ? 0 : islot + 1;
         slot = (slot + 1 == RG::SLOTS) ? 0 : slot + 1;
         slotx = (slotx + 1 == RG::SLOTS) ? 0 : slotx + 1;
         slot2 = (slot2 + 1 == RG::SLOTS) ? 0 : slot2 + 1;
@@ -1284,7 +1413,8 @@ cudaError_t configure_variant() {
     if (e == cudaSuccess) e = kernel_smem(k_step_bottom<R, MODE>, BND_SMEM);
     if (e == cudaSuccess) e = kernel_smem(k_step_strip<R, MODE, 1>, strip_smem<R, 1>());
     if (e == cudaSuccess) e = kernel_smem(k_step_strip<R, MODE, 2>, strip_smem<R, 2>());
-    if (e == cudaSuccess) e = kernel_smem(k_step2_interior<R, MODE>, F2Ring<R>::SMEM);
+    if (e == cudaSuccess) e = kernel_smem(k_step2_interior<R, MODE, false>, F2Ring<R>::SMEM);
+    if (e == cudaSuccess) e = kernel_smem(k_step2_interior<R, MODE, true>, F2Ring<R, MODE == 1>::SMEM);
     return e;
 }
 
@@ -1331,16 +1461,24 @@ cudaError_t launch_step(int acc, int mode, int kstrip, const StepParams& pm, con
     return cudaGetLastError();
 }
 
-// Two-step interior tiles (kind 4) of list pf on stream st.
+template <int R, int MODE>
+void launch_step2_variant(const StepParams& pf, int nb, cudaStream_t st) {
+    if (pf.snap >= 0) k_step2_interior<R, MODE, true><<<nb, 128, F2Ring<R, MODE == 1>::SMEM, st>>>(pf);
+    else k_step2_interior<R, MODE, false><<<nb, 128, F2Ring<R>::SMEM, st>>>(pf);
+}
+
+// Two-step interior tiles (kind 4) of list pf on stream st; pf.snap >= 0:
+// the first step stores that snapshot block / images with it.
 cudaError_t launch_step2(int acc, int mode, const StepParams& pf, cudaStream_t st) {
     const int nb = (pf.nitems + 3) / 4;
     if (!nb) return cudaSuccess;
+    if (mode == 0 && pf.snap >= 0 && pf.snap_form != 0) return cudaErrorInvalidValue;  // FP32 snapshots only
     if (acc == 3) {
-        if (mode == 0) k_step2_interior<3, 0><<<nb, 128, F2Ring<3>::SMEM, st>>>(pf);
-        else k_step2_interior<3, 1><<<nb, 128, F2Ring<3>::SMEM, st>>>(pf);
+        if (mode == 0) launch_step2_variant<3, 0>(pf, nb, st);
+        else launch_step2_variant<3, 1>(pf, nb, st);
     } else if (acc == 4) {
-        if (mode == 0) k_step2_interior<4, 0><<<nb, 128, F2Ring<4>::SMEM, st>>>(pf);
-        else k_step2_interior<4, 1><<<nb, 128, F2Ring<4>::SMEM, st>>>(pf);
+        if (mode == 0) launch_step2_variant<4, 0>(pf, nb, st);
+        else launch_step2_variant<4, 1>(pf, nb, st);
     } else {
         return cudaErrorInvalidValue;
     }

@@ -245,6 +245,11 @@ int fwi_survey_get_synthetic(fwi_survey* s, int shot, float* out);
 /* Algorithmic HBM bytes of one forward time step of the shots of the first
  * wave (the unit fwi_survey_time_steps advances). */
 int fwi_survey_step_bytes(fwi_survey* s, double* bytes);
+/* Algorithmic bytes of one time step of the first wave when the steps run as
+ * two-step passes (the two-step tiles move 20 B per cell for two steps, the
+ * single-step lists their usual bytes), and the tiles' bytes of one pass.
+ * Without two-step tiles per_step equals fwi_survey_step_bytes. */
+int fwi_survey_two_step_bytes(fwi_survey* s, double* per_step, double* tiles_per_pass);
 /* Tuning chosen for the survey (wave size, band rows). */
 int fwi_survey_tuning(fwi_survey* s, int* wave_shots, int* band_rows);
 /* Checkpointed recomputation plan: forward steps per segment and number of

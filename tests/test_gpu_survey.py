@@ -59,20 +59,25 @@ def test_survey_gradient_vs_oracle(kw):
     assert mis2 == mis and np.array_equal(grad2, grad)
 
 
-@pytest.mark.parametrize("kw", [dict(), dict(acc=4, dpml=20, ny=33, nxm=170, nshots=4),
-                                dict(nshots=3, nxm=300, windows=[(0, 150), (70, 230), (140, 160)]),
-                                dict(store_snap=3, nt=151), dict(acc=4, store_snap=7, nt=97, ny=12)])
-def test_two_step_passes_bit_identical(kw):
+@pytest.mark.parametrize("kw,rc,form", [
+    (dict(), False, 0), (dict(acc=4, dpml=20, ny=33, nxm=170, nshots=4), False, 0),
+    (dict(nshots=3, nxm=300, windows=[(0, 150), (70, 230), (140, 160)]), False, 0),
+    (dict(store_snap=3, nt=151), False, 0), (dict(acc=4, store_snap=7, nt=97, ny=12), False, 0),
+    (dict(store_snap=3, nt=151), False, 2), (dict(store_snap=4, nt=120), False, 1),
+    (dict(nt=301, store_snap=5), True, 0), (dict(acc=4, nt=160, store_snap=4), True, 2)])
+def test_two_step_passes_bit_identical(kw, rc, form):
     """Pairs of steps advanced by the two-step interior kernel (with the
     single-step lists beside it) give the same bits as single steps: traces,
-    misfit and gradient, forward and adjoint."""
+    misfit and gradient, forward and adjoint, with snapshot stores and imaging
+    inside passes (FP32 snapshots; 16-bit ones are stored by single steps),
+    and with checkpointed recomputation."""
     import fwi_gb300 as F
     from fwi_gb300.synth import lam_from_vp
     spec, vp = make(9, **kw)
     lam = lam_from_vp(vp)
     res = []
     for two in (True, False):
-        sv = F.Survey(spec, two_step=two)
+        sv = F.Survey(spec, snap_form=form, two_step=two, recompute=rc)
         sv.set_lambda(lam)
         g = np.zeros((spec.ny, spec.nx_model), np.float32, order="F")
         m, _ = sv.run(1, g)

@@ -1,7 +1,9 @@
 // FWI time-step kernels for sm_103a.
 //
 // Three launches advance every shot of a wave by one time step of the
-// reference solver (solver_acoustic_SS.f90:313-586):
+// reference solver (solver_acoustic_SS.f90:313-586); a fourth,
+// k_step2_interior, advances the interior of the model rows by two steps in
+// one sweep (two-step passes, below):
 //
 //   k_step_interior  model rows dn..dn+ny-1, interior columns: interior
 //                    update with source injection (:319-330, :433-434),
@@ -21,11 +23,12 @@
 // float4) and march down a band of rows; the y-stencil comes from a register
 // queue of 2R+1 rows, the x-stencil from warp shuffles of the current row
 // plus one halo float4 at each end of the tile.  Strip warps hold one column
-// per lane.  The wavefield is ping-ponged between two buffers: p_3
-// overwrites p_1 in place (each cell reads its own p_1 only), and every cell
-// is written by exactly one warp.  The CPML memory variables are updated in
-// place: the strip-local derivative of phi only reads phi values of the same
-// warp, loaded before they are overwritten.
+// per lane.  The wavefield lives in two buffer pairs (ShotDev::pf): a single
+// step reads p and p_1 of one pair and writes p_3 over p_1 (each cell reads
+// its own p_1 only); a two-step pass reads one pair and writes both new
+// steps to the other.  Every cell is written by exactly one warp.  The CPML
+// memory variables are updated in place: the strip-local derivative of phi
+// only reads phi values of the same warp, loaded before they are overwritten.
 //
 // This file is compiled with --fmad=false: every a*b+c below is a rounded
 // multiply followed by a rounded add, in the order the Fortran source writes

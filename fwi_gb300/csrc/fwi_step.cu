@@ -408,6 +408,11 @@ __device__ __forceinline__ void interior_update2(const float4* q, float4 L, floa
                                                  const float* sv, const float2* cp, float* p3);
 
 // The same update with the 2R+1 rows given by an accessor: q(i) is row y-R+i.
+// The centre terms of both derivatives and the 2p term are the same rounded
+// sum p + p; each derivative sum starts from its centre product (the
+// reference adds it to 0, which changes nothing but the sign of a zero).
+// x-neighbour pairs at odd offsets straddle two register pairs: their sums
+// are formed with two scalar adds straight into a pair.
 template <int R, typename QF>
 __device__ __forceinline__ void interior_update2f(QF q, float4 L, float4 Rt, float4 pm1, float4 cc, const float* sv,
                                                   const float2* cp, float* p3) {
@@ -415,20 +420,25 @@ __device__ __forceinline__ void interior_update2f(QF q, float4 L, float4 Rt, flo
     const float w[12] = {L.x, L.y, L.z, L.w, C.x, C.y, C.z, C.w, Rt.x, Rt.y, Rt.z, Rt.w};
 #pragma unroll
     for (int k = 0; k < 2; ++k) {
+        const float2 pc = pr(C, k);
+        const float2 p2 = __fadd2_rn(pc, pc);  // p(j) + p(j)
+        const float2 c0 = mul0(cp[0], p2);     // centre term, x and y alike
         // space_deriv2x: s = s + coef(i)*(p(j+i) + p(j-i))
-        float2 ax = make_float2(0.f, 0.f);
+        float2 ax = c0;
 #pragma unroll
-        for (int i = 0; i <= R; ++i) {
+        for (int i = 1; i <= R; ++i) {
             const int a = 4 + 2 * k + i, b = 4 + 2 * k - i;
-            ax = __fadd2_rn(ax, mul0(cp[i], __fadd2_rn(make_float2(w[a], w[a + 1]), make_float2(w[b], w[b + 1]))));
+            const float2 sx = (i & 1) ? make_float2(w[a] + w[b], w[a + 1] + w[b + 1])
+                                      : __fadd2_rn(make_float2(w[a], w[a + 1]), make_float2(w[b], w[b + 1]));
+            ax = __fadd2_rn(ax, mul0(cp[i], sx));
         }
         // space_deriv2y: s = s + (p(j+i) + p(j-i))*coef(i)
-        float2 ay = make_float2(0.f, 0.f);
+        float2 ay = c0;
 #pragma unroll
-        for (int i = 0; i <= R; ++i) ay = __fadd2_rn(ay, mul0(__fadd2_rn(pr(q(R + i), k), pr(q(R - i), k)), cp[i]));
+        for (int i = 1; i <= R; ++i) ay = __fadd2_rn(ay, mul0(__fadd2_rn(pr(q(R + i), k), pr(q(R - i), k)), cp[i]));
         // p_3 = -p_1 + 2p + (d2x + d2y + source)*c2
-        const float2 pc = pr(C, k), pm = pr(pm1, k);
-        const float2 t = __fadd2_rn(make_float2(-pm.x, -pm.y), __fadd2_rn(pc, pc));
+        const float2 pm = pr(pm1, k);
+        const float2 t = __fadd2_rn(make_float2(-pm.x, -pm.y), p2);
         const float2 u = mul0(__fadd2_rn(__fadd2_rn(ax, ay), make_float2(sv[2 * k], sv[2 * k + 1])), pr(cc, k));
         const float2 r = __fadd2_rn(t, u);
         p3[2 * k] = r.x;

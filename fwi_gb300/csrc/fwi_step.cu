@@ -1126,12 +1126,22 @@ __device__ __forceinline__ float4 gather_sources(const StepParams& P, const Shot
     return inj[1 + lane];
 }
 
-__device__ __forceinline__ void record_row_t(const StepParams& P, const ShotDev& S, int y, int xl, int t, int& ri,
-                                             int r1, int& rrow, const float* p3) {
+// Receivers of row y (entries sorted by row, the cursor ri at the first one
+// of row y): p_3 of the warp's 128 columns starting at physical column c0 is
+// in `line` (entry [1 + lane] for lane l's columns c0 + 4l ..), visible to
+// the whole warp; the lanes take the row's receivers 32 at a time.  Called by
+// the whole warp when rrow == y.
+__device__ __forceinline__ void record_row_par(const StepParams& P, const ShotDev& S, int y, int c0, int t, int& ri,
+                                               int r1, int& rrow, const float4* line, int lane) {
     while (rrow == y) {
-        const RecEnt r = P.recs[ri];
-        if ((r.col >> 2) == (xl >> 2)) S.rec[(size_t)r.ridx * S.nt + t] = sel(p3, r.col & 3);
-        ++ri;
+        const int i = ri + lane;
+        bool mine = false;
+        if (i < r1) {
+            const RecEnt r = P.recs[i];
+            mine = r.row == y;
+            if (mine) S.rec[(size_t)r.ridx * S.nt + t] = reinterpret_cast<const float*>(line + 1)[r.col - c0];
+        }
+        ri += __popc(__ballot_sync(FULL, mine));  // the row's entries are consecutive
         rrow = (ri < r1) ? P.recs[ri].row : INT_MAX;
     }
 }
@@ -1353,7 +1363,11 @@ __global__ void __launch_bounds__(128, (MODE == 1 && SNAP) ? 2 : 3) k_step2_inte
                 for (int e = 0; e < 4; ++e)
                     if (e >= lo && e < hi) O2[(size_t)y2 * pitch + e] = np2[e];
             }
-            if (MODE == 0 && P.record && rrow2 == y2) record_row_t(P, S, y2, xl, P.t + 1, ri2, it.r1, rrow2, np2);
+            if (MODE == 0 && P.record && rrow2 == y2) {
+                inj[1 + lane] = from_arr(np2);  // the injection line is free again
+                __syncwarp();
+                record_row_par(P, S, y2, x0 - 4, P.t + 1, ri2, it.r1, rrow2, inj, lane);
+            }
         }
         if (y >= y0 && y < y1) {
             if (full) {
@@ -1363,7 +1377,10 @@ __global__ void __launch_bounds__(128, (MODE == 1 && SNAP) ? 2 : 3) k_step2_inte
                 for (int e = 0; e < 4; ++e)
                     if (e >= lo && e < hi) O1[(size_t)y * pitch + e] = np1[e];
             }
-            if (MODE == 0 && P.record && rrow1 == y) record_row_t(P, S, y, xl, P.t, ri1, it.r1, rrow1, np1);
+            if (MODE == 0 && P.record && rrow1 == y) {
+                __syncwarp();  // np1 of every lane is in its p_{n+1} line
+                record_row_par(P, S, y, x0 - 4, P.t, ri1, it.r1, rrow1, q1l + l1 * F2_LINE, lane);
+            }
             if (SNAP && (full || part))
                 snap_or_image<MODE>(P, S, y - dn, xl, lo, hi, full, np1, st[F2_P1 + lane], iring + islot * F2_ISIZE,
                                     lane);

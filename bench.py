@@ -421,7 +421,7 @@ def main():
         torch.cuda.synchronize()
         tp = p0.elapsed_time(p1) / 1e3 / nplain
         plain = {"value": 1.0 / tp, "unit": METRIC, "batched_over_plain": value / world * tp,
-                 "how": "same workload one shot at a time, one kernel launch per time step, no CUDA graph"}
+                 "how": "same workload one shot at a time, direct kernel launches, no CUDA graph"}
         pv.close()
         del pv
         torch.cuda.synchronize()

@@ -21,7 +21,7 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_lib")
 LIB = os.path.join(OUT_DIR, "libfwi_gb300.so")
-SOURCES = ["fwi_step.cu", "fwi_aux.cu", "fwi_host.cu", "fwi_prep.cu", "fwi_io.cpp"]
+SOURCES = ["fwi_step.cu", "fwi_aux.cu", "fwi_host.cu", "fwi_prep.cu", "fwi_io.cpp", "fwi_lists.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CUDA_LIB = "/usr/local/cuda/lib64"  # cuFFT (the trace filter) is linked dynamically from the toolkit
 

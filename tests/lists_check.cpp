@@ -1,0 +1,162 @@
+// CPU checks of the step kernels' work lists (fwi_lists.cpp), over many grid
+// shapes:
+//  * single-step lists: every cell of the model rows and the bottom pad rows
+//    (all columns) is updated by exactly one item;
+//  * two-step passes: every interior cell of the model rows is stored by
+//    exactly one two-step tile or leftover item, and nothing else;
+//  * a two-step tile's first-step cells that its second step uses are plain
+//    interior cells (no CPML column, no bottom pad row), its reads stay inside
+//    the field, and core tiles read no cell a single-step item writes;
+//  * source and receiver lists are sorted by row and lie inside the item.
+// Prints "all ok" and exits 0, or prints the first failure and exits 1.
+#include <cstdio>
+#include <cstdlib>
+#include <vector>
+
+#include "fwi_lists.h"
+
+using namespace fwi;
+
+namespace {
+
+unsigned rng_state = 12345u;
+int rnd(int n) {
+    rng_state = rng_state * 1664525u + 1013904223u;
+    return (int)((rng_state >> 8) % (unsigned)n);
+}
+
+int fails = 0;
+#define CHECK(cond, ...)                   \
+    do {                                   \
+        if (!(cond)) {                     \
+            std::printf(__VA_ARGS__);      \
+            std::printf("\n");             \
+            ++fails;                       \
+            return;                        \
+        }                                  \
+    } while (0)
+
+// columns [c0, c1) of a single-step item
+void item_cols(const WorkItem& it, const Layout& l, int& c0, int& c1) {
+    const int xa = l.off + l.sl, xb = l.off + l.sr;
+    if (it.kind == 0 || it.kind == 1) {
+        c0 = std::max(it.tile * TILE, xa);
+        c1 = std::min((it.tile + 1) * TILE, xb);
+    } else {
+        c0 = l.off + (it.tile ? l.sr : 0);
+        c1 = l.off + (it.tile ? l.nxt : l.sl);
+    }
+}
+
+void check(int ny, int nx, int acc, int dpml, int nsrc, int band, int fband) {
+    const Layout l = make_layout(ny, nx, acc, dpml);
+    ShotGeom g;
+    g.nx = nx;
+    for (int i = 0; i < nsrc; ++i) {
+        g.nxS.push_back(1 + rnd(nx));
+        g.nyS.push_back(1 + rnd(ny));
+    }
+    for (int i = 0; i < 60; ++i) {
+        g.nxR.push_back(1 + rnd(nx));
+        g.nyR.push_back(1 + rnd(ny));
+    }
+    const Lists L = build_lists({g}, {l}, band, fband);
+    const int R = l.acc, xa = l.off + l.sl, xb = l.off + l.sr;
+    const size_t n = (size_t)l.nyt * l.pitch;
+    auto at = [&](int y, int c) { return (size_t)y * l.pitch + c; };
+
+    // single-step lists: model rows and bottom pad rows, columns [0, nxt)
+    std::vector<int> own(n, 0);
+    for (const auto* v : {&L.int_fwd, &L.bnd_fwd})
+        for (const WorkItem& it : *v) {
+            int c0, c1;
+            item_cols(it, l, c0, c1);
+            for (int y = it.y0; y < it.y1; ++y)
+                for (int c = c0; c < c1; ++c) own[at(y, c)]++;
+            for (int i = it.s0; i < it.s1; ++i) {
+                const SrcEnt& e = L.src_fwd[i];
+                CHECK(e.row >= it.y0 && e.row < it.y1 && e.col >= c0 && e.col < c1, "single-step source outside its item");
+                CHECK(i == it.s0 || L.src_fwd[i - 1].row <= e.row, "single-step sources not sorted");
+            }
+        }
+    for (int y = 0; y < l.nyt; ++y)
+        for (int c = 0; c < l.pitch; ++c) {
+            const bool upd = y >= l.dn && c >= l.off && c < l.off + l.nxt;
+            CHECK(own[at(y, c)] == (upd ? 1 : 0), "single step: cell (%d,%d) updated %d times (ny %d nx %d acc %d dpml %d)",
+                  y, c, own[at(y, c)], ny, nx, acc, dpml);
+        }
+    if (fband <= 0) return;
+
+    // two-step lists
+    std::fill(own.begin(), own.end(), 0);
+    const int ylast = l.nyt - l.dn - R;  // first leftover row
+    for (size_t k = 0; k < L.fus_fwd.size(); ++k) {
+        const WorkItem& it = L.fus_fwd[k];
+        const int x0 = it.tile;
+        CHECK(it.kind == 4 && x0 % 4 == 0, "two-step tile misaligned");
+        CHECK(it.y0 >= l.dn && it.y1 <= ylast, "two-step tile rows outside [dn, nyt-dn-R)");
+        // reads: p_n rows [y0-2R-1, y1+2R], columns [x0-8, x0+128)
+        const long long lo = (long long)(it.y0 - 2 * R - 1) * l.pitch + x0 - 8;
+        const long long hi = (long long)(it.y1 + 2 * R) * l.pitch + x0 + 128;
+        CHECK(lo >= 0 && hi <= (long long)n, "two-step tile reads outside the field");
+        // first-step cells used by the second step are plain interior cells
+        const int ca = std::max(x0, xa) - R, cb = std::min(x0 + 120, xb) + R;
+        CHECK(ca >= l.off + l.dn && cb <= l.off + l.dn + l.nx, "two-step halo columns not plain");
+        CHECK(it.y1 + R <= l.nyt - l.dn, "two-step halo rows reach the bottom pad");
+        for (int y = it.y0; y < it.y1; ++y)
+            for (int c = std::max(x0, xa); c < std::min(x0 + 120, xb); ++c) own[at(y, c)]++;
+        if ((int)k < L.ncore)
+            for (int y = it.y0 - 2 * R - 1; y <= it.y1 + 2 * R; ++y)
+                for (int c = x0 - 8; c < x0 + 128; ++c) {
+                    const bool top = y < l.dn, two = y < ylast && c >= xa && c < xb;
+                    CHECK(top || two, "core tile reads single-step cell (%d,%d)", y, c);
+                }
+        for (int i = it.s0; i < it.s1; ++i) {
+            const SrcEnt& e = L.src_fwd[i];
+            CHECK(e.row >= it.y0 - R && e.row < it.y1 + R && e.col >= x0 - 4 && e.col < x0 + 124,
+                  "two-step source outside the first-step region");
+            CHECK(i == it.s0 || L.src_fwd[i - 1].row <= e.row, "two-step sources not sorted");
+        }
+        for (int i = it.r0; i < it.r1; ++i) {
+            const RecEnt& r = L.recs[i];
+            CHECK(r.row >= it.y0 && r.row < it.y1 && r.col >= std::max(x0, xa) && r.col < std::min(x0 + 120, xb),
+                  "two-step receiver outside the stored cells");
+            CHECK(i == it.r0 || L.recs[i - 1].row <= r.row, "two-step receivers not sorted");
+        }
+    }
+    for (const WorkItem& it : L.lft_fwd) {
+        int c0, c1;
+        item_cols(it, l, c0, c1);
+        for (int y = it.y0; y < it.y1; ++y)
+            for (int c = c0; c < c1; ++c) own[at(y, c)]++;
+    }
+    if (xa < xb)
+        for (int y = 0; y < l.nyt; ++y)
+            for (int c = 0; c < l.pitch; ++c) {
+                const bool in = y >= l.dn && y < l.dn + ny && c >= xa && c < xb;
+                CHECK(own[at(y, c)] == (in ? 1 : 0), "two-step: cell (%d,%d) stored %d times (two_step_ok %d)", y, c,
+                      own[at(y, c)], (int)two_step_ok(l));
+            }
+    if (two_step_ok(l)) CHECK(!L.fus_fwd.empty(), "a two-step shot without tiles");
+}
+
+}  // namespace
+
+int main() {
+    check(400, 2000, 3, 20, 5, 16, 64);
+    check(400, 2000, 4, 20, 5, 16, 64);
+    check(37, 61, 3, 20, 3, 32, 48);
+    check(12, 90, 4, 8, 3, 16, 64);
+    int cases = 4;
+    for (int nx = 20; nx < 400 && !fails; nx += 7)
+        for (int dpml : {1, 5, 10, 20, 25, 30, 40, 54})
+            for (int acc : {3, 4}) {
+                if (dpml + 2 * acc > MAXDN - 2) continue;
+                check(6 + nx % 53, nx, acc, dpml, 4, 8 + nx % 40, 16 + nx % 50);
+                ++cases;
+                if (fails) break;
+            }
+    if (fails) return 1;
+    std::printf("all ok (%d grids)\n", cases);
+    return 0;
+}

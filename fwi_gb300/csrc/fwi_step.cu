@@ -194,6 +194,51 @@ __device__ __forceinline__ void record_row(const StepParams& P, const ShotDev& S
     }
 }
 
+// Injected values of row y for the warp's 128 columns starting at physical
+// column c0 (entries sorted by row, one per cell, all inside those columns;
+// the cursor si at the first entry of row y).  The lanes take the row's
+// entries 32 at a time and scatter their values into the warp's line `inj`
+// (a float4 per lane, entry [1 + lane] for lane l's columns c0 + 4l ..);
+// each lane then reads its own float4.  Called by the whole warp when srow == y.
+__device__ __forceinline__ float4 gather_sources(const StepParams& P, const ShotDev& S, int y, int c0, int t, int& si,
+                                                 int s1, int& srow, float4* inj, int lane) {
+    inj[1 + lane] = make_float4(0.f, 0.f, 0.f, 0.f);
+    __syncwarp();
+    while (srow == y) {
+        const int i = si + lane;
+        bool mine = false;
+        if (i < s1) {
+            const SrcEnt e = P.srcs[i];
+            mine = e.row == y;
+            if (mine) reinterpret_cast<float*>(inj + 1)[e.col - c0] = __ldg(S.srcv + (size_t)e.vidx * S.nt + t);
+        }
+        si += __popc(__ballot_sync(FULL, mine));  // the row's entries are consecutive
+        srow = (si < s1) ? P.srcs[si].row : INT_MAX;
+    }
+    __syncwarp();
+    return inj[1 + lane];
+}
+
+// Receivers of row y (entries sorted by row, the cursor ri at the first one
+// of row y): p_3 of the warp's 128 columns starting at physical column c0 is
+// in `line` (entry [1 + lane] for lane l's columns c0 + 4l ..), visible to
+// the whole warp; the lanes take the row's receivers 32 at a time.  Called by
+// the whole warp when rrow == y.
+__device__ __forceinline__ void record_row_par(const StepParams& P, const ShotDev& S, int y, int c0, int t, int& ri,
+                                               int r1, int& rrow, const float4* line, int lane) {
+    while (rrow == y) {
+        const int i = ri + lane;
+        bool mine = false;
+        if (i < r1) {
+            const RecEnt r = P.recs[i];
+            mine = r.row == y;
+            if (mine) S.rec[(size_t)r.ridx * S.nt + t] = reinterpret_cast<const float*>(line + 1)[r.col - c0];
+        }
+        ri += __popc(__ballot_sync(FULL, mine));  // the row's entries are consecutive
+        rrow = (ri < r1) ? P.recs[ri].row : INT_MAX;
+    }
+}
+
 }  // namespace
 
 // Per-lane asynchronous prefetch of the rows a warp will need (cp.async,
@@ -463,8 +508,9 @@ __device__ __forceinline__ void interior_update2(const float4* q, float4 L, floa
 constexpr int IN_P = 0, IN_P1 = 32, IN_C2 = 64, IN_HL = 96, IN_HR = 97, IN_F = 98, IN_FS = 130, IN_K = 131;
 constexpr int IN_SIZE = 98, IN_SIZE_IMG = 195;
 constexpr int IN_DEPTH = 6, IN_DEPTH_IMG = 4;
-constexpr int IN_SMEM = 4 * IN_DEPTH * IN_SIZE * 16;
-constexpr int IN_SMEM_IMG = 4 * IN_DEPTH_IMG * IN_SIZE_IMG * 16;
+constexpr int IN_LINE = 34;  // per warp after its ring: injected values / p_3 of a row, [1 + lane]
+constexpr int IN_SMEM = 4 * (IN_DEPTH * IN_SIZE + IN_LINE) * 16;
+constexpr int IN_SMEM_IMG = 4 * (IN_DEPTH_IMG * IN_SIZE_IMG + IN_LINE) * 16;
 
 __device__ __forceinline__ void cp4(void* smem_dst, const void* gmem_src) {
     const unsigned d = (unsigned)__cvta_generic_to_shared(smem_dst);
@@ -484,7 +530,8 @@ __global__ void __launch_bounds__(128, (MODE == 1 && SNAP) ? 3 : 5) k_step_inter
     const int lane = threadIdx.x & 31;
     const int wid = blockIdx.x * 4 + (threadIdx.x >> 5);
     if (wid >= P.nitems) return;
-    float4* ring = smem + (threadIdx.x >> 5) * (DEPTH * SZ);
+    float4* ring = smem + (threadIdx.x >> 5) * (DEPTH * SZ + IN_LINE);
+    float4* line = ring + DEPTH * SZ;
     const WorkItem it = P.items[wid];
     const ShotDev& S = P.shots[it.shot];
     const int pitch = S.pitch;
@@ -562,19 +609,7 @@ __global__ void __launch_bounds__(128, (MODE == 1 && SNAP) ? 3 : 5) k_step_inter
 
         // source injection: source(nys,nxs) = S(k-1,j)  (solver_acoustic_SS.f90:319-330)
         float sv[4] = {0.f, 0.f, 0.f, 0.f};
-        while (srow == y) {
-            const SrcEnt s = P.srcs[si];
-            if ((s.col >> 2) == (xl >> 2)) {
-                const float val = __ldg(S.srcv + (size_t)s.vidx * S.nt + P.t);
-                const int el = s.col & 3;
-                sv[0] = el == 0 ? val : sv[0];
-                sv[1] = el == 1 ? val : sv[1];
-                sv[2] = el == 2 ? val : sv[2];
-                sv[3] = el == 3 ? val : sv[3];
-            }
-            ++si;
-            srow = (si < it.s1) ? P.srcs[si].row : INT_MAX;
-        }
+        if (srow == y) to_arr(gather_sources(P, S, y, x0, P.t, si, it.s1, srow, line, lane), sv);
         // p_3 = -p_1 + 2p + (d2x + d2y + source)*c2  (:433-434)
         float p3[4];
         interior_update2<R>(q, Lf, Rf, from_arr(pm1), from_arr(cc), sv, cp, p3);
@@ -637,7 +672,13 @@ __global__ void __launch_bounds__(128, (MODE == 1 && SNAP) ? 3 : 5) k_step_inter
             for (int e = 0; e < 4; ++e)
                 if (e >= lo && e < hi) PO[(size_t)y * pitch + e] = p3[e];
         }
-        if (MODE == 0 && P.record) record_row(P, S, y, xl, ri, it.r1, rrow, p3);
+        // receivers: every receiver in this cell gets p_3 (:551-555)
+        if (MODE == 0 && P.record && rrow == y) {
+            line[1 + lane] = from_arr(p3);
+            __syncwarp();
+            record_row_par(P, S, y, x0, P.t, ri, it.r1, rrow, line, lane);
+            __syncwarp();
+        }
 
 #pragma unroll
         for (int i = 0; i < 2 * R; ++i) q[i] = q[i + 1];
@@ -1101,50 +1142,7 @@ struct F2Ring {
     static constexpr int SMEM = 4 * WARP * 16;
 };
 
-// Injected values of row y for the warp's 128 columns starting at physical
-// column c0 (entries sorted by row, one per cell, all inside those columns;
-// the cursor si at the first entry of row y).  The lanes take the row's
-// entries 32 at a time and scatter their values into the warp's line `inj`
-// (a float4 per lane, entry [1 + lane] for lane l's columns c0 + 4l ..);
-// each lane then reads its own float4.  Called by the whole warp when srow == y.
-__device__ __forceinline__ float4 gather_sources(const StepParams& P, const ShotDev& S, int y, int c0, int t, int& si,
-                                                 int s1, int& srow, float4* inj, int lane) {
-    inj[1 + lane] = make_float4(0.f, 0.f, 0.f, 0.f);
-    __syncwarp();
-    while (srow == y) {
-        const int i = si + lane;
-        bool mine = false;
-        if (i < s1) {
-            const SrcEnt e = P.srcs[i];
-            mine = e.row == y;
-            if (mine) reinterpret_cast<float*>(inj + 1)[e.col - c0] = __ldg(S.srcv + (size_t)e.vidx * S.nt + t);
-        }
-        si += __popc(__ballot_sync(FULL, mine));  // the row's entries are consecutive
-        srow = (si < s1) ? P.srcs[si].row : INT_MAX;
-    }
-    __syncwarp();
-    return inj[1 + lane];
-}
 
-// Receivers of row y (entries sorted by row, the cursor ri at the first one
-// of row y): p_3 of the warp's 128 columns starting at physical column c0 is
-// in `line` (entry [1 + lane] for lane l's columns c0 + 4l ..), visible to
-// the whole warp; the lanes take the row's receivers 32 at a time.  Called by
-// the whole warp when rrow == y.
-__device__ __forceinline__ void record_row_par(const StepParams& P, const ShotDev& S, int y, int c0, int t, int& ri,
-                                               int r1, int& rrow, const float4* line, int lane) {
-    while (rrow == y) {
-        const int i = ri + lane;
-        bool mine = false;
-        if (i < r1) {
-            const RecEnt r = P.recs[i];
-            mine = r.row == y;
-            if (mine) S.rec[(size_t)r.ridx * S.nt + t] = reinterpret_cast<const float*>(line + 1)[r.col - c0];
-        }
-        ri += __popc(__ballot_sync(FULL, mine));  // the row's entries are consecutive
-        rrow = (ri < r1) ? P.recs[ri].row : INT_MAX;
-    }
-}
 
 // SNAP: the first of the two steps stores a snapshot (MODE 0, FP32 form) or
 // applies the imaging condition (MODE 1) at the tile's own cells, as

@@ -587,11 +587,6 @@ int run_range(int acc, int mode, int k0, int k1, SnOf sn_of, StepSet& ps, const 
     return FWI_OK;
 }
 
-int run_plain_range(int acc, int mode, int k0, int k1, StepSet& ps, const TwoStep* tw, cudaStream_t st,
-                    cudaStream_t st2) {
-    return run_range(acc, mode, k0, k1, [](int) { return -1; }, ps, tw, st, st2);
-}
-
 // One pass over the time loop k = 2..nt for a set of shots.
 // mode 0: forward (snapshots if store, receivers recorded); mode 1: adjoint.
 // tw: two-step passes (null: single steps only).

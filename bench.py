@@ -16,6 +16,7 @@ host cores, one shot per thread, on a bounded number of time steps.
 from __future__ import annotations
 
 import argparse
+import copy
 import ctypes as C
 import json
 import os
@@ -310,7 +311,16 @@ def main():
     F.set_stream(stream.cuda_stream)
     snap_form = {"f32": F.SNAP_F32, "bf16": F.SNAP_BF16, "f16": F.SNAP_F16}[a.snap]
     budget = int(a.budget * 1e9)
-    spec, vp_true, vp0 = make_workload(a, rank)
+    # N > 1: one survey of N x (the workload's shots) on one model, shot ranges
+    # split over the ranks (each rank holds one copy of the workload's shots),
+    # the gradient stack and misfit summed over the ranks in every step
+    spec, vp_true, vp0 = make_workload(a)
+    global_spec = None
+    if world > 1:
+        from fwi_gb300 import multi
+        global_spec = copy.copy(spec)
+        global_spec.shots = list(spec.shots) * world
+        spec, _ = multi.shard_spec(global_spec, rank, world)
     lam_true, lam0 = lam_from_vp(vp_true), lam_from_vp(vp0)
 
     if a.profile:
@@ -340,8 +350,13 @@ def main():
     sv.set_lambda(lam0_dev.data_ptr())
     grad_dev = torch.zeros(spec.ny * spec.nx_model, dtype=torch.float32, device="cuda")
 
+    grad_host = np.zeros((spec.ny, spec.nx_model), np.float32, order="F")
+
     def step():
-        return sv.run_device_grad(1, grad_dev.data_ptr())
+        if world == 1:
+            return sv.run_device_grad(1, grad_dev.data_ptr())
+        grad_host[...] = 0.0
+        return multi.misfit_gradient(sv, global_spec, 1, grad_host)[0]
 
     for _ in range(a.warmup):
         step()
@@ -457,6 +472,10 @@ def main():
                                                C.c_void_p(h_grad.ctypes.data))
             if rc:
                 raise F.FwiError(rc, lib.fwi_last_error().decode())
+            if world > 1:  # the ranks' gradients summed (the reference's MPI_REDUCE of Grad)
+                tg = torch.from_numpy(h_grad).cuda()
+                torch.distributed.all_reduce(tg)
+                h_grad[:] = tg.cpu().numpy()
         for _ in range(a.warmup):
             e2e_step()
         torch.cuda.synchronize()

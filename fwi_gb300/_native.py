@@ -29,7 +29,7 @@ EXPORTS = [
     "fwi_kernel_launch_count", "fwi_solver_acoustic_ss", "fwi_misfit_function", "fwi_beta_calculous",
     "fwi_mcs_geometry", "fwi_ricker", "fwi_time_rules", "fwi_survey_create", "fwi_survey_destroy",
     "fwi_survey_set_lambda", "fwi_survey_set_observed", "fwi_survey_set_sources", "fwi_survey_run",
-    "fwi_survey_grad_device", "fwi_survey_get_synthetic", "fwi_survey_step_bytes", "fwi_survey_two_step_bytes", "fwi_survey_tuning",
+    "fwi_survey_grad_device", "fwi_survey_get_stack", "fwi_survey_get_synthetic", "fwi_survey_step_bytes", "fwi_survey_two_step_bytes", "fwi_survey_tuning",
     "fwi_survey_recompute", "fwi_survey_set_time", "fwi_time_filter", "fwi_set_filter_order",
     "fwi_interpolation_akima", "fwi_su_info", "fwi_su_read", "fwi_su_write", "fwi_read_nav",
     "fwi_survey_time_steps", "fwi_misfit_gradient_batch", "fwi_solver_forward_noalloc",
@@ -96,6 +96,7 @@ def load():
     lib.fwi_read_nav.argtypes = [C.c_char_p, I, P, P, P, P]
     lib.fwi_survey_run.argtypes = [P, I, P, P]
     lib.fwi_survey_grad_device.argtypes = [P, C.POINTER(C.c_void_p)]
+    lib.fwi_survey_get_stack.argtypes = [P, C.c_void_p]
     lib.fwi_survey_get_synthetic.argtypes = [P, I, P]
     lib.fwi_survey_step_bytes.argtypes = [P, C.POINTER(C.c_double)]
     lib.fwi_survey_two_step_bytes.argtypes = [P, C.POINTER(C.c_double), C.POINTER(C.c_double)]

@@ -292,6 +292,13 @@ class Survey:
         N.check(N.load().fwi_survey_get_synthetic(self.handle, shot, _p(out)))
         return out
 
+    def stack(self):
+        """The FP64 gradient stack of the last step-1 run, (ny, nx_model) Fortran
+        order, before the numtasks divisor and the water mask."""
+        out = np.zeros((self.spec.ny, self.spec.nx_model), np.float64, order="F")
+        N.check(N.load().fwi_survey_get_stack(self.handle, _p(out)))
+        return out
+
     def grad_stack_device_ptr(self):
         p = C.c_void_p()
         N.check(N.load().fwi_survey_grad_device(self.handle, C.byref(p)))

@@ -1764,6 +1764,15 @@ int fwi_survey_grad_device(fwi_survey* s, const double** ptr) {
     return FWI_OK;
 }
 
+int fwi_survey_get_stack(fwi_survey* s, double* out) {
+    std::lock_guard<std::recursive_mutex> g(L().mu);
+    if (!s || !out) return fail(FWI_ERR_STATE, "null argument");
+    const size_t n = (size_t)s->desc.ny * s->desc.nx_model * sizeof(double);
+    CK(cudaMemcpyAsync(out, s->d_G.p, n, cudaMemcpyDeviceToHost, stream()));
+    CK(cudaStreamSynchronize(stream()));
+    return FWI_OK;
+}
+
 int fwi_survey_get_synthetic(fwi_survey* s, int shot, float* out) {
     std::lock_guard<std::recursive_mutex> g(L().mu);
     if (!s || !out) return fail(FWI_ERR_STATE, "null argument");

@@ -239,6 +239,10 @@ int fwi_survey_run(fwi_survey* s, int step, double* misfit, float* grad);
 /* Device pointer to the FP64 gradient stack of the last run
  * ((ny, nx_model) column-major, before the numtasks divisor and mask). */
 int fwi_survey_grad_device(fwi_survey* s, const double** ptr);
+/* The same FP64 stack copied to host memory (ny*nx_model doubles, column-
+ * major): the per-rank term of the reference's MPI_REDUCE of Grad
+ * (calculate_misfit_gradient.f90:299-300) when shots are split over ranks. */
+int fwi_survey_get_stack(fwi_survey* s, double* out);
 /* Synthetic traces of shot i from the last run: Rec_point(nt, num_rec),
  * copied to host. */
 int fwi_survey_get_synthetic(fwi_survey* s, int shot, float* out);

@@ -40,19 +40,20 @@ def parse():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--config", type=int, choices=[2, 3, 4, 5], default=2,
-                    help="2: batched MCS survey (the metric's workload); 3: uneven-window WAS batch; "
-                         "4: config 2 in the precision form (snapshots every 4 steps in 16 bits, checkpointed "
-                         "recomputation under a 120 GB budget); 5: NLCG inversion with frequency continuation")
-    ap.add_argument("--budget", type=float, default=0.0, help="HBM budget in GB (0: all; config 4: 120)")
-    ap.add_argument("--recompute", action="store_true", help="checkpointed recomputation (config 4: on)")
-    ap.add_argument("--iters", type=int, default=10, help="config 5: NLCG iterations per band")
-    ap.add_argument("--bands", default="3,5,7", help="config 5: low-pass corner frequencies (Hz), one band each")
-    ap.add_argument("--order", type=int, default=4, help="config 5: Butterworth order")
-    ap.add_argument("--shots", type=int, default=0, help="shots (0 = the config's: 64 or 30)")
-    ap.add_argument("--nt", type=int, default=0, help="time steps (0 = the config's: 6000 or 12800)")
+    ap.add_argument("--workload", choices=["mcs", "was", "mcs-f16", "inversion"], default="mcs",
+                    help="mcs: batched MCS survey, 400x2000 cells, 64 shots, 6000 steps (the metric's workload); "
+                         "was: uneven-window WAS batch; mcs-f16: the MCS survey with snapshots every 4 steps in "
+                         "16 bits and checkpointed recomputation under a 120 GB budget; inversion: NLCG inversion "
+                         "with frequency continuation (600x3000 cells, 128 shots)")
+    ap.add_argument("--budget", type=float, default=0.0, help="HBM budget in GB (0: all; mcs-f16: 120)")
+    ap.add_argument("--recompute", action="store_true", help="checkpointed recomputation (mcs-f16: on)")
+    ap.add_argument("--iters", type=int, default=10, help="inversion: NLCG iterations per band")
+    ap.add_argument("--bands", default="3,5,7", help="inversion: low-pass corner frequencies (Hz), one band each")
+    ap.add_argument("--order", type=int, default=4, help="inversion: Butterworth order")
+    ap.add_argument("--shots", type=int, default=0, help="shots (0 = the workload's: 64 or 30)")
+    ap.add_argument("--nt", type=int, default=0, help="time steps (0 = the workload's: 6000 or 12800)")
     ap.add_argument("--snap", choices=["f32", "bf16", "f16"], default=None,
-                    help="snapshot form (default f32; config 4: f16)")
+                    help="snapshot form (default f32; mcs-f16: f16)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg")
     ap.add_argument("--no-plain", action="store_true", help="skip the plain-path leg")
@@ -61,7 +62,7 @@ def parse():
     ap.add_argument("--wave", type=int, default=0, help="shots per wave (0 = tuner)")
     ap.add_argument("--band", type=int, default=0, help="rows per warp work item (0 = tuner)")
     a = ap.parse_args()
-    if a.config == 4:
+    if a.workload == "mcs-f16":
         a.snap = a.snap or "f16"
         a.budget = a.budget or 120.0
         a.recompute = True
@@ -70,11 +71,11 @@ def parse():
 
 
 def workload_name(a):
-    if a.config == 3:
+    if a.workload == "was":
         return (f"uneven-window WAS batch: 600x6000 cells @25 m crustal model, {a.shots} OBS sources on 30-100 km "
                 f"windows, 1200 receivers @125 m, nt={a.nt} (dt=1.5625 ms, the CFL rule; 2.5 ms is unstable), "
                 f"acc=3, dPML=20, store_snap=10, {a.snap} snapshots, FP64 gradient stack")
-    if a.config == 4:
+    if a.workload == "mcs-f16":
         return (f"precision form of the batched MCS survey: 400x2000 cells @12.5 m, {a.shots} shots x 480 ch, "
                 f"nt={a.nt} (dt=1 ms), acc=3, dPML=20, store_snap=4, {a.snap} snapshots with a power-of-two scale "
                 f"per row segment, checkpointed recomputation under a {a.budget:g} GB HBM budget, FP64 stack")
@@ -84,15 +85,15 @@ def workload_name(a):
 
 def make_workload(a, seed_offset=0):
     from fwi_gb300 import synth
-    if a.config == 3:
+    if a.workload == "was":
         a.shots = a.shots or 30
-        spec, vp_true, vp0 = synth.config3(seed=3 + seed_offset, nt=a.nt or None, nshots=a.shots)
+        spec, vp_true, vp0 = synth.was_batch(seed=3 + seed_offset, nt=a.nt or None, nshots=a.shots)
         a.nt = spec.nt
     else:
         a.shots = a.shots or 64
         a.nt = a.nt or 6000
-        spec, vp_true, vp0 = synth.config2(seed=2 + seed_offset, nshots=a.shots, nt=a.nt,
-                                           store_snap=4 if a.config == 4 else 10)
+        spec, vp_true, vp0 = synth.mcs_batch(seed=2 + seed_offset, nshots=a.shots, nt=a.nt,
+                                           store_snap=4 if a.workload == "mcs-f16" else 10)
     return spec, vp_true, vp0
 
 
@@ -107,7 +108,7 @@ def peaks():
 
 def traffic_from_profile():
     """DRAM bytes per step launch pair from the committed ncu summary."""
-    path = os.path.join(ROOT, "profiles", "step_kernels_config2.md")
+    path = os.path.join(ROOT, "profiles", "step_kernels_mcs64_400x2000.md")
     try:
         for line in open(path):
             if line.startswith("traffic_bytes_per_step_per_shot:"):
@@ -197,7 +198,7 @@ def run_reference(a):
         return 0
     spec, vp_true, vp0 = make_workload(a)
     nthreads = os.cpu_count() or 1
-    nt_sample = 100 if a.config in (2, 4) else 40
+    nt_sample = 100 if a.workload in ("mcs", "mcs-f16") else 40
     for _ in range(a.warmup):
         cpu_sample(spec, vp0, nthreads, nt_sample)
     times = []
@@ -240,7 +241,7 @@ def run_inversion(a):
     F.set_stream(stream.cuda_stream)
     snap_form = {"f32": F.SNAP_F32, "bf16": F.SNAP_BF16, "f16": F.SNAP_F16}[a.snap]
     nshots, nt = a.shots or 128, a.nt or 8000
-    spec, vp_true, vp0 = synth.config5(nshots=nshots, nt=nt)
+    spec, vp_true, vp0 = synth.inversion_workload(nshots=nshots, nt=nt)
     lam_t, lam0 = synth.lam_from_vp(vp_true), synth.lam_from_vp(vp0)
     # observed data on the true model at the acquisition sampling (untimed)
     sv = F.Survey(spec)
@@ -287,13 +288,13 @@ def run_inversion(a):
 
 def main():
     a = parse()
-    if a.impl == "reference" and a.config == 5:
-        print(json.dumps({"impl": "reference", "unavailable": "config 5 is an inversion run; the CPU reference "
-                          "arm times the gradient path (configs 2 and 3)"}))
+    if a.impl == "reference" and a.workload == "inversion":
+        print(json.dumps({"impl": "reference", "unavailable": "the inversion workload is an NLCG run; the CPU "
+                          "reference arm times the gradient path (the mcs and was workloads)"}))
         return 0
     if a.impl == "reference":
         return run_reference(a)
-    if a.config == 5:
+    if a.workload == "inversion":
         return run_inversion(a)
     import torch
 
@@ -403,7 +404,7 @@ def main():
     achieved = bytes_step / step_s / 1e9
     tr = traffic_from_profile()
     roof = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
-            "traffic": tr * wave if (tr and a.config in (2, 4)) else None,
+            "traffic": tr * wave if (tr and a.workload in ("mcs", "mcs-f16")) else None,
             "kernel": "one time step of all shots of a wave, run as two-step passes: k_step2_interior (model-row "
                       "interior, two steps per sweep) beside k_step_strip + k_step_bottom + k_step_interior "
                       "(single-step lists, twice per pass)",
@@ -422,8 +423,8 @@ def main():
         from fwi_gb300.survey import SurveySpec
         one = SurveySpec(ny=spec.ny, nx_model=spec.nx_model, d=spec.d, dt=spec.dt, nt=spec.nt, shots=[spec.shots[0]],
                          store_snap=spec.store_snap, acc=spec.acc, dpml=spec.dpml, water_rows=spec.water_rows)
-        # config 4 compares with the FP32-snapshot plain path
-        pv = F.Survey(one, snap_form=F.SNAP_F32 if a.config == 4 else snap_form, graph=False)
+        # the 16-bit form compares with the FP32-snapshot plain path
+        pv = F.Survey(one, snap_form=F.SNAP_F32 if a.workload == "mcs-f16" else snap_form, graph=False)
         pv.set_lambda(lam0_dev.data_ptr())
         pv.run_device_grad(1, grad_dev.data_ptr())
         torch.cuda.synchronize()
@@ -498,7 +499,7 @@ def main():
     cpu = None
     if rank == 0 and world == 1 and not a.no_cpu:
         nthreads = os.cpu_count() or 1
-        rate, tcpu, desc = cpu_sample(spec, vp0, nthreads, 600 if a.config in (2, 4) else 150)
+        rate, tcpu, desc = cpu_sample(spec, vp0, nthreads, 600 if a.workload in ("mcs", "mcs-f16") else 150)
         cpu = {"value": rate, "unit": METRIC, "cores": nthreads, "kind": "port", "sample": desc,
                "seconds": tcpu}
 

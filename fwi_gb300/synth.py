@@ -1,8 +1,8 @@
-"""Seeded synthetic models and acquisition geometries of the benchmark configs.
+"""Seeded synthetic models and acquisition geometries of the benchmark workloads.
 
 The reference ships no data (its sample datasets are not published), so the
 workloads are synthetic with the shapes, sizes and value ranges of each
-config; receiver and source grid indices are computed with the reference's
+workload; receiver and source grid indices are computed with the reference's
 own FP32 rules (fwi_mcs_geometry).  Observed data are synthesised from the
 true model by the same solver.
 """
@@ -27,7 +27,7 @@ def ricker_shifted(freq, dt, nt, shift):
     return w
 
 
-def model_config1(seed=1, anomaly=True):
+def model_single_shot(seed=1, anomaly=True):
     """200 x 400 at 25 m: 500 m of water at 1500 m/s over a linear gradient
     1800 -> 4500 m/s, plus a +200 m/s Gaussian anomaly (sigma 300 m) at
     (x=5 km, z=2.5 km) with a seeded position jitter (+-100 m)."""
@@ -105,10 +105,10 @@ def mcs_survey(vp, d, dt, nt, xs_list, nrec, drec, near=150.0, sdepth=10.0, rdep
                       dpml=dpml, water_rows=wr)
 
 
-def config1(seed=1):
-    """Plain single shot (BASELINE config 1): returns (spec, vp_true, vp_start)."""
-    vp_true, wrows = model_config1(seed, anomaly=True)
-    vp0, _ = model_config1(seed, anomaly=False)
+def single_shot(seed=1):
+    """Plain single shot (200 x 400 cells, 8th order, 3000 steps): returns (spec, vp_true, vp_start)."""
+    vp_true, wrows = model_single_shot(seed, anomaly=True)
+    vp0, _ = model_single_shot(seed, anomaly=False)
     rng = np.random.default_rng(seed + 100)
     spec = mcs_survey(vp_true, 25.0, 0.002, 3000, [2637.5 + 25.0 * int(rng.integers(0, 40))], 200, 12.5, near=150.0,
                       sdepth=10.0, rdepth=10.0, freq=8.0, acc=4, dpml=20, seed=seed, water_rows=wrows,
@@ -116,8 +116,8 @@ def config1(seed=1):
     return spec, vp_true, vp0
 
 
-def config2(seed=2, nshots=64, nt=6000, store_snap=10):
-    """Batched MCS survey (BASELINE config 2): 400 x 2000 at 12.5 m, 64 shots
+def mcs_batch(seed=2, nshots=64, nt=6000, store_snap=10):
+    """Batched MCS survey: 400 x 2000 at 12.5 m, 64 shots
     at 250 m spacing, 480 channels at 12.5 m, 6 s at dt = 1 ms, 10 Hz.
     Returns (spec, vp_true, vp_start) where the start model is the true
     model smoothed laterally and vertically."""
@@ -128,8 +128,8 @@ def config2(seed=2, nshots=64, nt=6000, store_snap=10):
     return spec, vp_true, smooth(vp_true, 8)
 
 
-def config5(seed=5, nshots=128, nt=8000, store_snap=10, window_margin=2000.0):
-    """Full-inversion workload (BASELINE config 5): 600 x 3000 at 12.5 m, a
+def inversion_workload(seed=5, nshots=128, nt=8000, store_snap=10, window_margin=2000.0):
+    """Full-inversion workload: 600 x 3000 at 12.5 m, a
     layered model with two Gaussian low-velocity lenses, 128 MCS shots of 480
     channels at 12.5 m, 8 s records at dt = 1 ms, 10 Hz Ricker.  Each shot
     propagates on its own window: from window_margin metres behind the last
@@ -219,8 +219,8 @@ def model_crustal(seed=3, ny=600, nx=6000, d=25.0):
     return _F(vp), sea
 
 
-def config3(seed=3, nt=None, nshots=30, freq=5.0, tfin=20.0):
-    """Uneven-size WAS batch (BASELINE config 3) with OBS as reciprocal
+def was_batch(seed=3, nt=None, nshots=30, freq=5.0, tfin=20.0):
+    """Uneven-size WAS batch with OBS as reciprocal
     sources: 30 OBS at 5 km on the seafloor, 1200 surface receivers at 125 m
     (10 m deep), each shot on its own window of 30-100 km (seeded).  The
     stated dt = 2.5 ms violates the CFL limit at 8 km/s and 25 m, so the

@@ -50,9 +50,9 @@ def _both(spec, vp):
     return out
 
 
-def test_config1_full_run_bit_exact():
+def test_single_shot_full_run_bit_exact():
     from fwi_gb300 import synth
-    spec, vp_true, vp0 = synth.config1()
+    spec, vp_true, vp0 = synth.single_shot()
     assert (spec.ny, spec.nx_model, spec.nt, spec.acc) == (200, 400, 3000, 4)
     r = _both(spec, vp0)
     for a, b in zip(r["gpu"], r["oracle"]):
@@ -60,9 +60,9 @@ def test_config1_full_run_bit_exact():
     assert np.abs(r["gpu"][0]).max() > 0 and np.abs(r["gpu"][2]).max() > 0
 
 
-def test_config2_shot_truncated_bit_exact():
+def test_mcs_shot_truncated_bit_exact():
     from fwi_gb300 import synth
-    spec, vp_true, vp0 = synth.config2(nshots=1, nt=300)
+    spec, vp_true, vp0 = synth.mcs_batch(nshots=1, nt=300)
     r = _both(spec, vp0)
     for a, b in zip(r["gpu"], r["oracle"]):
         np.testing.assert_array_equal(a, b)
@@ -86,10 +86,10 @@ def _rel(a, b):
     return float(np.linalg.norm((a - b).astype(np.float64)) / np.linalg.norm(b.astype(np.float64)))
 
 
-def test_config2_full_grid_properties():
+def test_mcs_full_grid_properties():
     from fwi_gb300 import synth
     from fwi_gb300.synth import lam_from_vp
-    spec, vp_true, vp0 = synth.config2(nshots=4, nt=1200)
+    spec, vp_true, vp0 = synth.mcs_batch(nshots=4, nt=1200)
     lam_t, lam0 = lam_from_vp(vp_true), lam_from_vp(vp0)
     # observed data from the true model
     import fwi_gb300 as F
@@ -116,14 +116,14 @@ def test_config2_full_grid_properties():
         np.testing.assert_array_equal(a, b)
 
 
-def test_config3_uneven_windows_truncated():
+def test_was_uneven_windows_truncated():
     """The ragged WAS batch: three shots on windows of different widths
     (narrow, median, widest) of the 600 x 6000 crustal model, OBS at the
     seafloor as sources; batched survey vs the oracle shot by shot."""
     import fwi_gb300 as F
     from fwi_gb300 import synth
     from fwi_gb300.synth import lam_from_vp
-    spec, vp_true, vp0 = synth.config3(nt=150)
+    spec, vp_true, vp0 = synth.was_batch(nt=150)
     order = np.argsort([s.nx for s in spec.shots])
     spec.shots = [spec.shots[i] for i in (order[0], order[len(order) // 2], order[-1])]
     # 150 steps are too short for the seafloor OBS to reach the surface

@@ -22,7 +22,7 @@ def test_precision_form_vs_fp64_oracle():
     import fwi_gb300 as F
     from fwi_gb300 import synth
     from fwi_gb300.synth import lam_from_vp
-    spec, vp_true, vp0 = synth.config2(nshots=2, nt=1200, store_snap=4)
+    spec, vp_true, vp0 = synth.mcs_batch(nshots=2, nt=1200, store_snap=4)
     for i, sh in enumerate(spec.shots):  # windows holding each streamer
         x0 = 20 * i
         sh.nxSou = sh.nxSou - x0

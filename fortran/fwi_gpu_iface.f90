@@ -96,6 +96,56 @@ module fwi_gpu_iface
        integer(c_int) :: nt_Data, NumRec, nt
      end function fwi_interpolation_akima
 
+     !! device-resident survey: create once per band, run once per gradient or
+     !! line-search trial (the driver loop of FWI.f90), destroy at the end
+     integer(c_int) function fwi_survey_create(desc, s) bind(C, name="fwi_survey_create")
+       import :: c_int, c_ptr, fwi_survey_desc
+       type(fwi_survey_desc) :: desc
+       type(c_ptr)           :: s
+     end function fwi_survey_create
+
+     integer(c_int) function fwi_survey_destroy(s) bind(C, name="fwi_survey_destroy")
+       import :: c_int, c_ptr
+       type(c_ptr), value :: s
+     end function fwi_survey_destroy
+
+     integer(c_int) function fwi_survey_set_lambda(s, lambda) bind(C, name="fwi_survey_set_lambda")
+       import :: c_int, c_ptr, c_float
+       type(c_ptr), value :: s
+       real(c_float)      :: lambda(*)
+     end function fwi_survey_set_lambda
+
+     integer(c_int) function fwi_survey_set_observed(s, obs_packed) bind(C, name="fwi_survey_set_observed")
+       import :: c_int, c_ptr, c_float
+       type(c_ptr), value :: s
+       real(c_float)      :: obs_packed(*)
+     end function fwi_survey_set_observed
+
+     !! the per-trial time axis (FWI.f90:225-230): resampled sources and observed traces
+     integer(c_int) function fwi_survey_set_time(s, dt, nt, src, obs) bind(C, name="fwi_survey_set_time")
+       import :: c_int, c_ptr, c_float
+       type(c_ptr), value    :: s
+       real(c_float), value  :: dt
+       integer(c_int), value :: nt
+       real(c_float)         :: src(*), obs(*)
+     end function fwi_survey_set_time
+
+     !! calculate_misfit_gradient: step 1 gradient, step 2 line-search trial
+     integer(c_int) function fwi_survey_run(s, step, misfit, grad) bind(C, name="fwi_survey_run")
+       import :: c_int, c_ptr, c_float, c_double
+       type(c_ptr), value    :: s
+       integer(c_int), value :: step
+       real(c_double)        :: misfit
+       real(c_float)         :: grad(*)
+     end function fwi_survey_run
+
+     !! the FP64 gradient stack of the last run (the rank's term of the MPI_REDUCE of Grad)
+     integer(c_int) function fwi_survey_get_stack(s, stack) bind(C, name="fwi_survey_get_stack")
+       import :: c_int, c_ptr, c_double
+       type(c_ptr), value :: s
+       real(c_double)     :: stack(*)
+     end function fwi_survey_get_stack
+
      type(c_ptr) function fwi_last_error() bind(C, name="fwi_last_error")
        import :: c_ptr
      end function fwi_last_error

@@ -542,32 +542,10 @@ int two_step_run(int acc, int mode, const TwoStep& tw, int k, int npass, const i
 template <typename SnOf>
 int run_range(int acc, int mode, int k0, int k1, SnOf sn_of, StepSet& ps, const TwoStep* tw, cudaStream_t st,
               cudaStream_t st2) {
-    struct Unit {
-        int k, sn;
-        bool pass;
-    };
-    std::vector<Unit> units;
-    int npass = 0;
-    for (int k = k0; k <= k1;) {
-        const int s0 = sn_of(k);
-        if (tw && k + 1 <= k1 && sn_of(k + 1) < 0 && (s0 < 0 || tw->snap_ok)) {
-            units.push_back({k, s0, true});
-            ++npass;
-            k += 2;
-        } else {
-            units.push_back({k, s0, false});
-            k += 1;
-        }
-    }
-    if (npass & 1) {  // the last pass becomes two single steps
-        for (size_t i = units.size(); i-- > 0;)
-            if (units[i].pass) {
-                const Unit u = units[i];
-                units[i] = {u.k, u.sn, false};
-                units.insert(units.begin() + i + 1, Unit{u.k + 1, -1, false});
-                break;
-            }
-    }
+    if (k1 < k0) return FWI_OK;
+    std::vector<int> sn(k1 + 2, -1);
+    for (int k = k0; k <= k1; ++k) sn[k] = sn_of(k);
+    const std::vector<StepUnit> units = plan_steps(k0, k1, sn, tw != nullptr, tw && tw->snap_ok);
     int pair = 0;
     std::vector<int> sns;
     for (size_t i = 0; i < units.size();) {

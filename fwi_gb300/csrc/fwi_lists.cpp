@@ -269,4 +269,30 @@ Lists build_lists(const std::vector<ShotGeom>& geoms, const std::vector<Layout>&
     return out;
 }
 
+std::vector<StepUnit> plan_steps(int k0, int k1, const std::vector<int>& sn, bool two_step, bool snap_ok) {
+    std::vector<StepUnit> units;
+    int npass = 0;
+    for (int k = k0; k <= k1;) {
+        const int s0 = sn[k];
+        if (two_step && k + 1 <= k1 && sn[k + 1] < 0 && (s0 < 0 || snap_ok)) {
+            units.push_back({k, s0, true});
+            ++npass;
+            k += 2;
+        } else {
+            units.push_back({k, s0, false});
+            k += 1;
+        }
+    }
+    if (npass & 1) {  // the last pass becomes two single steps
+        for (size_t i = units.size(); i-- > 0;)
+            if (units[i].pass) {
+                const StepUnit u = units[i];
+                units[i] = {u.k, u.sn, false};
+                units.insert(units.begin() + i + 1, StepUnit{u.k + 1, -1, false});
+                break;
+            }
+    }
+    return units;
+}
+
 }  // namespace fwi

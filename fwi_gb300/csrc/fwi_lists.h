@@ -59,4 +59,18 @@ bool two_step_ok(const Layout& l);
 // fband > 0 also builds the two-step lists (two-step tiles in bands of fband rows).
 Lists build_lists(const std::vector<ShotGeom>& geoms, const std::vector<Layout>& lays, int band_rows, int fband = 0);
 
+// One unit of a time loop: a two-step pass (steps k, k+1) or a single step
+// k; sn = the snapshot block step k stores or images with, -1 for none.
+struct StepUnit {
+    int k, sn;
+    bool pass;
+};
+
+// Steps k0..k1 (sn[k]: snapshot block of step k or -1; sn.size() > k1) as
+// two-step passes and single steps: a pair (k, k+1) is a pass when
+// two_step, step k+1 has no snapshot and step k has none or snap_ok; the
+// number of passes is even (the last one becomes two single steps when it
+// is not), so the state returns to the buffer pair it started in.
+std::vector<StepUnit> plan_steps(int k0, int k1, const std::vector<int>& sn, bool two_step, bool snap_ok);
+
 }  // namespace fwi

@@ -7,7 +7,9 @@
 //  * a two-step tile's first-step cells that its second step uses are plain
 //    interior cells (no CPML column, no bottom pad row), its reads stay inside
 //    the field, and core tiles read no cell a single-step item writes;
-//  * source and receiver lists are sorted by row and lie inside the item.
+//  * source and receiver lists are sorted by row and lie inside the item;
+//  * the time-loop planner (two-step passes and single steps) keeps its
+//    invariants on random loops.
 // Prints "all ok" and exits 0, or prints the first failure and exits 1.
 #include <cstdio>
 #include <cstdlib>
@@ -140,9 +142,40 @@ void check(int ny, int nx, int acc, int dpml, int nsrc, int band, int fband) {
     if (two_step_ok(l)) CHECK(!L.fus_fwd.empty(), "a two-step shot without tiles");
 }
 
+// The step planner: every step of k0..k1 once and in order, a pass never
+// has a snapshot in its second step nor, unless allowed, in its first, the
+// number of passes is even, and no pass is made when two-step is off.
+void check_plan(int k0, int k1, const std::vector<int>& sn, bool two, bool snap_ok) {
+    const std::vector<StepUnit> u = plan_steps(k0, k1, sn, two, snap_ok);
+    int k = k0, npass = 0;
+    for (const StepUnit& x : u) {
+        CHECK(x.k == k, "plan: step %d expected, got %d", k, x.k);
+        CHECK(x.sn == sn[x.k], "plan: wrong snapshot block at step %d", x.k);
+        if (x.pass) {
+            CHECK(two, "plan: pass without two-step");
+            CHECK(x.k + 1 <= k1 && sn[x.k + 1] < 0, "plan: snapshot in the second step of a pass at %d", x.k);
+            CHECK(snap_ok || x.sn < 0, "plan: snapshot in a pass at %d", x.k);
+            ++npass;
+            k += 2;
+        } else {
+            k += 1;
+        }
+    }
+    CHECK(k == k1 + 1, "plan: steps %d..%d not all planned (%d)", k0, k1, k);
+    CHECK(npass % 2 == 0, "plan: odd number of passes");
+}
+
 }  // namespace
 
 int main() {
+    for (int trial = 0; trial < 3000 && !fails; ++trial) {
+        const int k0 = 2 + rnd(5), k1 = k0 - 1 + rnd(60);
+        const int ss = 1 + rnd(12);
+        std::vector<int> sn(k1 + 2, -1);
+        for (int k = k0; k <= k1; ++k)
+            if (k % ss == 0) sn[k] = k / ss;
+        check_plan(k0, k1, sn, trial % 4 != 0, trial % 3 != 0);
+    }
     check(400, 2000, 3, 20, 5, 16, 64);
     check(400, 2000, 4, 20, 5, 16, 64);
     check(37, 61, 3, 20, 3, 32, 48);

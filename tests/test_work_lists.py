@@ -2,7 +2,8 @@
 (fwi_gb300/csrc/fwi_lists.cpp, no CUDA dependency) compiled with g++ together
 with tests/lists_check.cpp and run over ~900 grid shapes (acc 3/4, CPML widths
 1..54, narrow and wide grids): single-step coverage, two-step ownership, halo
-plainness, read bounds, core tiles, sorted source/receiver lists."""
+plainness, read bounds, core tiles, sorted source/receiver lists; and the
+time-loop planner (two-step passes and single steps) on 3000 random loops."""
 import os
 import shutil
 import subprocess

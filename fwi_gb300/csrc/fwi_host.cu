@@ -250,7 +250,8 @@ struct ShotState {
     DBuf ckpt;     // forward-state checkpoints when recomputing
     Layout lay{};
     size_t field_bytes = 0, snap_bytes = 0;
-    // the seven state fields in ShotDev order: pa, pb, phx, chx, phy, phy2, chy
+    // the seven fields of a checkpointed state (the state is in wavefield pair 0
+    // at every checkpoint): pa, pb, phx, chx, phy, phy2, chy
     void* state(int i) {
         DBuf* a[7] = {&pa, &pb, &phx, &chx, &phy, &phy2, &chy};
         return a[i]->p;

@@ -593,6 +593,7 @@ int run_time_loop(int acc, int mode, int nt, int store_snap, int nt_store, bool 
 struct Single {
     ShotState sh;
     DBuf d_ctmp, d_srcv, d_rec, d_items_m, d_items_b, d_src, d_recs, d_shot, d_fA, d_fB, d_stage, d_flag;
+    DBuf d_items_f, d_items_l;  // two-step tiles; single-step interior items beside them
 };
 Single& single() {
     static Single s;
@@ -786,10 +787,12 @@ int fwi_solver_acoustic_ss(const int* rank, const int* iprop_, const int* NumSou
     // work lists (the adjoint injects at the receivers)
     std::vector<ShotGeom> geoms{geo};
     std::vector<Layout> lays{l};
-    Lists lists = build_lists(geoms, lays, 64);
+    Lists lists = build_lists(geoms, lays, 64, TWO_STEP_BAND);
     const bool adj = (iprop == 2);
     TRY(upload(sg.d_items_m, adj ? lists.int_adj : lists.int_fwd, st));
     TRY(upload(sg.d_items_b, adj ? lists.bnd_adj : lists.bnd_fwd, st));
+    TRY(upload(sg.d_items_f, adj ? lists.fus_adj : lists.fus_fwd, st));
+    TRY(upload(sg.d_items_l, adj ? lists.lft_adj : lists.lft_fwd, st));
     TRY(upload(sg.d_src, adj ? lists.src_adj : lists.src_fwd, st));
     TRY(upload(sg.d_recs, lists.recs, st));
     std::vector<ShotDev> sd{sg.sh.dev(nt, NumRec, 0, sg.d_srcv.as<float>(), sg.d_rec.as<float>())};
@@ -808,7 +811,11 @@ int fwi_solver_acoustic_ss(const int* rank, const int* iprop_, const int* NumSou
     ps.pb.nitems = (int)(adj ? lists.bnd_adj.size() : lists.bnd_fwd.size());
     ps.pb.nstrip = lists.nstrip;
     ps.kstrip = lists.kstrip;
-    TRY(run_time_loop(acc, adj ? 1 : 0, nt, store_snap, nt_store, iprop == 1, ps, st, L().aux));
+    // pairs of steps as two-step passes (FP32 snapshots: a pass may store or image)
+    const TwoStep tw = two_step_set(ps, adj ? 1 : 0, sg.d_items_f, (int)lists.fus_fwd.size(), lists.ncore,
+                                    sg.d_items_l, (int)lists.lft_fwd.size());
+    TRY(run_time_loop(acc, adj ? 1 : 0, nt, store_snap, nt_store, iprop == 1, ps, st, L().aux,
+                      lists.fus_fwd.empty() ? nullptr : &tw));
 
     if (!adj) LK(launch_rec_last(sg.d_rec.as<float>(), nt, NumRec, st));
     // outputs

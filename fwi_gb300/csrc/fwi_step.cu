@@ -1114,15 +1114,21 @@ __global__ void __launch_bounds__(128) k_step_strip(const __grid_constant__ Step
 // x0 + 124): the first step (p_{n+1}) is computed on all 128 columns, the
 // second (p_{n+2}) on the 120 columns of lanes 1..30, whose x-neighbours
 // (R <= 4 columns) are all on the warp.  The first step runs over rows
-// [y0 - R, y1 + R) (rows above the model rows are the free-surface pad:
-// zero), the second R rows behind it.  p_n comes through a register queue of
-// 2R+1 rows, p_{n+1} through a second one; p_{n-1}, c2 and the halo float4s
-// of p_n through a cp.async ring whose slots are kept R rows longer, for the
-// second step's c2.  Both results go to buffers other than the inputs (the
-// warp reads its neighbours' p_n and p_{n-1}), and the cells a warp computes
-// outside its own columns and rows are bit-identical to their owners' (same
-// arithmetic, same source injection; the host only makes tiles whose halo
-// cells are plain interior cells).
+// [y0 - R, y1 + R] (rows above the model rows are the free-surface pad:
+// zero; the last row only keeps the loop uniform), the second R+1 rows
+// behind it, so the two updates of one row iteration are independent.  p_n
+// comes through a register queue of 2R+2 rows, p_{n+1} through one of 2R+1;
+// p_{n-1}, c2 and p_n with its halo float4s through a cp.async ring whose
+// slots are kept R+1 rows longer (the x-neighbours of p_n row y sit in the
+// slot of row y - R, the second step's c2 in that of row y - R - 1).  The
+// x-neighbours of both steps are shared-memory reads from lines laid out
+// [halo | 32 lanes | halo]; a row's injected values and recorded receivers go
+// through a shared line too, 32 entries at a time.  Both results go to
+// buffers other than the inputs (the warp reads its neighbours' p_n and
+// p_{n-1}), and the cells a warp computes outside its own columns and rows
+// are bit-identical to their owners' (same arithmetic, same source
+// injection; the host only makes tiles whose halo cells are plain interior
+// cells).
 // ---------------------------------------------------------------------------
 constexpr int F2_W = 120;
 // ring slot of row y: p_n row y+R with its halo float4s [HL | 32 lanes | HR],

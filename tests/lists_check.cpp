@@ -9,7 +9,11 @@
 //    the field, and core tiles read no cell a single-step item writes;
 //  * source and receiver lists are sorted by row and lie inside the item;
 //  * the time-loop planner (two-step passes and single steps) keeps its
-//    invariants on random loops.
+//    invariants on random loops;
+//  * the two-step pipeline is race-free: over three passes, kernels the
+//    stream order and events leave unordered never write a wavefield cell
+//    another one reads or writes (and dropping any one dependency edge
+//    produces such a conflict).
 // Prints "all ok" and exits 0, or prints the first failure and exits 1.
 #include <cstdio>
 #include <cstdlib>
@@ -165,9 +169,124 @@ void check_plan(int k0, int k1, const std::vector<int>& sn, bool two, bool snap_
     CHECK(npass % 2 == 0, "plan: odd number of passes");
 }
 
+// The two-step pipeline (two_step_run in fwi_host.cu): the kernels of three
+// consecutive passes with their wavefield read sets (the cells whose values
+// are used) and write sets, per buffer of the two pairs; every two kernels
+// that the pipeline's stream order and events leave unordered must not have
+// one write what the other reads or writes.  The dependency edges below
+// mirror two_step_run: C (core tiles, main stream), E (edge tiles, after A2
+// on the second stream), A2/B2 (leftover interior rows and bottom tiles,
+// second stream), A3/B3 (side strips, third stream).
+struct Kern {
+    const char* name;
+    int pass;
+    std::vector<std::vector<char>> rd, wr;  // [buffer 0..3][cell]
+    std::vector<int> deps;                  // direct predecessors
+};
+
+void check_pipeline(int ny, int nx, int acc, int dpml, int fband) {
+    const Layout l = make_layout(ny, nx, acc, dpml);
+    if (!two_step_ok(l)) return;
+    ShotGeom g;
+    g.nx = nx;
+    const Lists L = build_lists({g}, {l}, 16, fband);
+    const int R = l.acc;
+    const size_t n = (size_t)l.nyt * l.pitch;
+    auto cur = [](int k, int pair) { return 2 * pair + ((k & 1) ? 0 : 1); };
+    auto prev = [](int k, int pair) { return 2 * pair + ((k & 1) ? 1 : 0); };
+    std::vector<Kern> K;
+    auto mk = [&](const char* name, int pass) {
+        Kern k{name, pass, std::vector<std::vector<char>>(4, std::vector<char>(n, 0)),
+               std::vector<std::vector<char>>(4, std::vector<char>(n, 0)), {}};
+        K.push_back(k);
+        return (int)K.size() - 1;
+    };
+    auto box = [&](std::vector<char>& m, int ya, int yb, int ca, int cb) {  // rows [ya, yb), cols [ca, cb), clipped
+        for (int y = std::max(ya, 0); y < std::min(yb, l.nyt); ++y)
+            for (int c = std::max(ca, 0); c < std::min(cb, l.pitch); ++c) m[(size_t)y * l.pitch + c] = 1;
+    };
+    const int xa = l.off + l.sl, xb = l.off + l.sr;
+    // single-step item at step k reading pair (rp, rp1) and writing wo
+    auto single = [&](Kern& kk, const WorkItem& it, int rp, int rp1, int wo) {
+        int c0, c1;
+        item_cols(it, l, c0, c1);
+        box(kk.wr[wo], it.y0, it.y1, c0, c1);
+        box(kk.rd[rp], it.y0 - R, it.y1 + R, c0 - R, c1 + R);
+        box(kk.rd[rp1], it.y0, it.y1, c0, c1);
+    };
+    auto tiles = [&](Kern& kk, int from, int to, int k, int X, int Y) {
+        for (int i = from; i < to; ++i) {
+            const WorkItem& it = L.fus_fwd[i];
+            const int o0 = std::max(it.tile, xa), o1 = std::min(it.tile + 120, xb);
+            box(kk.wr[prev(k, Y)], it.y0, it.y1, o0, o1);
+            box(kk.wr[prev(k + 1, Y)], it.y0, it.y1, o0, o1);
+            box(kk.rd[cur(k, X)], std::max(it.y0 - 2 * R, l.dn), it.y1 + 2 * R, o0 - 2 * R, o1 + 2 * R);
+            box(kk.rd[prev(k, X)], std::max(it.y0 - R, l.dn), it.y1 + R, o0 - R, o1 + R);
+        }
+    };
+    const int nstrip = L.nstrip, nb = (int)L.bnd_fwd.size();
+    int lastC = -1, lastE = -1, lastA3 = -1, lastB2 = -1, lastB3 = -1, lastst2 = -1;
+    for (int j = 0, k = 2, X = 0; j < 3; ++j, k += 2, X ^= 1) {
+        const int Y = X ^ 1;
+        const int c = mk("C", j), e = mk("E", j), a2 = mk("A2", j), a3 = mk("A3", j), b2 = mk("B2", j),
+                  b3 = mk("B3", j);
+        tiles(K[c], 0, L.ncore, k, X, Y);
+        tiles(K[e], L.ncore, (int)L.fus_fwd.size(), k, X, Y);
+        for (const WorkItem& it : L.lft_fwd) {
+            single(K[a2], it, cur(k, X), prev(k, X), prev(k, Y));
+            single(K[b2], it, cur(k + 1, Y), cur(k, X), prev(k + 1, Y));
+        }
+        for (int i = nstrip; i < nb; ++i) {
+            single(K[a2], L.bnd_fwd[i], cur(k, X), prev(k, X), prev(k, Y));
+            single(K[b2], L.bnd_fwd[i], cur(k + 1, Y), cur(k, X), prev(k + 1, Y));
+        }
+        for (int i = 0; i < nstrip; ++i) {
+            single(K[a3], L.bnd_fwd[i], cur(k, X), prev(k, X), prev(k, Y));
+            single(K[b3], L.bnd_fwd[i], cur(k + 1, Y), cur(k, X), prev(k + 1, Y));
+        }
+        auto dep = [&](int v, int u) {
+            if (u >= 0) K[v].deps.push_back(u);
+        };
+        dep(c, lastC), dep(c, lastE);                      // C(j): stream order, E(j-1)
+        dep(a3, lastA3 >= 0 ? lastB3 : -1), dep(a3, lastB2);  // A3(j): B3(j-1) (stream), B2(j-1)
+        dep(a2, lastst2), dep(a2, lastB3);                 // A2(j): B2(j-1) (stream), B3(j-1)
+        dep(e, a2), dep(e, lastC);                         // E(j): A2(j) (stream), C(j-1)
+        dep(b3, a3), dep(b3, e);                           // B3(j): A3(j) (stream), E(j)
+        dep(b2, e), dep(b2, a3);                           // B2(j): E(j) (stream), A3(j)
+        lastC = c, lastE = e, lastA3 = a3, lastB2 = b2, lastB3 = b3, lastst2 = b2;
+    }
+    // reachability
+    const int nk = (int)K.size();
+    std::vector<std::vector<char>> reach(nk, std::vector<char>(nk, 0));
+    for (bool grew = true; grew;) {  // transitive closure (edges do not follow creation order)
+        grew = false;
+        for (int v = 0; v < nk; ++v)
+            for (int u : K[v].deps) {
+                if (!reach[v][u]) reach[v][u] = 1, grew = true;
+                for (int w = 0; w < nk; ++w)
+                    if (reach[u][w] && !reach[v][w]) reach[v][w] = 1, grew = true;
+            }
+    }
+    for (int a = 0; a < nk; ++a)
+        for (int b = a + 1; b < nk; ++b) {
+            if (reach[a][b] || reach[b][a]) continue;
+            for (int buf = 0; buf < 4; ++buf)
+                for (size_t i = 0; i < n; ++i) {
+                    const bool ab = K[a].wr[buf][i] && (K[b].rd[buf][i] || K[b].wr[buf][i]);
+                    const bool ba = K[b].wr[buf][i] && K[a].rd[buf][i];
+                    CHECK(!ab && !ba, "pipeline race: %s(%d) and %s(%d) on buffer %d cell (%zu,%zu) (ny %d nx %d acc %d)",
+                          K[a].name, K[a].pass, K[b].name, K[b].pass, buf, i / l.pitch, i % l.pitch, ny, nx, acc);
+                }
+        }
+}
+
 }  // namespace
 
 int main() {
+    for (int acc : {3, 4})
+        for (int dpml : {8, 20})
+            for (int nx : {90, 250, 400}) check_pipeline(40 + nx % 37, nx, acc, dpml, 16 + nx % 20);
+    if (fails) return 1;
     for (int trial = 0; trial < 3000 && !fails; ++trial) {
         const int k0 = 2 + rnd(5), k1 = k0 - 1 + rnd(60);
         const int ss = 1 + rnd(12);

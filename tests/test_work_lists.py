@@ -2,8 +2,10 @@
 (fwi_gb300/csrc/fwi_lists.cpp, no CUDA dependency) compiled with g++ together
 with tests/lists_check.cpp and run over ~900 grid shapes (acc 3/4, CPML widths
 1..54, narrow and wide grids): single-step coverage, two-step ownership, halo
-plainness, read bounds, core tiles, sorted source/receiver lists; and the
-time-loop planner (two-step passes and single steps) on 3000 random loops."""
+plainness, read bounds, core tiles, sorted source/receiver lists; the
+time-loop planner (two-step passes and single steps) on 3000 random loops; and
+the race-freedom of the two-step pipeline's concurrent kernels (read and
+write sets of three passes against the dependency graph of two_step_run)."""
 import os
 import shutil
 import subprocess

@@ -61,6 +61,9 @@ def parse():
                     help="only build the survey and run this many forward time steps (for ncu captures)")
     ap.add_argument("--wave", type=int, default=0, help="shots per wave (0 = tuner)")
     ap.add_argument("--band", type=int, default=0, help="rows per warp work item (0 = tuner)")
+    ap.add_argument("--tile-kernel", type=int, default=0, choices=[0, 1, 2],
+                    help="two-step tile kernel: 1 register queues, 2 shared-memory queue (0 = tuner)")
+    ap.add_argument("--tile-rows", type=int, default=0, help="rows per two-step tile (0 = tuner)")
     a = ap.parse_args()
     if a.workload == "mcs-f16":
         a.snap = a.snap or "f16"
@@ -326,7 +329,7 @@ def main():
 
     if a.profile:
         sv = F.Survey(spec, snap_form=snap_form, wave_shots=a.wave, band_rows=a.band, hbm_budget=budget,
-                      recompute=a.recompute)
+                      recompute=a.recompute, tile_kernel=a.tile_kernel, tile_rows=a.tile_rows)
         sv.set_lambda(lam0)
         torch.cuda.synchronize()
         p0, p1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -335,12 +338,15 @@ def main():
         p1.record(stream)
         torch.cuda.synchronize()
         ms = p0.elapsed_time(p1) / a.profile
+        tb = sv.two_step_bytes()[0]
         print(json.dumps({"profile_steps": a.profile, "ms_per_step": ms, "step_bytes": sv.step_bytes(),
-                          "GBps": sv.step_bytes() / ms / 1e6, "tuning": sv.tuning()}))
+                          "two_step_bytes": tb, "GBps": tb / ms / 1e6, "frac": tb / ms / 1e6 / peaks()[0],
+                          "tuning": sv.tuning(), "tiles": [sv.tiles()[0], sv.tiles()[1]],
+                          "tuner_ms_per_pass": {f"{k}/{r}": v for (k, r), v in sv.tiles()[2].items()}}))
         return 0
     # observed data from the true model (untimed setup)
     sv = F.Survey(spec, snap_form=snap_form, wave_shots=a.wave, band_rows=a.band, hbm_budget=budget,
-                  recompute=a.recompute)
+                  recompute=a.recompute, tile_kernel=a.tile_kernel, tile_rows=a.tile_rows)
     sv.set_lambda(lam_true)
     sv.run(2)
     for i, sh in enumerate(spec.shots):
@@ -400,6 +406,7 @@ def main():
     bytes_single = sv.step_bytes()
     bytes_step, tile_bytes_pass = sv.two_step_bytes()
     wave, band = sv.tuning()
+    tile_kernel, tile_rows, tile_ms = sv.tiles()
     rc_plan = sv.recompute_plan()
     achieved = bytes_step / step_s / 1e9
     tr = traffic_from_profile()
@@ -456,7 +463,8 @@ def main():
         h_src = pin(nsrc)
         h_src[:] = np.concatenate([np.asarray(s.src, np.float32).reshape(-1, order="F") for s in spec.shots])
         dh = _DescHolder(spec, snap_form, F.GRAD_F64, hbm_budget=budget,
-                         flags=F.SURVEY_RECOMPUTE if a.recompute else 0)
+                         flags=F.SURVEY_RECOMPUTE if a.recompute else 0, tile_kernel=a.tile_kernel,
+                         tile_rows=a.tile_rows)
         so = oo = 0
         for i, s in enumerate(spec.shots):
             ns, nr = s.src.size, len(s.nxRec) * spec.nt
@@ -509,7 +517,9 @@ def main():
                 "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded layered model, Ricker sources, "
                 "observed data synthesised on the true model)",
                 "config": {"workload": workload_name(a), "shots_per_gpu": len(spec.shots), "wave_shots": wave,
-                           "band_rows": band, "recompute_segment_steps": rc_plan[0], "recompute_segments": rc_plan[1],
+                           "band_rows": band, "tile_kernel": tile_kernel, "tile_rows": tile_rows,
+                           "tuner_ms_per_pass": {f"{k}/{r}": v for (k, r), v in tile_ms.items()},
+                           "recompute_segment_steps": rc_plan[0], "recompute_segments": rc_plan[1],
                            "l2": "inputs larger than L2 (wavefields of all shots of a wave and their snapshots: "
                                  "tens to hundreds of GB)"},
                 "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "plain": plain, "gpu_launches": int(launches),

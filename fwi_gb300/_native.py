@@ -32,7 +32,7 @@ EXPORTS = [
     "fwi_survey_grad_device", "fwi_survey_get_stack", "fwi_survey_get_synthetic", "fwi_survey_step_bytes", "fwi_survey_two_step_bytes", "fwi_survey_tuning",
     "fwi_survey_recompute", "fwi_survey_set_time", "fwi_time_filter", "fwi_set_filter_order",
     "fwi_interpolation_akima", "fwi_su_info", "fwi_su_read", "fwi_su_write", "fwi_read_nav",
-    "fwi_survey_time_steps", "fwi_misfit_gradient_batch", "fwi_solver_forward_noalloc",
+    "fwi_survey_time_steps", "fwi_misfit_gradient_batch", "fwi_solver_forward_noalloc", "fwi_survey_tiles",
 ]
 
 
@@ -53,7 +53,8 @@ class FwiSurveyDesc(C.Structure):
                 ("store_snap", C.c_int), ("acc", C.c_int), ("dpml", C.c_int), ("numtasks", C.c_int),
                 ("snap_form", C.c_int), ("grad_form", C.c_int), ("nshots", C.c_int),
                 ("shots", C.POINTER(FwiShot)), ("water_rows", C.c_void_p), ("hbm_budget", C.c_size_t),
-                ("wave_shots", C.c_int), ("band_rows", C.c_int), ("flags", C.c_int)]
+                ("wave_shots", C.c_int), ("band_rows", C.c_int), ("flags", C.c_int), ("tile_kernel", C.c_int),
+                ("tile_rows", C.c_int)]
 
 
 _lib = None
@@ -102,6 +103,7 @@ def load():
     lib.fwi_survey_two_step_bytes.argtypes = [P, C.POINTER(C.c_double), C.POINTER(C.c_double)]
     lib.fwi_survey_tuning.argtypes = [P, IP, IP]
     lib.fwi_survey_recompute.argtypes = [P, IP, IP]
+    lib.fwi_survey_tiles.argtypes = [P, IP, IP, P, P, IP]
     lib.fwi_survey_time_steps.argtypes = [P, I]
     lib.fwi_misfit_gradient_batch.argtypes = [C.POINTER(FwiSurveyDesc), P, I, P, P]
     lib.fwi_solver_forward_noalloc.argtypes = [I, I, P, P, P, P, P, F, F, I, I, P, I, P]

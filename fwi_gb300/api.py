@@ -195,7 +195,7 @@ class _DescHolder:
     """Keeps the numpy arrays behind a FwiSurveyDesc alive."""
 
     def __init__(self, spec: SurveySpec, snap_form=0, grad_form=1, hbm_budget=0, wave_shots=0, band_rows=0,
-                 flags=0):
+                 flags=0, tile_kernel=0, tile_rows=0):
         self.keep = []
         shots = (N.FwiShot * len(spec.shots))()
         for i, sh in enumerate(spec.shots):
@@ -212,18 +212,21 @@ class _DescHolder:
             self.keep.append(water)
         self.desc = N.FwiSurveyDesc(spec.ny, spec.nx_model, spec.d, spec.dt, spec.nt, spec.store_snap, spec.acc,
                                     spec.dpml, spec.numtasks, snap_form, grad_form, len(spec.shots), shots,
-                                    _p(water), hbm_budget, wave_shots, band_rows, flags)
+                                    _p(water), hbm_budget, wave_shots, band_rows, flags, tile_kernel, tile_rows)
 
 
 class Survey:
     """Device-resident batched survey (fwi_survey_create & co)."""
 
     def __init__(self, spec: SurveySpec, snap_form=N.SNAP_F32, grad_form=N.GRAD_F64, hbm_budget=0, wave_shots=0,
-                 band_rows=0, graph=True, recompute=False, two_step=True):
+                 band_rows=0, graph=True, recompute=False, two_step=True, tile_kernel=0, tile_rows=0):
+        """tile_kernel: 0 = the tuner's choice, 1 = register-queue, 2 = shared-queue
+        two-step kernel; tile_rows: rows per two-step tile (0 = the tuner's)."""
         self.spec = spec
         flags = ((0 if graph else N.SURVEY_NO_GRAPH) | (N.SURVEY_RECOMPUTE if recompute else 0)
                  | (0 if two_step else N.SURVEY_SINGLE_STEP))
-        self._h = _DescHolder(spec, snap_form, grad_form, hbm_budget, wave_shots, band_rows, flags)
+        self._h = _DescHolder(spec, snap_form, grad_form, hbm_budget, wave_shots, band_rows, flags, tile_kernel,
+                              tile_rows)
         handle = C.c_void_p()
         N.check(N.load().fwi_survey_create(C.byref(self._h.desc), C.byref(handle)))
         self.handle = handle
@@ -319,6 +322,20 @@ class Survey:
         w, b = C.c_int(0), C.c_int(0)
         N.check(N.load().fwi_survey_tuning(self.handle, C.byref(w), C.byref(b)))
         return w.value, b.value
+
+    def tiles(self):
+        """(tile kernel 1|2 or 0 without two-step tiles, rows per tile, {(kernel, rows): ms per
+        forward two-step pass of the first wave} as measured by the tuner)."""
+        k, r, n = C.c_int(0), C.c_int(0), C.c_int(0)
+        cand = (C.c_int * 8)()
+        times = (C.c_float * 16)()
+        N.check(N.load().fwi_survey_tiles(self.handle, C.byref(k), C.byref(r), cand, times, C.byref(n)))
+        meas = {}
+        for kk in range(2):
+            for c in range(n.value):
+                if times[kk * n.value + c] >= 0:
+                    meas[(kk + 1, cand[c])] = float(times[kk * n.value + c])
+        return k.value, r.value, meas
 
     def recompute_plan(self):
         """(forward steps per segment, segments); (0, 0) without recomputation."""

@@ -7,10 +7,12 @@
 // wave sizing against the HBM budget, CUDA-graph capture of whole waves,
 // and the misfit/gradient reductions of calculate_misfit_gradient.f90.
 #include <cuda_runtime.h>
+#include <sys/stat.h>
 
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <memory>
@@ -23,7 +25,7 @@
 #include "fwi_lists.h"
 
 namespace fwi {
-cudaError_t launch_step2(int acc, int mode, const StepParams& pf, cudaStream_t st);
+cudaError_t launch_step2(int acc, int mode, int var, const StepParams& pf, cudaStream_t st);
 cudaError_t launch_step(int acc, int mode, int kstrip, const StepParams& pm, const StepParams& pb, cudaStream_t sm,
                         cudaStream_t sb, cudaStream_t ss);
 cudaError_t configure_step_kernels();
@@ -98,6 +100,9 @@ struct LibState {
     cudaEvent_t ev2[10] = {};  // two-step pipeline (two sets of five)
     int prio_hi = 0;
     int acc = 3, dpml = 20;
+    // two-step kernel and tile height of the drop-in solver: the choice of
+    // the last survey tuned in this process (the tuner's default before)
+    int tile_var = 1, tile_band = TWO_STEP_BAND;
     long long launches = 0;
     std::recursive_mutex mu;
 };
@@ -387,14 +392,17 @@ struct TwoStep {
     StepParams pf;  // the first ncore items are core tiles
     StepSet lo;
     int ncore = 0;
+    int var = 0;           // two-step kernel: 0 k_step2_interior, 1 k_step2s_interior
     bool snap_ok = false;  // a pass's first step may store a snapshot / image
 };
 
 // Two-step lists of a wave from its single-step set: the two-step tiles,
 // and the single-step interior items outside them beside the boundary list.
-TwoStep two_step_set(const StepSet& ps, int mode, const DBuf& fus, int nfus, int ncore, const DBuf& lft, int nlft) {
+TwoStep two_step_set(const StepSet& ps, int mode, const DBuf& fus, int nfus, int ncore, const DBuf& lft, int nlft,
+                     int var) {
     TwoStep tw;
     tw.ncore = ncore;
+    tw.var = var;
     tw.pf = ps.pm;
     tw.pf.items = fus.as<WorkItem>();
     tw.pf.nitems = nfus;
@@ -509,7 +517,7 @@ int two_step_run(int acc, int mode, const TwoStep& tw, int k, int npass, const i
         L().launches += 2 * step_kernels(a) + (fc.nitems > 0) + (fe.nitems > 0);
         // C(j)
         CK(cudaStreamWaitEvent(st, E(q), 0));
-        CK(launch_step2(acc, mode, fc, st));
+        CK(launch_step2(acc, mode, tw.var, fc, st));
         CK(cudaEventRecord(C(p), st));
         // A3(j)
         CK(cudaStreamWaitEvent(st3, B2(q), 0));
@@ -519,7 +527,7 @@ int two_step_run(int acc, int mode, const TwoStep& tw, int k, int npass, const i
         CK(cudaStreamWaitEvent(st2, B3(q), 0));
         CK(launch_step(acc, mode, a2.kstrip, a2.pm, a2.pb, st2, st2, st2));
         CK(cudaStreamWaitEvent(st2, C(q), 0));
-        CK(launch_step2(acc, mode, fe, st2));
+        CK(launch_step2(acc, mode, tw.var, fe, st2));
         CK(cudaEventRecord(E(p), st2));
         // B3(j) after A2(j) and E(j); B2(j) after A3(j)
         CK(cudaStreamWaitEvent(st3, E(p), 0));
@@ -787,7 +795,7 @@ int fwi_solver_acoustic_ss(const int* rank, const int* iprop_, const int* NumSou
     // work lists (the adjoint injects at the receivers)
     std::vector<ShotGeom> geoms{geo};
     std::vector<Layout> lays{l};
-    Lists lists = build_lists(geoms, lays, 64, TWO_STEP_BAND);
+    Lists lists = build_lists(geoms, lays, 64, L().tile_band);
     const bool adj = (iprop == 2);
     TRY(upload(sg.d_items_m, adj ? lists.int_adj : lists.int_fwd, st));
     TRY(upload(sg.d_items_b, adj ? lists.bnd_adj : lists.bnd_fwd, st));
@@ -812,8 +820,9 @@ int fwi_solver_acoustic_ss(const int* rank, const int* iprop_, const int* NumSou
     ps.pb.nstrip = lists.nstrip;
     ps.kstrip = lists.kstrip;
     // pairs of steps as two-step passes (FP32 snapshots: a pass may store or image)
-    const TwoStep tw = two_step_set(ps, adj ? 1 : 0, sg.d_items_f, (int)lists.fus_fwd.size(), lists.ncore,
-                                    sg.d_items_l, (int)lists.lft_fwd.size());
+    const TwoStep tw = two_step_set(ps, adj ? 1 : 0, sg.d_items_f, (int)(adj ? lists.fus_adj : lists.fus_fwd).size(),
+                                    lists.ncore, sg.d_items_l, (int)(adj ? lists.lft_adj : lists.lft_fwd).size(),
+                                    L().tile_var);
     TRY(run_time_loop(acc, adj ? 1 : 0, nt, store_snap, nt_store, iprop == 1, ps, st, L().aux,
                       lists.fus_fwd.empty() ? nullptr : &tw));
 
@@ -969,6 +978,8 @@ struct fwi_survey {
     std::vector<int> tr_off;  // trace offsets per shot (size nshots+1)
     int ntr = 0;
     int wave = 1, band = 64;
+    int tile_var = 1, tile_band = TWO_STEP_BAND;  // two-step kernel and rows per two-step tile
+    std::vector<float> tune_ms;                   // tuner: [variant][band candidate] ms per pass (-1: not run)
     std::vector<std::vector<int>> waves;  // shot indices per wave
     // resident data
     DBuf d_lambda, d_src, d_obs, d_synth, d_adj, d_mis_tr, d_mis_shot, d_tr_off, d_G, d_grad, d_water, d_fA, d_fB;
@@ -1063,7 +1074,7 @@ int survey_prepare_waves(fwi_survey* s) {
             g.push_back(s->geoms[sh]);
             l.push_back(s->lays[sh]);
         }
-        Lists lists = build_lists(g, l, s->band, (D.flags & FWI_SURVEY_SINGLE_STEP) ? 0 : TWO_STEP_BAND);
+        Lists lists = build_lists(g, l, s->band, (D.flags & FWI_SURVEY_SINGLE_STEP) ? 0 : s->tile_band);
         std::unique_ptr<fwi_survey::WaveDev> wd(new fwi_survey::WaveDev());
         TRY(upload(wd->items_if, lists.int_fwd, st));
         TRY(upload(wd->items_ia, lists.int_adj, st));
@@ -1150,42 +1161,176 @@ int survey_prepare_waves(fwi_survey* s) {
     return FWI_OK;
 }
 
-// Autotuner for the band height of the step kernels' work items: times a
-// few forward steps of the first wave for each candidate and keeps the
-// fastest.  Results are cached per (device, grid, order, CPML, wave shape).
-int time_wave0_steps(fwi_survey* s, int steps, float* ms);
+// ---- autotuner -------------------------------------------------------------
+//
+// Timed on the first wave, each candidate after a warm-up (the fastest of
+// three timings of a few steps):
+//   * the two-step tiles, when the survey runs two-step passes: the kernel
+//     (k_step2_interior or k_step2s_interior) and the rows per tile
+//     (TILE_BANDS), timed as forward two-step passes of the whole wave (the
+//     tiles beside the single-step lists, as a gradient runs them);
+//   * the band height of the single-step interior items (BANDS), timed as
+//     single steps, when single steps carry a share of the run
+//     (FWI_SURVEY_SINGLE_STEP, no two-step tiles, or 16-bit snapshots, whose
+//     forward snapshot steps are single steps).
+// A choice forced in the descriptor is not tuned.  Results are cached per
+// (device name, rows, order, CPML, wave size, window widths of the first
+// wave, time stepping, snapshot form) in memory and in a text file that
+// persists across processes: $FWI_TUNE_CACHE, else
+// $XDG_CACHE_HOME/fwi_gb300/tuning.txt or $HOME/.cache/fwi_gb300/tuning.txt
+// (FWI_TUNE_CACHE set to an empty string: memory only).
 
-int tune_band(fwi_survey* s) {
-    static std::map<std::string, int> cache;
-    const auto& D = s->desc;
-    cudaDeviceProp prop;
-    CK(cudaGetDeviceProperties(&prop, L().device));
-    std::string key = std::string(prop.name) + "|" + std::to_string(D.ny) + "|" + std::to_string(D.acc) + "|" +
-                      std::to_string(D.dpml) + "|" + std::to_string(s->wave);
-    for (int sh : s->waves[0]) key += "|" + std::to_string(s->geoms[sh].nx);
-    auto it = cache.find(key);
-    if (it != cache.end()) {
-        s->band = it->second;
-        return FWI_OK;
+int time_wave0_steps(fwi_survey* s, int steps, float* ms, bool single_only = false);
+
+constexpr int TILE_BANDS[] = {48, 64, 96};
+constexpr int NTB = 3;
+constexpr int BANDS[] = {16, 24, 32, 48, 64};
+constexpr int TUNE_PASSES = 24;
+
+std::string tune_cache_path() {
+    const char* e = getenv("FWI_TUNE_CACHE");
+    if (e) return std::string(e);
+    std::string dir;
+    if (const char* x = getenv("XDG_CACHE_HOME")) dir = x;
+    else if (const char* h = getenv("HOME")) dir = std::string(h) + "/.cache";
+    else return std::string();
+    return dir + "/fwi_gb300/tuning.txt";
+}
+
+std::map<std::string, std::vector<int>>& tune_mem() {
+    static std::map<std::string, std::vector<int>> m;
+    return m;
+}
+
+// band, tile kernel, tile rows of `key` (memory, then the file: last line wins)
+bool tune_lookup(const std::string& key, std::vector<int>& out) {
+    auto it = tune_mem().find(key);
+    if (it != tune_mem().end()) {
+        out = it->second;
+        return true;
     }
-    const int cands[] = {16, 24, 32, 48, 64};
-    int best = 64;
-    float best_ms = 1e30f;
-    for (int c : cands) {
-        if (c > D.ny && c != cands[0]) break;
-        s->band = c;
-        TRY(survey_prepare_waves(s));
-        float ms = 0.f;
-        TRY(time_wave0_steps(s, 2, &ms));  // warm-up
-        TRY(time_wave0_steps(s, 6, &ms));
-        if (ms < best_ms) {
-            best_ms = ms;
-            best = c;
+    const std::string path = tune_cache_path();
+    if (path.empty()) return false;
+    FILE* f = fopen(path.c_str(), "r");
+    if (!f) return false;
+    char line[1024];
+    bool found = false;
+    while (fgets(line, sizeof line, f)) {
+        char k[900];
+        int b = 0, v = 0, r = 0;
+        if (sscanf(line, "%899s %d %d %d", k, &b, &v, &r) == 4 && key == k && b > 0 && (v == 0 || v == 1) && r > 0) {
+            out = {b, v, r};
+            found = true;
         }
     }
-    s->band = best;
-    cache[key] = best;
-    return FWI_OK;
+    fclose(f);
+    if (found) tune_mem()[key] = out;
+    return found;
+}
+
+void tune_store(const std::string& key, const std::vector<int>& v) {
+    tune_mem()[key] = v;
+    const std::string path = tune_cache_path();
+    if (path.empty()) return;
+    // create the directory chain (best effort; a failure only loses the file cache)
+    for (size_t p = path.find('/', 1); p != std::string::npos; p = path.find('/', p + 1))
+        mkdir(path.substr(0, p).c_str(), 0755);
+    if (FILE* f = fopen(path.c_str(), "a")) {
+        fprintf(f, "%s %d %d %d\n", key.c_str(), v[0], v[1], v[2]);
+        fclose(f);
+    }
+}
+
+int tune_plan(fwi_survey* s) {
+    const auto& D = s->desc;
+    bool two = (D.flags & FWI_SURVEY_SINGLE_STEP) == 0;
+    if (two) {
+        two = false;
+        for (int sh : s->waves[0]) two = two || two_step_ok(s->lays[sh]);
+    }
+    if (D.tile_kernel > 0) s->tile_var = D.tile_kernel - 1;
+    if (D.tile_rows > 0) s->tile_band = D.tile_rows;
+    if (D.band_rows > 0) s->band = D.band_rows;
+    s->tune_ms.assign(2 * NTB, -1.f);
+    const bool do_band = D.band_rows <= 0 && (!two || D.snap_form != FWI_SNAP_F32);
+    const bool do_tiles = two && (D.tile_kernel <= 0 || D.tile_rows <= 0);
+    if (do_band || do_tiles) {
+        cudaDeviceProp prop;
+        CK(cudaGetDeviceProperties(&prop, L().device));
+        std::string key = prop.name;
+        for (char& c : key)
+            if (c == ' ' || c == '|') c = '_';
+        key += "|" + std::to_string(D.ny) + "|" + std::to_string(D.acc) + "|" + std::to_string(D.dpml) + "|" +
+               std::to_string(s->wave) + "|" + std::to_string(two ? 2 : 1) + "|" + std::to_string(D.snap_form) +
+               "|" + std::to_string(D.tile_kernel) + "|" + std::to_string(D.tile_rows) + "|" +
+               std::to_string(D.band_rows) + "|w";
+        for (int sh : s->waves[0]) key += "," + std::to_string(s->geoms[sh].nx);
+        std::vector<int> hit;
+        if (tune_lookup(key, hit)) {
+            if (do_band) s->band = hit[0];
+            if (two && D.tile_kernel <= 0) s->tile_var = hit[1];
+            if (two && D.tile_rows <= 0) s->tile_band = hit[2];
+        } else {
+            if (do_band) {
+                // single steps: the two-step lists play no part
+                int best = 64;
+                float best_ms = 1e30f;
+                for (int c : BANDS) {
+                    if (c > D.ny && c != BANDS[0]) break;
+                    s->band = c;
+                    TRY(survey_prepare_waves(s));
+                    float ms = 0.f, m = 1e30f;
+                    TRY(time_wave0_steps(s, 2, &ms, true));  // warm-up
+                    for (int r = 0; r < 3; ++r) {
+                        TRY(time_wave0_steps(s, 4, &ms, true));
+                        m = std::min(m, ms);
+                    }
+                    if (m < best_ms) {
+                        best_ms = m;
+                        best = c;
+                    }
+                }
+                s->band = best;
+            }
+            if (do_tiles) {
+                float best_ms = 1e30f;
+                int bv = s->tile_var, bb = s->tile_band;
+                for (int c = 0; c < NTB; ++c) {
+                    const int fb = D.tile_rows > 0 ? D.tile_rows : TILE_BANDS[c];
+                    if (D.tile_rows > 0 && c > 0) break;
+                    s->tile_band = fb;
+                    TRY(survey_prepare_waves(s));
+                    for (int v = 0; v < 2; ++v) {
+                        if (D.tile_kernel > 0 && v != D.tile_kernel - 1) continue;
+                        s->tile_var = v;
+                        // the fastest of three runs of TUNE_PASSES passes after a warm-up
+                        // (a few passes alone read too fast: the measured order
+                        // then differs from the order of long runs)
+                        float ms = 0.f, m = 1e30f;
+                        TRY(time_wave0_steps(s, 8, &ms));
+                        for (int r = 0; r < 3; ++r) {
+                            TRY(time_wave0_steps(s, 2 * TUNE_PASSES, &ms));
+                            m = std::min(m, ms);
+                        }
+                        s->tune_ms[v * NTB + c] = m / TUNE_PASSES;
+                        if (m < best_ms) {
+                            best_ms = m;
+                            bv = v;
+                            bb = fb;
+                        }
+                    }
+                }
+                s->tile_var = bv;
+                s->tile_band = bb;
+            }
+            tune_store(key, {s->band, s->tile_var, s->tile_band});
+        }
+        if (two) {
+            L().tile_var = s->tile_var;
+            L().tile_band = s->tile_band;
+        }
+    }
+    return survey_prepare_waves(s);
 }
 
 // ---- checkpointed recomputation -------------------------------------------
@@ -1317,8 +1462,8 @@ int rc_adjoint(fwi_survey* s, size_t wi, StepSet ps, cudaStream_t st, cudaStream
     ps.pb.nitems = wd.n_ba;
     ps.pb.nstrip = wd.n_strip;
     ps.kstrip = wd.kstrip;
-    const TwoStep twf = two_step_set(psf, 0, wd.items_ff, wd.n_ff, wd.n_core, wd.items_lf, wd.n_lf);
-    const TwoStep twa = two_step_set(ps, 1, wd.items_fa, wd.n_fa, wd.n_core, wd.items_la, wd.n_la);
+    const TwoStep twf = two_step_set(psf, 0, wd.items_ff, wd.n_ff, wd.n_core, wd.items_lf, wd.n_lf, s->tile_var);
+    const TwoStep twa = two_step_set(ps, 1, wd.items_fa, wd.n_fa, wd.n_core, wd.items_la, wd.n_la, s->tile_var);
     const TwoStep* pf = wd.n_ff ? &twf : nullptr;
     const TwoStep* pa = wd.n_fa ? &twa : nullptr;
     // imaging steps: the block each uses (solver_acoustic_SS.f90:460) and its
@@ -1391,7 +1536,7 @@ int issue_wave(fwi_survey* s, size_t wi, int step, cudaStream_t st, cudaStream_t
     ps.pb.nstrip = wd.n_strip;
     ps.kstrip = wd.kstrip;
     {
-        const TwoStep tw = two_step_set(ps, 0, wd.items_ff, wd.n_ff, wd.n_core, wd.items_lf, wd.n_lf);
+        const TwoStep tw = two_step_set(ps, 0, wd.items_ff, wd.n_ff, wd.n_core, wd.items_lf, wd.n_lf, s->tile_var);
         const TwoStep* ptw = wd.n_ff ? &tw : nullptr;
         if (s->rc_C) TRY(rc_forward(s, wi, step, ps, ptw, st, st2));
         else TRY(run_time_loop(D.acc, 0, D.nt, D.store_snap, s->nt_store, step == 1, ps, st, st2, ptw));
@@ -1437,7 +1582,7 @@ int issue_wave(fwi_survey* s, size_t wi, int step, cudaStream_t st, cudaStream_t
     ps.pb.nitems = wd.n_ba;
     ps.pb.nstrip = wd.n_strip;
     ps.kstrip = wd.kstrip;
-    TwoStep tw = two_step_set(ps, 1, wd.items_fa, wd.n_fa, wd.n_core, wd.items_la, wd.n_la);
+    TwoStep tw = two_step_set(ps, 1, wd.items_fa, wd.n_fa, wd.n_core, wd.items_la, wd.n_la, s->tile_var);
     TRY(run_time_loop(D.acc, 1, D.nt, D.store_snap, s->nt_store, true, ps, st, st2, wd.n_fa ? &tw : nullptr));
     LK(launch_stack(s->d_G.as<double>(), D.ny, D.nx_model, wd.stack.p, (int)w.size(), D.grad_form, st));
     return FWI_OK;
@@ -1502,10 +1647,9 @@ int survey_plan(fwi_survey* s, bool tune) {
     wave = (D.nshots + nw - 1) / nw;
     s->wave = wave;
     TRY(survey_prepare_slots(s));
+    if (tune) return tune_plan(s);
     if (D.band_rows > 0) s->band = D.band_rows;
-    else if (tune) TRY(tune_band(s));
-    TRY(survey_prepare_waves(s));
-    return FWI_OK;
+    return survey_prepare_waves(s);
 }
 
 extern "C" {
@@ -1590,7 +1734,7 @@ int fwi_survey_create(const fwi_survey_desc* desc, fwi_survey** out) {
     }
     CK(cudaStreamSynchronize(st));
     s->desc.shots = nullptr;  // host pointers are not kept
-    TRY(survey_plan(s.get(), D.band_rows <= 0));
+    TRY(survey_plan(s.get(), true));
     *out = s.release();
     return FWI_OK;
 }
@@ -1798,6 +1942,21 @@ int fwi_survey_tuning(fwi_survey* s, int* wave_shots, int* band_rows) {
     return FWI_OK;
 }
 
+int fwi_survey_tiles(fwi_survey* s, int* tile_kernel, int* tile_rows, int* cand, float* times, int* ncand) {
+    if (!s || s->wdev.empty()) return fail(FWI_ERR_STATE, "survey not prepared");
+    const bool two = s->wdev[0]->n_ff > 0;
+    if (tile_kernel) *tile_kernel = two ? s->tile_var + 1 : 0;
+    if (tile_rows) *tile_rows = two ? s->tile_band : 0;
+    if (ncand) *ncand = NTB;
+    for (int c = 0; c < NTB; ++c) {
+        if (cand) cand[c] = TILE_BANDS[c];
+        if (times)
+            for (int v = 0; v < 2; ++v) times[v * NTB + c] = s->tune_ms.empty() ? -1.f : s->tune_ms[v * NTB + c];
+    }
+    if (cand && s->desc.tile_rows > 0) cand[0] = s->desc.tile_rows;
+    return FWI_OK;
+}
+
 int fwi_survey_recompute(fwi_survey* s, int* segment_steps, int* segments) {
     if (!s) return fail(FWI_ERR_STATE, "null survey");
     if (segment_steps) *segment_steps = s->rc_C;
@@ -1814,7 +1973,10 @@ int fwi_survey_time_steps(fwi_survey* s, int steps) {
 }  // extern "C"
 
 namespace {
-int time_wave0_steps(fwi_survey* s, int steps, float* ms) {
+// `steps` forward steps of the first wave: two-step passes where the wave has
+// two-step tiles (an even number of them, so that the state stays in pair 0)
+// and single steps for the rest; single_only: single steps only.
+int time_wave0_steps(fwi_survey* s, int steps, float* ms, bool single_only) {
     const auto& D = s->desc;
     auto& wd = *s->wdev[0];
     StepSet ps;
@@ -1838,8 +2000,8 @@ int time_wave0_steps(fwi_survey* s, int steps, float* ms) {
     }
     // pairs of steps as two-step passes when the wave has two-step tiles
     // (an even number of them, so that the state stays in pair 0)
-    const TwoStep tw = two_step_set(ps, 0, wd.items_ff, wd.n_ff, wd.n_core, wd.items_lf, wd.n_lf);
-    const int npass = (wd.n_ff && D.nt >= 3) ? (steps / 4) * 2 : 0;
+    const TwoStep tw = two_step_set(ps, 0, wd.items_ff, wd.n_ff, wd.n_core, wd.items_lf, wd.n_lf, s->tile_var);
+    const int npass = (wd.n_ff && D.nt >= 3 && !single_only) ? (steps / 4) * 2 : 0;
     // (in runs that stay inside the time axis: steps 2..nt)
     for (int done = 0, pair = 0; done < npass;) {
         const int n = std::min(npass - done, (D.nt - 1) / 2);

@@ -1412,6 +1412,217 @@ __global__ void __launch_bounds__(128, (MODE == 1 && SNAP) ? 2 : 3) k_step2_inte
     cp_wait<0>();
 }
 
+// ---------------------------------------------------------------------------
+// Two-step tiles, variant 1: the same tile, rows and arithmetic as
+// k_step2_interior, with the p_{n+1} rows kept only in shared lines (no
+// register queue), so that the kernel fits in 128 registers and four blocks
+// of four warps share an SM.  Per warp (float4 units):
+//   row slots  NS = R + D + 1 slots; padded row r lives in slot (r - ya) mod NS:
+//              p_n row r with its halo float4s [HL | 32 lanes | HR] (the
+//              x-neighbours of the first step at row r, and the register
+//              queue's new entry when row r - R is computed) and c2 row r (the
+//              first step at row r, the second step at row r);
+//   p_{n-1}    D lines, row r in line (r - ya) mod D;
+//   p_{n+1}    NQ = 2R + 2 lines [garbage | 32 lanes | garbage], row r in line
+//              (r - ya) mod NQ: the y- and x-neighbours of the second step;
+//   inj        one line for a row's injected values / recorded receivers;
+//   imaging    D slots of F2_ISIZE (snapshot row, accumulator row).
+// D rows are in flight.  Every shared line a lane reads was written before
+// the __syncwarp that opens the row iteration, or by the lane itself.
+// ---------------------------------------------------------------------------
+template <int R, bool IMG>
+struct F2S {
+    static constexpr int D = IMG ? 2 : 3;
+    static constexpr int NS = R + D + 1;
+    static constexpr int SLOT = 66, SPN = 0, SC2 = 34;
+    static constexpr int NQ = 2 * R + 2;
+    static constexpr int P1 = NS * SLOT;
+    static constexpr int Q = P1 + D * 32;
+    static constexpr int INJ = Q + NQ * F2_LINE;
+    static constexpr int IR = INJ + F2_LINE;
+    static constexpr int WARP = IR + (IMG ? D * F2_ISIZE : 0);  // float4 per warp
+    static constexpr int SMEM = 4 * WARP * 16;
+    // blocks per SM that the 228 KB of shared memory allow (1 KB reserved per block)
+    static constexpr int BLOCKS = (228 * 1024) / (SMEM + 1024) >= 4 ? 4 : 3;
+};
+
+// x mod N for 0 <= x < 2N
+template <int N>
+__device__ __forceinline__ int wrapn(int x) {
+    if constexpr ((N & (N - 1)) == 0) return x & (N - 1);
+    else return x >= N ? x - N : x;
+}
+
+template <int R, int MODE, bool SNAP>
+__global__ void __launch_bounds__(128, F2S<R, MODE == 1 && SNAP>::BLOCKS)
+    k_step2s_interior(const __grid_constant__ StepParams P) {
+    constexpr bool IMG = MODE == 1 && SNAP;
+    using G = F2S<R, IMG>;
+    constexpr int D = G::D, NS = G::NS, NQ = G::NQ;
+    extern __shared__ float4 smem[];
+    const int lane = threadIdx.x & 31;
+    const int wid = blockIdx.x * 4 + (threadIdx.x >> 5);
+    if (wid >= P.nitems) return;
+    float4* const wb = smem + (threadIdx.x >> 5) * G::WARP;
+    float4* const slots = wb;
+    float4* const p1r = wb + G::P1;
+    float4* const q1l = wb + G::Q;
+    float4* const inj = wb + G::INJ;
+    float4* const iring = wb + G::IR;
+    const WorkItem it = P.items[wid];
+    const ShotDev& S = P.shots[it.shot];
+    const int pitch = S.pitch, dn = S.dn;
+    const int x0 = it.tile, xl = x0 - 4 + 4 * lane;
+    const float* PN = S.pf[P.rp] + xl;    // p_n
+    const float* PM = S.pf[P.rp1] + xl;   // p_{n-1}
+    float* O1 = S.pf[P.wo] + xl;          // p_{n+1}
+    float* O2 = S.pf[P.wo2] + xl;         // p_{n+2}
+    const float* C2 = S.c2 + xl;
+    // lanes 0 and 31 also fetch the halo float4 beyond the warp's columns
+    const bool has_h = (lane == 0) || (lane == 31);
+    const int hidx = (lane == 0) ? 0 : 33, hoff = (lane == 0) ? -4 : 4;
+    // lanes 1..30 store their elements [lo, hi): the interior columns [sl, sr)
+    const int lo = S.off + S.sl - xl, hi = S.off + S.sr - xl;
+    const bool mine = lane >= 1 && lane <= 30;
+    const bool full = mine && lo <= 0 && hi >= 4, part = mine && !full && lo < 4 && hi > 0;
+    const int y0 = it.y0, y1 = it.y1, ya = y0 - R, yb = y1 + R + 1;
+
+    auto issue_pn = [&](int r, int s) {  // p_n row r (with halos) into slot s
+        float4* d = slots + s * G::SLOT + G::SPN;
+        const float* src = PN + (size_t)r * pitch;
+        cp16(d + 1 + lane, src);
+        if (has_h) cp16(d + hidx, src + hoff);
+    };
+    auto issue_row = [&](int r, int s, int l) {  // p_{n-1} row r into line l, c2 row r into slot s
+        cp16(p1r + l * 32 + lane, PM + (size_t)r * pitch);
+        cp16(slots + s * G::SLOT + G::SC2 + lane, C2 + (size_t)r * pitch);
+    };
+    auto issue_img = [&](int y, int islot) {
+        if (!IMG || y < y0 || y >= y1) return;
+        float4* isl = iring + islot * F2_ISIZE;
+        const int yrow = y - dn;
+        const size_t fo = (size_t)P.snap * (size_t)S.snap_stride + (size_t)yrow * pitch + xl;
+        if (P.snap_form == 0) {
+            cp16(isl + F2_IF + lane, reinterpret_cast<const float*>(S.snaps) + fo);
+        } else {
+            cp8(reinterpret_cast<uint2*>(isl + F2_IF) + lane, reinterpret_cast<const unsigned short*>(S.snaps) + fo);
+            cp4(reinterpret_cast<float*>(isl + F2_IS) + lane,
+                S.sscale + ((size_t)P.snap * S.ny + yrow) * (S.ntiles + 2) + (xl >> 7));
+        }
+        const size_t ko = (size_t)yrow * pitch + xl;
+        if (P.grad_form == 0) {
+            cp16(isl + F2_IK + lane, S.k32 + ko);
+        } else {
+            cp16(isl + F2_IK + 2 * lane, S.k64 + ko);
+            cp16(isl + F2_IK + 2 * lane + 1, S.k64 + ko + 2);
+        }
+    };
+    // p_n rows ya .. ya+R-1 (x-neighbours only), then D groups of row ya+j
+#pragma unroll
+    for (int i = 0; i < R; ++i) issue_pn(ya + i, i);
+    cp_commit();
+#pragma unroll
+    for (int j = 0; j < D; ++j) {
+        issue_pn(ya + j + R, j + R);
+        issue_row(ya + j, j, j);
+        issue_img(ya + j, j);
+        cp_commit();
+    }
+    // qn: p_n rows y-R-1 .. y+R (the last one from the slot in the row iteration)
+    float4 qn[2 * R + 2];
+#pragma unroll
+    for (int i = 0; i < 2 * R + 1; ++i) qn[i] = ldg4(PN + (size_t)(ya - R - 1 + i) * pitch);
+
+    // source cursors: first step from the list start, second step from row y0
+    int si1 = it.s0, si2 = it.s0, ri1 = it.r0, ri2 = it.r0;
+    while (si2 < it.s1 && P.srcs[si2].row < y0) ++si2;
+    int srow1 = (si1 < it.s1) ? P.srcs[si1].row : INT_MAX, srow2 = (si2 < it.s1) ? P.srcs[si2].row : INT_MAX;
+    int rrow1 = (ri1 < it.r1) ? P.recs[ri1].row : INT_MAX, rrow2 = rrow1;
+    float2 cp[R + 1];
+#pragma unroll
+    for (int i = 0; i <= R; ++i) cp[i] = make_float2(P.c2[i], P.c2[i]);
+
+    // slot of row y (s0), of row y+R (sR), of row y-R-1 = row y+D (s2), of row
+    // y-1 = row y+D+R (sp); p_{n-1} line of row y (l1); p_{n+1} line of row y (lq)
+    int s0 = 0, sR = R, s2 = D, sp = NS - 1, l1 = 0, lq = 0;
+    for (int y = ya; y < yb; ++y) {
+        cp_wait<D - 1>();
+        __syncwarp();
+        const float4* st = slots + s0 * G::SLOT;
+        qn[2 * R + 1] = slots[sR * G::SLOT + G::SPN + 1 + lane];
+        const float4 pm1 = p1r[l1 * 32 + lane];
+        // first step, row y: p_{n+1} = -p_{n-1} + 2p_n + (d2x + d2y + source)*c2
+        float np1[4] = {0.f, 0.f, 0.f, 0.f};
+        {
+            float sv[4] = {0.f, 0.f, 0.f, 0.f};
+            if (srow1 == y) to_arr(gather_sources(P, S, y, x0 - 4, P.t, si1, it.s1, srow1, inj, lane), sv);
+            if (y >= dn)
+                interior_update2<R>(qn + 1, st[G::SPN + lane], st[G::SPN + 2 + lane], pm1, st[G::SC2 + lane], sv, cp,
+                                    np1);
+        }
+        float4* const lnw = q1l + lq * F2_LINE;
+        lnw[1 + lane] = from_arr(np1);
+        // second step, row y - R - 1, from the p_{n+1} lines of rows y-2R-1 .. y-1
+        // (lines lq+1 .. lq+2R+1 mod NQ)
+        const int y2 = y - R - 1;
+        if (y2 >= y0) {
+            const int b = wrapn<NQ>(lq + 1);
+            const float4* lc = q1l + wrapn<NQ>(b + R) * F2_LINE;
+            float sv[4] = {0.f, 0.f, 0.f, 0.f};
+            if (srow2 == y2) to_arr(gather_sources(P, S, y2, x0 - 4, P.t + 1, si2, it.s1, srow2, inj, lane), sv);
+            float np2[4];
+            interior_update2f<R>(
+                [&](int j) { return q1l[wrapn<NQ>(b + j) * F2_LINE + 1 + lane]; }, lc[lane], lc[lane + 2], qn[0],
+                slots[s2 * G::SLOT + G::SC2 + lane], sv, cp, np2);
+            if (full) {
+                st4(O2 + (size_t)y2 * pitch, from_arr(np2));
+            } else if (part) {
+#pragma unroll
+                for (int e = 0; e < 4; ++e)
+                    if (e >= lo && e < hi) O2[(size_t)y2 * pitch + e] = np2[e];
+            }
+            if (MODE == 0 && P.record && rrow2 == y2) {
+                inj[1 + lane] = from_arr(np2);  // the injection line is free again
+                __syncwarp();
+                record_row_par(P, S, y2, x0 - 4, P.t + 1, ri2, it.r1, rrow2, inj, lane);
+            }
+        }
+        if (y >= y0 && y < y1) {
+            if (full) {
+                st4(O1 + (size_t)y * pitch, from_arr(np1));
+            } else if (part) {
+#pragma unroll
+                for (int e = 0; e < 4; ++e)
+                    if (e >= lo && e < hi) O1[(size_t)y * pitch + e] = np1[e];
+            }
+            if (MODE == 0 && P.record && rrow1 == y) {
+                __syncwarp();  // np1 of every lane is in its p_{n+1} line
+                record_row_par(P, S, y, x0 - 4, P.t, ri1, it.r1, rrow1, lnw, lane);
+            }
+            if (SNAP && (full || part))
+                snap_or_image<MODE>(P, S, y - dn, xl, lo, hi, full, np1, pm1, iring + l1 * F2_ISIZE, lane);
+        }
+#pragma unroll
+        for (int i = 0; i < 2 * R + 1; ++i) qn[i] = qn[i + 1];
+        // row y + D: p_n row y+D+R into the slot of row y-1 (its p_n was last
+        // read in the previous iteration), p_{n-1} and c2 into the line and slot
+        // whose rows this lane has just used
+        if (y + D < yb) {
+            issue_pn(y + D + R, sp);
+            issue_row(y + D, s2, l1);
+            issue_img(y + D, l1);  // the imaging slot of row y, used above
+        }
+        cp_commit();
+        s0 = wrapn<NS>(s0 + 1);
+        sR = wrapn<NS>(sR + 1);
+        s2 = wrapn<NS>(s2 + 1);
+        sp = wrapn<NS>(sp + 1);
+        l1 = wrapn<D>(l1 + 1);
+        lq = wrapn<NQ>(lq + 1);
+    }
+    cp_wait<0>();
+}
+
 // Bottom pad rows, interior columns: the boundary list after its nstrip
 // side-strip items.  Runs on its own stream, concurrently with
 // k_step_interior and k_step_strip.
@@ -1449,6 +1660,8 @@ cudaError_t configure_variant() {
     if (e == cudaSuccess) e = kernel_smem(k_step_strip<R, MODE, 2>, strip_smem<R, 2>());
     if (e == cudaSuccess) e = kernel_smem(k_step2_interior<R, MODE, false>, F2Ring<R>::SMEM);
     if (e == cudaSuccess) e = kernel_smem(k_step2_interior<R, MODE, true>, F2Ring<R, MODE == 1>::SMEM);
+    if (e == cudaSuccess) e = kernel_smem(k_step2s_interior<R, MODE, false>, F2S<R, false>::SMEM);
+    if (e == cudaSuccess) e = kernel_smem(k_step2s_interior<R, MODE, true>, F2S<R, MODE == 1>::SMEM);
     return e;
 }
 
@@ -1496,23 +1709,32 @@ cudaError_t launch_step(int acc, int mode, int kstrip, const StepParams& pm, con
 }
 
 template <int R, int MODE>
-void launch_step2_variant(const StepParams& pf, int nb, cudaStream_t st) {
+void launch_step2_variant(int var, const StepParams& pf, int nb, cudaStream_t st) {
+    if (var == 1) {
+        if (pf.snap >= 0) k_step2s_interior<R, MODE, true><<<nb, 128, F2S<R, MODE == 1>::SMEM, st>>>(pf);
+        else k_step2s_interior<R, MODE, false><<<nb, 128, F2S<R, false>::SMEM, st>>>(pf);
+        return;
+    }
     if (pf.snap >= 0) k_step2_interior<R, MODE, true><<<nb, 128, F2Ring<R, MODE == 1>::SMEM, st>>>(pf);
     else k_step2_interior<R, MODE, false><<<nb, 128, F2Ring<R>::SMEM, st>>>(pf);
 }
 
 // Two-step interior tiles (kind 4) of list pf on stream st; pf.snap >= 0:
-// the first step stores that snapshot block / images with it.
-cudaError_t launch_step2(int acc, int mode, const StepParams& pf, cudaStream_t st) {
+// the first step stores that snapshot block / images with it.  var selects
+// the kernel: 0 = k_step2_interior (register queues, three blocks per SM),
+// 1 = k_step2s_interior (p_{n+1} rows in shared memory, up to four blocks
+// per SM); both compute the same cells with the same arithmetic.
+cudaError_t launch_step2(int acc, int mode, int var, const StepParams& pf, cudaStream_t st) {
     const int nb = (pf.nitems + 3) / 4;
     if (!nb) return cudaSuccess;
     if (mode == 0 && pf.snap >= 0 && pf.snap_form != 0) return cudaErrorInvalidValue;  // FP32 snapshots only
+    if (var != 0 && var != 1) return cudaErrorInvalidValue;
     if (acc == 3) {
-        if (mode == 0) launch_step2_variant<3, 0>(pf, nb, st);
-        else launch_step2_variant<3, 1>(pf, nb, st);
+        if (mode == 0) launch_step2_variant<3, 0>(var, pf, nb, st);
+        else launch_step2_variant<3, 1>(var, pf, nb, st);
     } else if (acc == 4) {
-        if (mode == 0) launch_step2_variant<4, 0>(pf, nb, st);
-        else launch_step2_variant<4, 1>(pf, nb, st);
+        if (mode == 0) launch_step2_variant<4, 0>(var, pf, nb, st);
+        else launch_step2_variant<4, 1>(var, pf, nb, st);
     } else {
         return cudaErrorInvalidValue;
     }

@@ -190,6 +190,9 @@ typedef struct fwi_survey_desc {
     int wave_shots;       /* shots per concurrent wave (0 = chosen by the tuner) */
     int band_rows;        /* rows per warp work item (0 = chosen by the tuner)   */
     int flags;            /* FWI_SURVEY_* bits                                   */
+    int tile_kernel;      /* two-step tile kernel: 0 = chosen by the tuner,
+                             1 = register queues, 2 = shared-memory queue        */
+    int tile_rows;        /* rows per two-step tile (0 = chosen by the tuner)    */
 } fwi_survey_desc;
 
 /* fwi_survey_desc.flags: launch every time step directly instead of
@@ -256,6 +259,13 @@ int fwi_survey_step_bytes(fwi_survey* s, double* bytes);
 int fwi_survey_two_step_bytes(fwi_survey* s, double* per_step, double* tiles_per_pass);
 /* Tuning chosen for the survey (wave size, band rows). */
 int fwi_survey_tuning(fwi_survey* s, int* wave_shots, int* band_rows);
+/* Two-step tiles chosen for the survey: kernel (1 = register queues, 2 =
+ * shared-memory queue; 0 when the survey runs single steps only) and rows per
+ * tile.  With times != NULL, also the tuner's measurements: times[k*ncand+c]
+ * = ms per forward two-step pass of the first wave for kernel k+1 and tile
+ * height cand[c] (-1 where not measured; cached or forced choices measure
+ * nothing); *ncand receives the number of tile heights tried (at most 8). */
+int fwi_survey_tiles(fwi_survey* s, int* tile_kernel, int* tile_rows, int* cand, float* times, int* ncand);
 /* Checkpointed recomputation plan: forward steps per segment and number of
  * segments (0, 0 when all snapshots are stored). */
 int fwi_survey_recompute(fwi_survey* s, int* segment_steps, int* segments);

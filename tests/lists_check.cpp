@@ -296,7 +296,10 @@ int main() {
         check_plan(k0, k1, sn, trial % 4 != 0, trial % 3 != 0);
     }
     check(400, 2000, 3, 20, 5, 16, 64);
+    check(400, 2000, 3, 20, 5, 16, 48);
+    check(400, 2000, 3, 20, 5, 16, 96);
     check(400, 2000, 4, 20, 5, 16, 64);
+    check(600, 3000, 3, 20, 5, 16, 96);
     check(37, 61, 3, 20, 3, 32, 48);
     check(12, 90, 4, 8, 3, 16, 64);
     int cases = 4;

@@ -66,29 +66,52 @@ def test_survey_gradient_vs_oracle(kw):
     (dict(store_snap=3, nt=151), False, 2), (dict(store_snap=4, nt=120), False, 1),
     (dict(nt=301, store_snap=5), True, 0), (dict(acc=4, nt=160, store_snap=4), True, 2)])
 def test_two_step_passes_bit_identical(kw, rc, form):
-    """Pairs of steps advanced by the two-step interior kernel (with the
-    single-step lists beside it) give the same bits as single steps: traces,
-    misfit and gradient, forward and adjoint, with snapshot stores and imaging
-    inside passes (FP32 snapshots; 16-bit ones are stored by single steps),
-    and with checkpointed recomputation."""
+    """Pairs of steps advanced by either two-step interior kernel (register
+    queues, or the p_{n+1} rows in shared memory), in one band or in bands of
+    13 rows, with the single-step lists beside them, give the same bits as
+    single steps: traces, misfit and gradient, forward and adjoint, with
+    snapshot stores and imaging inside passes (FP32 snapshots; 16-bit ones are
+    stored by single steps), and with checkpointed recomputation."""
     import fwi_gb300 as F
     from fwi_gb300.synth import lam_from_vp
     spec, vp = make(9, **kw)
     lam = lam_from_vp(vp)
     res = []
-    for two in (True, False):
-        sv = F.Survey(spec, snap_form=form, two_step=two, recompute=rc)
+    for two, kern, rows in ((False, 0, 0), (True, 1, 64), (True, 2, 64), (True, 2, 13)):
+        sv = F.Survey(spec, snap_form=form, two_step=two, recompute=rc, tile_kernel=kern, tile_rows=rows)
+        if two:
+            assert sv.tiles()[:2] == (kern, rows)
         sv.set_lambda(lam)
         g = np.zeros((spec.ny, spec.nx_model), np.float32, order="F")
         m, _ = sv.run(1, g)
         res.append((m, g, [sv.synthetic(i).copy() for i in range(len(spec.shots))]))
         sv.close()
-    (m2, g2, s2), (m1, g1, s1) = res
-    for a, b in zip(s2, s1):
-        np.testing.assert_array_equal(a, b)
-    assert m2 == m1
-    np.testing.assert_array_equal(g2, g1)
+    m1, g1, s1 = res[0]
+    for m2, g2, s2 in res[1:]:
+        for a, b in zip(s2, s1):
+            np.testing.assert_array_equal(a, b)
+        assert m2 == m1
+        np.testing.assert_array_equal(g2, g1)
     assert np.abs(g1).max() > 0
+
+
+def test_tuner_picks_a_measured_tile(monkeypatch):
+    """The tuner times both two-step kernels at each tile height on the first
+    wave and keeps the fastest; its choice is one of the measured ones."""
+    monkeypatch.setenv("FWI_TUNE_CACHE", "")  # no cross-process cache file
+    import fwi_gb300 as F
+    from fwi_gb300.synth import lam_from_vp
+    spec, vp = make(11, ny=70, nxm=400, nshots=4)
+    sv = F.Survey(spec)
+    kern, rows, meas = sv.tiles()
+    assert kern in (1, 2) and rows in (48, 64, 96)
+    if meas:  # empty when the choice came from the tuning cache
+        assert (kern, rows) in meas and meas[(kern, rows)] == min(meas.values())
+    sv.set_lambda(lam_from_vp(vp))
+    g = np.zeros((spec.ny, spec.nx_model), np.float32, order="F")
+    sv.run(1, g)
+    assert np.isfinite(g).all()
+    sv.close()
 
 
 def test_wave_split_is_bit_identical_and_fp32_form():

@@ -40,11 +40,15 @@ def parse():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=["mcs", "was", "mcs-f16", "inversion"], default="mcs",
+    ap.add_argument("--workload", choices=["mcs", "single", "was", "mcs-f16", "inversion"], default="mcs",
                     help="mcs: batched MCS survey, 400x2000 cells, 64 shots, 6000 steps (the metric's workload); "
+                         "single: one plain shot, 200x400 cells at 25 m, 8th order, 3000 steps; "
                          "was: uneven-window WAS batch; mcs-f16: the MCS survey with snapshots every 4 steps in "
                          "16 bits and checkpointed recomputation under a 120 GB budget; inversion: NLCG inversion "
                          "with frequency continuation (600x3000 cells, 128 shots)")
+    ap.add_argument("--errors", action="store_true",
+                    help="instead of timing: gradient and misfit errors of the GPU path against an FP64 run of the "
+                         "oracle on two shots of the workload at its full grid and record length")
     ap.add_argument("--budget", type=float, default=0.0, help="HBM budget in GB (0: all; mcs-f16: 120)")
     ap.add_argument("--recompute", action="store_true", help="checkpointed recomputation (mcs-f16: on)")
     ap.add_argument("--iters", type=int, default=10, help="inversion: NLCG iterations per band")
@@ -74,6 +78,10 @@ def parse():
 
 
 def workload_name(a):
+    if a.workload == "single":
+        return (f"plain single shot: 200x400 cells @25 m (water over a 1800-4500 m/s gradient with a Gaussian "
+                f"anomaly), 1 shot x 200 ch, nt={a.nt} (dt=2 ms), acc=4 (8th order), dPML=20, store_snap=10, "
+                f"{a.snap} snapshots, FP64 gradient stack")
     if a.workload == "was":
         return (f"uneven-window WAS batch: 600x6000 cells @25 m crustal model, {a.shots} OBS sources on 30-100 km "
                 f"windows, 1200 receivers @125 m, nt={a.nt} (dt=1.5625 ms, the CFL rule; 2.5 ms is unstable), "
@@ -88,6 +96,15 @@ def workload_name(a):
 
 def make_workload(a, seed_offset=0):
     from fwi_gb300 import synth
+    if a.workload == "single":
+        spec, vp_true, vp0 = synth.single_shot()
+        a.shots = 1
+        a.nt = spec.nt
+        return spec, vp_true, vp0
+    if a.workload == "inversion":
+        a.shots = a.shots or 128
+        a.nt = a.nt or 8000
+        return synth.inversion_workload(nshots=a.shots, nt=a.nt)
     if a.workload == "was":
         a.shots = a.shots or 30
         spec, vp_true, vp0 = synth.was_batch(seed=3 + seed_offset, nt=a.nt or None, nshots=a.shots)
@@ -190,8 +207,11 @@ def cpu_sample(spec, vp, nthreads, nt_sample):
     O.gradient_batch(sub, vp, step=1, nthreads=nthreads)
     t = time.perf_counter() - t0
     rate = nthreads / (t * (spec.nt / nt_sample))
-    desc = (f"{nthreads} shot-gradients of this workload (one per thread), each truncated to {nt_sample} of "
-            f"{spec.nt} time steps forward and adjoint, scaled by {spec.nt}/{nt_sample}")
+    if nt_sample >= spec.nt:
+        desc = f"{nthreads} full-length shot-gradients of this workload (one per thread)"
+    else:
+        desc = (f"{nthreads} shot-gradients of this workload (one per thread), each truncated to {nt_sample} of "
+                f"{spec.nt} time steps forward and adjoint, scaled by {spec.nt}/{nt_sample}")
     return rate, t, desc
 
 
@@ -201,7 +221,7 @@ def run_reference(a):
         return 0
     spec, vp_true, vp0 = make_workload(a)
     nthreads = os.cpu_count() or 1
-    nt_sample = 100 if a.workload in ("mcs", "mcs-f16") else 40
+    nt_sample = {"mcs": 100, "mcs-f16": 100, "single": 600}.get(a.workload, 40)
     for _ in range(a.warmup):
         cpu_sample(spec, vp0, nthreads, nt_sample)
     times = []
@@ -267,6 +287,7 @@ def run_inversion(a):
     grads = sum(1 for it in log) + 0.0
     trials = sum(len(it.trials) for it in log)
     calls = dev.calls
+    times, axes = dict(dev.times), dev.axes
     dev.close()
     err0 = float(np.linalg.norm(vp0 - vp_true) / np.linalg.norm(vp_true))
     # gradient-equivalents: a step-1 call is one shot-gradient per shot, a
@@ -281,6 +302,7 @@ def run_inversion(a):
                        f"{[b[1] for b in bands]} Hz (Butterworth order {a.order}), {a.iters} iterations per "
                        f"band, {a.snap} snapshots, FP64 stack", "bands": bands, "iters_per_band": a.iters},
             "inversion": {"model_error_start": err0, "seconds": secs, "calls": calls, "line_search_trials": trials,
+                          "time_axes": axes, "seconds_by_part": times,
                           "iterations": [{"iter": it.iter, "band_hz": it.band[1], "misfit": it.misfit,
                                           "model_error": it.model_error, "step": it.step,
                                           "trials": len(it.trials)} for it in log]},
@@ -289,8 +311,69 @@ def run_inversion(a):
     return 0
 
 
+def run_errors(a):
+    """Gradient and misfit errors of the GPU path against an FP64 run of the
+    oracle (every operation in double precision) on two shots of the workload
+    at its full grid and record length, for each snapshot form the workload
+    uses.  The observed data are the GPU's FP32 traces on the true model; both
+    paths image the starting model.  The GPU gradient is its FP64 stack (before
+    the water mask, which both sides would apply alike)."""
+    import torch
+    import fwi_gb300 as F
+    from fwi_gb300.synth import lam_from_vp
+    from oracle import oracle as O
+
+    F.init(0)
+    stream = torch.cuda.Stream()
+    F.set_stream(stream.cuda_stream)
+    spec, vp_true, vp0 = make_workload(a)
+    n = len(spec.shots)
+    if a.workload == "was":  # the two narrowest windows (a 100 km window takes the FP64 oracle over 20 minutes)
+        order = sorted(range(n), key=lambda i: spec.shots[i].nx)
+        pick = sorted(order[:2])
+    else:
+        pick = sorted({0, n // 2})
+    spec.shots = [spec.shots[i] for i in pick]
+    lam_t, lam0 = lam_from_vp(vp_true), lam_from_vp(vp0)
+    sv = F.Survey(spec)
+    sv.set_lambda(lam_t)
+    sv.run(2)
+    for i, sh in enumerate(spec.shots):
+        sh.obs = sv.synthetic(i)
+    sv.close()
+    forms = {"single": ["f32"], "mcs": ["f32"], "was": ["f32"], "mcs-f16": ["f32", "f16", "bf16"],
+             "inversion": ["f32", "f16"]}[a.workload]
+    gpu = {}
+    for f in forms:
+        form = {"f32": F.SNAP_F32, "bf16": F.SNAP_BF16, "f16": F.SNAP_F16}[f]
+        sv = F.Survey(spec, snap_form=form)
+        sv.set_lambda(lam0)
+        m, _ = sv.run(1)
+        gpu[f] = (m, sv.stack())
+        sv.close()
+    vp_ref = np.sqrt(lam0 / np.float32(1000.0)).astype(np.float64)
+    t0 = time.perf_counter()
+    kern, _, m64, _ = O.gradient_batch(spec, vp_ref, step=1, fp64=True, nthreads=len(spec.shots))
+    t_or = time.perf_counter() - t0
+    G = np.zeros((spec.ny, spec.nx_model))
+    for sh, k in zip(spec.shots, kern):
+        G[:, sh.x0:sh.x0 + sh.nx] += sh.grad_weight * k
+    mo = float(np.sum(m64))
+    out = {f: {"grad_rel_l2": float(np.linalg.norm(g - G) / np.linalg.norm(G)), "misfit": m,
+               "misfit_rel": abs(m - mo) / abs(mo)} for f, (m, g) in gpu.items()}
+    line = {"errors_vs_fp64_oracle": out, "misfit_fp64_oracle": mo, "workload": workload_name(a),
+            "shots": [{"index": i, "x0": s.x0, "nx": s.nx} for i, s in zip(pick, spec.shots)], "nt": spec.nt,
+            "oracle_seconds": t_or, "oracle_threads": len(spec.shots),
+            "how": "GPU: FP32 stencil, the snapshot form named, FP64 stack and misfit; oracle: the same solver "
+                   "with every operation in FP64 (CPU); observed data = GPU FP32 traces on the true model"}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     a = parse()
+    if a.errors:
+        return run_errors(a)
     if a.impl == "reference" and a.workload == "inversion":
         print(json.dumps({"impl": "reference", "unavailable": "the inversion workload is an NLCG run; the CPU "
                           "reference arm times the gradient path (the mcs and was workloads)"}))
@@ -420,6 +503,9 @@ def main():
             "two_step_tile_bytes_per_pass": tile_bytes_pass,
             "peak_kind": f"{peak_kind} copy bandwidth (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured"
             else "fallback 6.8 TB/s"}
+    if a.workload == "single":
+        roof["note"] = ("one 200x400 shot: its wavefields (10 x 256 x 512 floats = 5 MB) stay in the 129 MB L2, "
+                        "so the step is latency-bound and its fraction of the HBM peak is not meaningful")
     sv.close()
     del sv
     torch.cuda.synchronize()
@@ -507,7 +593,8 @@ def main():
     cpu = None
     if rank == 0 and world == 1 and not a.no_cpu:
         nthreads = os.cpu_count() or 1
-        rate, tcpu, desc = cpu_sample(spec, vp0, nthreads, 600 if a.workload in ("mcs", "mcs-f16") else 150)
+        nts = {"mcs": 600, "mcs-f16": 600, "single": spec.nt}.get(a.workload, 150)
+        rate, tcpu, desc = cpu_sample(spec, vp0, nthreads, nts)
         cpu = {"value": rate, "unit": METRIC, "cores": nthreads, "kind": "port", "sample": desc,
                "seconds": tcpu}
 

@@ -26,10 +26,12 @@ from .api import (  # noqa: E402,F401
     Ricker_mcs,
     Survey,
     calculate_misfit_gradient,
+    first_step,
     init,
     interpolation_akima,
     kernel_launch_count,
     mcs_geometry,
+    model_update,
     read_nav,
     set_filter_order,
     set_solver_options,

@@ -33,6 +33,7 @@ EXPORTS = [
     "fwi_survey_recompute", "fwi_survey_set_time", "fwi_time_filter", "fwi_set_filter_order",
     "fwi_interpolation_akima", "fwi_su_info", "fwi_su_read", "fwi_su_write", "fwi_read_nav",
     "fwi_survey_time_steps", "fwi_misfit_gradient_batch", "fwi_solver_forward_noalloc", "fwi_survey_tiles",
+    "fwi_batch_plans", "fwi_batch_release", "fwi_first_step", "fwi_model_update",
 ]
 
 
@@ -76,9 +77,12 @@ def load():
     lib.fwi_set_stream.argtypes = [P]
     lib.fwi_set_solver_options.argtypes = [I, I]
     lib.fwi_kernel_launch_count.restype = C.c_int64
+    lib.fwi_batch_plans.restype = C.c_int64
     lib.fwi_solver_acoustic_ss.argtypes = [P] * 21
     lib.fwi_misfit_function.argtypes = [P] * 10
     lib.fwi_beta_calculous.argtypes = [P] * 7
+    lib.fwi_first_step.argtypes = [P] * 5
+    lib.fwi_model_update.argtypes = [P] * 6
     lib.fwi_mcs_geometry.argtypes = [F, F, F, F, F, F, I, P, P, P, P]
     lib.fwi_ricker.argtypes = [F, F, I, P]
     lib.fwi_time_rules.argtypes = [P, I, I, F, F, I, P, P, P]
@@ -109,7 +113,7 @@ def load():
     lib.fwi_solver_forward_noalloc.argtypes = [I, I, P, P, P, P, P, F, F, I, I, P, I, P]
     for name in EXPORTS:
         fn = getattr(lib, name)
-        if fn.restype is None and name not in ("fwi_last_error", "fwi_kernel_launch_count"):
+        if fn.restype is None and name not in ("fwi_last_error", "fwi_kernel_launch_count", "fwi_batch_plans"):
             fn.restype = C.c_int
     _lib = lib
     return lib

@@ -101,6 +101,24 @@ def Beta_calculous(Grad, OldGrad, nx, ny):
     return np.float32(b.value), n64.value, d64.value
 
 
+def first_step(Search, var_orig):
+    """nut = 1/100/maxval(abs(Search/log(var_orig))) on the device (FWI.f90:175)."""
+    s, v = _f32(Search), _f32(var_orig)
+    ny, nx = s.shape
+    nut = C.c_float(0.0)
+    N.check(N.load().fwi_first_step(_p(s), _p(v), _ri(nx), _ri(ny), C.byref(nut)))
+    return np.float32(nut.value)
+
+
+def model_update(Search, var_orig, step):
+    """lambda = exp(Search*step)*var_orig on the device (FWI.f90:227, :315)."""
+    s, v = _f32(Search), _f32(var_orig)
+    ny, nx = s.shape
+    out = np.zeros((ny, nx), np.float32, order="F")
+    N.check(N.load().fwi_model_update(_p(s), _p(v), _rf(step), _ri(nx), _ri(ny), _p(out)))
+    return out
+
+
 def Ricker_mcs(freq, dt, nt):
     out = np.zeros(nt, np.float32)
     N.check(N.load().fwi_ricker(freq, dt, nt, _p(out)))

@@ -241,6 +241,35 @@ __global__ void k_nonfinite(const float* a, size_t n, int* flag) {
         if (!isfinite(a[i])) { *flag = 1; return; }
 }
 
+// The NLCG model arithmetic of FWI.f90 in the reference's FP32 operations,
+// with exp and log evaluated in FP64 and rounded once to FP32 (the correctly
+// rounded value of the FP32 function).
+//
+// max|Search/log(var_orig)| (FWI.f90:175): per element the FP32 log, the
+// FP32 quotient and its magnitude; the maximum over all elements (NaN
+// entries skipped, as MAXVAL compares with >) as the bits of a non-negative
+// float, which order like integers.
+__global__ void k_search_max(const float* search, const float* var, size_t n, unsigned* out) {
+    float m = 0.f;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const float lg = __double2float_rn(log((double)var[i]));
+        const float v = fabsf(__fdiv_rn(search[i], lg));
+        if (v > m) m = v;
+    }
+    m = warp_max(m);
+    if ((threadIdx.x & 31) == 0) atomicMax(out, __float_as_uint(m));
+}
+
+// lambda = exp(Search*step)*var_orig (FWI.f90:227, :315): FP32 product, exp,
+// FP32 product.
+__global__ void k_model_update(const float* search, const float* var, float step, size_t n, float* lam) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const float t = __fmul_rn(search[i], step);
+        const float e = __double2float_rn(exp((double)t));
+        lam[i] = __fmul_rn(e, var[i]);
+    }
+}
+
 }  // namespace
 
 // ---------------------------------------------------------------------------
@@ -293,6 +322,15 @@ cudaError_t launch_kernel_io(float* dev, float* fort, int ny, int nx, int pitch,
 cudaError_t launch_dot(const float* g, const float* o, size_t n, double* part, int nb, double* out, cudaStream_t st) {
     k_dot_partial<<<nb, 256, 0, st>>>(g, o, n, part);
     k_dot_final<<<1, 32, 0, st>>>(part, nb, out);
+    return cudaGetLastError();
+}
+cudaError_t launch_search_max(const float* search, const float* var, size_t n, unsigned* out, cudaStream_t st) {
+    k_search_max<<<2 * 152, 256, 0, st>>>(search, var, n, out);
+    return cudaGetLastError();
+}
+cudaError_t launch_model_update(const float* search, const float* var, float step, size_t n, float* lam,
+                                cudaStream_t st) {
+    k_model_update<<<4 * 152, 256, 0, st>>>(search, var, step, n, lam);
     return cudaGetLastError();
 }
 size_t copy_job_size() { return sizeof(CopyJob); }

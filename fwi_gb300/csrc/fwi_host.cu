@@ -45,6 +45,9 @@ cudaError_t launch_kernel_io(float* dev, float* fort, int ny, int nx, int pitch,
                              cudaStream_t st);
 cudaError_t launch_dot(const float* g, const float* o, size_t n, double* part, int nb, double* out, cudaStream_t st);
 cudaError_t launch_nonfinite(const float* a, size_t n, int* flag, cudaStream_t st);
+cudaError_t launch_search_max(const float* search, const float* var, size_t n, unsigned* out, cudaStream_t st);
+cudaError_t launch_model_update(const float* search, const float* var, float step, size_t n, float* lam,
+                                cudaStream_t st);
 size_t copy_job_size();
 void fill_copy_job(void* dst, const void* src, void* to, size_t bytes);
 cudaError_t launch_copy_jobs(const void* jobs, int njobs, cudaStream_t st);
@@ -351,6 +354,9 @@ StepParams base_params(int acc, float dt, int store_snap, int snap_form, int gra
     p.fA = dfA;
     p.fB = dfB;
     p.dt = dt;
+    // RN(1/dt) for the snapshot quotient (fwi_div.cuh); a dt whose reciprocal
+    // is not a normal float falls back to the division
+    p.rdt = (dt >= 0x1p-60f && dt <= 0x1p60f) ? 1.f / dt : 0.f;
     p.ss = (float)store_snap;
     p.snap_form = snap_form;
     p.grad_form = grad_form;
@@ -608,6 +614,24 @@ Single& single() {
     return s;
 }
 
+// The plan of fwi_misfit_gradient_batch: the survey of the last geometry seen
+// (one survey: a new geometry frees the previous one's device memory before
+// it plans, so the wave sizes always see the whole device).
+struct BatchPlan {
+    std::string key;
+    fwi_survey* s = nullptr;
+    long long plans = 0;
+    void release() {
+        if (s) fwi_survey_destroy(s);
+        s = nullptr;
+        key.clear();
+    }
+};
+BatchPlan& batch_plan() {
+    static BatchPlan b;
+    return b;
+}
+
 int check_nonfinite(const float* dptr, size_t n, DBuf& flag, cudaStream_t st, const char* what) {
     TRY(flag.ensure(sizeof(int)));
     CK(cudaMemsetAsync(flag.p, 0, sizeof(int), st));
@@ -675,6 +699,7 @@ int fwi_finalize(void) {
     std::lock_guard<std::recursive_mutex> g(L().mu);
     if (!L().init) return FWI_OK;
     cudaDeviceSynchronize();
+    batch_plan().release();
     Single& s = single();
     s.~Single();
     new (&s) Single();
@@ -921,6 +946,72 @@ int fwi_beta_calculous(const float* Grad, const float* OldGrad, const int* nx_, 
     return FWI_OK;
 }
 
+// Inputs of the NLCG model kernels: device pointers as given, host arrays
+// staged through buffers of this call.
+namespace {
+int nlcg_inputs(const float* a, const float* b, size_t n, DBuf& da, DBuf& db, const float** pa, const float** pb,
+                cudaStream_t st) {
+    *pa = a;
+    *pb = b;
+    if (!is_device_ptr(a)) {
+        TRY(da.alloc(n * 4));
+        CK(cudaMemcpyAsync(da.p, a, n * 4, cudaMemcpyHostToDevice, st));
+        *pa = da.as<float>();
+    }
+    if (!is_device_ptr(b)) {
+        TRY(db.alloc(n * 4));
+        CK(cudaMemcpyAsync(db.p, b, n * 4, cudaMemcpyHostToDevice, st));
+        *pb = db.as<float>();
+    }
+    return FWI_OK;
+}
+}  // namespace
+
+int fwi_first_step(const float* Search, const float* var_orig, const int* nx_, const int* ny_, float* nut) {
+    std::lock_guard<std::recursive_mutex> g(L().mu);
+    TRY(ensure_init());
+    if (!Search || !var_orig || !nx_ || !ny_ || !nut) return fail(FWI_ERR_ARG, "null argument");
+    if (*nx_ < 1 || *ny_ < 1) return fail(FWI_ERR_ARG, "nx, ny must be >= 1");
+    const size_t n = (size_t)(*nx_) * (*ny_);
+    cudaStream_t st = stream();
+    DBuf ds, dv, dm;
+    const float *ps = nullptr, *pv = nullptr;
+    TRY(nlcg_inputs(Search, var_orig, n, ds, dv, &ps, &pv, st));
+    TRY(dm.alloc(sizeof(unsigned)));
+    CK(cudaMemsetAsync(dm.p, 0, sizeof(unsigned), st));
+    LK(launch_search_max(ps, pv, n, dm.as<unsigned>(), st));
+    unsigned bits = 0;
+    CK(cudaMemcpyAsync(&bits, dm.p, sizeof bits, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    float mx;
+    std::memcpy(&mx, &bits, sizeof mx);
+    *nut = (1.f / 100.f) / mx;  // FWI.f90:175 (mx = 0 gives +Inf, as the reference)
+    return FWI_OK;
+}
+
+int fwi_model_update(const float* Search, const float* var_orig, const float* step, const int* nx_, const int* ny_,
+                     float* lambda) {
+    std::lock_guard<std::recursive_mutex> g(L().mu);
+    TRY(ensure_init());
+    if (!Search || !var_orig || !step || !nx_ || !ny_ || !lambda) return fail(FWI_ERR_ARG, "null argument");
+    if (*nx_ < 1 || *ny_ < 1) return fail(FWI_ERR_ARG, "nx, ny must be >= 1");
+    const size_t n = (size_t)(*nx_) * (*ny_);
+    cudaStream_t st = stream();
+    DBuf ds, dv, dl;
+    const float *ps = nullptr, *pv = nullptr;
+    TRY(nlcg_inputs(Search, var_orig, n, ds, dv, &ps, &pv, st));
+    const bool dev_out = is_device_ptr(lambda);
+    float* pl = lambda;
+    if (!dev_out) {
+        TRY(dl.alloc(n * 4));
+        pl = dl.as<float>();
+    }
+    LK(launch_model_update(ps, pv, *step, n, pl, st));
+    if (!dev_out) CK(cudaMemcpyAsync(lambda, pl, n * 4, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    return FWI_OK;
+}
+
 int fwi_mcs_geometry(float xs, float shot_depth, float streamer_depth, float near_offset, float drec, float dmodel,
                      int num_rec, int* nxSou, int* nySou, int* nxRec, int* nyRec) {
     if (num_rec < 0 || !(dmodel > 0.f)) return fail(FWI_ERR_ARG, "num_rec >= 0 and dmodel > 0 required");
@@ -994,6 +1085,7 @@ struct fwi_survey {
         double fus_cells = 0.0;
         cudaGraphExec_t graph[3] = {nullptr, nullptr, nullptr};
         long long graph_kernels[3] = {0, 0, 0};  // kernel nodes per graph
+        int direct_runs[3] = {0, 0, 0};          // runs launched directly since the graph was dropped
         DBuf save_jobs, restore_jobs;  // checkpoint copies: [ckpt][shot][field]
     };
     std::vector<std::unique_ptr<WaveDev>> wdev;
@@ -1182,8 +1274,8 @@ int survey_prepare_waves(fwi_survey* s) {
 
 int time_wave0_steps(fwi_survey* s, int steps, float* ms, bool single_only = false);
 
-constexpr int TILE_BANDS[] = {48, 64, 96};
-constexpr int NTB = 3;
+constexpr int TILE_BANDS[] = {16, 32, 48, 64, 96};  // short tiles: more warps for small grids
+constexpr int NTB = 5;
 constexpr int BANDS[] = {16, 24, 32, 48, 64};
 constexpr int TUNE_PASSES = 24;
 
@@ -1776,12 +1868,14 @@ int fwi_survey_set_time(fwi_survey* s, float dt, int nt, const float* src, const
         TRY(survey_plan(s, false));
     } else {
         // dt is baked into the captured graphs (c2, the snapshot scaling)
-        for (auto& w : s->wdev)
+        for (auto& w : s->wdev) {
             for (auto& gexec : w->graph)
                 if (gexec) {
                     cudaGraphExecDestroy(gexec);
                     gexec = nullptr;
                 }
+            for (int& n : w->direct_runs) n = 0;
+        }
     }
     CK(cudaStreamSynchronize(st));
     return FWI_OK;
@@ -1836,8 +1930,13 @@ int fwi_survey_run(fwi_survey* s, int step, double* misfit, float* grad) {
     const int gi = step == 1 ? 0 : 1;
     for (size_t wi = 0; wi < s->waves.size(); ++wi) {
         auto& wd = *s->wdev[wi];
-        if (D.flags & FWI_SURVEY_NO_GRAPH) {
+        // the first run of a time axis launches directly: capturing and
+        // instantiating a long time loop costs seconds, which a time axis run
+        // once (a line-search trial) would not win back; the second run
+        // captures the graph, later runs replay it
+        if ((D.flags & FWI_SURVEY_NO_GRAPH) || (!wd.graph[gi] && wd.direct_runs[gi] == 0)) {
             TRY(issue_wave(s, wi, step, st, L().aux));
+            ++wd.direct_runs[gi];
             continue;
         }
         if (!wd.graph[gi]) {
@@ -2031,33 +2130,44 @@ int fwi_misfit_gradient_batch(const fwi_survey_desc* desc, const float* lambda, 
     std::lock_guard<std::recursive_mutex> g(L().mu);
     TRY(ensure_init());
     if (!desc || !lambda) return fail(FWI_ERR_ARG, "null argument");
-    // plan cache keyed by the geometry (sizes and indices); data re-uploaded
-    static std::map<std::string, std::unique_ptr<fwi_survey>> cache;
+    if (desc->nshots < 1 || !desc->shots) return fail(FWI_ERR_ARG, "nshots must be >= 1");
+    // plan key: the geometry (sizes, indices, weights, forms, tuning), not the
+    // time axis -- the line search of FWI.f90:225-227 recomputes dt and nt from
+    // every trial model (calculate_misfit_gradient.f90:198-203), which only
+    // moves the survey to a new time axis (fwi_survey_set_time)
     std::string key;
     auto add = [&](const void* p, size_t n) { key.append(reinterpret_cast<const char*>(p), n); };
     fwi_survey_desc k0 = *desc;
     k0.shots = nullptr;
     k0.water_rows = nullptr;
+    k0.dt = 0.f;
+    k0.nt = 0;
     add(&k0, sizeof k0);
     for (int i = 0; i < desc->nshots; ++i) {
         const fwi_shot& sh = desc->shots[i];
         add(&sh.x0, sizeof(int) * 4);
         add(&sh.grad_weight, sizeof(double) * 2);
-        if (sh.num_sou) { add(sh.nxSou, 4 * sh.num_sou); add(sh.nySou, 4 * sh.num_sou); }
-        if (sh.num_rec) { add(sh.nxRec, 4 * sh.num_rec); add(sh.nyRec, 4 * sh.num_rec); }
+        if (sh.num_sou > 0 && sh.nxSou && sh.nySou) { add(sh.nxSou, 4 * sh.num_sou); add(sh.nySou, 4 * sh.num_sou); }
+        if (sh.num_rec > 0 && sh.nxRec && sh.nyRec) { add(sh.nxRec, 4 * sh.num_rec); add(sh.nyRec, 4 * sh.num_rec); }
     }
     if (desc->water_rows) add(desc->water_rows, 4 * desc->nx_model);
-    auto it = cache.find(key);
+    BatchPlan& bp = batch_plan();
     fwi_survey* s = nullptr;
-    if (it == cache.end()) {
-        if (cache.size() >= 4) cache.clear();
+    if (!bp.s || bp.key != key) {
+        bp.release();  // the previous geometry's buffers first
         fwi_survey* ns = nullptr;
         TRY(fwi_survey_create(desc, &ns));
-        cache[key].reset(ns);
+        bp.s = ns;
+        bp.key = key;
+        ++bp.plans;
         s = ns;
     } else {
-        s = it->second.get();
-        // new data for the same geometry
+        s = bp.s;
+        if (desc->nt != s->desc.nt || desc->dt != s->desc.dt) {
+            // a new time axis: the sources and data below are uploaded at the new length
+            TRY(fwi_survey_set_time(s, desc->dt, desc->nt, nullptr, nullptr));
+        }
+        // this call's sources and observed data
         cudaStream_t st = stream();
         size_t so = 0, to = 0;
         const size_t nt = desc->nt;
@@ -2065,8 +2175,12 @@ int fwi_misfit_gradient_batch(const fwi_survey_desc* desc, const float* lambda, 
             const fwi_shot& sh = desc->shots[i];
             if (sh.num_sou && sh.src)
                 CK(cudaMemcpyAsync(s->d_src.as<float>() + so, sh.src, nt * sh.num_sou * 4, cudaMemcpyHostToDevice, st));
+            else if (sh.num_sou)
+                CK(cudaMemsetAsync(s->d_src.as<float>() + so, 0, nt * sh.num_sou * 4, st));
             if (sh.num_rec && sh.obs)
                 CK(cudaMemcpyAsync(s->d_obs.as<float>() + to, sh.obs, nt * sh.num_rec * 4, cudaMemcpyHostToDevice, st));
+            else if (sh.num_rec)
+                CK(cudaMemsetAsync(s->d_obs.as<float>() + to, 0, nt * sh.num_rec * 4, st));
             so += nt * sh.num_sou;
             to += nt * sh.num_rec;
         }
@@ -2076,6 +2190,14 @@ int fwi_misfit_gradient_batch(const fwi_survey_desc* desc, const float* lambda, 
     const int rc = fwi_survey_run(s, step, &m, step == 1 ? Grad : nullptr);
     if (Misfit) *Misfit = *Misfit + (float)m;
     return rc;
+}
+
+int64_t fwi_batch_plans(void) { return batch_plan().plans; }
+
+int fwi_batch_release(void) {
+    std::lock_guard<std::recursive_mutex> g(L().mu);
+    batch_plan().release();
+    return FWI_OK;
 }
 
 }  // extern "C"

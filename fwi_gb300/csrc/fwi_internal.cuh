@@ -65,6 +65,7 @@ struct StepParams {
     int grad_form;              // FWI_GRAD_*
     int record;                 // 1: record receivers
     float dt;                   // for ((p3-p1)*0.5)/dt
+    float rdt;                  // RN(1/dt) for div_by_const (0: divide)
     float ss;                   // float(store_snap) for the imaging condition
     float c1[MAXR + 1];         // first-derivative taps
     float c2[MAXR + 1];         // second-derivative taps (centre halved)

@@ -38,6 +38,7 @@
 
 #include <climits>
 
+#include "fwi_div.cuh"
 #include "fwi_internal.cuh"
 
 namespace fwi {
@@ -133,7 +134,7 @@ __device__ __forceinline__ void store_snapshot(const StepParams& P, const ShotDe
 #pragma unroll
     for (int e = 0; e < 4; ++e) {
         in[e] = (e >= lo) && (e < hi);
-        v[e] = in[e] ? ((p3[e] - pm1[e]) * 0.5f) / P.dt : 0.f;
+        v[e] = in[e] ? div_by_const((p3[e] - pm1[e]) * 0.5f, P.dt, P.rdt) : 0.f;
     }
     const bool full = in[0] && in[3];
     const size_t base = (size_t)P.snap * (size_t)S.snap_stride + (size_t)yrow * S.pitch + xl;
@@ -1013,7 +1014,7 @@ __device__ __forceinline__ void strip_rows(const StepParams& P, const WorkItem& 
                 // Fields(j, snap*nx+i) = (p_3 - p_1)*0.5/dt  (:447)
                 float v[K];
 #pragma unroll
-                for (int k = 0; k < K; ++k) v[k] = in[k] ? ((p3[k] - pm1[k]) * 0.5f) / P.dt : 0.f;
+                for (int k = 0; k < K; ++k) v[k] = in[k] ? div_by_const((p3[k] - pm1[k]) * 0.5f, P.dt, P.rdt) : 0.f;
                 if (P.snap_form == 0) {
 #pragma unroll
                     for (int k = 0; k < K; ++k)
@@ -1168,7 +1169,7 @@ __device__ __forceinline__ void snap_or_image(const StepParams& P, const ShotDev
     if (MODE == 0) {
         float v[4];
 #pragma unroll
-        for (int e = 0; e < 4; ++e) v[e] = ((p3[e] - pm1[e]) * 0.5f) / P.dt;
+        for (int e = 0; e < 4; ++e) v[e] = div_by_const((p3[e] - pm1[e]) * 0.5f, P.dt, P.rdt);
         float* F = reinterpret_cast<float*>(S.snaps) + fo;
         if (full) {
             st4(F, from_arr(v));

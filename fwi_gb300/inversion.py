@@ -16,8 +16,9 @@ The host driver mirrors the reference's Fortran driver:
   elimination it calls (LEGS/ELGS, T. Pang, *An Introduction to
   Computational Physics*), in FP64 with the reference's FP32 trial points.
 
-Model arithmetic (search direction, exponential update) is FP32 numpy, as the
-reference's REAL arrays.  ``DeviceGradient`` is calculate_misfit_gradient for
+The search direction is FP32 numpy, as the reference's REAL arrays; the first
+trial step and the exponential model update run on the device
+(``DeviceModelOps``).  ``DeviceGradient`` is calculate_misfit_gradient for
 all shots on the device: the observed traces and the source are filtered once
 per band (``time_filter``), every call takes dt and nt from the trial model
 (``time_rules``), resamples the filtered traces to them
@@ -169,6 +170,12 @@ class DeviceGradient:
         self.cur = None  # (dt, nt, band id) of the data in the survey
         self.band_id = 0
         self.calls = 0
+        # wall time (s): resampling the data to a new time axis, moving the
+        # survey to it (fwi_survey_set_time: re-plan when nt changes), the
+        # first run on each axis (direct launches) and the later runs
+        self.times = {"resample": 0.0, "set_time": 0.0, "first_runs": 0.0, "runs": 0.0}
+        self.axes = 0
+        self._fresh = False
 
     def set_source(self, wavelet):
         """Replace the source wavelet S0(nt_data) (source estimation); the
@@ -188,7 +195,9 @@ class DeviceGradient:
         self.band_id += 1
 
     def _prepare(self, lam):
+        import time
         torch = self.torch
+        t0 = time.perf_counter()
         dt, nt, _ = api.time_rules(lam, self.spec.d, self.raw.tfin, self.store_snap)
         key = (float(dt), int(nt), self.band_id)
         if key == self.cur:
@@ -201,6 +210,8 @@ class DeviceGradient:
                                 out=s1.data_ptr())
         src = s1.expand(sum(self.nsou), nt).contiguous()
         torch.cuda.synchronize(self.dev)
+        t1 = time.perf_counter()
+        self.times["resample"] += t1 - t0
         if self.survey is None:
             shots = [dataclasses.replace(sh, obs=None, src=None) for sh in self.spec.shots]
             spec = dataclasses.replace(self.spec, nt=int(nt), dt=float(dt), shots=shots)
@@ -209,12 +220,19 @@ class DeviceGradient:
         self.survey.set_time(float(dt), int(nt), src.data_ptr(), obs.data_ptr())
         self._keep = (obs, src)
         self.cur = key
+        self.times["set_time"] += time.perf_counter() - t1
+        self.axes += 1
+        self._fresh = True
 
     def __call__(self, lam: np.ndarray, step: int, grad: Optional[np.ndarray] = None) -> Tuple[float, Optional[np.ndarray]]:
+        import time
         lam = np.asfortranarray(lam, dtype=np.float32)
         self._prepare(lam)
+        t0 = time.perf_counter()
         self.survey.set_lambda(lam)
         m, g = self.survey.run(step, grad if step == 1 else None)
+        self.times["first_runs" if self._fresh else "runs"] += time.perf_counter() - t0
+        self._fresh = False
         self.calls += 1
         return m, g
 
@@ -244,15 +262,32 @@ def _beta(grad: np.ndarray, old: np.ndarray) -> float:
     return float(api.Beta_calculous(grad, old, nx, ny)[0])
 
 
+class DeviceModelOps:
+    """The model arithmetic of FWI.f90 on the device: the first trial step
+    1/100/maxval(abs(Search/log(var_orig))) (FWI.f90:175, fwi_first_step) and
+    the update exp(Search*step)*var_orig (FWI.f90:227, :315,
+    fwi_model_update), in the reference's FP32 operations with exp and log
+    rounded once from FP64."""
+
+    @staticmethod
+    def first_step(search: np.ndarray, var_orig: np.ndarray) -> np.float32:
+        return api.first_step(search, var_orig)
+
+    @staticmethod
+    def update(search: np.ndarray, var_orig: np.ndarray, step) -> np.ndarray:
+        return api.model_update(search, var_orig, step)
+
+
 def fwi_band(lam: np.ndarray, gradient: Callable, f1: float, f2: float, n_iter: int, iter0: int = 1,
              method: int = 1, beta_fn: Callable = _beta, vp_true: Optional[np.ndarray] = None,
-             log: Optional[List[IterationLog]] = None) -> Tuple[np.ndarray, int]:
+             log: Optional[List[IterationLog]] = None, ops=DeviceModelOps) -> Tuple[np.ndarray, int]:
     """FWI(iter, f1, f2) (FWI.f90:1-368) for one band: n_iter NLCG iterations
     with the reference's line search.  lam (ny, nx) FP32 is the starting
     model (the reference's global lambda); returns the final model and the
     next global iteration number.  ``gradient(lam, step, grad)`` is
     calculate_misfit_gradient over all shots (step 1: misfit and gradient,
-    step 2: misfit only)."""
+    step 2: misfit only); ``ops`` the model arithmetic (first trial step and
+    exponential update), on the device by default."""
     lam = np.asfortranarray(lam, dtype=np.float32).copy()
     ny, nx = lam.shape
     var_orig = lam.copy()
@@ -280,8 +315,7 @@ def fwi_band(lam: np.ndarray, gradient: Callable, f1: float, f2: float, n_iter: 
         old_grad = grad
         # first trial step: 1 % of the largest relative model change (FWI.f90:186-190)
         if end_step == 0.0:
-            with np.errstate(divide="ignore", invalid="ignore"):
-                nut = F32(F32(F32(1.0) / F32(100.0)) / np.abs(search / np.log(var_orig)).max())
+            nut = F32(ops.first_step(search, var_orig))
         else:
             nut = end_step
         m_test0 = m_test1 = misfit
@@ -293,8 +327,7 @@ def fwi_band(lam: np.ndarray, gradient: Callable, f1: float, f2: float, n_iter: 
         while not looptest:                               # line search (FWI.f90:206-274)
             loopind += 1
             looptotal += 1
-            with np.errstate(over="ignore"):
-                lam = (np.exp(search * nut) * var_orig).astype(np.float32)
+            lam = ops.update(search, var_orig, nut)
             if loopind >= 2:
                 m_test0 = m_test1
                 m_test1 = m_test
@@ -322,8 +355,7 @@ def fwi_band(lam: np.ndarray, gradient: Callable, f1: float, f2: float, n_iter: 
         if restart:
             continue
         end_step = polyfit(nut, misfit if loopind == 2 else m_test0, m_test1, m_test, loopind)
-        with np.errstate(over="ignore"):
-            lam = (np.exp(search * end_step) * var_orig).astype(np.float32)
+        lam = ops.update(search, var_orig, end_step)
         var_orig = lam.copy()
         err = None
         if vp_true is not None:

@@ -106,11 +106,16 @@ def mcs_survey(vp, d, dt, nt, xs_list, nrec, drec, near=150.0, sdepth=10.0, rdep
 
 
 def single_shot(seed=1):
-    """Plain single shot (200 x 400 cells, 8th order, 3000 steps): returns (spec, vp_true, vp_start)."""
+    """Plain single shot (200 x 400 cells, 8th order, 3000 steps): returns
+    (spec, vp_true, vp_start).  The shot sits at a seeded x in [6000, 7000) m,
+    so that its 200-channel streamer (150 m near offset, trailing towards
+    x = 0) lies inside the model and over the anomaly at x = 5 km; a shot near
+    x = 2.6 km would record almost nothing of the anomaly (a residual at the
+    FP32 rounding level)."""
     vp_true, wrows = model_single_shot(seed, anomaly=True)
     vp0, _ = model_single_shot(seed, anomaly=False)
     rng = np.random.default_rng(seed + 100)
-    spec = mcs_survey(vp_true, 25.0, 0.002, 3000, [2637.5 + 25.0 * int(rng.integers(0, 40))], 200, 12.5, near=150.0,
+    spec = mcs_survey(vp_true, 25.0, 0.002, 3000, [6000.0 + 25.0 * int(rng.integers(0, 40))], 200, 12.5, near=150.0,
                       sdepth=10.0, rdepth=10.0, freq=8.0, acc=4, dpml=20, seed=seed, water_rows=wrows,
                       shift_max=0.02)
     return spec, vp_true, vp0

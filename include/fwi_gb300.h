@@ -102,6 +102,16 @@ int fwi_misfit_function(const int* rank, const float* freq, const float* Data_Sy
 int fwi_beta_calculous(const float* Grad, const float* OldGrad, const int* nx, const int* ny,
                        float* Beta, double* num64, double* den64);
 
+/* The NLCG model arithmetic of FWI.f90 on the device, in the reference's
+ * FP32 operations with exp and log evaluated in FP64 and rounded once (the
+ * correctly rounded FP32 value).  Arrays (ny, nx) column-major, host or device
+ * pointers (the call detects which).
+ *   fwi_first_step:   nut = 1/100/maxval(abs(Search/log(var_orig)))   FWI.f90:175
+ *   fwi_model_update: lambda = exp(Search*step)*var_orig         FWI.f90:227, :315 */
+int fwi_first_step(const float* Search, const float* var_orig, const int* nx, const int* ny, float* nut);
+int fwi_model_update(const float* Search, const float* var_orig, const float* step, const int* nx,
+                     const int* ny, float* lambda);
+
 /* ---- geometry and wavelet (host arithmetic, bit-exact FP32) -------------- */
 
 /* One MCS shot: shot x position xs (m), depths, near offset, channel
@@ -274,12 +284,21 @@ int fwi_survey_recompute(fwi_survey* s, int* segment_steps, int* segments);
 int fwi_survey_time_steps(fwi_survey* s, int steps);
 
 /* calculate_misfit_gradient(iter,step,f1,f2,dt,nt,tfin,S0,Misfit,Grad) for
- * all shots in one call, with host buffers: plans (or reuses a cached plan
- * for the same geometry), uploads lambda, sources and observed data, runs,
- * and downloads Misfit (+=) and Grad (updated, masked).
- * src/calculate_misfit_gradient.f90:1-366 */
+ * all shots in one call, with host buffers: uploads lambda, sources and
+ * observed data, runs, and downloads Misfit (+=) and Grad (updated, masked).
+ * src/calculate_misfit_gradient.f90:1-366
+ * The library keeps the plan (device buffers, work lists, tuning, graphs) of
+ * the last geometry it was called with -- sizes, grid indices, weights and
+ * forms, not dt and nt: a call with a new dt/nt (the line search of
+ * FWI.f90:225-227 derives them from every trial model) moves that plan to the
+ * new time axis as fwi_survey_set_time does; a new geometry frees the old
+ * plan before it plans. */
 int fwi_misfit_gradient_batch(const fwi_survey_desc* desc, const float* lambda, int step,
                               float* Misfit, float* Grad);
+/* Number of plans fwi_misfit_gradient_batch has built in this process. */
+int64_t fwi_batch_plans(void);
+/* Free the plan fwi_misfit_gradient_batch holds (its device memory). */
+int fwi_batch_release(void);
 
 /* ---- forward traces without device allocation --------------------------- */
 

@@ -97,7 +97,9 @@ def test_inversion_two_bands_vs_oracle_backend():
         g64, o64 = g.astype(np.float64), o.astype(np.float64)
         return float(F32(np.sum(g64 * (g64 - o64)) / np.sum(o64 * o64)))
 
-    lam_o, log_o = invert(lam0, OracleGradient(spec, raw), bands, 2, vp_true=vp_true, beta_fn=beta64)
+    from oracle.nlcg import HostModelOps
+    lam_o, log_o = invert(lam0, OracleGradient(spec, raw), bands, 2, vp_true=vp_true, beta_fn=beta64,
+                          ops=HostModelOps)
     for lg, lo in zip(log_g, log_o):
         print(f"iter {lg.iter} band {lg.band}: misfit {lg.misfit:.6e} / {lo.misfit:.6e}, step {lg.step:.4e} / "
               f"{lo.step:.4e}, trials {len(lg.trials)} / {len(lo.trials)}, model error {lg.model_error:.5f}")
@@ -118,3 +120,42 @@ def test_inversion_two_bands_vs_oracle_backend():
     err0 = float(np.linalg.norm(np.sqrt(lam0 / 1000.0) - vp_true) / np.linalg.norm(vp_true))
     assert log_g[-1].model_error < err0
     assert np.abs(lam_g.astype(np.float64) / lam_o - 1.0).max() <= 1e-3
+
+
+def test_nlcg_model_ops_on_device():
+    """fwi_first_step and fwi_model_update (FWI.f90:175, :227, :315): exp and
+    log rounded once from FP64 give the bits of the float64-rounded
+    restatement, and stay within one unit in the last place of numpy's
+    float32 functions; host and device pointers give the same result."""
+    import fwi_gb300 as F
+    from oracle import nlcg as ON
+    rng = np.random.default_rng(17)
+    ny, nx = 300, 700
+    var = np.asfortranarray((1000.0 * rng.uniform(1450.0, 5200.0, (ny, nx)) ** 2).astype(F32))
+    search = np.asfortranarray((rng.standard_normal((ny, nx)) * 10.0 ** rng.uniform(-12, -6, (ny, nx))).astype(F32))
+    search[:5, :5] = 0.0
+    nut = F.first_step(search, var)
+    assert nut == ON.first_step_rounded(search, var)
+    assert abs(float(nut) / float(ON.HostModelOps.first_step(search, var)) - 1.0) <= 4 * 2.0 ** -23
+    ones = np.ones_like(var)
+    for step in (nut, F32(0.0), F32(nut * F32(37.5))):
+        lam = F.model_update(search, var, step)
+        np.testing.assert_array_equal(lam, ON.update_rounded(search, var, step))
+        # the exp factor alone (var = 1) is within a few units of numpy's float32
+        # exp, which is not correctly rounded itself (up to two units here)
+        e_dev = F.model_update(search, ones, step)
+        e_np = ON.HostModelOps.update(search, ones, step)
+        ulp = np.abs(e_dev.view(np.int32).astype(np.int64) - e_np.view(np.int32).astype(np.int64))
+        assert ulp.max() <= 4
+    np.testing.assert_array_equal(F.model_update(search[:5, :5], var[:5, :5], nut), var[:5, :5])
+    # device pointers (the call detects them)
+    import torch
+    s_d = torch.from_numpy(np.ascontiguousarray(search.reshape(-1, order="F"))).cuda()
+    v_d = torch.from_numpy(np.ascontiguousarray(var.reshape(-1, order="F"))).cuda()
+    out = torch.empty_like(v_d)
+    import ctypes as C
+    st = C.c_float(nut)
+    F.load().fwi_model_update(C.c_void_p(s_d.data_ptr()), C.c_void_p(v_d.data_ptr()), C.byref(st),
+                              C.byref(C.c_int(nx)), C.byref(C.c_int(ny)), C.c_void_p(out.data_ptr()))
+    torch.cuda.synchronize()
+    np.testing.assert_array_equal(out.cpu().numpy().reshape((ny, nx), order="F"), F.model_update(search, var, nut))

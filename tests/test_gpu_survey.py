@@ -104,7 +104,7 @@ def test_tuner_picks_a_measured_tile(monkeypatch):
     spec, vp = make(11, ny=70, nxm=400, nshots=4)
     sv = F.Survey(spec)
     kern, rows, meas = sv.tiles()
-    assert kern in (1, 2) and rows in (48, 64, 96)
+    assert kern in (1, 2) and rows in (16, 32, 48, 64, 96)
     if meas:  # empty when the choice came from the tuning cache
         assert (kern, rows) in meas and meas[(kern, rows)] == min(meas.values())
     sv.set_lambda(lam_from_vp(vp))
@@ -243,3 +243,49 @@ def test_small_budget_selects_recompute():
     g = np.zeros_like(g0)
     m, _ = sv.run(1, g)
     assert m == m0 and np.array_equal(g, g0)
+
+
+def test_batch_entry_line_search_trials_one_plan():
+    """Three line-search trials through the drop-in batch call, each with the
+    dt and nt that FWI.f90:225-227 derives from its trial model
+    (calculate_misfit_gradient.f90:198-203), build one plan: the later trials
+    move it to their time axis, with results bit-identical to a survey moved
+    by fwi_survey_set_time."""
+    import copy
+
+    import fwi_gb300 as F
+    from fwi_gb300 import _native as N
+    from fwi_gb300.synth import lam_from_vp
+    spec, vp = make(12, nshots=2, nt=200)
+    lam = lam_from_vp(vp)
+    rng = np.random.default_rng(3)
+    tfin = 0.4
+    trials = []
+    for scale in (1.0, 1.3, 0.75):  # trial models: lambda scaled, dt from the CFL rule (nt 200, 230, 170)
+        lam_k = np.asfortranarray(lam * np.float32(scale))
+        dt, nt, _ = F.time_rules(lam_k, spec.d, tfin, spec.store_snap)
+        sp = copy.deepcopy(spec)
+        sp.dt, sp.nt = float(dt), int(nt)
+        for sh in sp.shots:
+            sh.src = np.asfortranarray(rng.standard_normal((nt, len(sh.nxSou))).astype(np.float32))
+            sh.obs = np.asfortranarray(rng.standard_normal((nt, len(sh.nxRec))).astype(np.float32))
+        trials.append((lam_k, sp))
+    assert len({sp.nt for _, sp in trials}) == 3
+    p0 = N.load().fwi_batch_plans()
+    sv = F.Survey(trials[0][1])
+    for k, (lam_k, sp) in enumerate(trials):
+        g = np.zeros((sp.ny, sp.nx_model), np.float32, order="F")
+        m = F.calculate_misfit_gradient(sp, lam_k, 1, np.float32(0.0), g)
+        if k:
+            src = np.concatenate([np.asarray(sh.src).reshape(-1, order="F") for sh in sp.shots])
+            sv.set_time(sp.dt, sp.nt, src, sp.obs_packed())
+        else:
+            sv.set_observed(sp.obs_packed())
+        sv.set_lambda(lam_k)
+        g2 = np.zeros_like(g)
+        m2, _ = sv.run(1, g2)
+        np.testing.assert_array_equal(g, g2)
+        assert m == np.float32(m2) and np.abs(g).max() > 0
+    assert N.load().fwi_batch_plans() - p0 == 1
+    sv.close()
+    F.load().fwi_batch_release()

@@ -6,6 +6,7 @@ import os
 import numpy as np
 
 from fwi_gb300.inversion import fwi_band, polyfit
+from oracle.nlcg import HostModelOps
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 
@@ -45,7 +46,7 @@ def test_fwi_band_line_search_rules():
     w = rng.uniform(0.5, 2.0, (ny, nx))
     q = Quadratic(lam_t, w)
     log = []
-    lam, it = fwi_band(lam0, q, 0.0, 5.0, 4, iter0=3, beta_fn=_beta_fp64, log=log)
+    lam, it = fwi_band(lam0, q, 0.0, 5.0, 4, iter0=3, beta_fn=_beta_fp64, log=log, ops=HostModelOps)
     assert it == 7 and [l.iter for l in log] == [3, 4, 5, 6]
     mis = [l.misfit for l in log]
     assert all(b < a for a, b in zip(mis, mis[1:]))               # misfit falls every iteration

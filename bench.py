@@ -219,6 +219,12 @@ def run_reference(a):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return 0
+    # the workload from the oracle's geometry, wavelet and time rules (pinned to
+    # the reference's golden vectors): this arm never loads the product library
+    from fwi_gb300 import synth
+    from oracle import oracle as O
+    from oracle import prep as OP
+    synth.use_host_functions(O.mcs_geometry, O.ricker, O.time_rules, OP.was_geometry)
     spec, vp_true, vp0 = make_workload(a)
     nthreads = os.cpu_count() or 1
     nt_sample = {"mcs": 100, "mcs-f16": 100, "single": 600}.get(a.workload, 40)

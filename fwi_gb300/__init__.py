@@ -42,4 +42,5 @@ from .api import (  # noqa: E402,F401
     su_write,
     time_filter,
     time_rules,
+    was_geometry,
 )

@@ -33,7 +33,7 @@ EXPORTS = [
     "fwi_survey_recompute", "fwi_survey_set_time", "fwi_time_filter", "fwi_set_filter_order",
     "fwi_interpolation_akima", "fwi_su_info", "fwi_su_read", "fwi_su_write", "fwi_read_nav",
     "fwi_survey_time_steps", "fwi_misfit_gradient_batch", "fwi_solver_forward_noalloc", "fwi_survey_tiles",
-    "fwi_batch_plans", "fwi_batch_release", "fwi_first_step", "fwi_model_update",
+    "fwi_batch_plans", "fwi_batch_release", "fwi_first_step", "fwi_model_update", "fwi_was_geometry",
 ]
 
 
@@ -85,6 +85,7 @@ def load():
     lib.fwi_model_update.argtypes = [P] * 6
     lib.fwi_mcs_geometry.argtypes = [F, F, F, F, F, F, I, P, P, P, P]
     lib.fwi_ricker.argtypes = [F, F, I, P]
+    lib.fwi_was_geometry.argtypes = [I, P, P, I, P, P, F, F, I, I, P, P, P, P, P, P]
     lib.fwi_time_rules.argtypes = [P, I, I, F, F, I, P, P, P]
     lib.fwi_survey_create.argtypes = [C.POINTER(FwiSurveyDesc), C.POINTER(C.c_void_p)]
     lib.fwi_survey_destroy.argtypes = [P]

@@ -134,6 +134,22 @@ def mcs_geometry(xs, shot_depth, streamer_depth, near_offset, drec, dmodel, num_
     return a.value, b.value, xr, yr
 
 
+def was_geometry(xobs, zobs, xshot, bat, shot_depth, dmodel, nxmodel, relocate=True):
+    """WAS geometry of get_was_data.f90 (OBS as sources, shots as
+    receivers): returns dict(nxSou, nySou, nxRec, nyRec, bat_model,
+    bat_model_grid) with 1-based grid indices."""
+    xo, zo = np.ascontiguousarray(xobs, np.float32), np.ascontiguousarray(zobs, np.float32)
+    xs, bt = np.ascontiguousarray(xshot, np.float32), np.ascontiguousarray(bat, np.float32)
+    no, ns = xo.size, xs.size
+    nxS, nyS, nxR = np.zeros(no, np.int32), np.zeros(no, np.int32), np.zeros(ns, np.int32)
+    nyR = C.c_int(0)
+    bm, bg = np.zeros(nxmodel, np.float32), np.zeros(nxmodel, np.int32)
+    N.check(N.load().fwi_was_geometry(no, _p(xo), _p(zo), ns, _p(xs), _p(bt), C.c_float(shot_depth),
+                                      C.c_float(dmodel), int(nxmodel), int(bool(relocate)), _p(nxS), _p(nyS),
+                                      _p(nxR), C.byref(nyR), _p(bm), _p(bg)))
+    return dict(nxSou=nxS, nySou=nyS, nxRec=nxR, nyRec=nyR.value, bat_model=bm, bat_model_grid=bg)
+
+
 def time_rules(lam, dmodel, tfin, store_snap=10):
     """(dt, nt, nt_Store) of calculate_misfit_gradient.f90:198-203."""
     lam = _f32(lam)

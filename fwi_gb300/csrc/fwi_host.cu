@@ -115,9 +115,14 @@ LibState& L() {
 }
 cudaStream_t stream() { return L().user ? L().user : L().own; }
 
+// Every entry point works on the library's device: it is made current on the
+// calling thread (a caller that switched devices, or another host thread,
+// would otherwise launch on a device that does not own the library's streams).
 int ensure_init() {
-    if (L().init) return FWI_OK;
-    return fwi_init(0);
+    if (!L().init) return fwi_init(0);
+    int cur = -1;
+    if (cudaGetDevice(&cur) != cudaSuccess || cur != L().device) CK(cudaSetDevice(L().device));
+    return FWI_OK;
 }
 
 // device allocation with RAII
@@ -665,10 +670,15 @@ extern "C" {
 
 int fwi_init(int device) {
     std::lock_guard<std::recursive_mutex> g(L().mu);
-    if (L().init && L().device == device) return FWI_OK;
+    if (L().init && L().device == device) {
+        CK(cudaSetDevice(device));
+        return FWI_OK;
+    }
     int n = 0;
     CK(cudaGetDeviceCount(&n));
     if (device < 0 || device >= n) return fail(FWI_ERR_ARG, "invalid CUDA device index");
+    // a new device: the streams, events and buffers of the old one are released
+    if (L().init) TRY(fwi_finalize());
     CK(cudaSetDevice(device));
     if (!L().own) CK(cudaStreamCreateWithFlags(&L().own, cudaStreamNonBlocking));
     if (!L().aux) {
@@ -2208,12 +2218,11 @@ int fwi_batch_release(void) {
 //
 // Some callers cannot call cudaMalloc: code that runs inside a framework
 // which owns the device memory pool (a raw cudaMalloc synchronises the
-// device and sits outside the pool's budget), and code paths that must not
-// allocate once set up (latency-critical loops, work recorded once and
-// replayed).  For them the forward propagation of one shot can run with all
-// of its working state (wavefields, c2, CPML memory variables, work lists)
-// in the fixed array below, which every GPU that loads this library holds
-// until the process exits.
+// device and sits outside the pool's budget), and latency-critical code paths
+// that must not allocate once they are set up.  For them the forward
+// propagation of one shot can run with all of its working state (wavefields,
+// c2, CPML memory variables, work lists) in the fixed array below, which
+// every GPU that loads this library holds until the process exits.
 
 namespace {
 
@@ -2227,8 +2236,7 @@ constexpr int NOALLOC_MAX_DEVICES = 64;
 void* g_noalloc_addr[NOALLOC_MAX_DEVICES] = {nullptr};
 
 int noalloc_scratch(void** out) {
-    int dev = 0;
-    CK(cudaGetDevice(&dev));
+    const int dev = L().device;  // current on this thread (ensure_init)
     if (dev < 0 || dev >= NOALLOC_MAX_DEVICES) return fail(FWI_ERR_ARG, "device index too large");
     if (!g_noalloc_addr[dev]) {
         void* p = nullptr;

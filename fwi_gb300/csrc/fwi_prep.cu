@@ -22,6 +22,7 @@
 
 #include <cmath>
 #include <complex>
+#include <vector>
 #include <map>
 #include <mutex>
 #include <string>
@@ -45,19 +46,32 @@ namespace {
 
 // Abscissa i (1-based) of a uniform axis: real(i-1)*dt, as the reference
 // builds Time_Data and time (interpolation_akima.f90:14-20).
-__device__ __forceinline__ float axis(int i, float d) { return (float)(i - 1) * d; }
+__host__ __device__ __forceinline__ float axis(int i, float d) { return (float)(i - 1) * d; }
+
+// Abscissae for the interpolation below: a uniform axis, or the values of an
+// array x(1..L).  The evaluation is compiled for the device (trace
+// resampling) and for the host (the WAS bathymetry model of the geometry).
+struct UniformAxis {
+    float d;
+    __host__ __device__ float operator()(int i) const { return axis(i, d); }
+};
+struct ArrayAxis {
+    const float* x;
+    __host__ __device__ float operator()(int i) const { return x[i - 1]; }
+};
 
 // Interval index I of u among x(1..L) (x strictly increasing): 1 before
 // x(1), L+1 at or after x(L), else the smallest i >= 2 with x(i) > u, found
 // by the same bisection (akima433.f90, the routine that locates the point).
-__device__ __forceinline__ int akima_interval(float u, int L, float dx) {
+template <typename AX>
+__host__ __device__ __forceinline__ int akima_interval(float u, int L, AX ax) {
     if (L == 2) return 2;
-    if (u >= axis(L, dx)) return L + 1;
-    if (u < axis(1, dx)) return 1;
+    if (u >= ax(L)) return L + 1;
+    if (u < ax(1)) return 1;
     int lo = 2, hi = L;
     do {
         const int i = (lo + hi) / 2;
-        if (u >= axis(i, dx)) lo = i + 1;
+        if (u >= ax(i)) lo = i + 1;
         else hi = i;
     } while (hi > lo);
     return hi;
@@ -68,13 +82,14 @@ __device__ __forceinline__ int akima_interval(float u, int L, float dx) {
 // ends extrapolated linearly), Akima's weighted slope estimates at the two
 // interval ends, and the cubic through them; before x(1) and after x(L) the
 // end interval's cubic is shifted outward as in the reference.
-__device__ float akima_eval(const float* y, int L, float dx, float u) {
-    const int I = akima_interval(u, L, dx);
+template <typename AX>
+__host__ __device__ float akima_eval(const float* y, int L, AX ax, float u) {
+    const int I = akima_interval(u, L, ax);
     int J = I;
     if (J == 1) J = 2;
     if (J == L + 1) J = L;
-    float x3 = axis(J - 1, dx), y3 = y[J - 2];
-    const float x4 = axis(J, dx), y4 = y[J - 1];
+    float x3 = ax(J - 1), y3 = y[J - 2];
+    const float x4 = ax(J), y4 = y[J - 1];
     float a3 = x4 - x3;
     float m3 = (y4 - y3) / a3;
     float a2 = 0.f, a4 = 0.f, m1, m2 = 0.f, m4, m5;
@@ -84,7 +99,7 @@ __device__ float akima_eval(const float* y, int L, float dx, float u) {
         m4 = m3;
     } else {
         if (J != 2) {
-            x2 = axis(J - 2, dx);
+            x2 = ax(J - 2);
             y2 = y[J - 3];
             a2 = x3 - x2;
             m2 = (y3 - y2) / a2;
@@ -92,7 +107,7 @@ __device__ float akima_eval(const float* y, int L, float dx, float u) {
         if (J == L) {
             m4 = m3 + m3 - m2;
         } else {
-            x5 = axis(J + 1, dx);
+            x5 = ax(J + 1);
             y5 = y[J];
             a4 = x5 - x4;
             m4 = (y5 - y4) / a4;
@@ -102,13 +117,13 @@ __device__ float akima_eval(const float* y, int L, float dx, float u) {
     if (J <= 3) {
         m1 = m2 + m2 - m3;
     } else {
-        const float a1 = x2 - axis(J - 3, dx);
+        const float a1 = x2 - ax(J - 3);
         m1 = (y2 - y[J - 4]) / a1;
     }
     if (J >= L - 1) {
         m5 = m4 + m4 - m3;
     } else {
-        const float a5 = axis(J + 2, dx) - x5;
+        const float a5 = ax(J + 2) - x5;
         m5 = (y[J + 1] - y5) / a5;
     }
     // numerical differentiation: slope estimates t3 (left end), t4 (right end)
@@ -161,7 +176,7 @@ __global__ void k_akima(const float* __restrict__ in, int nt_in, float dt_in, fl
     for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < n;
          idx += (long long)gridDim.x * blockDim.x) {
         const int tr = (int)(idx / nt_out), k = (int)(idx % nt_out);
-        out[idx] = akima_eval(in + (size_t)tr * nt_in, nt_in, dt_in, axis(k + 1, dt_out));
+        out[idx] = akima_eval(in + (size_t)tr * nt_in, nt_in, UniformAxis{dt_in}, axis(k + 1, dt_out));
     }
 }
 
@@ -422,6 +437,73 @@ int fwi_interpolation_akima(const float* Data_tmp, const float* dt_Data_, const 
     PTRY(akima_device(src, nt_in, dt_in, dst, nt_out, dt_out, ntr));
     if (!dout) PCK(cudaMemcpyAsync(Data_trace, dst, bout, cudaMemcpyDeviceToHost, st));
     PCK(cudaStreamSynchronize(st));
+    return FWI_OK;
+}
+
+// The WAS geometry of get_was_data.f90 (host arithmetic in the reference's
+// FP32 operations and order; added_space_model = 0, modules.f90:153):
+//   shots (the receivers of the reciprocal inversion): grid column
+//     1+ceiling((0+|xs|)/dmodel)                                   :155-156
+//   OBS (its sources): grid column 1+ceiling((0+|x|)/dmodel), depth |z| :201-205
+//   bathymetry model: Akima's interpolation (INTRPL) through (0, shot
+//     positions, length_model) and the shots' water depths (|bat|, the first
+//     and last repeated at the ends) at (i-1)*dmodel, i = 1..nxmodel, with
+//     length_model = (nxmodel-1)*dmodel (modules.f90:431)            :584-613
+//   relocation: each OBS depth replaced by the model bathymetry at its
+//     column, then its grid row 1+ceiling(z/dmodel)                   :112-115
+//   indices: nxSou/nySou = the OBS column/row, nxRec = the shot columns,
+//     nyRec = 1+ceiling(shot_depth/dmodel)                            :223-231
+int fwi_was_geometry(int num_obs, const float* xobs, const float* zobs, int num_shots, const float* xshot,
+                     const float* bat, float shot_depth, float dmodel, int nxmodel, int relocate, int* nxSou,
+                     int* nySou, int* nxRec, int* nyRec, float* bat_model, int* bat_model_grid) {
+    if (num_obs < 0 || num_shots < 0 || !(dmodel > 0.f)) return prep_fail(FWI_ERR_ARG, "bad WAS geometry sizes");
+    if ((num_obs && (!xobs || !zobs)) || (num_shots && !xshot)) return prep_fail(FWI_ERR_ARG, "null argument");
+    const bool need_model = relocate || bat_model || bat_model_grid;
+    if (need_model && (num_shots < 1 || !bat || nxmodel < 1))
+        return prep_fail(FWI_ERR_ARG, "the bathymetry model needs the shots' water depths and nxmodel >= 1");
+    const float added_space_model = 0.f;
+    std::vector<float> pos_shot(num_shots), pos_bat(num_shots);
+    for (int i = 0; i < num_shots; ++i) {
+        pos_shot[i] = added_space_model + fabsf(xshot[i]);
+        if (nxRec) nxRec[i] = 1 + (int)ceilf(pos_shot[i] / dmodel);
+        if (bat) pos_bat[i] = fabsf(bat[i]);
+    }
+    if (nyRec) *nyRec = 1 + (int)ceilf(shot_depth / dmodel);
+    std::vector<float> model;
+    if (need_model) {
+        const int L = num_shots + 2;
+        std::vector<float> xm(L), yb(L);
+        for (int i = 2; i <= num_shots + 1; ++i) {
+            yb[i - 1] = pos_bat[i - 2];
+            xm[i - 1] = pos_shot[i - 2];
+        }
+        const float length_model = (float)(nxmodel - 1) * dmodel;
+        xm[0] = 0.f;
+        xm[L - 1] = length_model;
+        yb[0] = yb[1];
+        yb[L - 1] = yb[L - 2];
+        for (int i = 1; i < L; ++i)  // INTRPL's check: abscissae increasing (akima433.f90:160-168)
+            if (!(xm[i] > xm[i - 1]))
+                return prep_fail(FWI_ERR_ARG, "shot positions must increase inside (0, (nxmodel-1)*dmodel)");
+        model.resize(nxmodel);
+        for (int i = 1; i <= nxmodel; ++i) {
+            const float u = (float)(i - 1) * dmodel;
+            model[i - 1] = akima_eval(yb.data(), L, ArrayAxis{xm.data()}, u);
+            if (bat_model) bat_model[i - 1] = model[i - 1];
+            if (bat_model_grid) bat_model_grid[i - 1] = 1 + (int)ceilf(model[i - 1] / dmodel);
+        }
+    }
+    for (int i = 0; i < num_obs; ++i) {
+        const float px = added_space_model + fabsf(xobs[i]);
+        const int gx = 1 + (int)ceilf(px / dmodel);
+        float pz = fabsf(zobs[i]);
+        if (relocate) {
+            if (gx < 1 || gx > nxmodel) return prep_fail(FWI_ERR_ARG, "OBS outside the bathymetry model");
+            pz = model[gx - 1];
+        }
+        if (nxSou) nxSou[i] = gx;
+        if (nySou) nySou[i] = 1 + (int)ceilf(pz / dmodel);
+    }
     return FWI_OK;
 }
 

@@ -17,10 +17,34 @@ def _F(a):
     return np.asfortranarray(np.asarray(a, dtype=np.float32))
 
 
+# The FP32 index rules, wavelet and time rules the generators use: the
+# library's (fwi_mcs_geometry, fwi_ricker, fwi_time_rules) unless a caller
+# supplies host functions with the same signatures and results -- a CPU
+# baseline that must not load the library does.
+_HOST = {}
+
+
+def use_host_functions(mcs_geometry=None, ricker=None, time_rules=None, was_geometry=None):
+    """Generate workloads with these functions instead of the library's
+    (None: the library's)."""
+    _HOST.clear()
+    for k, f in (("mcs_geometry", mcs_geometry), ("ricker", ricker), ("time_rules", time_rules),
+                 ("was_geometry", was_geometry)):
+        if f is not None:
+            _HOST[k] = f
+
+
+def _fn(name):
+    if name in _HOST:
+        return _HOST[name]
+    from . import api
+    return {"mcs_geometry": api.mcs_geometry, "ricker": api.Ricker_mcs, "time_rules": api.time_rules,
+            "was_geometry": api.was_geometry}[name]
+
+
 def ricker_shifted(freq, dt, nt, shift):
     """Ricker_mcs wavelet (get_mcs_data.f90:346-362) delayed by `shift` s."""
-    from .api import Ricker_mcs
-    w = Ricker_mcs(freq, dt, nt)
+    w = _fn("ricker")(freq, dt, nt)
     if shift:
         t = np.arange(nt) * dt
         w = np.interp(t - shift, t, w, left=0.0, right=0.0).astype(np.float32)
@@ -87,7 +111,7 @@ def mcs_survey(vp, d, dt, nt, xs_list, nrec, drec, near=150.0, sdepth=10.0, rdep
     in [0, shift_max]) and a trailing streamer of nrec channels.  `windows`
     optionally gives (x0, nx) per shot; geometry indices are window
     relative."""
-    from .api import mcs_geometry
+    mcs_geometry = _fn("mcs_geometry")
     rng = np.random.default_rng(seed)
     ny, nxm = vp.shape
     shots = []
@@ -231,7 +255,7 @@ def was_batch(seed=3, nt=None, nshots=30, freq=5.0, tfin=20.0):
     stated dt = 2.5 ms violates the CFL limit at 8 km/s and 25 m, so the
     reference's own rule dt = d/(2 vmax) (calculate_misfit_gradient.f90:198)
     is used: 1.5625 ms, nt = 12800 for 20 s.  Returns (spec, vp_true, vp_start)."""
-    from .api import time_rules
+    time_rules = _fn("time_rules")
     rng = np.random.default_rng(seed + 1)
     d = 25.0
     vp, sea = model_crustal(seed)
@@ -240,16 +264,21 @@ def was_batch(seed=3, nt=None, nshots=30, freq=5.0, tfin=20.0):
     dt, nt_full, _ = time_rules(lam, d, tfin, 10)
     nt = nt_full if nt is None else nt
     f32 = np.float32
-    grid = lambda pos: 1 + int(np.ceil(f32(abs(pos)) / f32(d)))  # noqa: E731  get_was_data.f90:155-159
-    rec_x = np.array([62.5 + 125.0 * j for j in range(1200)], np.float64)
-    rec_grid = np.array([grid(xr) for xr in rec_x], np.int32)
-    rec_row = grid(10.0)
+    # the reference's WAS geometry (get_was_data.f90): shots (the receivers) at
+    # 125 m with the model's water depth under each, OBS (the sources) at 5 km
+    # relocated to the bathymetry model that INTRPL draws through the shots'
+    # water depths
+    rec_x = np.array([62.5 + 125.0 * j for j in range(1200)], np.float32)
+    cols = np.minimum((rec_x / f32(d)).astype(np.int64), nxm - 1)
+    xo_all = np.array([2500.0 + 5000.0 * i for i in range(nshots)], np.float32)
+    geo = _fn("was_geometry")(xo_all, np.zeros(nshots, np.float32), rec_x, np.asarray(sea, np.float32)[cols], 10.0,
+                              d, nxm, True)
+    rec_grid = np.asarray(geo["nxRec"], np.int32)
+    rec_row = int(geo["nyRec"])
     shots = []
     for i in range(nshots):
-        xo = 2500.0 + 5000.0 * i
-        xg = grid(xo)
-        zo = sea[min(xg - 1, nxm - 1)]          # OBS relocated to the seafloor (get_was_data.f90:112-115)
-        zg = grid(zo)
+        xo = float(xo_all[i])
+        xg, zg = int(geo["nxSou"][i]), int(geo["nySou"][i])
         width = rng.uniform(30e3, 100e3)
         c0 = max(0, int((xo - width / 2) / d))
         c1 = min(nxm, int((xo + width / 2) / d))
@@ -258,7 +287,7 @@ def was_batch(seed=3, nt=None, nshots=30, freq=5.0, tfin=20.0):
         src = ricker_shifted(freq, float(dt), nt, 0.0).reshape(nt, 1, order="F")
         shots.append(ShotSpec(x0=c0, nx=c1 - c0, nxSou=np.array([xg - c0], np.int32), nySou=np.array([zg], np.int32),
                               nxRec=nxr, nyRec=np.full(nxr.size, rec_row, np.int32), src=_F(src)))
-    water = np.array([grid(s) for s in sea], np.int32)
+    water = (1 + np.ceil(np.asarray(sea, np.float32) / f32(d))).astype(np.int32)
     spec = SurveySpec(ny=ny, nx_model=nxm, d=d, dt=float(dt), nt=nt, shots=shots, store_snap=10, acc=3, dpml=20,
                       water_rows=water)
     return spec, vp, smooth(vp, 6)

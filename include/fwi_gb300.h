@@ -17,6 +17,7 @@
  *                             shots of one call; the MPI shot loop
  *                             :73-360 becomes on-device batching)
  *   fwi_mcs_geometry          src/get_mcs_data.f90:113-114,147-155,503-512
+ *   fwi_was_geometry          src/get_was_data.f90:112-115,155-159,201-205,223-231,584-613
  *   fwi_ricker                src/get_mcs_data.f90:331 (Ricker_mcs)
  *   fwi_time_rules            src/calculate_misfit_gradient.f90:198-203
  *   fwi_time_filter           src/time_filter.f90:1 (time_filter), src/filters.f90:1 (filters_function1D)
@@ -54,7 +55,10 @@ extern "C" {
 /* ---- library state ------------------------------------------------------ */
 
 /* Select the CUDA device and create the library's stream.  Optional: every
- * other entry point initialises device 0 on first use. */
+ * other entry point initialises device 0 on first use.  The library serves
+ * one device at a time: every entry point makes that device current on the
+ * calling thread, and fwi_init with another device first releases everything
+ * held on the previous one (as fwi_finalize). */
 int fwi_init(int device);
 /* Free every device buffer the library holds and destroy its stream. */
 int fwi_finalize(void);
@@ -119,6 +123,19 @@ int fwi_model_update(const float* Search, const float* var_orig, const float* st
  * get_geometry_mcs and get_pos_channels (offset_header = 0) compute them. */
 int fwi_mcs_geometry(float xs, float shot_depth, float streamer_depth, float near_offset, float drec,
                      float dmodel, int num_rec, int* nxSou, int* nySou, int* nxRec, int* nyRec);
+/* WAS geometry (get_was_data.f90: read_nav_shot_was :155-159, read_nav_obs
+ * :201-205, get_bathymetry_model_was :584-613, relocation_zOBS :112-115,
+ * get_geometry_WAS :223-231), host FP32 in the reference's order: the OBS are
+ * the sources, the shots the receivers.  Inputs: OBS x and z (m), shot x and
+ * water depth bat (m), streamer/shot depth, grid step, model columns.
+ * relocate = 1 moves every OBS to the bathymetry model (Akima through the
+ * shots' water depths) at its column, as the reference does.  Outputs (any
+ * may be NULL): nxSou, nySou (num_obs), nxRec (num_shots), *nyRec, and the
+ * bathymetry model bat_model, bat_model_grid (nxmodel; bat may be NULL
+ * when neither the model nor the relocation is asked for). */
+int fwi_was_geometry(int num_obs, const float* xobs, const float* zobs, int num_shots, const float* xshot,
+                     const float* bat, float shot_depth, float dmodel, int nxmodel, int relocate, int* nxSou,
+                     int* nySou, int* nxRec, int* nyRec, float* bat_model, int* bat_model_grid);
 /* Ricker_mcs: out(nt) for peak frequency freq and sampling dt. */
 int fwi_ricker(float freq, float dt, int nt, float* out);
 /* dt = dmodel/sqrt(max(lambda/1000))/2, nt = 1+ceil(tfin/dt) truncated to a
@@ -323,7 +340,8 @@ int fwi_batch_release(void);
  * call before any stream capture.  Every call shares the one array, which
  * keeps the last call's contents (the call clears what must start at zero):
  * calls that overlap on the GPU -- from several host threads or streams --
- * race and must not be issued. */
+ * race and must not be issued.  The call waits for its stream to finish
+ * before it returns. */
 int fwi_solver_forward_noalloc(int NumSou, int NumRec, const int* nxSou, const int* nySou,
                                const int* nxRec, const int* nyRec, const float* S_dev, float d, float dt,
                                int ny, int nx, const float* ctmp_dev, int nt, float* Rec_point_dev);

@@ -10,6 +10,8 @@ filter and resampler; the product package never imports it.
   transformed back; the output is the real part of the last nt samples.
   FFT in float64 (numpy), H from the reference's product formula with the
   frequency advanced by an FP32 accumulation of fe/ts (filters.f90:94-98).
+* was_geometry -- the WAS geometry of get_was_data.f90 (:112-115, :155-159,
+  :201-205, :223-231, :584-613), with INTRPL for the bathymetry model.
 * akima        -- interpolation_akima.f90:1-31 with INTRPL (akima433.f90:6-170,
   ACM Algorithm 433, Comm. ACM 15(10):914): per output abscissa, the interval
   by bisection, slopes of the neighbouring intervals (end slopes extrapolated),
@@ -83,10 +85,23 @@ def time_filter(data: np.ndarray, dt: float, typef: int, f1: float, fc: float, o
 def akima(data: np.ndarray, dt_in: float, dt_out: float, nt_out: int) -> np.ndarray:
     """data (L, ntr) float32 sampled at (i-1)*dt_in -> (nt_out, ntr) at (i-1)*dt_out."""
     y = np.asarray(data, dtype=np.float32)
-    L, ntr = y.shape
+    L = y.shape[0]
     dt_in, dt_out = F32(dt_in), F32(dt_out)
     X = (np.arange(L, dtype=np.float32) * dt_in).astype(np.float32)       # x(i) = real(i-1)*dt
     U = (np.arange(nt_out, dtype=np.float32) * dt_out).astype(np.float32)
+    return akima_x(X, y, U)
+
+
+def akima_x(X: np.ndarray, data: np.ndarray, U: np.ndarray) -> np.ndarray:
+    """INTRPL: data (L, ntr) at the increasing abscissae X (L) -> (len(U), ntr)
+    at the abscissae U."""
+    y = np.asarray(data, dtype=np.float32)
+    if y.ndim == 1:
+        return akima_x(X, y[:, None], U)[:, 0]
+    X = np.asarray(X, np.float32)
+    U = np.asarray(U, np.float32)
+    L, ntr = y.shape
+    nt_out = U.size
     # interval index I (1-based): 1 before x(1), L+1 at or after x(L), else the
     # smallest i >= 2 with x(i) > u (the bisection's result)
     if L == 2:
@@ -169,3 +184,29 @@ def akima(data: np.ndarray, dt_in: float, dt_out: float, nt_out: int) -> np.ndar
         q3 = ((-M3 - M3 + T3 + T4) / (A3 * A3)).astype(np.float32)
     d = (col(U) - X3).astype(np.float32)
     return (Y3 + d * (T3 + d * (q2 + d * q3))).astype(np.float32)
+
+
+def was_geometry(xobs, zobs, xshot, bat, shot_depth, dmodel, nxmodel, relocate=True):
+    """WAS geometry (OBS as sources, shots as receivers; added_space_model = 0):
+    shot columns 1+ceiling(|xs|/d) (get_was_data.f90:155-156); the bathymetry
+    model by INTRPL through (0, shot positions, (nxmodel-1)*d) and the shots'
+    water depths, ends repeated, at (i-1)*d (:584-613); OBS columns
+    1+ceiling(|x|/d) and rows 1+ceiling(z/d) with z the model bathymetry at
+    the OBS column when relocated (:112-115, :201-205); the receiver row
+    1+ceiling(shot_depth/d) (:223-231).  FP32 as the reference's REALs."""
+    d = F32(dmodel)
+    grid = lambda v: (1 + np.ceil(np.asarray(v, np.float32) / d)).astype(np.int32)  # noqa: E731
+    pos_shot = (F32(0.0) + np.abs(np.asarray(xshot, np.float32))).astype(np.float32)
+    pos_bat = np.abs(np.asarray(bat, np.float32)).astype(np.float32)
+    L = pos_shot.size + 2
+    xm = np.zeros(L, np.float32)
+    yb = np.zeros(L, np.float32)
+    xm[1:-1], yb[1:-1] = pos_shot, pos_bat
+    xm[-1] = F32(F32(nxmodel - 1) * d)
+    yb[0], yb[-1] = yb[1], yb[-2]
+    U = (np.arange(nxmodel, dtype=np.float32) * d).astype(np.float32)
+    model = akima_x(xm, yb, U)
+    gx = grid(F32(0.0) + np.abs(np.asarray(xobs, np.float32)))
+    z = model[gx - 1] if relocate else np.abs(np.asarray(zobs, np.float32))
+    return dict(nxSou=gx, nySou=grid(z), nxRec=grid(pos_shot), nyRec=int(grid([shot_depth])[0]), bat_model=model,
+                bat_model_grid=grid(model))

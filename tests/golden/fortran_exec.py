@@ -8,13 +8,26 @@ multiply-add, no reassociation: what gfortran emits for x86-64 without
 -march flags), default INTEGER as Python int, ``x**2`` as ``x*x`` and
 ``exp``/``log`` through the C library's ``expf``/``logf``.
 
-Supported: subroutines and functions, type declarations (explicit-shape,
-allocatable), allocate/deallocate, scalar/array/section/vector-subscript
+Supported: subroutines and functions, internal procedures after CONTAINS
+(host association), type declarations (explicit-shape, assumed-size,
+allocatable; INTEGER, REAL, DOUBLE PRECISION, COMPLEX, LOGICAL, with or
+without KIND=), allocate/deallocate, scalar/array/section/vector-subscript
 assignment, DO / DO WHILE / IF blocks, one-line IF, CALL with
-pass-by-reference (dummies alias the actual argument; explicit-shape dummies
-are reshaped views, i.e. sequence association), EXIT/CYCLE/RETURN, and the
-intrinsics the solver files use.  I/O statements (write/print/open/close) are
-skipped; READ is rejected.
+pass-by-reference (dummies alias the actual argument; explicit-shape and
+assumed-size dummies are reshaped views, i.e. sequence association, also
+from an array element onward and between COMPLEX actuals and REAL dummies,
+which see the interleaved real and imaginary parts), EXIT/CYCLE/RETURN, and
+the intrinsics these sources use.  I/O statements (write/print/open/close)
+are skipped; READ is rejected.
+
+COMPLEX arithmetic follows what gfortran emits (GCC's complex lowering under
+-fcx-fortran-rules): an operand known to be real is combined componentwise
+(r*(c,d) = (r*c, r*d), (a,b)/r = (a/r, b/r), r+(c,d) = (r+c, d)); complex
+products are (ac - bd, ad + bc); a complex divisor uses the scaled division
+of GCC's wide-range method (ratio = the smaller over the larger component of
+the divisor); each operation rounded to single precision, x**2 = x*x.
+Procedures that stand outside the executed sources (a trace reader, a
+forward solver) can be supplied as Python callables (``natives``).
 """
 from __future__ import annotations
 
@@ -30,6 +43,10 @@ _libm.expf.restype = ctypes.c_float
 _libm.expf.argtypes = [ctypes.c_float]
 _libm.logf.restype = ctypes.c_float
 _libm.logf.argtypes = [ctypes.c_float]
+for _f in ("cosf", "sinf", "atanf"):
+    getattr(_libm, _f).restype = ctypes.c_float
+    getattr(_libm, _f).argtypes = [ctypes.c_float]
+C64 = np.complex64
 
 F32 = np.float32
 
@@ -254,6 +271,11 @@ class Parser:
             return ("not", self.expr(3))
         if kind == "op" and val == "(":
             e = self.expr(0)
+            if self.peek() == ("op", ","):  # complex constant (re, im)
+                self.next()
+                im = self.expr(0)
+                self.expect("op", ")")
+                return ("cplx", e, im)
             self.expect("op", ")")
             return ("paren", e)
         if kind == "name":
@@ -340,7 +362,18 @@ def _match_paren(s: str, start: int) -> int:
     raise SyntaxError(f"unbalanced parentheses in {s!r}")
 
 
-_DECL = re.compile(r"^(integer(\*\d+)?|real(\*\d+)?|logical|character(\s*\([^)]*\))?(\*\d+)?|double\s+precision)\b(.*)$")
+_DECL = re.compile(r"^(?P<base>integer(\*\d+)?|real(\*\d+)?|complex(\*\d+)?|logical|character(\s*\([^)]*\))?(\*\d+)?"
+                   r"|double\s+precision)\b(?P<rest>.*)$")
+_KIND = re.compile(r"^(integer|real|complex|logical)\s*\(\s*kind\s*=\s*(\d+)\s*\)")
+
+
+def _kind_spec(m):
+    t, k = m.group(1), int(m.group(2))
+    if t == "real" and k == 8:
+        return "real*8"
+    if t == "complex" and k == 8:
+        return "complex*16"
+    return t
 _SKIP = re.compile(r"^(write|print|open|close|format|inquire|rewind)\b")
 
 
@@ -378,11 +411,14 @@ def parse_stmt(no, s):
         return ("equiv", no, groups)
     if re.match(r"^(implicit|use|include|save|intrinsic|external)\b", s):
         return ("skip", no)
+    if s == "contains":
+        return ("contains", no)
+    s = _KIND.sub(_kind_spec, s)
     m = _DECL.match(s)
     if m:
         if True:
-            base = m.group(1).replace(" ", "")
-            rest = m.group(6)
+            base = m.group("base").replace(" ", "")
+            rest = m.group("rest")
             attrs = ""
             if "::" in rest:
                 attrs, ents = rest.split("::", 1)
@@ -391,7 +427,8 @@ def parse_stmt(no, s):
             ftype = "integer" if base.startswith("integer") else (
                 "real" if base.startswith("real") and base in ("real", "real*4") else (
                     "double" if base in ("real*8", "doubleprecision") else (
-                        "logical" if base == "logical" else "character")))
+                        "complex" if base in ("complex", "complex*8") else (
+                            "logical" if base == "logical" else "character"))))
             alloc = "allocatable" in attrs
             # a DIMENSION(...) attribute gives every entity without its own
             # bounds that shape
@@ -401,7 +438,7 @@ def parse_stmt(no, s):
                 start = md.end() - 1
                 end = _match_paren(attrs, start)
                 attr_dims = [d.strip() for d in _split_top(attrs[start + 1:end])]
-                attr_dims = [None if d == ":" else parse_expr(d) for d in attr_dims]
+                attr_dims = [None if d == ":" else (("star",) if d == "*" else parse_expr(d)) for d in attr_dims]
             entities = []
             for ent in _split_top(ents):
                 ent = ent.strip()
@@ -417,7 +454,7 @@ def parse_stmt(no, s):
                 dims = attr_dims
                 if mm.group(2):
                     dims = [d.strip() for d in _split_top(mm.group(3))]
-                    dims = [None if d == ":" else parse_expr(d) for d in dims]
+                    dims = [None if d == ":" else (("star",) if d == "*" else parse_expr(d)) for d in dims]
                 entities.append((mm.group(1), dims, None))
             return ("decl", no, ftype, alloc, entities)
     if s in ("return",):
@@ -435,7 +472,16 @@ def parse_stmt(no, s):
             mm = re.match(r"^([a-z_][a-z0-9_]*)\s*(\((.*)\))?$", it.strip())
             if not mm:
                 continue  # stat= etc.
-            dims = [parse_expr(d) for d in _split_top(mm.group(3))] if mm.group(2) else None
+            dims = None
+            if mm.group(2):
+                dims = []
+                for d in _split_top(mm.group(3)):
+                    lo_hi = _split_top(d, ":")
+                    if len(lo_hi) == 2:
+                        if lo_hi[0].strip() != "1":
+                            raise SyntaxError(f"line {no}: lower bound other than 1 in {s!r}")
+                        d = lo_hi[1]
+                    dims.append(parse_expr(d))
             items.append((mm.group(1), dims))
         return (m.group(1), no, items)
     m = re.match(r"^call\s+([a-z_][a-z0-9_]*)\s*(\((.*)\))?$", s)
@@ -538,11 +584,27 @@ class Unit:
         self.kind, self.name, self.args, self.body, self.decls, self.result = kind, name, args, body, decls, result
 
 
+def _make_unit(cur, stmts, labels, implicit_none):
+    decls = [x for x in stmts if x[0] == "decl"]
+    equivs = [g for x in stmts if x[0] == "equiv" for g in x[2]]
+    rest = [(x, lab) for x, lab in zip(stmts, labels) if x[0] not in ("decl", "equiv")]
+    flat = any(x[0] in ("goto", "dolab") or (x[0] == "if1" and x[3][0] == "goto") for x, _ in rest)
+    body = [] if flat else build_blocks([x for x, _ in rest])
+    u = Unit(cur[0], cur[1], cur[2], body, decls)
+    u.implicit = not implicit_none
+    u.equivs = equivs
+    u.flat = rest if flat else None  # statements with labels, run by a program counter
+    u.internals = {}
+    u.host = None
+    return u
+
+
 def parse_units(text: str):
     units = {}
     cur = None
     stmts = []
     labels = []
+    host = None  # a unit whose internal procedures (after CONTAINS) are being read
     for no, s, label in logical_lines(text, with_labels=True):
         m = re.match(r"^(?:(?:integer|real|logical)\s+)?(subroutine|function)\s+([a-z_][a-z0-9_]*)\s*(\((.*)\))?", s)
         if m and cur is None:
@@ -553,6 +615,15 @@ def parse_units(text: str):
             implicit_none = False
             continue
         if cur is None:
+            if host is not None and re.match(r"^end(\s*(subroutine|function|program)\b.*)?$", s):
+                hcur, hstmts, hlabels, himpl, internals = host
+                u = _make_unit(hcur, hstmts, hlabels, himpl)
+                u.internals = internals
+                for iu in internals.values():
+                    iu.host = u
+                    iu.implicit = iu.implicit and not himpl
+                units[hcur[1]] = u
+                host = None
             continue  # module code, program code: not executed here
         if re.match(r"^implicit\s+none", s):
             implicit_none = True
@@ -560,17 +631,16 @@ def parse_units(text: str):
             st = parse_stmt(no, s)
         except SyntaxError:
             st = ("bad", no, s)
+        if st[0] == "contains" and host is None:
+            host = (cur, stmts, labels, implicit_none, {})
+            cur = None
+            continue
         if st[0] == "end" and not _open_blocks(stmts):
-            decls = [x for x in stmts if x[0] == "decl"]
-            equivs = [g for x in stmts if x[0] == "equiv" for g in x[2]]
-            rest = [(x, lab) for x, lab in zip(stmts, labels) if x[0] not in ("decl", "equiv")]
-            flat = any(x[0] in ("goto", "dolab") or (x[0] == "if1" and x[3][0] == "goto") for x, _ in rest)
-            body = [] if flat else build_blocks([x for x, _ in rest])
-            u = Unit(cur[0], cur[1], cur[2], body, decls)
-            u.implicit = not implicit_none
-            u.equivs = equivs
-            u.flat = rest if flat else None  # statements with labels, run by a program counter
-            units[cur[1]] = u
+            u = _make_unit(cur, stmts, labels, implicit_none)
+            if host is not None:
+                host[4][cur[1]] = u
+            else:
+                units[cur[1]] = u
             cur = None
             continue
         stmts.append(st)
@@ -608,6 +678,76 @@ def _to_real(x):
     return F32(x)
 
 
+def _is_c(x):
+    return isinstance(x, (complex, np.complexfloating)) or (isinstance(x, np.ndarray) and x.dtype.kind == "c")
+
+
+def _cre(x):
+    if _is_c(x):
+        return x.real.astype(np.float32) if isinstance(x, np.ndarray) else F32(x.real)
+    return _to_real(x)
+
+
+def _cim(x):
+    return x.imag.astype(np.float32) if isinstance(x, np.ndarray) else F32(x.imag)
+
+
+def _cmk(re, im):
+    if isinstance(re, np.ndarray) or isinstance(im, np.ndarray):
+        re, im = np.broadcast_arrays(np.asarray(re, np.float32), np.asarray(im, np.float32))
+        out = np.empty(re.shape, C64, order="F")
+        out.real = re
+        out.imag = im
+        return out
+    return C64(complex(float(re), float(im)))
+
+
+def _cbin(op, a, b):
+    """One COMPLEX operation as gfortran lowers it (see the module docstring):
+    single-precision rounding of every real operation."""
+    ca, cb = _is_c(a), _is_c(b)
+    if op in ("+", "-"):
+        f = (lambda x, y: x + y) if op == "+" else (lambda x, y: x - y)
+        if ca and cb:
+            return _cmk(f(_cre(a), _cre(b)), f(_cim(a), _cim(b)))
+        if ca:
+            return _cmk(f(_cre(a), _to_real(b)), _cim(a))
+        return _cmk(f(_to_real(a), _cre(b)), _cim(b) if op == "+" else -_cim(b))
+    if op == "*":
+        if ca and cb:
+            ar, ai, br, bi = _cre(a), _cim(a), _cre(b), _cim(b)
+            return _cmk(ar * br - ai * bi, ar * bi + ai * br)
+        if ca:
+            r = _to_real(b)
+            return _cmk(_cre(a) * r, _cim(a) * r)
+        r = _to_real(a)
+        return _cmk(r * _cre(b), r * _cim(b))
+    if op == "/":
+        if not cb:
+            r = _to_real(b)
+            return _cmk(_cre(a) / r, _cim(a) / r)
+        ar = _cre(a)
+        ai = _cim(a) if ca else (np.zeros_like(ar) if isinstance(ar, np.ndarray) else F32(0))
+        br, bi = _cre(b), _cim(b)
+        with np.errstate(all="ignore"):
+            # |br| < |bi|: ratio = br/bi, else ratio = bi/br (GCC's wide-range division)
+            r1 = br / bi
+            d1 = br * r1 + bi
+            t1r, t1i = ar * r1 + ai, ai * r1 - ar
+            r2 = bi / br
+            d2 = bi * r2 + br
+            t2r, t2i = ai * r2 + ar, ai - ar * r2
+            small = np.abs(br) < np.abs(bi)
+            tr = np.where(small, t1r, t2r).astype(np.float32)
+            ti = np.where(small, t1i, t2i).astype(np.float32)
+            dv = np.where(small, d1, d2).astype(np.float32)
+            re, im = tr / dv, ti / dv
+        if not isinstance(re, np.ndarray) or re.ndim == 0:
+            re, im = F32(re), F32(im)
+        return _cmk(re, im)
+    raise RuntimeError(f"operator {op} on COMPLEX operands")
+
+
 def _int_div(a, b):
     if isinstance(a, np.ndarray) or isinstance(b, np.ndarray):
         q = np.abs(a) // np.abs(b)
@@ -628,25 +768,39 @@ def _power(a, b):
         r = a
         # gfortran expands small integer powers by repeated multiplication
         for _ in range(n - 1):
-            r = r * a
+            r = _cbin("*", r, a) if _is_c(a) else r * a
         return r
     return np.power(_to_real(a), _to_real(b))
 
 
 class Interp:
-    def __init__(self, units, globals_=None, overrides=None):
+    def __init__(self, units, globals_=None, overrides=None, natives=None):
         self.units = units
         self.globals = globals_ or {}
         self.overrides = overrides or {}
+        self.natives = natives or {}
+
+    def resolve(self, ctx, name):
+        """(unit, host env) of a procedure called from ctx: an internal
+        procedure of the calling unit or of its host, else a top-level one."""
+        u = ctx["unit"]
+        if name in getattr(u, "internals", {}):
+            return u.internals[name], ctx["env"]
+        host = getattr(u, "host", None)
+        if host is not None and name in host.internals:
+            return host.internals[name], ctx.get("host_env")
+        if name in self.units:
+            return self.units[name], None
+        return None, None
 
     # -- entry ------------------------------------------------------------
-    def call(self, name, actuals):
+    def call(self, name, actuals, unit=None, host_env=None):
         """Call a unit with a list of Var objects (by reference)."""
-        u = self.units[name]
+        u = unit if unit is not None else self.units[name]
         env = {}
         for dummy, act in zip(u.args, actuals):
             env[dummy] = act
-        ctx = {"unit": u, "env": env, "implicit": getattr(u, "implicit", False)}
+        ctx = {"unit": u, "env": env, "implicit": getattr(u, "implicit", False), "host_env": host_env}
         # declarations: args first bound; now declare locals and reshape dummies
         for d in u.decls:
             _, no, ftype, alloc, entities = d
@@ -654,15 +808,7 @@ class Interp:
                 if nm in env and nm in u.args:
                     v = env[nm]
                     if dims is not None and not alloc and isinstance(v.value, np.ndarray):
-                        shape = self._dims(ctx, dims, v.value)
-                        if shape is not None and tuple(shape) != v.value.shape:
-                            arr = v.value
-                            if not (arr.flags.f_contiguous or arr.ndim <= 1):
-                                raise RuntimeError(f"{name}: non-contiguous actual for {nm}")
-                            view = arr.reshape(tuple(shape), order="F")
-                            if not np.shares_memory(view, arr):
-                                raise RuntimeError("reshape copied")
-                            env[nm] = Var(view, v.ftype)
+                        env[nm] = Var(self._dummy_view(ctx, name, nm, dims, ftype, v.value), ftype)
                     continue
                 if nm == name and u.kind == "function":
                     env[nm] = Var(self._zero(ftype), ftype)
@@ -703,13 +849,38 @@ class Interp:
             return None
         return [int(self.eval(ctx, d)) for d in dims]
 
+    def _dummy_view(self, ctx, unit, nm, dims, ftype, arr):
+        """The array dummy nm of the given declared shape (a trailing '*' takes
+        the rest) over the storage of its actual: sequence association, from
+        the actual's first element on; a COMPLEX actual seen by a REAL dummy
+        is its interleaved real and imaginary parts."""
+        flat = arr.reshape(-1, order="F")
+        if arr.size and not np.shares_memory(flat, arr):
+            raise RuntimeError(f"{unit}: non-contiguous actual for {nm}")
+        want = self._dtype(ftype)
+        if flat.dtype != want:
+            if flat.dtype == C64 and want == np.float32:
+                flat = flat.view(np.float32)
+            else:
+                raise RuntimeError(f"{unit}: actual of type {flat.dtype} for dummy {nm} of type {ftype}")
+        shape = [None if d[0] == "star" else int(self.eval(ctx, d)) for d in dims]
+        if None in shape:
+            known = int(np.prod([x for x in shape if x is not None])) if len(shape) > 1 else 1
+            shape = [x if x is not None else flat.size // max(known, 1) for x in shape]
+        n = int(np.prod(shape))
+        if n > flat.size:
+            raise RuntimeError(f"{unit}: dummy {nm}{tuple(shape)} larger than its actual ({flat.size})")
+        return flat[:n].reshape(tuple(shape), order="F")
+
     @staticmethod
     def _dtype(ftype):
-        return {"integer": np.int64, "real": np.float32, "double": np.float64, "logical": np.bool_}.get(ftype, np.float32)
+        return {"integer": np.int64, "real": np.float32, "double": np.float64, "logical": np.bool_,
+                "complex": C64}.get(ftype, np.float32)
 
     @staticmethod
     def _zero(ftype):
-        return {"integer": 0, "real": F32(0), "double": np.float64(0), "logical": False}.get(ftype, None)
+        return {"integer": 0, "real": F32(0), "double": np.float64(0), "logical": False,
+                "complex": C64(0)}.get(ftype, None)
 
     # -- statements ---------------------------------------------------------
     def run_flat(self, ctx, flat):
@@ -836,6 +1007,9 @@ class Interp:
         env = ctx["env"]
         if name in env:
             return env[name]
+        host = ctx.get("host_env")
+        if host is not None and name in host:
+            return host[name]
         if name in self.globals:
             return self.globals[name]
         if ctx.get("implicit", True):
@@ -846,7 +1020,8 @@ class Interp:
         raise NameError(f"{ctx['unit'].name}: unknown variable {name}")
 
     def has_var(self, ctx, name):
-        return name in ctx["env"] or name in self.globals
+        host = ctx.get("host_env")
+        return name in ctx["env"] or (host is not None and name in host) or name in self.globals
 
     # -- calls --------------------------------------------------------------
     def do_call(self, ctx, name, args):
@@ -857,14 +1032,26 @@ class Interp:
             if name in ("mpi_comm_size", "mpi_comm_rank"):
                 self.lookup(ctx, args[1][1]).value = 1 if name == "mpi_comm_size" else 0
             return
+        callee, host_env = self.resolve(ctx, name)
+        array_dummy = set()
+        if callee is not None:
+            for d in callee.decls:
+                for (nm, dims, init) in d[4]:
+                    if nm in callee.args and dims is not None and not d[3]:
+                        array_dummy.add(callee.args.index(nm))
         actuals, writeback = [], []
-        for a in args:
+        for k, a in enumerate(args):
             if a[0] == "name" and self.has_var(ctx, a[1]):
                 actuals.append(self.lookup(ctx, a[1]))
             elif a[0] == "ref" and self.has_var(ctx, a[1]):
                 base = self.lookup(ctx, a[1])
                 idx, basic, scalar = self.index(ctx, base.value, a[2])
-                if scalar:
+                if scalar and k in array_dummy:
+                    # an array element actual for an array dummy: the storage
+                    # from that element on (sequence association)
+                    off = int(np.ravel_multi_index(idx, base.value.shape, order="F"))
+                    actuals.append(Var(base.value.reshape(-1, order="F")[off:], base.ftype))
+                elif scalar:
                     box = Var(base.value[idx], base.ftype)
                     actuals.append(box)
                     writeback.append((base, idx, box))
@@ -876,9 +1063,12 @@ class Interp:
                 val = self.eval(ctx, a)
                 ftype = "integer" if _is_int(val) else ("logical" if isinstance(val, (bool, np.bool_)) else "real")
                 actuals.append(Var(val, ftype))
-        if name not in self.units:
+        if name in self.natives:
+            self.natives[name](*actuals)
+        elif callee is None:
             raise NameError(f"unknown subroutine {name}")
-        self.call(name, actuals)
+        else:
+            self.call(name, actuals, unit=callee, host_env=host_env)
         for base, idx, box in writeback:
             base.value[idx] = box.value
 
@@ -921,16 +1111,24 @@ class Interp:
         if dtype.kind in "iu":
             if isinstance(val, np.ndarray):
                 return np.trunc(val).astype(dtype) if val.dtype.kind == "f" else val.astype(dtype)
-            return int(math.trunc(val)) if not _is_int(val) else val
+            return int(math.trunc(float(val))) if not _is_int(val) else val
+        if dtype == C64:
+            if _is_c(val):
+                return val.astype(C64) if isinstance(val, np.ndarray) else C64(val)
+            return _cmk(_to_real(val), F32(0))
         if dtype == np.float32:
+            if _is_c(val):
+                return _cre(val)
             return val.astype(np.float32) if isinstance(val, np.ndarray) else F32(val)
         return val
 
     def _conv_scalar(self, val, ftype):
         if ftype == "integer":
-            return int(math.trunc(val)) if not _is_int(val) else int(val)
+            return int(math.trunc(float(val))) if not _is_int(val) else int(val)
         if ftype == "real":
-            return F32(val)
+            return _cre(val) if _is_c(val) else F32(val)
+        if ftype == "complex":
+            return C64(val) if _is_c(val) else _cmk(_to_real(val), F32(0))
         if ftype == "double":
             return np.float64(val)
         if ftype == "logical":
@@ -998,6 +1196,8 @@ class Interp:
             return e[1]
         if k == "paren":
             return self.eval(ctx, e[1])
+        if k == "cplx":
+            return _cmk(_to_real(self.eval(ctx, e[1])), _to_real(self.eval(ctx, e[2])))
         if k == "neg":
             v = self.eval(ctx, e[1])
             return -v
@@ -1023,7 +1223,8 @@ class Interp:
                 if isinstance(out, np.ndarray):
                     return np.array(out, order="F")
                 return out
-            if name in self.units:
+            callee, host_env = self.resolve(ctx, name)
+            if callee is not None:
                 actuals = []
                 for a in args:
                     if a[0] == "name" and self.has_var(ctx, a[1]):
@@ -1031,11 +1232,13 @@ class Interp:
                     else:
                         val = self.eval(ctx, a)
                         actuals.append(Var(val, "integer" if _is_int(val) else "real"))
-                return self.call(name, actuals)
+                return self.call(name, actuals, unit=callee, host_env=host_env)
             return self.intrinsic(ctx, name, args)
         raise RuntimeError(f"cannot evaluate {e}")
 
     def binop(self, op, a, b):
+        if op in ("+", "-", "*", "/") and (_is_c(a) or _is_c(b)):
+            return _cbin(op, a, b)
         if op in ("+", "-", "*", "/"):
             if _is_int(a) and _is_int(b):
                 if op == "+":
@@ -1075,20 +1278,28 @@ class Interp:
             return _vec(_libm.expf, _to_real(vals[0]))
         if name == "log":
             return _vec(_libm.logf, _to_real(vals[0]))
+        if name in ("cos", "sin", "atan"):
+            return _vec(getattr(_libm, name + "f"), _to_real(vals[0]))
+        if name == "aimag":
+            return _cim(vals[0])
+        if name == "conjg":
+            return _cmk(_cre(vals[0]), -_cim(vals[0]))
+        if name == "cmplx":
+            return _cmk(_to_real(vals[0]), _to_real(vals[1]) if len(vals) > 1 else F32(0))
         if name in ("maxval", "minval"):
             arr = vals[0]
             return arr.max() if name == "maxval" else arr.min()
         if name in ("real", "float"):
-            return _to_real(vals[0])
+            return _cre(vals[0])
         if name == "int":
             v = vals[0]
-            return np.trunc(v).astype(np.int64) if isinstance(v, np.ndarray) else int(math.trunc(v))
+            return np.trunc(v).astype(np.int64) if isinstance(v, np.ndarray) else int(math.trunc(float(v)))
         if name == "nint":
             return int(np.rint(vals[0]))
         if name == "ceiling":
-            return int(math.ceil(vals[0]))
+            return int(math.ceil(float(vals[0])))
         if name == "floor":
-            return int(math.floor(vals[0]))
+            return int(math.floor(float(vals[0])))
         if name == "mod":
             a, b = vals
             if _is_int(a) and _is_int(b):
@@ -1130,28 +1341,31 @@ class _MeshIndex(tuple):
 class Program:
     """All subroutines of a set of Fortran source files."""
 
-    def __init__(self, paths, globals_=None, overrides=None, mpi_stub=False):
+    def __init__(self, paths, globals_=None, overrides=None, mpi_stub=False, natives=None):
         self.units = {}
         for p in paths:
             with open(p, encoding="latin-1") as f:
                 self.units.update(parse_units(f.read()))
-        self.interp = Interp(self.units, globals_, overrides)
+        self.interp = Interp(self.units, globals_, overrides, natives)
         self.interp.mpi_stub = mpi_stub
 
     def call(self, name, *actuals):
         return self.interp.call(name, list(actuals))
 
 
-def run_snippet(path, first, last, env, globals_=None):
+def run_snippet(path, first, last, env, globals_=None, program=None):
     """Execute source lines first..last (1-based, inclusive) of a file as a
-    statement sequence in an environment of Var objects."""
+    statement sequence in an environment of Var objects; CALLs go to the
+    procedures of `program` (a Program) when given."""
     with open(path, encoding="latin-1") as f:
         text = f.read()
     lines = text.split("\n")[first - 1:last]
     stmts = [parse_stmt(no, s) for no, s in logical_lines("\n".join(lines))]
     body = build_blocks([x for x in stmts if x[0] != "decl"])
     unit = Unit("snippet", f"{path}:{first}-{last}", [], body, [])
-    interp = Interp({}, globals_)
+    interp = Interp(program.units if program is not None else {}, globals_)
+    if program is not None:
+        interp.natives = program.interp.natives
     ctx = {"unit": unit, "env": env}
     interp.run(ctx, body)
     return env

@@ -1,17 +1,18 @@
 """Generate the golden vectors in tests/golden/*.npz from the reference source.
 
-Run in a container where the reference checkout exists (its path is the
-first argument, default /root/reference).  Each case executes the
+Run where a checkout of the reference exists: its path is the first
+argument, or the environment variable FWI_REFERENCE.  Each case executes the
 reference's own Fortran routines -- solver_acoustic_SS and the files it
 calls, Misfit_function/Misfit_L2, Beta_calculous, Ricker_mcs, polyfit,
-interpolation_akima/INTRPL, and the geometry and time-step statements of
-get_mcs_data.f90 and calculate_misfit_gradient.f90 -- through fortran_exec.py
-in IEEE single precision, on small seeded inputs, and stores inputs and
-outputs.
+interpolation_akima/INTRPL, time_filter with filters_function1D/butterworth
+and the FFTPACK5 transforms, the post-solver part of source_estimation, and
+the geometry and time-step statements of get_mcs_data.f90, get_was_data.f90
+and calculate_misfit_gradient.f90 -- through fortran_exec.py in IEEE single
+precision, on small seeded inputs, and stores inputs and outputs.
 
 The fixtures are committed; tests read them and never need the reference.
 
-    python tests/golden/make_golden.py [/path/to/reference [case ...]]
+    python tests/golden/make_golden.py /path/to/reference [case ...]
 """
 from __future__ import annotations
 
@@ -251,21 +252,155 @@ def case_akima(src):
     print("akima: done")
 
 
+def case_filter(src):
+    """time_filter (time_filter.f90) -> filters_function1D/butterworth
+    (filters.f90) -> cfft1i/cfft1f/cfft1b (fftpack.f90) on a 20-sample record
+    (480-point transforms: radix 4, 4, 2, 3, 5), three traces of which one is
+    zero (left untouched), for the low-pass, high-pass and band-pass types and
+    the reference's order 6, plus the low-pass at order 4 (the order set
+    through the interpreter's override of n = 6)."""
+    t0 = time.time()
+    paths = [os.path.join(src, f) for f in ("time_filter.f90", "filters.f90", "fftpack.f90", "auxiliar.f90")]
+    rng = np.random.default_rng(21)
+    nt, num, dt = 20, 3, F32(0.004)
+    base = farr(np.zeros((nt, num)))
+    base[:, 0] = rng.standard_normal(nt).astype(F32)
+    tt = np.arange(nt, dtype=np.float32) * dt
+    base[:, 1] = (np.sin(F32(2 * np.pi * 12.0) * tt) + F32(0.5) * np.sin(F32(2 * np.pi * 70.0) * tt)).astype(F32)
+    cases = [(1, 0.0, 30.0, 6), (2, 0.0, 30.0, 6), (3, 10.0, 60.0, 6), (1, 0.0, 25.0, 4)]
+    out = {"data": base, "dt": dt, "nt": nt}
+    for k, (typef, f1, fc, order) in enumerate(cases):
+        prog = fe.Program(paths, overrides={("filters_function1d", "n"): order})
+        d = farr(base.copy())
+        prog.call("time_filter", V(d), V(nt, "integer"), V(dt), V(num, "integer"), V(typef, "integer"),
+                  V(F32(f1)), V(F32(fc)))
+        out.update({f"c{k}_typef": typef, f"c{k}_f1": F32(f1), f"c{k}_fc": F32(fc), f"c{k}_order": order,
+                    f"c{k}_out": d})
+        print(f"filter case {k}: {time.time() - t0:.0f} s", flush=True)
+    out["ncases"] = len(cases)
+    np.savez_compressed(os.path.join(HERE, "filter.npz"), **out)
+    print("filter: done")
+
+
+def case_was(src):
+    """The WAS geometry (get_was_data.f90): shot navigation (receivers of the
+    reciprocal inversion, :153-159), OBS navigation (:201-205), the
+    bathymetry model by INTRPL over the shots' water depths (:584-613), the
+    relocation of the OBS to it (:112-115) and the source/receiver indices
+    (:223-231), executed statement by statement from the source with the
+    module variables they use; added_space_model = 0 as no parfile key sets
+    it (modules.f90:153)."""
+    path = os.path.join(src, "get_was_data.f90")
+    prog = fe.Program([os.path.join(src, "akima433.f90")])
+    rng = np.random.default_rng(31)
+    ns, nobs, d, nxm = 9, 4, F32(25.0), 120
+    xs = (F32(100.0) + F32(337.5) * np.arange(ns, dtype=np.float32) + rng.uniform(-40, 40, ns).astype(F32)).astype(F32)
+    bat = (F32(1800.0) + rng.uniform(-300, 300, ns).astype(F32)).astype(F32)
+    xobs = np.array([212.0, 1010.0, 1999.9, 2600.3], np.float32)
+    zobs = np.array([1700.0, 1900.0, 2100.0, 1750.0], np.float32)
+    g = {}
+
+    def gv(name, value, ftype):
+        g[name] = V(value, ftype)
+
+    gv("numshots_was", ns, "integer")
+    gv("numrec_was", ns, "integer")
+    gv("numobs", nobs, "integer")
+    gv("dmodel", d, "real")
+    gv("added_space_model", F32(0.0), "real")
+    gv("shot_depth_was", F32(10.0), "real")
+    gv("nxmodel", nxm, "integer")
+    gv("length_model", F32(F32(nxm - 1) * d), "real")  # modules.f90:431
+    for nm, n, ft in (("shotid_nav_was", ns, "integer"), ("pos_shot_was", ns, "real"), ("pos_shot_grid_was", ns, "integer"),
+                      ("pos_bat_was", ns, "real"), ("pos_bat_grid_was", ns, "integer"), ("pos_xobs", nobs, "real"),
+                      ("pos_xobs_grid", nobs, "integer"), ("pos_zobs", nobs, "real"), ("pos_zobs_grid", nobs, "integer"),
+                      ("bat_model_was", nxm, "real"), ("bat_model_grid_was", nxm, "integer"),
+                      ("nxsou_was", nobs, "integer"), ("nysou_was", nobs, "integer")):
+        gv(nm, np.zeros(n, np.int64 if ft == "integer" else np.float32), ft)
+    gv("nxrec_was", np.zeros((ns, nobs), np.int64, order="F"), "integer")
+    gv("nyrec_was", np.zeros((ns, nobs), np.int64, order="F"), "integer")
+    for i in range(ns):
+        env = {"i": V(i + 1, "integer"), "xs": V(xs[i]), "bat": V(bat[i]), "shotid": V(i + 1, "integer")}
+        fe.run_snippet(path, 153, 159, env, g)
+    for i in range(nobs):
+        env = {"i": V(i + 1, "integer"), "xs": V(xobs[i]), "xz": V(zobs[i])}
+        fe.run_snippet(path, 201, 205, env, g)
+    obs_grid_nav = g["pos_zobs_grid"].value.copy()
+    env = {"i": V(0, "integer"), "err": V(0, "integer"), "xmodel": V(None, "real", alloc=True),
+           "xmodel_": V(None, "real", alloc=True), "xbat_": V(None, "real", alloc=True)}
+    fe.run_snippet(path, 584, 613, env, g, program=prog)
+    fe.run_snippet(path, 112, 115, {"i": V(0, "integer")}, g)
+    fe.run_snippet(path, 223, 231, {"iobs": V(0, "integer"), "irec": V(0, "integer")}, g)
+    out = {"xs": xs, "bat": bat, "xobs": xobs, "zobs": zobs, "dmodel": d, "nxmodel": nxm,
+           "shot_depth": F32(10.0), "zobs_grid_nav": obs_grid_nav}
+    for nm in ("pos_shot_grid_was", "pos_bat_grid_was", "pos_xobs_grid", "pos_zobs", "pos_zobs_grid", "bat_model_was",
+               "bat_model_grid_was", "nxsou_was", "nysou_was", "nxrec_was", "nyrec_was"):
+        v = g[nm].value
+        out[nm] = v.astype(np.int32) if v.dtype.kind in "iu" else v
+    np.savez_compressed(os.path.join(HERE, "was_geometry.npz"), **out)
+    print("was geometry: done")
+
+
+def case_source(src):
+    """source_estimation (source_estimation.f90) after its forward solve: the
+    water-bottom mute (:76-107), normalisation (:109-110), FFTPACK5 transforms
+    of Gs and Go (:124-134), the receiver sums kk and bb (:144-154), eps and
+    the Wiener quotient (:156-159) and the inverse transform (:169-171).  The
+    Green's functions Gs (solver_forward_simple) and the observed traces Go
+    (get_shot_data) are supplied inputs: the two calls are replaced by Python
+    stand-ins that copy them in."""
+    paths = [os.path.join(src, f) for f in ("source_estimation.f90", "fftpack.f90")]
+    rng = np.random.default_rng(41)
+    ny, nx, nt, nr = 24, 40, 120, 6
+    d, dt, f1, f2 = F32(10.0), F32(0.002), F32(0.0), F32(30.0)
+    z = np.arange(ny)[:, None] * np.ones((1, nx))
+    model = farr(np.where(z < 9, 1500.0, 1800.0 + 30.0 * (z - 9)))
+    nxs, nys = 12, 2
+    nxr = np.array([14, 17, 20, 23, 26, 29], np.int64)
+    nyr = np.full(nr, 2, np.int64)
+    tt = np.arange(nt, dtype=np.float64) * float(dt)
+    Gs = np.zeros((nt, nr))
+    Go = np.zeros((nt, nr))
+    for r in range(nr):
+        t0 = 0.02 + 0.003 * r
+        a = (np.pi * 25.0 * (tt - t0)) ** 2
+        Gs[:, r] = (1 - 2 * a) * np.exp(-a) * (1.0 + 0.1 * r)
+        a2 = (np.pi * 18.0 * (tt - t0 - 0.01)) ** 2
+        Go[:, r] = (1 - 2 * a2) * np.exp(-a2) * (0.8 + 0.05 * r) + 0.01 * rng.standard_normal(nt)
+    Gs, Go = farr(Gs), farr(Go)
+
+    def get_shot_data(k, arr):
+        arr.value[...] = Go
+
+    def solver_forward_simple(*a):
+        a[-1].value[...] = Gs
+
+    prog = fe.Program(paths, natives={"get_shot_data": get_shot_data, "solver_forward_simple": solver_forward_simple})
+    sst = farr(np.zeros(nt))
+    prog.call("source_estimation", V(1, "integer"), V(f1), V(f2), V(nx, "integer"), V(ny, "integer"),
+              V(nt, "integer"), V(nr, "integer"), V(d), V(dt), V(nxs, "integer"), V(nys, "integer"),
+              V(nxr.copy(), "integer"), V(nyr.copy(), "integer"), V(model), V(sst))
+    np.savez_compressed(os.path.join(HERE, "source_estimation.npz"), Gs=Gs, Go=Go, model=model, nxs=nxs, nys=nys,
+                        nxr=nxr.astype(np.int32), nyr=nyr.astype(np.int32), d=d, dt=dt, f1=f1, f2=f2, sst=sst)
+    print("source estimation: done")
+
+
 def main():
-    src = os.path.join(sys.argv[1] if len(sys.argv) > 1 else "/root/reference", "src")
-    only = set(sys.argv[2:])  # optional case names: coeffs misfit geometry polyfit akima solver
+    ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("FWI_REFERENCE")
+    if not ref:
+        sys.exit("usage: make_golden.py /path/to/reference [case ...]  (or set FWI_REFERENCE)")
+    src = os.path.join(ref, "src")
+    only = set(sys.argv[2:])  # optional case names: coeffs misfit geometry polyfit akima filter was source solver
+    names = ("coeffs", "misfit", "geometry", "polyfit", "akima", "filter", "was", "source")
     if only:
-        for name in ("coeffs", "misfit", "geometry", "polyfit", "akima"):
+        for name in names:
             if name in only:
                 globals()["case_" + name](src)
         if "solver" not in only:
             return
     else:
-        case_coeffs(src)
-        case_misfit(src)
-        case_geometry(src)
-        case_polyfit(src)
-        case_akima(src)
+        for name in names:
+            globals()["case_" + name](src)
     # acc=3 (the reference's hard-coded order), snapshots every 10 steps;
     # sources incl. one outside the interior; receivers with duplicates,
     # in the left pad, in the bottom strip and in a bottom corner.

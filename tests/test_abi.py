@@ -56,6 +56,21 @@ def test_geometry_ricker_time_rules_bit_exact(golden):
         assert dt == g[f"time_{t}_dt"] and nt == g[f"time_{t}_nt"] and nts == g[f"time_{t}_ntstore"]
 
 
+def test_was_geometry_bit_exact(golden):
+    """fwi_was_geometry (host FP32) against the statements of
+    get_was_data.f90 executed from the reference: shot and OBS columns, the
+    bathymetry model by INTRPL and its rows, the OBS relocated to it."""
+    from fwi_gb300 import api
+    z = golden("was_geometry")
+    args = (z["xobs"], z["zobs"], z["xs"], z["bat"], float(z["shot_depth"]), float(z["dmodel"]), int(z["nxmodel"]))
+    g = api.was_geometry(*args)
+    assert np.array_equal(g["bat_model"], z["bat_model_was"])
+    assert np.array_equal(g["bat_model_grid"], z["bat_model_grid_was"])
+    assert np.array_equal(g["nxSou"], z["nxsou_was"]) and np.array_equal(g["nySou"], z["nysou_was"])
+    assert np.array_equal(g["nxRec"], z["nxrec_was"][:, 0]) and g["nyRec"] == z["nyrec_was"][0, 0]
+    assert np.array_equal(api.was_geometry(*args, relocate=False)["nySou"], z["zobs_grid_nav"])
+
+
 def test_argument_errors_are_reported():
     from fwi_gb300 import _native as N
     lib = N.load()

@@ -75,6 +75,28 @@ def test_time_filter_vs_oracle(typef, f1, fc, order):
         assert err <= 2e-5, (i, err)
 
 
+def test_time_filter_vs_reference_golden():
+    """The device filter (cuFFT, FP32) against time_filter executed from the
+    reference (FFTPACK5, FP32): low-, high- and band-pass at order 6, low-pass
+    at order 4; the two FP32 transforms round differently, within 1e-5."""
+    import os
+
+    import fwi_gb300 as F
+    z = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "filter.npz"))
+    data = z["data"]
+    nt, num = data.shape
+    for k in range(int(z["ncases"])):
+        F.set_filter_order(int(z[f"c{k}_order"]))
+        try:
+            got = F.time_filter(np.asfortranarray(data.copy()), nt, float(z["dt"]), num, int(z[f"c{k}_typef"]),
+                                float(z[f"c{k}_f1"]), float(z[f"c{k}_fc"]))
+        finally:
+            F.set_filter_order(6)
+        out = z[f"c{k}_out"]
+        assert np.array_equal(got[:, 2], out[:, 2])
+        assert _rel(got[:, :2], out[:, :2].astype(np.float64)) <= 1e-5, k
+
+
 def test_time_filter_device_pointer_and_batches():
     import torch
     import fwi_gb300 as F

@@ -74,3 +74,49 @@ def test_ricker_geometry_time_rules(golden):
         dm, tf = (float(v) for v in g[f"time_{t}_par"])
         dt, nt, nts = O.time_rules(g[f"time_{t}_lambda"], dm, tf)
         assert dt == g[f"time_{t}_dt"] and nt == g[f"time_{t}_nt"] and nts == g[f"time_{t}_ntstore"]
+
+
+def test_filter_oracle_vs_reference_golden(golden):
+    """oracle/prep.time_filter (float64 FFT) against time_filter ->
+    filters_function1D/butterworth -> FFTPACK5 executed from the reference in
+    FP32 (the FFTPACK5 rounding is the difference): low-, high- and
+    band-pass at order 6 and a low-pass at order 4; the all-zero trace is left
+    untouched."""
+    from oracle import prep as P
+    z = golden("filter")
+    data = z["data"]
+    for k in range(int(z["ncases"])):
+        out = z[f"c{k}_out"]
+        got = P.time_filter(data, float(z["dt"]), int(z[f"c{k}_typef"]), float(z[f"c{k}_f1"]), float(z[f"c{k}_fc"]),
+                            order=int(z[f"c{k}_order"]))
+        assert np.array_equal(out[:, 2], data[:, 2]) and not np.any(got[:, 2])
+        e = np.linalg.norm(got[:, :2] - out[:, :2]) / np.linalg.norm(out[:, :2].astype(np.float64))
+        assert e <= 1e-6, (k, e)
+
+
+def test_was_geometry_oracle_vs_reference_golden(golden):
+    """oracle/prep.was_geometry against the statements of get_was_data.f90
+    executed from the reference: bit-exact indices and bathymetry model."""
+    from oracle import prep as P
+    z = golden("was_geometry")
+    args = (z["xobs"], z["zobs"], z["xs"], z["bat"], float(z["shot_depth"]), float(z["dmodel"]), int(z["nxmodel"]))
+    g = P.was_geometry(*args)
+    assert np.array_equal(g["bat_model"], z["bat_model_was"])
+    assert np.array_equal(g["bat_model_grid"], z["bat_model_grid_was"])
+    assert np.array_equal(g["nxSou"], z["nxsou_was"]) and np.array_equal(g["nySou"], z["nysou_was"])
+    assert np.array_equal(g["nxRec"], z["nxrec_was"][:, 0]) and g["nyRec"] == z["nyrec_was"][0, 0]
+    assert np.array_equal(P.was_geometry(*args, relocate=False)["nySou"], z["zobs_grid_nav"])
+
+
+def test_wiener_estimate_vs_reference_golden(golden):
+    """The Wiener step of source estimation (fwi_gb300/source.py:
+    wiener_estimate, float64 FFT) against source_estimation.f90 executed
+    from the reference after its forward solve (mute, normalisation,
+    FFTPACK5, kk/bb sums, eps, inverse transform) on the same Green's
+    functions and observed traces."""
+    from fwi_gb300.source import wiener_estimate
+    z = golden("source_estimation")
+    got = wiener_estimate(z["Gs"], z["Go"], z["model"], float(z["d"]), float(z["dt"]), float(z["f1"]),
+                          float(z["f2"]), int(z["nxs"]), z["nxr"])
+    sst = z["sst"].astype(np.float64)
+    assert np.linalg.norm(got - sst) / np.linalg.norm(sst) <= 1e-6

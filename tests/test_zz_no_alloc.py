@@ -40,7 +40,10 @@ def _reference_entry(z):
     return rec
 
 
-def _noalloc(z):
+def _noalloc(z, calls=1):
+    """Device buffers from torch, then `calls` calls of the entry point.
+    Returns the traces and the device's free bytes (cudaMemGetInfo) before
+    and after each call."""
     import torch
 
     import fwi_gb300 as F
@@ -53,12 +56,16 @@ def _noalloc(z):
     rec = torch.full((nrec * z["nt"],), 5.0, dtype=torch.float32, device=dev)
     torch.cuda.synchronize()
     p = lambda a: a.ctypes.data_as(C.c_void_p)  # noqa: E731
-    rc = lib.fwi_solver_forward_noalloc(len(z["nxSou"]), nrec, p(z["nxSou"]), p(z["nySou"]), p(z["nxRec"]),
-                                        p(z["nyRec"]), C.c_void_p(S.data_ptr()), z["d"], z["dt"], z["ny"], z["nx"],
-                                        C.c_void_p(ct.data_ptr()), z["nt"], C.c_void_p(rec.data_ptr()))
-    assert rc == 0, lib.fwi_last_error()
-    torch.cuda.synchronize()
-    return rec.cpu().numpy().reshape(z["nt"], nrec, order="F")
+    free = []
+    for _ in range(calls):
+        f0 = torch.cuda.mem_get_info(dev)[0]
+        rc = lib.fwi_solver_forward_noalloc(len(z["nxSou"]), nrec, p(z["nxSou"]), p(z["nySou"]), p(z["nxRec"]),
+                                            p(z["nyRec"]), C.c_void_p(S.data_ptr()), z["d"], z["dt"], z["ny"],
+                                            z["nx"], C.c_void_p(ct.data_ptr()), z["nt"], C.c_void_p(rec.data_ptr()))
+        assert rc == 0, lib.fwi_last_error()
+        torch.cuda.synchronize()
+        free.append((f0, torch.cuda.mem_get_info(dev)[0]))
+    return rec.cpu().numpy().reshape(z["nt"], nrec, order="F"), free
 
 
 def test_noalloc_matches_drop_in_on_two_calls():
@@ -66,11 +73,24 @@ def test_noalloc_matches_drop_in_on_two_calls():
     F.init(0)
     for z in (_case(1, 60, 150, 300), _case(2, 40, 333, 250, acc=4)):
         ref = _reference_entry(z)
-        first = _noalloc(z)
-        second = _noalloc(z)
+        first, _ = _noalloc(z)
+        second, _ = _noalloc(z)
         assert np.abs(ref).max() > 0
         np.testing.assert_array_equal(first, ref)
         np.testing.assert_array_equal(second, ref)
+
+
+def test_noalloc_leaves_device_memory_untouched():
+    """The property the entry point exists for: once the library is set up
+    and a first call has been made, a call takes no device memory -- the free
+    bytes the driver reports are the same before and after it."""
+    import fwi_gb300 as F
+    F.init(0)
+    z = _case(4, 50, 200, 200)
+    traces, free = _noalloc(z, calls=3)
+    np.testing.assert_array_equal(traces, _reference_entry(z))
+    for before, after in free[1:]:
+        assert before == after, f"free device memory changed across a call: {before} -> {after}"
 
 
 def test_noalloc_rejects_grids_beyond_its_scratch():

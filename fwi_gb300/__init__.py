@@ -39,6 +39,7 @@ from .api import (  # noqa: E402,F401
     solver_acoustic_SS,
     su_info,
     su_read,
+    su_supershot,
     su_write,
     time_filter,
     time_rules,

@@ -33,7 +33,7 @@ EXPORTS = [
     "fwi_survey_recompute", "fwi_survey_set_time", "fwi_time_filter", "fwi_set_filter_order",
     "fwi_interpolation_akima", "fwi_su_info", "fwi_su_read", "fwi_su_write", "fwi_read_nav",
     "fwi_survey_time_steps", "fwi_misfit_gradient_batch", "fwi_solver_forward_noalloc", "fwi_survey_tiles",
-    "fwi_batch_plans", "fwi_batch_release", "fwi_first_step", "fwi_model_update", "fwi_was_geometry",
+    "fwi_batch_plans", "fwi_batch_release", "fwi_first_step", "fwi_model_update", "fwi_was_geometry", "fwi_su_supershot",
 ]
 
 
@@ -100,6 +100,7 @@ def load():
     lib.fwi_su_read.argtypes = [C.c_char_p, I, I, I, P]
     lib.fwi_su_write.argtypes = [C.c_char_p, P, I, I, F, I]
     lib.fwi_read_nav.argtypes = [C.c_char_p, I, P, P, P, P]
+    lib.fwi_su_supershot.argtypes = [C.POINTER(C.c_char_p), I, P, I, I, I, P]
     lib.fwi_survey_run.argtypes = [P, I, P, P]
     lib.fwi_survey_grad_device.argtypes = [P, C.POINTER(C.c_void_p)]
     lib.fwi_survey_get_stack.argtypes = [P, C.c_void_p]

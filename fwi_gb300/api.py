@@ -215,6 +215,18 @@ def su_write(path, data, dt, big_endian=False):
     N.check(N.load().fwi_su_write(str(path).encode(), _p(d), nt, ntr, C.c_float(dt), int(bool(big_endian))))
 
 
+def su_supershot(paths, coding, nt, ntr, big_endian=False):
+    """get_obs_data: the first ntr traces of each OBS file in `paths` summed
+    with their coding factors, raw_data (nt, ntr) float32 Fortran order."""
+    arr = (C.c_char_p * len(paths))(*[str(p).encode() for p in paths])
+    cod = np.ascontiguousarray(coding, np.float32)
+    if cod.size != len(paths):
+        raise ValueError("one coding factor per file")
+    out = np.zeros((nt, ntr), np.float32, order="F")
+    N.check(N.load().fwi_su_supershot(arr, len(paths), _p(cod), int(nt), int(ntr), int(bool(big_endian)), _p(out)))
+    return out
+
+
 def read_nav(path):
     """Navigation list of MCS shots: (shot numbers int32, x float32, water
     depth float32), as read_nav_shot_mcs reads it."""

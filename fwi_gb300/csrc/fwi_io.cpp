@@ -7,17 +7,24 @@
 //                 follow the 240-byte header; the file's byte order is given
 //                 (the reference's endianness_data, get_mcs_data.f90:317-323).
 //   fwi_su_write  write_new_data (auxiliar.f90:433-531) after its resampling:
-//                 the traces with SU headers whose tracl (bytes 0-3, 1-based
-//                 trace number), ns (bytes 114-115) and dt (bytes 116-117, in
-//                 microseconds) are set, as `suaddhead ns= | sushw key=dt a=`
-//                 produce them; every other header word is 0.
+//                 the traces with SU headers as `suaddhead ns= | sushw key=dt
+//                 a=` produce them (Seismic Unix, CWP; its documentation of
+//                 suaddhead: trace counters tracl and tracr, trace
+//                 identification trid = 1 for a live seismic trace, and ns;
+//                 sushw then sets dt): tracl (bytes 0-3) and tracr (4-7) the
+//                 1-based trace number, trid (28-29) 1, ns (114-115), dt
+//                 (116-117, microseconds); every other header word is 0.
+//   fwi_su_supershot  get_obs_data (get_was_data.f90:241-288): the traces of
+//                 several OBS files summed with their coding factors into one
+//                 gather, raw_data = raw_data + Coding(k)*data in FP32.
 //   fwi_su_info   ns and dt from the first header and the trace count from
 //                 the file size.
-//   fwi_read_nav  the navigation list of MCS shots (read_nav_shot_mcs,
-//                 get_mcs_data.f90:88-117, and the line count of
-//                 get_mcs_data.f90:228-245): one record per line, shot number,
-//                 shot x and water depth, read list-directed (blanks or
-//                 commas between values).
+//   fwi_read_nav  the navigation lists (read_nav_shot_mcs, get_mcs_data.f90:
+//                 88-117, with the line count of :228-245; read_nav_shot_was,
+//                 get_was_data.f90:148-164; read_nav_obs, :196-207): one
+//                 record per line, an integer (shot or OBS number) and two
+//                 reals (x and water depth, or x and OBS depth), read
+//                 list-directed (blanks or commas between values).
 //
 // Byte order: SU files are written in the host's order by the SU tools;
 // big_endian = 1 reads/writes big-endian files on any host.
@@ -128,12 +135,31 @@ int fwi_su_write(const char* path, const float* data, int nt, int ntr, float dt,
     for (int j = 0; j < ntr; ++j) {
         unsigned char h[SU_HEADER] = {0};
         put_i32(h, 0, j + 1, swap);                     // tracl
+        put_i32(h, 4, j + 1, swap);                     // tracr
+        put_u16(h, 28, 1, swap);                        // trid: live seismic trace
         put_u16(h, 114, (uint16_t)nt, swap);            // ns
         put_u16(h, 116, (uint16_t)(int)(dt * 1e6f), swap);  // dt (us), the reference's dt_head = dt2*1e6
         std::memcpy(tr.data(), data + (size_t)j * nt, 4 * (size_t)nt);
         if (swap) swap_bytes(tr.data(), (size_t)nt, 4);
         if (std::fwrite(h, 1, SU_HEADER, fh.f) != SU_HEADER || std::fwrite(tr.data(), 4, (size_t)nt, fh.f) != (size_t)nt)
             return fwi::prep_fail(FWI_ERR_ARG, std::string(path) + ": write failed");
+    }
+    return FWI_OK;
+}
+
+int fwi_su_supershot(const char* const* paths, int nsrc, const float* coding, int nt, int ntr, int big_endian,
+                     float* raw_data) {
+    if (!paths || !coding || !raw_data || nsrc < 0) return fwi::prep_fail(FWI_ERR_ARG, "null argument");
+    if (nt < 1 || ntr < 0) return fwi::prep_fail(FWI_ERR_ARG, "nt must be >= 1 and ntr >= 0");
+    const size_t n = (size_t)nt * ntr;
+    for (size_t i = 0; i < n; ++i) raw_data[i] = 0.f;  // raw_Data=0. (:265)
+    std::vector<float> tmp(n);
+    for (int k = 0; k < nsrc; ++k) {
+        if (!paths[k]) return fwi::prep_fail(FWI_ERR_ARG, "null path");
+        const int rc = fwi_su_read(paths[k], nt, ntr, big_endian, tmp.data());
+        if (rc != FWI_OK) return rc;
+        const float c = coding[k];
+        for (size_t i = 0; i < n; ++i) raw_data[i] = raw_data[i] + c * tmp[i];  // :282
     }
     return FWI_OK;
 }

@@ -22,9 +22,11 @@
  *   fwi_time_rules            src/calculate_misfit_gradient.f90:198-203
  *   fwi_time_filter           src/time_filter.f90:1 (time_filter), src/filters.f90:1 (filters_function1D)
  *   fwi_interpolation_akima   src/interpolation_akima.f90:1 (interpolation_akima, INTRPL of akima433.f90:6)
- *   fwi_su_read / fwi_su_info src/get_mcs_data.f90:167 (get_shot_data), src/get_was_data.f90:241 (get_obs_data)
+ *   fwi_su_read / fwi_su_info src/get_mcs_data.f90:167 (get_shot_data)
+ *   fwi_su_supershot          src/get_was_data.f90:241 (get_obs_data)
  *   fwi_su_write              src/auxiliar.f90:433 (write_new_data: the suaddhead/sushw pipeline)
- *   fwi_read_nav              src/get_mcs_data.f90:88 (read_nav_shot_mcs)
+ *   fwi_read_nav              src/get_mcs_data.f90:88 (read_nav_shot_mcs), src/get_was_data.f90:134
+ *                             (read_nav_shot_was), :180 (read_nav_obs)
  */
 #ifndef FWI_GB300_H
 #define FWI_GB300_H
@@ -176,11 +178,20 @@ int fwi_su_read(const char* path, int nt, int ntr, int big_endian, float* out);
  * dt = int(dt*1e6) microseconds in each header, every other word 0 (what
  * `suaddhead ns= | sushw key=dt a=` writes in write_new_data). */
 int fwi_su_write(const char* path, const float* data, int nt, int ntr, float dt, int big_endian);
-/* Navigation list of MCS shots (read_nav_shot_mcs, get_mcs_data.f90:88-117):
- * one record per line -- shot number, shot x (m), water depth (m) -- blanks
- * or commas between values.  Fills up to max_records entries and returns the
- * number of records in the file in *nrecords. */
+/* Navigation lists: MCS shots (read_nav_shot_mcs, get_mcs_data.f90:88-117),
+ * WAS shots (read_nav_shot_was, get_was_data.f90:148-164) and OBS
+ * (read_nav_obs, get_was_data.f90:196-207): one record per line -- an
+ * integer (shot or OBS number) and two reals (x in m, and water depth or OBS
+ * depth in m) -- blanks or commas between values.  Fills up to max_records
+ * entries and returns the number of records in the file in *nrecords. */
 int fwi_read_nav(const char* path, int max_records, int* shot_id, float* xs, float* bat, int* nrecords);
+/* get_obs_data(rank,iSS,NumSou_SS,NumRec_SS,Coding,raw_data)
+ * (get_was_data.f90:241-288): the first ntr traces (nt samples) of each of the
+ * nsrc OBS files paths[k] -- the reference's OBS number SourceNum(iSS,k,NumSS)
+ * = iSS+NumSS*(k-1) (auxiliar.f90:73-88) -- summed into raw_data(nt,ntr)
+ * (column-major, zeroed first) as raw_data = raw_data + Coding(k)*data, FP32. */
+int fwi_su_supershot(const char* const* paths, int nsrc, const float* coding, int nt, int ntr, int big_endian,
+                     float* raw_data);
 
 /* ---- batched misfit + gradient over shots ------------------------------ */
 

@@ -49,7 +49,9 @@ def test_su_write_headers_and_round_trip(tmp_path, big):
     assert len(raw) == 5 * (240 + 4 * 301)
     for j in range(5):
         h = raw[j * (240 + 1204): j * (240 + 1204) + 240]
-        assert struct.unpack_from(e + "i", h, 0)[0] == j + 1
+        assert struct.unpack_from(e + "i", h, 0)[0] == j + 1          # tracl
+        assert struct.unpack_from(e + "i", h, 4)[0] == j + 1          # tracr
+        assert struct.unpack_from(e + "H", h, 28)[0] == 1             # trid: live trace
         assert struct.unpack_from(e + "H", h, 114)[0] == 301
         assert struct.unpack_from(e + "H", h, 116)[0] == int(np.float32(0.0025) * np.float32(1e6))
         body = np.frombuffer(raw, dtype=e + "f4", count=301, offset=j * (240 + 1204) + 240)
@@ -67,3 +69,35 @@ def test_read_nav(tmp_path):
     (tmp_path / "bad.txt").write_text("101 6250.0\n")
     with pytest.raises(F.FwiError):
         F.read_nav(tmp_path / "bad.txt")
+
+
+@pytest.mark.parametrize("big", [False, True])
+def test_supershot_sum_of_coded_obs_files(tmp_path, big):
+    """get_obs_data (get_was_data.f90:241-288): the first traces of each OBS
+    file summed with their coding factors, in FP32 and in file order."""
+    import fwi_gb300 as F
+    rng = np.random.default_rng(5)
+    nt, ntr = 90, 6
+    gathers = [rng.standard_normal((nt, ntr + 2)).astype(np.float32) for _ in range(3)]
+    paths = []
+    for k, g in enumerate(gathers):
+        p = tmp_path / f"OBS{k + 1}.su"
+        _write_su_py(p, g, 4000, big)
+        paths.append(p)
+    coding = np.array([1.0, -1.0, 0.5], np.float32)
+    got = F.su_supershot(paths, coding, nt, ntr, big_endian=big)
+    ref = np.zeros((nt, ntr), np.float32)
+    for c, g in zip(coding, gathers):
+        ref = (ref + c * g[:, :ntr]).astype(np.float32)
+    assert np.array_equal(got, ref)
+    with pytest.raises(F.FwiError):
+        F.su_supershot(paths, coding, nt, ntr + 3, big_endian=big)
+
+
+def test_read_nav_obs_and_was_shot_lists(tmp_path):
+    """read_nav_obs / read_nav_shot_was lists: OBS number, x, depth."""
+    import fwi_gb300 as F
+    p = tmp_path / "nav_obs.txt"
+    p.write_text("1 2500.0 -2801.5\n2,7500.0,2790.25\n")
+    ids, xs, zs = F.read_nav(p)
+    assert ids.tolist() == [1, 2] and xs.tolist() == [2500.0, 7500.0] and zs.tolist() == [-2801.5, 2790.25]

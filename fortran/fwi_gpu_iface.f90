@@ -147,6 +147,120 @@ module fwi_gpu_iface
        real(c_double)     :: stack(*)
      end function fwi_survey_get_stack
 
+     !! the plan fwi_misfit_gradient_batch keeps: how many were built, free it
+     integer(c_int64_t) function fwi_batch_plans() bind(C, name="fwi_batch_plans")
+       import :: c_int64_t
+     end function fwi_batch_plans
+
+     integer(c_int) function fwi_batch_release() bind(C, name="fwi_batch_release")
+       import :: c_int
+     end function fwi_batch_release
+
+     !! FWI.f90:175: nut = 1/100/maxval(abs(Search/log(var_orig)))
+     integer(c_int) function fwi_first_step(Search, var_orig, nx, ny, nut) bind(C, name="fwi_first_step")
+       import :: c_int, c_float
+       real(c_float)  :: Search(*), var_orig(*), nut
+       integer(c_int) :: nx, ny
+     end function fwi_first_step
+
+     !! FWI.f90:227, :315: lambda = exp(Search*step)*var_orig
+     integer(c_int) function fwi_model_update(Search, var_orig, step, nx, ny, lambda) &
+          bind(C, name="fwi_model_update")
+       import :: c_int, c_float
+       real(c_float)  :: Search(*), var_orig(*), step, lambda(*)
+       integer(c_int) :: nx, ny
+     end function fwi_model_update
+
+     !! get_mcs_data.f90:113-114,147-155,503-512 (scalars by value)
+     integer(c_int) function fwi_mcs_geometry(xs, shot_depth, streamer_depth, near_offset, drec, dmodel, &
+          num_rec, nxSou, nySou, nxRec, nyRec) bind(C, name="fwi_mcs_geometry")
+       import :: c_int, c_float
+       real(c_float), value  :: xs, shot_depth, streamer_depth, near_offset, drec, dmodel
+       integer(c_int), value :: num_rec
+       integer(c_int)        :: nxSou, nySou, nxRec(*), nyRec(*)
+     end function fwi_mcs_geometry
+
+     !! get_was_data.f90:112-115,155-159,201-205,223-231,584-613
+     integer(c_int) function fwi_was_geometry(num_obs, xobs, zobs, num_shots, xshot, bat, shot_depth, dmodel, &
+          nxmodel, relocate, nxSou, nySou, nxRec, nyRec, bat_model, bat_model_grid) bind(C, name="fwi_was_geometry")
+       import :: c_int, c_float
+       integer(c_int), value :: num_obs, num_shots, nxmodel, relocate
+       real(c_float), value  :: shot_depth, dmodel
+       real(c_float)         :: xobs(*), zobs(*), xshot(*), bat(*), bat_model(*)
+       integer(c_int)        :: nxSou(*), nySou(*), nxRec(*), nyRec, bat_model_grid(*)
+     end function fwi_was_geometry
+
+     !! Ricker_mcs (get_mcs_data.f90:331)
+     integer(c_int) function fwi_ricker(freq, dt, nt, out) bind(C, name="fwi_ricker")
+       import :: c_int, c_float
+       real(c_float), value  :: freq, dt
+       integer(c_int), value :: nt
+       real(c_float)         :: out(*)
+     end function fwi_ricker
+
+     !! calculate_misfit_gradient.f90:198-203
+     integer(c_int) function fwi_time_rules(lambda, ny, nx, dmodel, tfin, store_snap, dt, nt, nt_Store) &
+          bind(C, name="fwi_time_rules")
+       import :: c_int, c_float
+       real(c_float)         :: lambda(*), dt
+       integer(c_int), value :: ny, nx, store_snap
+       real(c_float), value  :: dmodel, tfin
+       integer(c_int)        :: nt, nt_Store
+     end function fwi_time_rules
+
+     !! Butterworth order of fwi_time_filter (the reference's n = 6)
+     integer(c_int) function fwi_set_filter_order(order) bind(C, name="fwi_set_filter_order")
+       import :: c_int
+       integer(c_int), value :: order
+     end function fwi_set_filter_order
+
+     !! SU files (paths: null-terminated character strings)
+     integer(c_int) function fwi_su_info(path, big_endian, ns, dt, ntraces) bind(C, name="fwi_su_info")
+       import :: c_int, c_float, c_char
+       character(kind=c_char) :: path(*)
+       integer(c_int), value  :: big_endian
+       integer(c_int)         :: ns, ntraces
+       real(c_float)          :: dt
+     end function fwi_su_info
+
+     integer(c_int) function fwi_su_read(path, nt, ntr, big_endian, out) bind(C, name="fwi_su_read")
+       import :: c_int, c_float, c_char
+       character(kind=c_char) :: path(*)
+       integer(c_int), value  :: nt, ntr, big_endian
+       real(c_float)          :: out(*)
+     end function fwi_su_read
+
+     !! get_obs_data (get_was_data.f90:241-288): paths(k) = c_loc of each OBS file name
+     integer(c_int) function fwi_su_supershot(paths, nsrc, coding, nt, ntr, big_endian, raw_data) &
+          bind(C, name="fwi_su_supershot")
+       import :: c_int, c_float, c_ptr
+       type(c_ptr)           :: paths(*)
+       integer(c_int), value :: nsrc, nt, ntr, big_endian
+       real(c_float)         :: coding(*), raw_data(*)
+     end function fwi_su_supershot
+
+     !! write_new_data (auxiliar.f90:433)
+     integer(c_int) function fwi_su_write(path, data, nt, ntr, dt, big_endian) bind(C, name="fwi_su_write")
+       import :: c_int, c_float, c_char
+       character(kind=c_char) :: path(*)
+       real(c_float)          :: data(*)
+       integer(c_int), value  :: nt, ntr, big_endian
+       real(c_float), value   :: dt
+     end function fwi_su_write
+
+     !! navigation lists (read_nav_shot_mcs, read_nav_shot_was, read_nav_obs)
+     integer(c_int) function fwi_read_nav(path, max_records, shot_id, xs, bat, nrecords) bind(C, name="fwi_read_nav")
+       import :: c_int, c_float, c_char
+       character(kind=c_char) :: path(*)
+       integer(c_int), value  :: max_records
+       integer(c_int)         :: shot_id(*), nrecords
+       real(c_float)          :: xs(*), bat(*)
+     end function fwi_read_nav
+
+     integer(c_int) function fwi_finalize() bind(C, name="fwi_finalize")
+       import :: c_int
+     end function fwi_finalize
+
      type(c_ptr) function fwi_last_error() bind(C, name="fwi_last_error")
        import :: c_ptr
      end function fwi_last_error

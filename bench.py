@@ -68,6 +68,8 @@ def parse():
     ap.add_argument("--tile-kernel", type=int, default=0, choices=[0, 1, 2],
                     help="two-step tile kernel: 1 register queues, 2 shared-memory queue (0 = tuner)")
     ap.add_argument("--tile-rows", type=int, default=0, help="rows per two-step tile (0 = tuner)")
+    ap.add_argument("--tile-edge-rows", type=int, default=0,
+                    help="rows per edge tile (0 = tuner; above the model's rows: the core tiles' bands)")
     a = ap.parse_args()
     if a.workload == "mcs-f16":
         a.snap = a.snap or "f16"
@@ -418,7 +420,8 @@ def main():
 
     if a.profile:
         sv = F.Survey(spec, snap_form=snap_form, wave_shots=a.wave, band_rows=a.band, hbm_budget=budget,
-                      recompute=a.recompute, tile_kernel=a.tile_kernel, tile_rows=a.tile_rows)
+                      recompute=a.recompute, tile_kernel=a.tile_kernel, tile_rows=a.tile_rows,
+                      tile_edge_rows=a.tile_edge_rows)
         sv.set_lambda(lam0)
         torch.cuda.synchronize()
         p0, p1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -430,12 +433,13 @@ def main():
         tb = sv.two_step_bytes()[0]
         print(json.dumps({"profile_steps": a.profile, "ms_per_step": ms, "step_bytes": sv.step_bytes(),
                           "two_step_bytes": tb, "GBps": tb / ms / 1e6, "frac": tb / ms / 1e6 / peaks()[0],
-                          "tuning": sv.tuning(), "tiles": [sv.tiles()[0], sv.tiles()[1]],
+                          "tuning": sv.tuning(), "tiles": [sv.tiles()[0], sv.tiles()[1], sv.edge_tiles()[0]],
                           "tuner_ms_per_pass": {f"{k}/{r}": v for (k, r), v in sv.tiles()[2].items()}}))
         return 0
     # observed data from the true model (untimed setup)
     sv = F.Survey(spec, snap_form=snap_form, wave_shots=a.wave, band_rows=a.band, hbm_budget=budget,
-                  recompute=a.recompute, tile_kernel=a.tile_kernel, tile_rows=a.tile_rows)
+                  recompute=a.recompute, tile_kernel=a.tile_kernel, tile_rows=a.tile_rows,
+                      tile_edge_rows=a.tile_edge_rows)
     sv.set_lambda(lam_true)
     sv.run(2)
     for i, sh in enumerate(spec.shots):
@@ -496,6 +500,7 @@ def main():
     bytes_step, tile_bytes_pass = sv.two_step_bytes()
     wave, band = sv.tuning()
     tile_kernel, tile_rows, tile_ms = sv.tiles()
+    edge_rows, edge_ms = sv.edge_tiles()
     rc_plan = sv.recompute_plan()
     achieved = bytes_step / step_s / 1e9
     tr = traffic_from_profile()
@@ -556,7 +561,7 @@ def main():
         h_src[:] = np.concatenate([np.asarray(s.src, np.float32).reshape(-1, order="F") for s in spec.shots])
         dh = _DescHolder(spec, snap_form, F.GRAD_F64, hbm_budget=budget,
                          flags=F.SURVEY_RECOMPUTE if a.recompute else 0, tile_kernel=a.tile_kernel,
-                         tile_rows=a.tile_rows)
+                         tile_rows=a.tile_rows, tile_edge_rows=a.tile_edge_rows)
         so = oo = 0
         for i, s in enumerate(spec.shots):
             ns, nr = s.src.size, len(s.nxRec) * spec.nt
@@ -611,7 +616,9 @@ def main():
                 "observed data synthesised on the true model)",
                 "config": {"workload": workload_name(a), "shots_per_gpu": len(spec.shots), "wave_shots": wave,
                            "band_rows": band, "tile_kernel": tile_kernel, "tile_rows": tile_rows,
+                           "tile_edge_rows": edge_rows,
                            "tuner_ms_per_pass": {f"{k}/{r}": v for (k, r), v in tile_ms.items()},
+                           "tuner_edge_ms_per_pass": {str(k): v for k, v in edge_ms.items()},
                            "recompute_segment_steps": rc_plan[0], "recompute_segments": rc_plan[1],
                            "l2": "inputs larger than L2 (wavefields of all shots of a wave and their snapshots: "
                                  "tens to hundreds of GB)"},

@@ -29,7 +29,7 @@ module fwi_gpu_iface
      type(c_ptr)       :: shots, water_rows
      integer(c_size_t) :: hbm_budget
      integer(c_int)    :: wave_shots, band_rows, flags
-     integer(c_int)    :: tile_kernel, tile_rows
+     integer(c_int)    :: tile_kernel, tile_rows, tile_edge_rows
   end type fwi_survey_desc
 
   interface

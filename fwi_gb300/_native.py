@@ -33,7 +33,7 @@ EXPORTS = [
     "fwi_survey_recompute", "fwi_survey_set_time", "fwi_time_filter", "fwi_set_filter_order",
     "fwi_interpolation_akima", "fwi_su_info", "fwi_su_read", "fwi_su_write", "fwi_read_nav",
     "fwi_survey_time_steps", "fwi_misfit_gradient_batch", "fwi_solver_forward_noalloc", "fwi_survey_tiles",
-    "fwi_batch_plans", "fwi_batch_release", "fwi_first_step", "fwi_model_update", "fwi_was_geometry", "fwi_su_supershot",
+    "fwi_batch_plans", "fwi_batch_release", "fwi_first_step", "fwi_model_update", "fwi_was_geometry", "fwi_su_supershot", "fwi_survey_edge_tiles",
 ]
 
 
@@ -55,7 +55,7 @@ class FwiSurveyDesc(C.Structure):
                 ("snap_form", C.c_int), ("grad_form", C.c_int), ("nshots", C.c_int),
                 ("shots", C.POINTER(FwiShot)), ("water_rows", C.c_void_p), ("hbm_budget", C.c_size_t),
                 ("wave_shots", C.c_int), ("band_rows", C.c_int), ("flags", C.c_int), ("tile_kernel", C.c_int),
-                ("tile_rows", C.c_int)]
+                ("tile_rows", C.c_int), ("tile_edge_rows", C.c_int)]
 
 
 _lib = None
@@ -110,6 +110,7 @@ def load():
     lib.fwi_survey_tuning.argtypes = [P, IP, IP]
     lib.fwi_survey_recompute.argtypes = [P, IP, IP]
     lib.fwi_survey_tiles.argtypes = [P, IP, IP, P, P, IP]
+    lib.fwi_survey_edge_tiles.argtypes = [P, IP, P, P, IP]
     lib.fwi_survey_time_steps.argtypes = [P, I]
     lib.fwi_misfit_gradient_batch.argtypes = [C.POINTER(FwiSurveyDesc), P, I, P, P]
     lib.fwi_solver_forward_noalloc.argtypes = [I, I, P, P, P, P, P, F, F, I, I, P, I, P]

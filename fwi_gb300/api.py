@@ -241,7 +241,7 @@ class _DescHolder:
     """Keeps the numpy arrays behind a FwiSurveyDesc alive."""
 
     def __init__(self, spec: SurveySpec, snap_form=0, grad_form=1, hbm_budget=0, wave_shots=0, band_rows=0,
-                 flags=0, tile_kernel=0, tile_rows=0):
+                 flags=0, tile_kernel=0, tile_rows=0, tile_edge_rows=0):
         self.keep = []
         shots = (N.FwiShot * len(spec.shots))()
         for i, sh in enumerate(spec.shots):
@@ -258,21 +258,25 @@ class _DescHolder:
             self.keep.append(water)
         self.desc = N.FwiSurveyDesc(spec.ny, spec.nx_model, spec.d, spec.dt, spec.nt, spec.store_snap, spec.acc,
                                     spec.dpml, spec.numtasks, snap_form, grad_form, len(spec.shots), shots,
-                                    _p(water), hbm_budget, wave_shots, band_rows, flags, tile_kernel, tile_rows)
+                                    _p(water), hbm_budget, wave_shots, band_rows, flags, tile_kernel, tile_rows,
+                                    tile_edge_rows)
 
 
 class Survey:
     """Device-resident batched survey (fwi_survey_create & co)."""
 
     def __init__(self, spec: SurveySpec, snap_form=N.SNAP_F32, grad_form=N.GRAD_F64, hbm_budget=0, wave_shots=0,
-                 band_rows=0, graph=True, recompute=False, two_step=True, tile_kernel=0, tile_rows=0):
+                 band_rows=0, graph=True, recompute=False, two_step=True, tile_kernel=0, tile_rows=0,
+                 tile_edge_rows=0):
         """tile_kernel: 0 = the tuner's choice, 1 = register-queue, 2 = shared-queue
-        two-step kernel; tile_rows: rows per two-step tile (0 = the tuner's)."""
+        two-step kernel; tile_rows: rows per two-step tile, tile_edge_rows: per
+        edge tile (0 = the tuner's; tile_edge_rows above the model's rows: the
+        core tiles' bands)."""
         self.spec = spec
         flags = ((0 if graph else N.SURVEY_NO_GRAPH) | (N.SURVEY_RECOMPUTE if recompute else 0)
                  | (0 if two_step else N.SURVEY_SINGLE_STEP))
         self._h = _DescHolder(spec, snap_form, grad_form, hbm_budget, wave_shots, band_rows, flags, tile_kernel,
-                              tile_rows)
+                              tile_rows, tile_edge_rows)
         handle = C.c_void_p()
         N.check(N.load().fwi_survey_create(C.byref(self._h.desc), C.byref(handle)))
         self.handle = handle
@@ -382,6 +386,15 @@ class Survey:
                 if times[kk * n.value + c] >= 0:
                     meas[(kk + 1, cand[c])] = float(times[kk * n.value + c])
         return k.value, r.value, meas
+
+    def edge_tiles(self):
+        """(rows per edge tile, 0 = the core tiles' bands; {rows: ms per forward
+        two-step pass of the first wave} as measured by the tuner)."""
+        e, n = C.c_int(0), C.c_int(0)
+        cand = (C.c_int * 8)()
+        times = (C.c_float * 8)()
+        N.check(N.load().fwi_survey_edge_tiles(self.handle, C.byref(e), cand, times, C.byref(n)))
+        return e.value, {cand[c]: float(times[c]) for c in range(n.value) if times[c] >= 0}
 
     def recompute_plan(self):
         """(forward steps per segment, segments); (0, 0) without recomputation."""

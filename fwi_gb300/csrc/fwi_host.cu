@@ -105,7 +105,7 @@ struct LibState {
     int acc = 3, dpml = 20;
     // two-step kernel and tile height of the drop-in solver: the choice of
     // the last survey tuned in this process (the tuner's default before)
-    int tile_var = 1, tile_band = TWO_STEP_BAND;
+    int tile_var = 1, tile_band = TWO_STEP_BAND, tile_eband = 0;
     long long launches = 0;
     std::recursive_mutex mu;
 };
@@ -830,7 +830,7 @@ int fwi_solver_acoustic_ss(const int* rank, const int* iprop_, const int* NumSou
     // work lists (the adjoint injects at the receivers)
     std::vector<ShotGeom> geoms{geo};
     std::vector<Layout> lays{l};
-    Lists lists = build_lists(geoms, lays, 64, L().tile_band);
+    Lists lists = build_lists(geoms, lays, 64, L().tile_band, L().tile_eband);
     const bool adj = (iprop == 2);
     TRY(upload(sg.d_items_m, adj ? lists.int_adj : lists.int_fwd, st));
     TRY(upload(sg.d_items_b, adj ? lists.bnd_adj : lists.bnd_fwd, st));
@@ -1080,7 +1080,9 @@ struct fwi_survey {
     int ntr = 0;
     int wave = 1, band = 64;
     int tile_var = 1, tile_band = TWO_STEP_BAND;  // two-step kernel and rows per two-step tile
+    int tile_eband = 0;                           // rows per edge tile (0: the core tiles' bands)
     std::vector<float> tune_ms;                   // tuner: [variant][band candidate] ms per pass (-1: not run)
+    std::vector<float> tune_ems;                  // tuner: [edge band candidate] ms per pass
     std::vector<std::vector<int>> waves;  // shot indices per wave
     // resident data
     DBuf d_lambda, d_src, d_obs, d_synth, d_adj, d_mis_tr, d_mis_shot, d_tr_off, d_G, d_grad, d_water, d_fA, d_fB;
@@ -1176,7 +1178,7 @@ int survey_prepare_waves(fwi_survey* s) {
             g.push_back(s->geoms[sh]);
             l.push_back(s->lays[sh]);
         }
-        Lists lists = build_lists(g, l, s->band, (D.flags & FWI_SURVEY_SINGLE_STEP) ? 0 : s->tile_band);
+        Lists lists = build_lists(g, l, s->band, (D.flags & FWI_SURVEY_SINGLE_STEP) ? 0 : s->tile_band, s->tile_eband);
         std::unique_ptr<fwi_survey::WaveDev> wd(new fwi_survey::WaveDev());
         TRY(upload(wd->items_if, lists.int_fwd, st));
         TRY(upload(wd->items_ia, lists.int_adj, st));
@@ -1287,6 +1289,11 @@ int time_wave0_steps(fwi_survey* s, int steps, float* ms, bool single_only = fal
 constexpr int TILE_BANDS[] = {16, 32, 48, 64, 96};  // short tiles: more warps for small grids
 constexpr int NTB = 5;
 constexpr int BANDS[] = {16, 24, 32, 48, 64};
+// edge-tile heights (0: the core tiles' bands): the edge tiles run on the
+// pass's critical path beside the single-step lists, so shorter edge tiles
+// can pay for their extra halo rows
+constexpr int EDGE_BANDS[] = {0, 8, 16, 32};
+constexpr int NEB = 4;
 constexpr int TUNE_PASSES = 24;
 
 std::string tune_cache_path() {
@@ -1319,9 +1326,10 @@ bool tune_lookup(const std::string& key, std::vector<int>& out) {
     bool found = false;
     while (fgets(line, sizeof line, f)) {
         char k[900];
-        int b = 0, v = 0, r = 0;
-        if (sscanf(line, "%899s %d %d %d", k, &b, &v, &r) == 4 && key == k && b > 0 && (v == 0 || v == 1) && r > 0) {
-            out = {b, v, r};
+        int b = 0, v = 0, r = 0, e = 0;
+        if (sscanf(line, "%899s %d %d %d %d", k, &b, &v, &r, &e) == 5 && key == k && b > 0 && (v == 0 || v == 1) &&
+            r > 0 && e >= 0) {
+            out = {b, v, r, e};
             found = true;
         }
     }
@@ -1338,7 +1346,7 @@ void tune_store(const std::string& key, const std::vector<int>& v) {
     for (size_t p = path.find('/', 1); p != std::string::npos; p = path.find('/', p + 1))
         mkdir(path.substr(0, p).c_str(), 0755);
     if (FILE* f = fopen(path.c_str(), "a")) {
-        fprintf(f, "%s %d %d %d\n", key.c_str(), v[0], v[1], v[2]);
+        fprintf(f, "%s %d %d %d %d\n", key.c_str(), v[0], v[1], v[2], v[3]);
         fclose(f);
     }
 }
@@ -1352,10 +1360,12 @@ int tune_plan(fwi_survey* s) {
     }
     if (D.tile_kernel > 0) s->tile_var = D.tile_kernel - 1;
     if (D.tile_rows > 0) s->tile_band = D.tile_rows;
+    if (D.tile_edge_rows > 0) s->tile_eband = D.tile_edge_rows;
+    s->tune_ems.assign(NEB, -1.f);
     if (D.band_rows > 0) s->band = D.band_rows;
     s->tune_ms.assign(2 * NTB, -1.f);
     const bool do_band = D.band_rows <= 0 && (!two || D.snap_form != FWI_SNAP_F32);
-    const bool do_tiles = two && (D.tile_kernel <= 0 || D.tile_rows <= 0);
+    const bool do_tiles = two && (D.tile_kernel <= 0 || D.tile_rows <= 0 || D.tile_edge_rows <= 0);
     if (do_band || do_tiles) {
         cudaDeviceProp prop;
         CK(cudaGetDeviceProperties(&prop, L().device));
@@ -1365,13 +1375,14 @@ int tune_plan(fwi_survey* s) {
         key += "|" + std::to_string(D.ny) + "|" + std::to_string(D.acc) + "|" + std::to_string(D.dpml) + "|" +
                std::to_string(s->wave) + "|" + std::to_string(two ? 2 : 1) + "|" + std::to_string(D.snap_form) +
                "|" + std::to_string(D.tile_kernel) + "|" + std::to_string(D.tile_rows) + "|" +
-               std::to_string(D.band_rows) + "|w";
+               std::to_string(D.band_rows) + "|" + std::to_string(D.tile_edge_rows) + "|w";
         for (int sh : s->waves[0]) key += "," + std::to_string(s->geoms[sh].nx);
         std::vector<int> hit;
         if (tune_lookup(key, hit)) {
             if (do_band) s->band = hit[0];
             if (two && D.tile_kernel <= 0) s->tile_var = hit[1];
             if (two && D.tile_rows <= 0) s->tile_band = hit[2];
+            if (two && D.tile_edge_rows <= 0) s->tile_eband = hit[3];
         } else {
             if (do_band) {
                 // single steps: the two-step lists play no part
@@ -1394,7 +1405,23 @@ int tune_plan(fwi_survey* s) {
                 }
                 s->band = best;
             }
-            if (do_tiles) {
+            // one timing of TUNE_PASSES forward passes: the fastest of three runs
+            // after a warm-up (a few passes alone read too fast: the measured
+            // order then differs from the order of long runs)
+            auto time_passes = [&](float* out) -> int {
+                float ms = 0.f, m = 1e30f;
+                TRY(time_wave0_steps(s, 8, &ms));
+                for (int r = 0; r < 3; ++r) {
+                    TRY(time_wave0_steps(s, 2 * TUNE_PASSES, &ms));
+                    m = std::min(m, ms);
+                }
+                *out = m / TUNE_PASSES;
+                return FWI_OK;
+            };
+            if (do_tiles && (D.tile_kernel <= 0 || D.tile_rows <= 0)) {
+                // kernel and tile height, with the edge tiles in the core tiles' bands
+                const int keep_eb = s->tile_eband;
+                if (D.tile_edge_rows <= 0) s->tile_eband = 0;
                 float best_ms = 1e30f;
                 int bv = s->tile_var, bb = s->tile_band;
                 for (int c = 0; c < NTB; ++c) {
@@ -1405,16 +1432,9 @@ int tune_plan(fwi_survey* s) {
                     for (int v = 0; v < 2; ++v) {
                         if (D.tile_kernel > 0 && v != D.tile_kernel - 1) continue;
                         s->tile_var = v;
-                        // the fastest of three runs of TUNE_PASSES passes after a warm-up
-                        // (a few passes alone read too fast: the measured order
-                        // then differs from the order of long runs)
-                        float ms = 0.f, m = 1e30f;
-                        TRY(time_wave0_steps(s, 8, &ms));
-                        for (int r = 0; r < 3; ++r) {
-                            TRY(time_wave0_steps(s, 2 * TUNE_PASSES, &ms));
-                            m = std::min(m, ms);
-                        }
-                        s->tune_ms[v * NTB + c] = m / TUNE_PASSES;
+                        float m = 0.f;
+                        TRY(time_passes(&m));
+                        s->tune_ms[v * NTB + c] = m;
                         if (m < best_ms) {
                             best_ms = m;
                             bv = v;
@@ -1424,12 +1444,32 @@ int tune_plan(fwi_survey* s) {
                 }
                 s->tile_var = bv;
                 s->tile_band = bb;
+                s->tile_eband = keep_eb;
             }
-            tune_store(key, {s->band, s->tile_var, s->tile_band});
+            if (do_tiles && D.tile_edge_rows <= 0) {
+                // then the edge tiles' height for that kernel and tile height
+                float best_ms = 1e30f;
+                int be = 0;
+                for (int c = 0; c < NEB; ++c) {
+                    if (EDGE_BANDS[c] >= s->tile_band) continue;
+                    s->tile_eband = EDGE_BANDS[c];
+                    TRY(survey_prepare_waves(s));
+                    float m = 0.f;
+                    TRY(time_passes(&m));
+                    s->tune_ems[c] = m;
+                    if (m < best_ms) {
+                        best_ms = m;
+                        be = EDGE_BANDS[c];
+                    }
+                }
+                s->tile_eband = be;
+            }
+            tune_store(key, {s->band, s->tile_var, s->tile_band, s->tile_eband});
         }
         if (two) {
             L().tile_var = s->tile_var;
             L().tile_band = s->tile_band;
+            L().tile_eband = s->tile_eband;
         }
     }
     return survey_prepare_waves(s);
@@ -2063,6 +2103,17 @@ int fwi_survey_tiles(fwi_survey* s, int* tile_kernel, int* tile_rows, int* cand,
             for (int v = 0; v < 2; ++v) times[v * NTB + c] = s->tune_ms.empty() ? -1.f : s->tune_ms[v * NTB + c];
     }
     if (cand && s->desc.tile_rows > 0) cand[0] = s->desc.tile_rows;
+    return FWI_OK;
+}
+
+int fwi_survey_edge_tiles(fwi_survey* s, int* edge_rows, int* cand, float* times, int* ncand) {
+    if (!s || s->wdev.empty()) return fail(FWI_ERR_STATE, "survey not prepared");
+    if (edge_rows) *edge_rows = s->wdev[0]->n_ff > 0 ? s->tile_eband : 0;
+    if (ncand) *ncand = NEB;
+    for (int c = 0; c < NEB; ++c) {
+        if (cand) cand[c] = EDGE_BANDS[c];
+        if (times) times[c] = s->tune_ems.empty() ? -1.f : s->tune_ems[c];
+    }
     return FWI_OK;
 }
 

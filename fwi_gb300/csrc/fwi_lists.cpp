@@ -134,8 +134,9 @@ bool two_step_ok(const Layout& l) {
 // Work lists for a set of shots (local shot index = position in `geoms`).
 // All shots share dn (one acc / dpml per launch), hence one kstrip.
 // fband > 0 also builds the two-step lists (two-step tiles in bands of fband
-// rows).
-Lists build_lists(const std::vector<ShotGeom>& geoms, const std::vector<Layout>& lays, int band_rows, int fband) {
+// rows); eband > 0 gives the edge tiles their own height (see below).
+Lists build_lists(const std::vector<ShotGeom>& geoms, const std::vector<Layout>& lays, int band_rows, int fband,
+                  int eband) {
     Lists out;
     std::vector<WorkItem> sbot_f, sbot_a, strip_f, strip_a, bot_f, bot_a;
     // interior items grouped [shot][band] (a band = the tiles of one row band)
@@ -191,23 +192,58 @@ Lists build_lists(const std::vector<ShotGeom>& geoms, const std::vector<Layout>&
                     fus_a.emplace_back();
                     edge_f.emplace_back();
                     edge_a.emplace_back();
-                    bands(nr, fband, [&](int y0, int y1) {
-                        std::vector<WorkItem> vf, va, ef, ea;
-                        for (int x0 = xa & ~3; x0 < xb; x0 += 120) {
-                            // core: the wavefield cells it reads, rows [y0-2R-1, y1+2R] and columns
-                            // [x0-8, x0+128), are two-step cells or the top pad
-                            const bool core = x0 - 8 >= xa && x0 + 128 <= xb && l.dn + y1 + 2 * R < l.dn + nr;
-                            append_two_step(out, core ? vf : ef, out.src_fwd, cells_f, recs, (int)s, x0, l.dn + y0,
-                                            l.dn + y1, R, true, xa, xb);
-                            out.fus_cells += (double)(y1 - y0) * (std::min(x0 + 120, xb) - std::max(x0, xa));
-                            append_two_step(out, core ? va : ea, out.src_adj, cells_a, recs, (int)s, x0, l.dn + y0,
-                                            l.dn + y1, R, false, xa, xb);
-                        }
-                        fus_f.back().push_back(vf);
-                        fus_a.back().push_back(va);
+                    // core: the wavefield cells a tile reads, rows [y0-2R-1, y1+2R] and columns
+                    // [x0-8, x0+128), are two-step cells or the top pad; the other tiles are edge
+                    // tiles (next to the side strips or the rows next to the bottom pad), which run
+                    // beside the single-step lists on the pass's critical path
+                    auto is_core = [&](int x0, int y1) {
+                        return x0 - 8 >= xa && x0 + 128 <= xb && l.dn + y1 + 2 * R < l.dn + nr;
+                    };
+                    auto tile = [&](std::vector<WorkItem>& vf, std::vector<WorkItem>& va, int x0, int y0, int y1) {
+                        append_two_step(out, vf, out.src_fwd, cells_f, recs, (int)s, x0, l.dn + y0, l.dn + y1, R,
+                                        true, xa, xb);
+                        out.fus_cells += (double)(y1 - y0) * (std::min(x0 + 120, xb) - std::max(x0, xa));
+                        append_two_step(out, va, out.src_adj, cells_a, recs, (int)s, x0, l.dn + y0, l.dn + y1, R,
+                                        false, xa, xb);
+                    };
+                    const int eb = std::min(nr, std::max(eband, 2 * R + 1));
+                    if (eband <= 0 || nr - eb < 1) {
+                        // one band height for all tiles
+                        bands(nr, fband, [&](int y0, int y1) {
+                            std::vector<WorkItem> vf, va, ef, ea;
+                            for (int x0 = xa & ~3; x0 < xb; x0 += 120) {
+                                const bool core = is_core(x0, y1);
+                                tile(core ? vf : ef, core ? va : ea, x0, y0, y1);
+                            }
+                            fus_f.back().push_back(vf);
+                            fus_a.back().push_back(va);
+                            edge_f.back().push_back(ef);
+                            edge_a.back().push_back(ea);
+                        });
+                    } else {
+                        // edge tiles in eband rows: the rows [0, nr-eb) in bands of fband rows for the
+                        // tiles clear of the side strips (all core) and of eband rows for the side
+                        // tile columns, then the last eb rows as one band of edge tiles
+                        const int nc = nr - eb;
+                        bands(nc, fband, [&](int y0, int y1) {
+                            std::vector<WorkItem> vf, va;
+                            for (int x0 = xa & ~3; x0 < xb; x0 += 120)
+                                if (is_core(x0, y1)) tile(vf, va, x0, y0, y1);
+                            fus_f.back().push_back(vf);
+                            fus_a.back().push_back(va);
+                        });
+                        bands(nc, eband, [&](int y0, int y1) {
+                            std::vector<WorkItem> ef, ea;
+                            for (int x0 = xa & ~3; x0 < xb; x0 += 120)
+                                if (!is_core(x0, nc)) tile(ef, ea, x0, y0, y1);
+                            edge_f.back().push_back(ef);
+                            edge_a.back().push_back(ea);
+                        });
+                        std::vector<WorkItem> ef, ea;
+                        for (int x0 = xa & ~3; x0 < xb; x0 += 120) tile(ef, ea, x0, nc, nr);
                         edge_f.back().push_back(ef);
                         edge_a.back().push_back(ea);
-                    });
+                    }
                     for (int t = xa / TILE; t <= (xb - 1) / TILE; ++t) {
                         const int c0 = std::max(t * TILE, xa), c1 = std::min((t + 1) * TILE, xb);
                         append_item(out, out.lft_fwd, out.src_fwd, cells_f, recs, (int)s, t, l.dn + nr, l.dn + l.ny,

@@ -56,8 +56,11 @@ std::vector<SrcEnt> injection_cells(const std::vector<int>& xs, const std::vecto
 bool two_step_ok(const Layout& l);
 
 // Work lists for a set of shots (local shot index = position in `geoms`);
-// fband > 0 also builds the two-step lists (two-step tiles in bands of fband rows).
-Lists build_lists(const std::vector<ShotGeom>& geoms, const std::vector<Layout>& lays, int band_rows, int fband = 0);
+// fband > 0 also builds the two-step lists (two-step tiles in bands of fband
+// rows); eband > 0 puts the edge tiles -- the tile columns next to the side
+// strips and the last max(eband, 2R+1) rows -- in bands of eband rows.
+Lists build_lists(const std::vector<ShotGeom>& geoms, const std::vector<Layout>& lays, int band_rows, int fband = 0,
+                  int eband = 0);
 
 // One unit of a time loop: a two-step pass (steps k, k+1) or a single step
 // k; sn = the snapshot block step k stores or images with, -1 for none.

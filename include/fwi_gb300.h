@@ -231,6 +231,10 @@ typedef struct fwi_survey_desc {
     int tile_kernel;      /* two-step tile kernel: 0 = chosen by the tuner,
                              1 = register queues, 2 = shared-memory queue        */
     int tile_rows;        /* rows per two-step tile (0 = chosen by the tuner)    */
+    int tile_edge_rows;   /* rows per edge tile -- the tiles next to the side
+                             strips and the last rows -- (0 = chosen by the
+                             tuner; more than the model's rows: in the core
+                             tiles' bands)                                    */
 } fwi_survey_desc;
 
 /* fwi_survey_desc.flags: launch every time step directly instead of
@@ -304,6 +308,10 @@ int fwi_survey_tuning(fwi_survey* s, int* wave_shots, int* band_rows);
  * height cand[c] (-1 where not measured; cached or forced choices measure
  * nothing); *ncand receives the number of tile heights tried (at most 8). */
 int fwi_survey_tiles(fwi_survey* s, int* tile_kernel, int* tile_rows, int* cand, float* times, int* ncand);
+/* Rows per edge tile chosen for the survey (0: the core tiles' bands) and the
+ * tuner's measurements: times[c] = ms per forward two-step pass of the first
+ * wave with edge tiles of cand[c] rows (-1 where not measured; at most 8). */
+int fwi_survey_edge_tiles(fwi_survey* s, int* edge_rows, int* cand, float* times, int* ncand);
 /* Checkpointed recomputation plan: forward steps per segment and number of
  * segments (0, 0 when all snapshots are stored). */
 int fwi_survey_recompute(fwi_survey* s, int* segment_steps, int* segments);

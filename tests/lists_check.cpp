@@ -54,7 +54,7 @@ void item_cols(const WorkItem& it, const Layout& l, int& c0, int& c1) {
     }
 }
 
-void check(int ny, int nx, int acc, int dpml, int nsrc, int band, int fband) {
+void check(int ny, int nx, int acc, int dpml, int nsrc, int band, int fband, int eband = 0) {
     const Layout l = make_layout(ny, nx, acc, dpml);
     ShotGeom g;
     g.nx = nx;
@@ -66,7 +66,7 @@ void check(int ny, int nx, int acc, int dpml, int nsrc, int band, int fband) {
         g.nxR.push_back(1 + rnd(nx));
         g.nyR.push_back(1 + rnd(ny));
     }
-    const Lists L = build_lists({g}, {l}, band, fband);
+    const Lists L = build_lists({g}, {l}, band, fband, eband);
     const int R = l.acc, xa = l.off + l.sl, xb = l.off + l.sr;
     const size_t n = (size_t)l.nyt * l.pitch;
     auto at = [&](int y, int c) { return (size_t)y * l.pitch + c; };
@@ -184,12 +184,12 @@ struct Kern {
     std::vector<int> deps;                  // direct predecessors
 };
 
-void check_pipeline(int ny, int nx, int acc, int dpml, int fband) {
+void check_pipeline(int ny, int nx, int acc, int dpml, int fband, int eband = 0) {
     const Layout l = make_layout(ny, nx, acc, dpml);
     if (!two_step_ok(l)) return;
     ShotGeom g;
     g.nx = nx;
-    const Lists L = build_lists({g}, {l}, 16, fband);
+    const Lists L = build_lists({g}, {l}, 16, fband, eband);
     const int R = l.acc;
     const size_t n = (size_t)l.nyt * l.pitch;
     auto cur = [](int k, int pair) { return 2 * pair + ((k & 1) ? 0 : 1); };
@@ -285,7 +285,10 @@ void check_pipeline(int ny, int nx, int acc, int dpml, int fband) {
 int main() {
     for (int acc : {3, 4})
         for (int dpml : {8, 20})
-            for (int nx : {90, 250, 400}) check_pipeline(40 + nx % 37, nx, acc, dpml, 16 + nx % 20);
+            for (int nx : {90, 250, 400}) {
+                check_pipeline(40 + nx % 37, nx, acc, dpml, 16 + nx % 20);
+                check_pipeline(40 + nx % 37, nx, acc, dpml, 16 + nx % 20, 8 + nx % 9);
+            }
     if (fails) return 1;
     for (int trial = 0; trial < 3000 && !fails; ++trial) {
         const int k0 = 2 + rnd(5), k1 = k0 - 1 + rnd(60);
@@ -300,6 +303,10 @@ int main() {
     check(400, 2000, 3, 20, 5, 16, 96);
     check(400, 2000, 4, 20, 5, 16, 64);
     check(600, 3000, 3, 20, 5, 16, 96);
+    for (int eb : {1, 7, 8, 16, 32, 500}) {
+        check(400, 2000, 3, 20, 5, 16, 64, eb);
+        check(400, 2000, 4, 20, 5, 16, 48, eb);
+    }
     check(37, 61, 3, 20, 3, 32, 48);
     check(12, 90, 4, 8, 3, 16, 64);
     int cases = 4;
@@ -308,6 +315,7 @@ int main() {
             for (int acc : {3, 4}) {
                 if (dpml + 2 * acc > MAXDN - 2) continue;
                 check(6 + nx % 53, nx, acc, dpml, 4, 8 + nx % 40, 16 + nx % 50);
+                check(6 + nx % 53, nx, acc, dpml, 4, 8 + nx % 40, 16 + nx % 50, 4 + nx % 23);
                 ++cases;
                 if (fails) break;
             }

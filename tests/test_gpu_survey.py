@@ -68,7 +68,8 @@ def test_survey_gradient_vs_oracle(kw):
 def test_two_step_passes_bit_identical(kw, rc, form):
     """Pairs of steps advanced by either two-step interior kernel (register
     queues, or the p_{n+1} rows in shared memory), in one band or in bands of
-    13 rows, with the single-step lists beside them, give the same bits as
+    13 rows, with the edge tiles in the same bands or in bands of their own,
+    with the single-step lists beside them, give the same bits as
     single steps: traces, misfit and gradient, forward and adjoint, with
     snapshot stores and imaging inside passes (FP32 snapshots; 16-bit ones are
     stored by single steps), and with checkpointed recomputation."""
@@ -77,10 +78,12 @@ def test_two_step_passes_bit_identical(kw, rc, form):
     spec, vp = make(9, **kw)
     lam = lam_from_vp(vp)
     res = []
-    for two, kern, rows in ((False, 0, 0), (True, 1, 64), (True, 2, 64), (True, 2, 13)):
-        sv = F.Survey(spec, snap_form=form, two_step=two, recompute=rc, tile_kernel=kern, tile_rows=rows)
+    for two, kern, rows, edge in ((False, 0, 0, 0), (True, 1, 64, 10 ** 6), (True, 2, 64, 10 ** 6), (True, 2, 13, 10 ** 6),
+                                  (True, 2, 64, 8), (True, 1, 16, 7)):
+        sv = F.Survey(spec, snap_form=form, two_step=two, recompute=rc, tile_kernel=kern, tile_rows=rows,
+                      tile_edge_rows=edge)
         if two:
-            assert sv.tiles()[:2] == (kern, rows)
+            assert sv.tiles()[:2] == (kern, rows) and sv.edge_tiles()[0] == edge
         sv.set_lambda(lam)
         g = np.zeros((spec.ny, spec.nx_model), np.float32, order="F")
         m, _ = sv.run(1, g)
@@ -107,6 +110,10 @@ def test_tuner_picks_a_measured_tile(monkeypatch):
     assert kern in (1, 2) and rows in (16, 32, 48, 64, 96)
     if meas:  # empty when the choice came from the tuning cache
         assert (kern, rows) in meas and meas[(kern, rows)] == min(meas.values())
+    edge, emeas = sv.edge_tiles()
+    assert edge in (0, 8, 16, 32)
+    if emeas:
+        assert edge in emeas and emeas[edge] == min(emeas.values())
     sv.set_lambda(lam_from_vp(vp))
     g = np.zeros((spec.ny, spec.nx_model), np.float32, order="F")
     sv.run(1, g)

@@ -579,12 +579,63 @@ void oracle_time_rules(const float* lambda, size_t n, float dmodel, float tfin, 
 }  // extern "C"
 
 namespace {
+/* Round to the nearest bfloat16 (ties to even), returned as a float; finite inputs. */
+float to_bf16(float x) {
+    uint32_t u;
+    std::memcpy(&u, &x, 4);
+    u += 0x7FFFu + ((u >> 16) & 1u);
+    u &= 0xFFFF0000u;
+    float y;
+    std::memcpy(&y, &u, 4);
+    return y;
+}
+float to_f16(float x) { return (float)(_Float16)x; }
+
+/* Stored-snapshot forms, applied to Fields(ny, nx*(nt_Store+1)) between the
+ * forward and the adjoint run (the imaging reads the stored values back):
+ *   0 FP32 (the reference);
+ *   1 / 2 FP16 / BF16 with one max-abs scale per snapshot: q = r(F * (2^14/m)),
+ *     read back as q * (m/2^14), m = max|F| over the snapshot;
+ *   3 / 4 FP16 / BF16 with a power-of-two scale per 128-column segment of a
+ *     row: q = r(F * 2^(14-e)), read back exactly, 2^(e-1) <= the segment's
+ *     max|F| < 2^e. */
+void quantize_snapshots(float* F, int ny, int nx, int nsnap, int form) {
+    if (form == 0) return;
+    float (*rnd)(float) = (form == 1 || form == 3) ? to_f16 : to_bf16;
+    for (int k = 0; k < nsnap; ++k) {
+        float* A = F + (size_t)k * nx * ny;  // A[j + i*ny]
+        if (form <= 2) {
+            float m = 0.f;
+            for (size_t c = 0; c < (size_t)nx * ny; ++c) m = std::max(m, std::fabs(A[c]));
+            if (m == 0.f) continue;
+            const float up = 16384.f / m, down = m / 16384.f;
+            for (size_t c = 0; c < (size_t)nx * ny; ++c) A[c] = rnd(A[c] * up) * down;
+        } else {
+            for (int j = 0; j < ny; ++j)
+                for (int i0 = 0; i0 < nx; i0 += 128) {
+                    const int i1 = std::min(nx, i0 + 128);
+                    float m = 0.f;
+                    for (int i = i0; i < i1; ++i) m = std::max(m, std::fabs(A[j + (size_t)i * ny]));
+                    int ex = 0;
+                    if (m > 0.f) std::frexp(m, &ex);
+                    const int sh = 14 - ex;
+                    for (int i = i0; i < i1; ++i) {
+                        float& v = A[j + (size_t)i * ny];
+                        v = std::ldexp(rnd(std::ldexp(v, sh)), -sh);
+                    }
+                }
+        }
+    }
+}
+void quantize_snapshots(double*, int, int, int, int) {}
+
 /* One shot of calculate_misfit_gradient (:236-323) with numtasks = 1 in R:
  * forward, misfit, adjoint.  kernel_out gets the shot's Grad_thread. */
 template <typename R>
 void shot_gradient(int ny, int nx, R d, R dt, int nt, int store_snap, int acc, int dPML, const R* vp,
                           int NumSou, const int* nxS, const int* nyS, const R* S, int NumRec, const int* nxR,
-                          const int* nyR, const R* obs, int step, R* synth, R* kernel_out, R* mis_r, double* mis64) {
+                          const int* nyR, const R* obs, int step, R* synth, R* kernel_out, R* mis_r, double* mis64,
+                          int snap_form = 0) {
     const int nt_Store = nt / store_snap;
     std::vector<R> Fields((size_t)ny * nx * (nt_Store + 1), R(0));
     std::vector<R> adj((size_t)nt * NumRec, R(0)), dummy(1, R(0));
@@ -593,6 +644,7 @@ void shot_gradient(int ny, int nx, R d, R dt, int nt, int store_snap, int acc, i
     solver_acoustic_ss<R>(f);
     misfit_function<R>(NumRec, nt, dt, synth, obs, mis_r, mis64, adj.data());
     if (step != 1) return;
+    quantize_snapshots(Fields.data(), ny, nx, nt_Store + 1, snap_form);
     std::fill(kernel_out, kernel_out + (size_t)ny * nx, R(0));
     std::vector<R> rec2((size_t)nt * NumRec, R(0));
     SolverArgs<R> b{2, NumSou, NumRec, nxS, nyS, nxR, nyR, S, adj.data(), d, dt, ny, nx, vp,
@@ -612,7 +664,7 @@ int gradient_batch(int nshots, int ny, R d, R dt, int nt, int store_snap, int ac
                           int nx_model, const int* x0, const int* nxw, const int* nsou, const int* sou_off,
                           const int* nxS, const int* nyS, const R* S, const int* nrec, const int* rec_off,
                           const int* nxR, const int* nyR, const R* obs, int step, const size_t* kern_off, R* kernels,
-                          R* synth_all, R* mis_r, double* mis64, int nthreads) {
+                          R* synth_all, R* mis_r, double* mis64, int nthreads, int snap_form = 0) {
     std::atomic<int> next{0};
     auto worker = [&]() {
         for (;;) {
@@ -627,7 +679,8 @@ int gradient_batch(int nshots, int ny, R d, R dt, int nt, int store_snap, int ac
             if (!synth) { synth_local.assign((size_t)nt * nrec[s], R(0)); synth = synth_local.data(); }
             shot_gradient<R>(ny, nx, d, dt, nt, store_snap, acc, dPML, vp.data(), nsou[s], nxS + sou_off[s],
                              nyS + sou_off[s], S + (size_t)sou_off[s] * nt, nrec[s], nxR + rec_off[s], nyR + rec_off[s],
-                             obs + (size_t)rec_off[s] * nt, step, synth, kernels + kern_off[s], mis_r + s, mis64 + s);
+                             obs + (size_t)rec_off[s] * nt, step, synth, kernels + kern_off[s], mis_r + s, mis64 + s,
+                             snap_form);
         }
     };
     if (nthreads <= 1) { worker(); return 0; }
@@ -651,6 +704,18 @@ int oracle_gradient_batch_f32(int nshots, int ny, float d, float dt, int nt, int
     return gradient_batch<float>(nshots, ny, d, dt, nt, store_snap, acc, dPML, vp_model, nx_model, x0, nxw, nsou,
                                  sou_off, nxS, nyS, S, nrec, rec_off, nxR, nyR, obs, step, kern_off, kernels,
                                  synth_all, mis32, mis64, nthreads);
+}
+/* oracle_gradient_batch_f32 with the stored snapshots in the form snap_form
+ * (quantize_snapshots): the precision forms' error against FP64. */
+int oracle_gradient_batch_f32_form(int nshots, int ny, float d, float dt, int nt, int store_snap, int acc, int dPML,
+                                   const float* vp_model, int nx_model, const int* x0, const int* nxw,
+                                   const int* nsou, const int* sou_off, const int* nxS, const int* nyS, const float* S,
+                                   const int* nrec, const int* rec_off, const int* nxR, const int* nyR,
+                                   const float* obs, int step, const size_t* kern_off, float* kernels,
+                                   float* synth_all, float* mis32, double* mis64, int nthreads, int snap_form) {
+    return gradient_batch<float>(nshots, ny, d, dt, nt, store_snap, acc, dPML, vp_model, nx_model, x0, nxw, nsou,
+                                 sou_off, nxS, nyS, S, nrec, rec_off, nxR, nyR, obs, step, kern_off, kernels,
+                                 synth_all, mis32, mis64, nthreads, snap_form);
 }
 int oracle_gradient_batch_f64(int nshots, int ny, double d, double dt, int nt, int store_snap, int acc, int dPML,
                               const double* vp_model, int nx_model, const int* x0, const int* nxw, const int* nsou,

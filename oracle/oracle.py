@@ -51,6 +51,8 @@ def lib():
                                                   _P, _P, _P, _P, I, _P, _P, _P, _P, _P, I]
         _lib.oracle_gradient_batch_f64.argtypes = [I, I, D, D, I, I, I, I, _P, I, _P, _P, _P, _P, _P, _P, _P, _P,
                                                   _P, _P, _P, _P, I, _P, _P, _P, _P, _P, I]
+        _lib.oracle_gradient_batch_f32_form.argtypes = [I, I, F, F, I, I, I, I, _P, I, _P, _P, _P, _P, _P, _P, _P,
+                                                       _P, _P, _P, _P, _P, I, _P, _P, _P, _P, _P, I, I]
     return _lib
 
 
@@ -147,10 +149,18 @@ def pml_coeffs(acc, dpml, dt, d):
     return fA, fB, cA.transpose(0, 2, 1).copy(), cB.transpose(0, 2, 1).copy()
 
 
-def gradient_batch(survey, vp_model, step=1, fp64=False, nthreads=1, want_synth=False):
+# stored-snapshot forms of gradient_batch(snap_form=...) (FP32 solver only)
+SNAP_FORMS = {"f32": 0, "f16_snapshot_scale": 1, "bf16_snapshot_scale": 2, "f16_segment_pow2": 3,
+              "bf16_segment_pow2": 4}
+
+
+def gradient_batch(survey, vp_model, step=1, fp64=False, nthreads=1, want_synth=False, snap_form=0):
     """Per-shot forward + misfit + adjoint for a survey (see
     fwi_gb300.survey.Survey for the fields).  Returns (kernels list,
-    misfit_ref array, misfit64 array, synth list or None)."""
+    misfit_ref array, misfit64 array, synth list or None).  snap_form (FP32
+    only, SNAP_FORMS) stores the snapshots between the forward and the
+    adjoint run in a 16-bit form: FP16 or BF16 with one max-abs scale per
+    snapshot, or with a power-of-two scale per 128-column row segment."""
     dtp = np.float64 if fp64 else np.float32
     sv = survey
     ns = len(sv.shots)
@@ -176,10 +186,15 @@ def gradient_batch(survey, vp_model, step=1, fp64=False, nthreads=1, want_synth=
     mr = np.zeros(ns, dtp)
     m64 = np.zeros(ns, np.float64)
     vp = _f(vp_model, dtp)
+    if snap_form and fp64:
+        raise ValueError("the 16-bit snapshot forms run with the FP32 solver")
     fn = lib().oracle_gradient_batch_f64 if fp64 else lib().oracle_gradient_batch_f32
+    extra = ()
+    if snap_form:
+        fn, extra = lib().oracle_gradient_batch_f32_form, (int(snap_form),)
     fn(ns, sv.ny, sv.d, sv.dt, sv.nt, sv.store_snap, sv.acc, sv.dpml, _ptr(vp), vp.shape[1], _ptr(x0), _ptr(nxw),
        _ptr(nsou), _ptr(sou_off), _ptr(nxS), _ptr(nyS), _ptr(S), _ptr(nrec), _ptr(rec_off), _ptr(nxR), _ptr(nyR),
-       _ptr(obs), step, _ptr(koff), _ptr(kern), _ptr(synth), _ptr(mr), _ptr(m64), nthreads)
+       _ptr(obs), step, _ptr(koff), _ptr(kern), _ptr(synth), _ptr(mr), _ptr(m64), nthreads, *extra)
     kernels = [kern[int(koff[i]):int(koff[i]) + sizes[i]].reshape(sv.ny, sv.shots[i].nx, order="F")
                for i in range(ns)]
     synths = None

@@ -524,6 +524,7 @@ def main():
     tile_kernel, tile_rows, tile_ms = sv.tiles()
     edge_rows, edge_ms = sv.edge_tiles()
     rc_plan = sv.recompute_plan()
+    launch_form, launch_direct_ms, launch_graph_ms = sv.launch_form(1)
     achieved = bytes_step / step_s / 1e9
     tr = traffic_from_profile()
     roof = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
@@ -643,6 +644,8 @@ def main():
                            "tuner_ms_per_pass": {f"{k}/{r}": v for (k, r), v in tile_ms.items()},
                            "tuner_edge_ms_per_pass": {str(k): v for k, v in edge_ms.items()},
                            "recompute_segment_steps": rc_plan[0], "recompute_segments": rc_plan[1],
+                           "launch": {"form": launch_form, "direct_ms": launch_direct_ms,
+                                      "graph_replay_ms": launch_graph_ms},
                            "l2": "inputs larger than L2 (wavefields of all shots of a wave and their snapshots: "
                                  "tens to hundreds of GB)"},
                 "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "plain": plain, "gpu_launches": int(launches),

@@ -396,6 +396,15 @@ class Survey:
         N.check(N.load().fwi_survey_edge_tiles(self.handle, C.byref(e), cand, times, C.byref(n)))
         return e.value, {cand[c]: float(times[c]) for c in range(n.value) if times[c] >= 0}
 
+    def launch_form(self, step=1):
+        """("graph" | "direct" | "undecided", direct-launch ms, graph-replay ms)
+        of the first wave's runs with this step: the first run of a time axis
+        is timed as direct launches, the first replay of its graph as a
+        replay, and the slower form is dropped."""
+        f, d, g = C.c_int(0), C.c_float(0.0), C.c_float(0.0)
+        N.check(N.load().fwi_survey_launch_form(self.handle, int(step), C.byref(f), C.byref(d), C.byref(g)))
+        return {0: "undecided", 1: "graph", 2: "direct"}[f.value], float(d.value), float(g.value)
+
     def recompute_plan(self):
         """(forward steps per segment, segments); (0, 0) without recomputation."""
         c, j = C.c_int(0), C.c_int(0)

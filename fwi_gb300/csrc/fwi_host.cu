@@ -1098,6 +1098,14 @@ struct fwi_survey {
         cudaGraphExec_t graph[3] = {nullptr, nullptr, nullptr};
         long long graph_kernels[3] = {0, 0, 0};  // kernel nodes per graph
         int direct_runs[3] = {0, 0, 0};          // runs launched directly since the graph was dropped
+        // launch form per direction, chosen by measurement: the first run of
+        // a time axis is timed as direct launches, the first replay of its
+        // graph as a replay (CUDA events around the wave); a graph slower
+        // than the direct launches is dropped for good
+        cudaEvent_t tev[2] = {nullptr, nullptr};
+        int timing = 0, timing_gi = 0;            // in flight: 1 direct, 2 graph
+        float t_direct[3] = {0.f, 0.f, 0.f}, t_graph[3] = {0.f, 0.f, 0.f};
+        bool direct_only[3] = {false, false, false};
         DBuf save_jobs, restore_jobs;  // checkpoint copies: [ckpt][shot][field]
     };
     std::vector<std::unique_ptr<WaveDev>> wdev;
@@ -1108,9 +1116,12 @@ struct fwi_survey {
     int rc_C = 0, rc_J = 0, rc_slots = 0;
     std::vector<int> ev, blk_seg, blk_slot;
     ~fwi_survey() {
-        for (auto& w : wdev)
+        for (auto& w : wdev) {
             for (auto& gexec : w->graph)
                 if (gexec) cudaGraphExecDestroy(gexec);
+            for (auto& e : w->tev)
+                if (e) cudaEventDestroy(e);
+        }
     }
 };
 
@@ -1925,6 +1936,11 @@ int fwi_survey_set_time(fwi_survey* s, float dt, int nt, const float* src, const
                     gexec = nullptr;
                 }
             for (int& n : w->direct_runs) n = 0;
+            for (int i = 0; i < 3; ++i) {
+                w->t_direct[i] = w->t_graph[i] = 0.f;
+                w->direct_only[i] = false;
+            }
+            w->timing = 0;
         }
     }
     CK(cudaStreamSynchronize(st));
@@ -1984,8 +2000,20 @@ int fwi_survey_run(fwi_survey* s, int step, double* misfit, float* grad) {
         // instantiating a long time loop costs seconds, which a time axis run
         // once (a line-search trial) would not win back; the second run
         // captures the graph, later runs replay it
-        if ((D.flags & FWI_SURVEY_NO_GRAPH) || (!wd.graph[gi] && wd.direct_runs[gi] == 0)) {
+        const bool no_graph = (D.flags & FWI_SURVEY_NO_GRAPH) != 0;
+        if (!wd.tev[0] && !no_graph) {
+            CK(cudaEventCreate(&wd.tev[0]));
+            CK(cudaEventCreate(&wd.tev[1]));
+        }
+        if (no_graph || wd.direct_only[gi] || (!wd.graph[gi] && wd.direct_runs[gi] == 0)) {
+            const bool timed = !no_graph && wd.t_direct[gi] == 0.f;
+            if (timed) CK(cudaEventRecord(wd.tev[0], st));
             TRY(issue_wave(s, wi, step, st, L().aux));
+            if (timed) {
+                CK(cudaEventRecord(wd.tev[1], st));
+                wd.timing = 1;
+                wd.timing_gi = gi;
+            }
             ++wd.direct_runs[gi];
             continue;
         }
@@ -2007,8 +2035,16 @@ int fwi_survey_run(fwi_survey* s, int step, double* misfit, float* grad) {
             e = cudaGraphInstantiate(&wd.graph[gi], graph, cudaGraphInstantiateFlagUseNodePriority);
             cudaGraphDestroy(graph);
             if (e != cudaSuccess) return cuda_fail(e, "cudaGraphInstantiate", __LINE__);
+            CK(cudaGraphUpload(wd.graph[gi], st));  // outside the timed replay
         }
+        const bool timed = wd.t_graph[gi] == 0.f;
+        if (timed) CK(cudaEventRecord(wd.tev[0], st));
         CK(cudaGraphLaunch(wd.graph[gi], st));
+        if (timed) {
+            CK(cudaEventRecord(wd.tev[1], st));
+            wd.timing = 2;
+            wd.timing_gi = gi;
+        }
         L().launches += wd.graph_kernels[gi];
     }
     // per-shot misfits (FP64) in shot order
@@ -2024,6 +2060,22 @@ int fwi_survey_run(fwi_survey* s, int step, double* misfit, float* grad) {
         if (!dev) CK(cudaMemcpyAsync(grad, dg, n, cudaMemcpyDeviceToHost, st));
     }
     CK(cudaStreamSynchronize(st));
+    // launch form: both timings known -> keep the faster one (a graph must
+    // beat the direct launches by more than the 0.2 % run-to-run spread)
+    for (auto& w : s->wdev) {
+        auto& wd = *w;
+        if (!wd.timing) continue;
+        const int g2 = wd.timing_gi;
+        float ms = 0.f;
+        CK(cudaEventElapsedTime(&ms, wd.tev[0], wd.tev[1]));
+        (wd.timing == 1 ? wd.t_direct[g2] : wd.t_graph[g2]) = ms;
+        wd.timing = 0;
+        if (wd.t_direct[g2] > 0.f && wd.t_graph[g2] > 1.002f * wd.t_direct[g2] && wd.graph[g2]) {
+            CK(cudaGraphExecDestroy(wd.graph[g2]));
+            wd.graph[g2] = nullptr;
+            wd.direct_only[g2] = true;
+        }
+    }
     double tot = 0.0;
     bool finite = true;
     for (int i = 0; i < D.nshots; ++i) {
@@ -2114,6 +2166,22 @@ int fwi_survey_edge_tiles(fwi_survey* s, int* edge_rows, int* cand, float* times
         if (cand) cand[c] = EDGE_BANDS[c];
         if (times) times[c] = s->tune_ems.empty() ? -1.f : s->tune_ems[c];
     }
+    return FWI_OK;
+}
+
+int fwi_survey_launch_form(fwi_survey* s, int step, int* form, float* direct_ms, float* graph_ms) {
+    if (!s || s->wdev.empty()) return fail(FWI_ERR_STATE, "survey not prepared");
+    if (step != 1 && step != 2) return fail(FWI_ERR_ARG, "step must be 1 or 2");
+    const auto& wd = *s->wdev[0];
+    const int gi = step == 1 ? 0 : 1;
+    if (form) {
+        if (s->desc.flags & FWI_SURVEY_NO_GRAPH) *form = 2;
+        else if (wd.direct_only[gi]) *form = 2;
+        else if (wd.t_graph[gi] > 0.f) *form = 1;
+        else *form = 0;
+    }
+    if (direct_ms) *direct_ms = wd.t_direct[gi];
+    if (graph_ms) *graph_ms = wd.t_graph[gi];
     return FWI_OK;
 }
 

@@ -312,6 +312,13 @@ int fwi_survey_tiles(fwi_survey* s, int* tile_kernel, int* tile_rows, int* cand,
  * tuner's measurements: times[c] = ms per forward two-step pass of the first
  * wave with edge tiles of cand[c] rows (-1 where not measured; at most 8). */
 int fwi_survey_edge_tiles(fwi_survey* s, int* edge_rows, int* cand, float* times, int* ncand);
+/* Launch form of the first wave's runs with this step (1 gradient, 2
+ * forward and misfit): *form = 1 replays of a captured CUDA graph, 2 direct
+ * launches, 0 not decided yet.  A time axis runs directly the first time and
+ * as a graph replay the second; both runs are timed (*direct_ms, *graph_ms;
+ * 0 where not measured), and a graph slower than the direct launches is
+ * dropped.  FWI_SURVEY_NO_GRAPH: always 2. */
+int fwi_survey_launch_form(fwi_survey* s, int step, int* form, float* direct_ms, float* graph_ms);
 /* Checkpointed recomputation plan: forward steps per segment and number of
  * segments (0, 0 when all snapshots are stored). */
 int fwi_survey_recompute(fwi_survey* s, int* segment_steps, int* segments);

@@ -296,3 +296,36 @@ def test_batch_entry_line_search_trials_one_plan():
     assert N.load().fwi_batch_plans() - p0 == 1
     sv.close()
     F.load().fwi_batch_release()
+
+
+def test_launch_form_chosen_by_timing_bit_identical():
+    """The first run of a time axis launches directly, the second replays a
+    captured graph; both are timed and the slower form is dropped.  Every run
+    gives the same bits, whichever form it took."""
+    import fwi_gb300 as F
+    from fwi_gb300.synth import lam_from_vp
+    spec, vp = make(9, nshots=3)
+    sv = F.Survey(spec)
+    sv.set_lambda(lam_from_vp(vp))
+    assert sv.launch_form(1)[0] == "undecided"
+    outs = []
+    for k in range(4):
+        g = np.zeros((spec.ny, spec.nx_model), np.float32, order="F")
+        m, _ = sv.run(1, g)
+        outs.append((m, g))
+        form, t_direct, t_graph = sv.launch_form(1)
+        if k == 0:
+            assert form == "undecided" and t_direct > 0 and t_graph == 0
+        else:
+            assert form in ("graph", "direct") and t_direct > 0 and t_graph > 0
+            assert (form == "direct") == (t_graph > 1.002 * t_direct)
+    for m, g in outs[1:]:
+        assert m == outs[0][0] and np.array_equal(g, outs[0][1])
+    # the forward-only runs decide on their own
+    assert sv.launch_form(2)[0] == "undecided"
+    plain = F.Survey(spec, graph=False)
+    plain.set_lambda(lam_from_vp(vp))
+    g = np.zeros_like(outs[0][1])
+    m, _ = plain.run(1, g)
+    assert plain.launch_form(1)[0] == "direct"
+    assert m == outs[0][0] and np.array_equal(g, outs[0][1])

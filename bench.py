@@ -69,7 +69,7 @@ def parse():
                     help="two-step tile kernel: 1 register queues, 2 shared-memory queue (0 = tuner)")
     ap.add_argument("--tile-rows", type=int, default=0, help="rows per two-step tile (0 = tuner)")
     ap.add_argument("--tile-edge-rows", type=int, default=0,
-                    help="rows per edge tile (0 = tuner; above the model's rows: the core tiles' bands)")
+                    help="rows of the bottom edge band (0 = tuner; above the model's rows: the last core-height band)")
     a = ap.parse_args()
     if a.workload == "mcs-f16":
         a.snap = a.snap or "f16"

@@ -269,9 +269,9 @@ class Survey:
                  band_rows=0, graph=True, recompute=False, two_step=True, tile_kernel=0, tile_rows=0,
                  tile_edge_rows=0):
         """tile_kernel: 0 = the tuner's choice, 1 = register-queue, 2 = shared-queue
-        two-step kernel; tile_rows: rows per two-step tile, tile_edge_rows: per
-        edge tile (0 = the tuner's; tile_edge_rows above the model's rows: the
-        core tiles' bands)."""
+        two-step kernel; tile_rows: rows per two-step tile; tile_edge_rows: rows
+        of the bottom edge band, the last two-step rows (0 = the tuner's;
+        above the model's rows: the last core-height band)."""
         self.spec = spec
         flags = ((0 if graph else N.SURVEY_NO_GRAPH) | (N.SURVEY_RECOMPUTE if recompute else 0)
                  | (0 if two_step else N.SURVEY_SINGLE_STEP))
@@ -388,8 +388,9 @@ class Survey:
         return k.value, r.value, meas
 
     def edge_tiles(self):
-        """(rows per edge tile, 0 = the core tiles' bands; {rows: ms per forward
-        two-step pass of the first wave} as measured by the tuner)."""
+        """(rows of the bottom edge band, 0 = the last core-height band; {rows:
+        ms per forward two-step pass of the first wave} as measured by the
+        tuner)."""
         e, n = C.c_int(0), C.c_int(0)
         cand = (C.c_int * 8)()
         times = (C.c_float * 8)()

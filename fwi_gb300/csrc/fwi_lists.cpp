@@ -221,21 +221,19 @@ Lists build_lists(const std::vector<ShotGeom>& geoms, const std::vector<Layout>&
                             edge_a.back().push_back(ea);
                         });
                     } else {
-                        // edge tiles in eband rows: the rows [0, nr-eb) in bands of fband rows for the
-                        // tiles clear of the side strips (all core) and of eband rows for the side
-                        // tile columns, then the last eb rows as one band of edge tiles
+                        // a bottom edge band of eb rows: the rows [0, nr-eb) in bands of fband rows
+                        // (core tiles, and edge tiles in the side tile columns), then the last eb
+                        // rows -- the tiles whose second step reaches the single-step rows -- as one
+                        // band of edge tiles, so that most of the model rows' bottom band is core
                         const int nc = nr - eb;
                         bands(nc, fband, [&](int y0, int y1) {
-                            std::vector<WorkItem> vf, va;
-                            for (int x0 = xa & ~3; x0 < xb; x0 += 120)
-                                if (is_core(x0, y1)) tile(vf, va, x0, y0, y1);
+                            std::vector<WorkItem> vf, va, ef, ea;
+                            for (int x0 = xa & ~3; x0 < xb; x0 += 120) {
+                                const bool core = is_core(x0, y1);
+                                tile(core ? vf : ef, core ? va : ea, x0, y0, y1);
+                            }
                             fus_f.back().push_back(vf);
                             fus_a.back().push_back(va);
-                        });
-                        bands(nc, eband, [&](int y0, int y1) {
-                            std::vector<WorkItem> ef, ea;
-                            for (int x0 = xa & ~3; x0 < xb; x0 += 120)
-                                if (!is_core(x0, nc)) tile(ef, ea, x0, y0, y1);
                             edge_f.back().push_back(ef);
                             edge_a.back().push_back(ea);
                         });

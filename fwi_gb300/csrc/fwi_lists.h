@@ -57,8 +57,10 @@ bool two_step_ok(const Layout& l);
 
 // Work lists for a set of shots (local shot index = position in `geoms`);
 // fband > 0 also builds the two-step lists (two-step tiles in bands of fband
-// rows); eband > 0 puts the edge tiles -- the tile columns next to the side
-// strips and the last max(eband, 2R+1) rows -- in bands of eband rows.
+// rows); eband > 0 makes the last max(eband, 2R+1) two-step rows -- the rows
+// whose second step reaches the single-step rows next to the bottom pad --
+// one band of edge tiles, the rows above it bands of fband rows (edge tiles
+// only in the tile columns next to the side strips).
 Lists build_lists(const std::vector<ShotGeom>& geoms, const std::vector<Layout>& lays, int band_rows, int fband = 0,
                   int eband = 0);
 

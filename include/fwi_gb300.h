@@ -231,10 +231,11 @@ typedef struct fwi_survey_desc {
     int tile_kernel;      /* two-step tile kernel: 0 = chosen by the tuner,
                              1 = register queues, 2 = shared-memory queue        */
     int tile_rows;        /* rows per two-step tile (0 = chosen by the tuner)    */
-    int tile_edge_rows;   /* rows per edge tile -- the tiles next to the side
-                             strips and the last rows -- (0 = chosen by the
-                             tuner; more than the model's rows: in the core
-                             tiles' bands)                                    */
+    int tile_edge_rows;   /* rows of the bottom edge band -- the last
+                             two-step rows, next to the single-step rows above
+                             the bottom pad -- (0 = chosen by the tuner; more
+                             than the model's rows: the last core-height
+                             band)                                            */
 } fwi_survey_desc;
 
 /* fwi_survey_desc.flags: launch every time step directly instead of
@@ -308,9 +309,10 @@ int fwi_survey_tuning(fwi_survey* s, int* wave_shots, int* band_rows);
  * height cand[c] (-1 where not measured; cached or forced choices measure
  * nothing); *ncand receives the number of tile heights tried (at most 8). */
 int fwi_survey_tiles(fwi_survey* s, int* tile_kernel, int* tile_rows, int* cand, float* times, int* ncand);
-/* Rows per edge tile chosen for the survey (0: the core tiles' bands) and the
- * tuner's measurements: times[c] = ms per forward two-step pass of the first
- * wave with edge tiles of cand[c] rows (-1 where not measured; at most 8). */
+/* Rows of the bottom edge band chosen for the survey (0: the last core-height
+ * band) and the tuner's measurements: times[c] = ms per forward two-step pass
+ * of the first wave with a bottom edge band of cand[c] rows (-1 where not
+ * measured; at most 8). */
 int fwi_survey_edge_tiles(fwi_survey* s, int* edge_rows, int* cand, float* times, int* ncand);
 /* Launch form of the first wave's runs with this step (1 gradient, 2
  * forward and misfit): *form = 1 replays of a captured CUDA graph, 2 direct

@@ -345,9 +345,17 @@ __device__ __forceinline__ void bottom_rows(const StepParams& P, const WorkItem&
         c2p[i] = make_float2(P.c2[i], P.c2[i]);
     }
 
+    // the row's CPML factor, fetched one row ahead
+    float An = __ldg(P.fA + j0), Bn = __ldg(P.fB + j0);
     int slot = 0;
     for (int jl = j0; jl < j1; ++jl) {
         const int y = yb0 + jl;
+        // bottom strip: factor(j)  (solver_PML_coeffs.f90, pml_matrices_y)
+        const float A = An, B = Bn;
+        if (jl + 1 < j1) {
+            An = __ldg(P.fA + jl + 1);
+            Bn = __ldg(P.fB + jl + 1);
+        }
         cp_wait<BOT_DEPTH - 1>();
         const float4* st = ring + slot * SB_SIZE;
         if (y + R <= nyt - 1) q[2 * R] = st[SB_P + lane];
@@ -362,8 +370,6 @@ __device__ __forceinline__ void bottom_rows(const StepParams& P, const WorkItem&
         const int dmode = (jl < R) ? 0 : ((jl <= dn - 1 - R) ? 1 : 2);
         if (dmode == 1) f[2 * R] = st[SB_FA + lane];
         const bool yclamp = y > nyt - 1 - R;
-        // bottom strip: factor(j)  (solver_PML_coeffs.f90, pml_matrices_y)
-        const float A = __ldg(P.fA + jl), B = __ldg(P.fB + jl);
         const float2 Ap = make_float2(A, A), Bp = make_float2(B, B);
         float phy[4], chy[4], p3[4];
 #pragma unroll
@@ -873,6 +879,29 @@ __device__ __forceinline__ void strip_rows(const StepParams& P, const WorkItem& 
     int rrow = (ri < it.r1) ? P.recs[ri].row : INT_MAX;
     const size_t seg = (size_t)S.ntiles + (right ? 1 : 0);
 
+    // CPML factor index of each lane's column: per column in the model rows
+    // (xl strip: factor(dn-i+1), xr strip: factor(i), solver_PML_matrices.f90:296-312);
+    // in the bottom rows factor(j), in the corners factor(max(i,j)) with the
+    // ld/rd orientation (solver_PML_coeffs.f90:240-267).  The factors of a
+    // row are fetched one row ahead.
+    int cfi[K];
+#pragma unroll
+    for (int k = 0; k < K; ++k) cfi[k] = xc[k] ? ((col[k] < dn) ? (dn - 1 - col[k]) : (col[k] - dn - nx)) : 0;
+    auto fidx = [&](int k, int jrow) {
+        if (!BOT) return cfi[k];
+        int fi = jrow;
+        if (xc[k]) fi = max(jrow, cfi[k]);
+        if (!act[k]) fi = 0;
+        return fi;
+    };
+    float fa[K], fb[K];
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+        const int fi = fidx(k, BOT ? y0 - yb0 : 0);
+        fa[k] = __ldg(P.fA + fi);
+        fb[k] = __ldg(P.fB + fi);
+    }
+
     int qy = y0 % L::QN, sy = y0 % L::NA;  // ring line of row y, slot of row y
     // ring line of row y + i for a compile-time i in [-QN, QN]
     auto qat = [&](int i) {
@@ -883,6 +912,20 @@ __device__ __forceinline__ void strip_rows(const StepParams& P, const WorkItem& 
     };
 #pragma unroll 1
     for (int y = y0; y < y1; ++y) {
+        float ca[K], cb[K];  // this row's factors
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+            ca[k] = fa[k];
+            cb[k] = fb[k];
+        }
+        if (BOT && y + 1 < y1) {
+#pragma unroll
+            for (int k = 0; k < K; ++k) {
+                const int fi = fidx(k, y + 1 - yb0);
+                fa[k] = __ldg(P.fA + fi);
+                fb[k] = __ldg(P.fB + fi);
+            }
+        }
         cp_wait<L::LA - 1>();
         __syncwarp();
         const int jl = y - yb0;  // bottom rows: index inside the bottom strip
@@ -963,9 +1006,7 @@ __device__ __forceinline__ void strip_rows(const StepParams& P, const WorkItem& 
             const float base = (-pm1[k]) + 2.f * pc[k];
             if (!BOT) {
                 if (xc[k]) {
-                    // xl strip: factor(dn-i+1); xr strip: factor(i)  (solver_PML_matrices.f90:296-312)
-                    const int fi = (c < dn) ? (dn - 1 - c) : (c - dn - nx);
-                    const float A = __ldg(P.fA + fi), B = __ldg(P.fB + fi);
+                    const float A = ca[k], B = cb[k];
                     const float phn = A * px[j] + B * dx[k];
                     const float chn = A * sline(sy, L::S_CX)[j] + B * (d2x[k] + dphx[k]);
                     const float prop = dphx[k] + chn;
@@ -976,12 +1017,7 @@ __device__ __forceinline__ void strip_rows(const StepParams& P, const WorkItem& 
                     p3[k] = base + (((d2x[k] + d2y[k]) + sv[k]) * cc);
                 }
             } else {
-                // bottom strip factor(j); corners factor(max(i,j)) with the
-                // ld/rd orientation (solver_PML_coeffs.f90:240-267)
-                int fi = jl;
-                if (xc[k]) fi = max(jl, (c < dn) ? (dn - 1 - c) : (c - dn - nx));
-                if (!act[k]) fi = 0;
-                const float A = __ldg(P.fA + fi), B = __ldg(P.fB + fi);
+                const float A = ca[k], B = cb[k];
                 const float phyn = A * yline(qy)[j] + B * dy[k];
                 const float chyn = A * sline(sy, L::S_CY)[j] + B * (d2y[k] + dphy[k]);
                 const float propy = dphy[k] + chyn;

@@ -305,26 +305,8 @@ __device__ __forceinline__ void bottom_rows(const StepParams& P, const WorkItem&
         cp_commit();
     }
 
-    // clamped values: rows jl < R use the phi derivative at local row R, rows
-    // jl > dn-1-R that at dn-1-R (solver_space_derivs.f90:118-128 on the
-    // strip); rows below nyt-1-R use the p derivatives of row nyt-1-R.
-    float4 t[2 * R + 1];
-    float dphyTop[4] = {0.f, 0.f, 0.f, 0.f}, dphyBot[4] = {0.f, 0.f, 0.f, 0.f};
-    float d2yBot[4] = {0.f, 0.f, 0.f, 0.f}, dyBot[4] = {0.f, 0.f, 0.f, 0.f};
-    if (j0 < R) {
-#pragma unroll
-        for (int i = 0; i <= 2 * R; ++i) t[i] = ld4(PHO + (size_t)(yb0 + i) * pitch + xl);
-        yderiv1<R>(t, P, dphyTop);
-    }
-    if (j1 - 1 > dn - 1 - R) {
-#pragma unroll
-        for (int i = 0; i <= 2 * R; ++i) t[i] = ld4(PHO + (size_t)(nyt - 1 - 2 * R + i) * pitch + xl);
-        yderiv1<R>(t, P, dphyBot);
-#pragma unroll
-        for (int i = 0; i <= 2 * R; ++i) t[i] = ldg4(PC + (size_t)(nyt - 1 - 2 * R + i) * pitch + xl);
-        yderivs<R>(t, P, d2yBot, dyBot);
-    }
-
+    // the p and old y-phi queues, loaded first so that their latency
+    // overlaps the clamp loads below
     float4 q[2 * R + 1], f[2 * R + 1];
 #pragma unroll
     for (int i = 0; i < 2 * R; ++i) {
@@ -334,6 +316,30 @@ __device__ __forceinline__ void bottom_rows(const StepParams& P, const WorkItem&
     if (jA <= jB) {
 #pragma unroll
         for (int i = 0; i < 2 * R; ++i) f[i] = ld4(PHO + (size_t)(yb0 + jA - R + i) * pitch + xl);
+    }
+
+    // clamped values: rows jl < R use the phi derivative at local row R, rows
+    // jl > dn-1-R that at dn-1-R (solver_space_derivs.f90:118-128 on the
+    // strip); rows below nyt-1-R use the p derivatives of row nyt-1-R.  The
+    // latter two are the row loop's own derivatives at local row dn-1-R
+    // (row nyt-1-R): a band that holds that row takes them there; other
+    // bands compute them here.
+    const bool bot_clamp = j1 - 1 > dn - 1 - R, bot_in_loop = bot_clamp && j0 <= dn - 1 - R;
+    float4 t[2 * R + 1];
+    float dphyTop[4] = {0.f, 0.f, 0.f, 0.f}, dphyBot[4] = {0.f, 0.f, 0.f, 0.f};
+    float d2yBot[4] = {0.f, 0.f, 0.f, 0.f}, dyBot[4] = {0.f, 0.f, 0.f, 0.f};
+    if (j0 < R) {
+#pragma unroll
+        for (int i = 0; i <= 2 * R; ++i) t[i] = ld4(PHO + (size_t)(yb0 + i) * pitch + xl);
+        yderiv1<R>(t, P, dphyTop);
+    }
+    if (bot_clamp && !bot_in_loop) {
+#pragma unroll
+        for (int i = 0; i <= 2 * R; ++i) t[i] = ld4(PHO + (size_t)(nyt - 1 - 2 * R + i) * pitch + xl);
+        yderiv1<R>(t, P, dphyBot);
+#pragma unroll
+        for (int i = 0; i <= 2 * R; ++i) t[i] = ldg4(PC + (size_t)(nyt - 1 - 2 * R + i) * pitch + xl);
+        yderivs<R>(t, P, d2yBot, dyBot);
     }
 
     int ri = it.r0;
@@ -411,6 +417,14 @@ __device__ __forceinline__ void bottom_rows(const StepParams& P, const WorkItem&
                 dph = s1;
             } else {
                 dph = make_float2(dphyBot[2 * k], dphyBot[2 * k + 1]);
+            }
+            if (bot_in_loop && jl == dn - 1 - R) {  // the clamp values of the rows below
+                d2yBot[2 * k] = d2y.x;
+                d2yBot[2 * k + 1] = d2y.y;
+                dyBot[2 * k] = dy.x;
+                dyBot[2 * k + 1] = dy.y;
+                dphyBot[2 * k] = dph.x;
+                dphyBot[2 * k + 1] = dph.y;
             }
             // phi' = A phi + B dy, chi' = A chi + B (d2y + dphi), prop = dphi + chi',
             // p_3 = (-p_1 + 2p) + c2 ((d2x + d2y) + prop)

@@ -525,14 +525,17 @@ def main():
     edge_rows, edge_ms = sv.edge_tiles()
     rc_plan = sv.recompute_plan()
     launch_form, launch_direct_ms, launch_graph_ms = sv.launch_form(1)
+    stepping, step2_ms, step1_ms = sv.stepping()
     achieved = bytes_step / step_s / 1e9
     tr = traffic_from_profile()
     roof = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
             "traffic": tr * wave if (tr and a.workload in ("mcs", "mcs-f16")) else None,
-            "kernel": "one time step of all shots of a wave, run as two-step passes: "
-                      + ("k_step2s_interior" if tile_kernel == 2 else "k_step2_interior")
-                      + f" (model-row interior, two steps per sweep, {tile_rows}-row tiles) beside k_step_strip + "
-                      "k_step_bottom + k_step_interior (single-step lists, twice per pass)",
+            "kernel": ("one time step of all shots of a wave, run as two-step passes: "
+                       + ("k_step2s_interior" if tile_kernel == 2 else "k_step2_interior")
+                       + f" (model-row interior, two steps per sweep, {tile_rows}-row tiles) beside k_step_strip + "
+                       "k_step_bottom + k_step_interior (single-step lists, twice per pass)") if tile_kernel else
+                      ("one time step of all shots of a wave, run as single steps (the tuner measured them faster): "
+                       "k_step_interior beside k_step_strip + k_step_bottom"),
             "algorithmic_bytes_per_launch": bytes_step, "avg_launch_ms": step_s * 1e3,
             "single_step_bytes": bytes_single, "single_step_equivalent_GBps": bytes_single / step_s / 1e9,
             "two_step_tile_bytes_per_pass": tile_bytes_pass,
@@ -646,6 +649,8 @@ def main():
                            "recompute_segment_steps": rc_plan[0], "recompute_segments": rc_plan[1],
                            "launch": {"form": launch_form, "direct_ms": launch_direct_ms,
                                       "graph_replay_ms": launch_graph_ms},
+                           "time_stepping": {"form": stepping, "tuner_two_step_ms_per_2_steps": step2_ms,
+                                             "tuner_single_ms_per_2_steps": step1_ms},
                            "l2": "inputs larger than L2 (wavefields of all shots of a wave and their snapshots: "
                                  "tens to hundreds of GB)"},
                 "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "plain": plain, "gpu_launches": int(launches),

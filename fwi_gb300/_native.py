@@ -34,7 +34,7 @@ EXPORTS = [
     "fwi_interpolation_akima", "fwi_su_info", "fwi_su_read", "fwi_su_write", "fwi_read_nav",
     "fwi_survey_time_steps", "fwi_misfit_gradient_batch", "fwi_solver_forward_noalloc", "fwi_survey_tiles",
     "fwi_batch_plans", "fwi_batch_release", "fwi_first_step", "fwi_model_update", "fwi_was_geometry", "fwi_su_supershot", "fwi_survey_edge_tiles",
-    "fwi_survey_launch_form",
+    "fwi_survey_launch_form", "fwi_survey_stepping",
 ]
 
 
@@ -113,6 +113,7 @@ def load():
     lib.fwi_survey_tiles.argtypes = [P, IP, IP, P, P, IP]
     lib.fwi_survey_edge_tiles.argtypes = [P, IP, P, P, IP]
     lib.fwi_survey_launch_form.argtypes = [P, I, IP, C.POINTER(F), C.POINTER(F)]
+    lib.fwi_survey_stepping.argtypes = [P, IP, C.POINTER(F), C.POINTER(F)]
     lib.fwi_survey_time_steps.argtypes = [P, I]
     lib.fwi_misfit_gradient_batch.argtypes = [C.POINTER(FwiSurveyDesc), P, I, P, P]
     lib.fwi_solver_forward_noalloc.argtypes = [I, I, P, P, P, P, P, F, F, I, I, P, I, P]

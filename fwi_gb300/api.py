@@ -397,6 +397,14 @@ class Survey:
         N.check(N.load().fwi_survey_edge_tiles(self.handle, C.byref(e), cand, times, C.byref(n)))
         return e.value, {cand[c]: float(times[c]) for c in range(n.value) if times[c] >= 0}
 
+    def stepping(self):
+        """("two-step" | "single", two-step ms, single-step ms): the survey's
+        time stepping and the tuner's timings of the first wave per two time
+        steps (-1 where not measured)."""
+        t, a, b = C.c_int(0), C.c_float(0.0), C.c_float(0.0)
+        N.check(N.load().fwi_survey_stepping(self.handle, C.byref(t), C.byref(a), C.byref(b)))
+        return ("two-step" if t.value else "single"), float(a.value), float(b.value)
+
     def launch_form(self, step=1):
         """("graph" | "direct" | "undecided", direct-launch ms, graph-replay ms)
         of the first wave's runs with this step: the first run of a time axis

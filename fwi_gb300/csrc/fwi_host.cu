@@ -1080,7 +1080,11 @@ struct fwi_survey {
     int ntr = 0;
     int wave = 1, band = 64;
     int tile_var = 1, tile_band = TWO_STEP_BAND;  // two-step kernel and rows per two-step tile
-    int tile_eband = 0;                           // rows per edge tile (0: the core tiles' bands)
+    int tile_eband = 0;                           // rows of the bottom edge band (0: a core-height band)
+    // single steps chosen by the tuner over the two-step passes, and the two
+    // timings it compared (ms per two time steps of the first wave)
+    bool single_step = false;
+    float tune_two_ms = -1.f, tune_single_ms = -1.f;
     std::vector<float> tune_ms;                   // tuner: [variant][band candidate] ms per pass (-1: not run)
     std::vector<float> tune_ems;                  // tuner: [edge band candidate] ms per pass
     std::vector<std::vector<int>> waves;  // shot indices per wave
@@ -1189,7 +1193,9 @@ int survey_prepare_waves(fwi_survey* s) {
             g.push_back(s->geoms[sh]);
             l.push_back(s->lays[sh]);
         }
-        Lists lists = build_lists(g, l, s->band, (D.flags & FWI_SURVEY_SINGLE_STEP) ? 0 : s->tile_band, s->tile_eband);
+        Lists lists = build_lists(g, l, s->band,
+                                  ((D.flags & FWI_SURVEY_SINGLE_STEP) || s->single_step) ? 0 : s->tile_band,
+                                  s->tile_eband);
         std::unique_ptr<fwi_survey::WaveDev> wd(new fwi_survey::WaveDev());
         TRY(upload(wd->items_if, lists.int_fwd, st));
         TRY(upload(wd->items_ia, lists.int_adj, st));
@@ -1287,7 +1293,10 @@ int survey_prepare_waves(fwi_survey* s) {
 //   * the band height of the single-step interior items (BANDS), timed as
 //     single steps, when single steps carry a share of the run
 //     (FWI_SURVEY_SINGLE_STEP, no two-step tiles, or 16-bit snapshots, whose
-//     forward snapshot steps are single steps).
+//     forward snapshot steps are single steps);
+//   * single steps against the chosen two-step passes (when no tile choice is
+//     forced): a small wave (one 200 x 400 shot) runs faster in single steps,
+//     whose launch groups are fewer than the six of a two-step pass.
 // A choice forced in the descriptor is not tuned.  Results are cached per
 // (device name, rows, order, CPML, wave size, window widths of the first
 // wave, time stepping, snapshot form) in memory and in a text file that
@@ -1337,10 +1346,10 @@ bool tune_lookup(const std::string& key, std::vector<int>& out) {
     bool found = false;
     while (fgets(line, sizeof line, f)) {
         char k[900];
-        int b = 0, v = 0, r = 0, e = 0;
-        if (sscanf(line, "%899s %d %d %d %d", k, &b, &v, &r, &e) == 5 && key == k && b > 0 && (v == 0 || v == 1) &&
-            r > 0 && e >= 0) {
-            out = {b, v, r, e};
+        int b = 0, v = 0, r = 0, e = 0, one = 0;
+        const int n = sscanf(line, "%899s %d %d %d %d %d", k, &b, &v, &r, &e, &one);
+        if (n >= 5 && key == k && b > 0 && (v == 0 || v == 1) && r > 0 && e >= 0 && (one == 0 || one == 1)) {
+            out = {b, v, r, e, n == 6 ? one : 0};
             found = true;
         }
     }
@@ -1357,7 +1366,7 @@ void tune_store(const std::string& key, const std::vector<int>& v) {
     for (size_t p = path.find('/', 1); p != std::string::npos; p = path.find('/', p + 1))
         mkdir(path.substr(0, p).c_str(), 0755);
     if (FILE* f = fopen(path.c_str(), "a")) {
-        fprintf(f, "%s %d %d %d %d\n", key.c_str(), v[0], v[1], v[2], v[3]);
+        fprintf(f, "%s %d %d %d %d %d\n", key.c_str(), v[0], v[1], v[2], v[3], v[4]);
         fclose(f);
     }
 }
@@ -1394,6 +1403,10 @@ int tune_plan(fwi_survey* s) {
             if (two && D.tile_kernel <= 0) s->tile_var = hit[1];
             if (two && D.tile_rows <= 0) s->tile_band = hit[2];
             if (two && D.tile_edge_rows <= 0) s->tile_eband = hit[3];
+            if (two && D.tile_kernel <= 0 && D.tile_rows <= 0 && D.tile_edge_rows <= 0) {
+                s->single_step = hit[4] != 0;
+                if (s->single_step && D.band_rows <= 0) s->band = hit[0];
+            }
         } else {
             if (do_band) {
                 // single steps: the two-step lists play no part
@@ -1475,11 +1488,45 @@ int tune_plan(fwi_survey* s) {
                 }
                 s->tile_eband = be;
             }
-            tune_store(key, {s->band, s->tile_var, s->tile_band, s->tile_eband});
+            if (two && D.tile_kernel <= 0 && D.tile_rows <= 0 && D.tile_edge_rows <= 0) {
+                // the chosen two-step passes against single steps (their band
+                // height tuned too, unless forced), each per two time steps
+                float m2 = 0.f;
+                TRY(survey_prepare_waves(s));
+                TRY(time_passes(&m2));
+                const int keep_band = s->band;
+                float m1 = 1e30f;
+                int b1 = keep_band;
+                s->single_step = true;
+                for (int c : BANDS) {
+                    const int bb = D.band_rows > 0 ? D.band_rows : c;
+                    if (D.band_rows > 0 && c != BANDS[0]) break;
+                    if (bb > D.ny && c != BANDS[0]) break;
+                    s->band = bb;
+                    TRY(survey_prepare_waves(s));
+                    float ms = 0.f, m = 1e30f;
+                    TRY(time_wave0_steps(s, 8, &ms, true));
+                    for (int r = 0; r < 3; ++r) {
+                        TRY(time_wave0_steps(s, 2 * TUNE_PASSES, &ms, true));
+                        m = std::min(m, ms);
+                    }
+                    m /= TUNE_PASSES;
+                    if (m < m1) {
+                        m1 = m;
+                        b1 = bb;
+                    }
+                }
+                s->tune_two_ms = m2;
+                s->tune_single_ms = m1;
+                // single steps only where they are clearly faster (2 %)
+                s->single_step = m1 < 0.98f * m2;
+                s->band = s->single_step ? b1 : keep_band;
+            }
+            tune_store(key, {s->band, s->tile_var, s->tile_band, s->tile_eband, s->single_step ? 1 : 0});
         }
         if (two) {
             L().tile_var = s->tile_var;
-            L().tile_band = s->tile_band;
+            L().tile_band = s->single_step ? 0 : s->tile_band;
             L().tile_eband = s->tile_eband;
         }
     }
@@ -2166,6 +2213,14 @@ int fwi_survey_edge_tiles(fwi_survey* s, int* edge_rows, int* cand, float* times
         if (cand) cand[c] = EDGE_BANDS[c];
         if (times) times[c] = s->tune_ems.empty() ? -1.f : s->tune_ems[c];
     }
+    return FWI_OK;
+}
+
+int fwi_survey_stepping(fwi_survey* s, int* two_step, float* two_step_ms, float* single_ms) {
+    if (!s || s->wdev.empty()) return fail(FWI_ERR_STATE, "survey not prepared");
+    if (two_step) *two_step = s->wdev[0]->n_ff > 0 ? 1 : 0;
+    if (two_step_ms) *two_step_ms = s->tune_two_ms;
+    if (single_ms) *single_ms = s->tune_single_ms;
     return FWI_OK;
 }
 

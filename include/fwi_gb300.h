@@ -314,6 +314,13 @@ int fwi_survey_tiles(fwi_survey* s, int* tile_kernel, int* tile_rows, int* cand,
  * of the first wave with a bottom edge band of cand[c] rows (-1 where not
  * measured; at most 8). */
 int fwi_survey_edge_tiles(fwi_survey* s, int* edge_rows, int* cand, float* times, int* ncand);
+/* Time stepping chosen for the survey: *two_step = 1 two-step passes, 0
+ * single steps (FWI_SURVEY_SINGLE_STEP, no two-step tiles, or single steps
+ * measured faster by the tuner -- a small wave, whose time step is set by
+ * launch latency); *two_step_ms and *single_ms: the tuner's timings of the
+ * first wave per two time steps (-1 where not measured: a forced or cached
+ * choice). */
+int fwi_survey_stepping(fwi_survey* s, int* two_step, float* two_step_ms, float* single_ms);
 /* Launch form of the first wave's runs with this step (1 gradient, 2
  * forward and misfit): *form = 1 replays of a captured CUDA graph, 2 direct
  * launches, 0 not decided yet.  A time axis runs directly the first time and

@@ -100,19 +100,26 @@ def test_two_step_passes_bit_identical(kw, rc, form):
 
 def test_tuner_picks_a_measured_tile(monkeypatch):
     """The tuner times both two-step kernels at each tile height on the first
-    wave and keeps the fastest; its choice is one of the measured ones."""
+    wave and keeps the fastest, then the bottom edge band, then single steps
+    against the chosen two-step passes; every choice is the fastest
+    measured one."""
     monkeypatch.setenv("FWI_TUNE_CACHE", "")  # no cross-process cache file
     import fwi_gb300 as F
     from fwi_gb300.synth import lam_from_vp
     spec, vp = make(11, ny=70, nxm=400, nshots=4)
     sv = F.Survey(spec)
+    stepping, t2, t1 = sv.stepping()
     kern, rows, meas = sv.tiles()
-    assert kern in (1, 2) and rows in (16, 32, 48, 64, 96)
-    if meas:  # empty when the choice came from the tuning cache
-        assert (kern, rows) in meas and meas[(kern, rows)] == min(meas.values())
-    edge, emeas = sv.edge_tiles()
-    assert edge in (0, 8, 16, 32)
-    if emeas:
+    assert meas  # nothing cached: every candidate was timed
+    best = min(meas, key=meas.get)
+    assert t2 > 0 and t1 > 0
+    if stepping == "single":
+        assert kern == 0 and rows == 0 and t1 < 0.98 * t2
+    else:
+        assert t1 >= 0.98 * t2
+        assert kern in (1, 2) and rows in (16, 32, 48, 64, 96) and (kern, rows) == best
+        edge, emeas = sv.edge_tiles()
+        assert edge in (0, 8, 16, 32)
         assert edge in emeas and emeas[edge] == min(emeas.values())
     sv.set_lambda(lam_from_vp(vp))
     g = np.zeros((spec.ny, spec.nx_model), np.float32, order="F")

@@ -525,7 +525,7 @@ def main():
     edge_rows, edge_ms = sv.edge_tiles()
     rc_plan = sv.recompute_plan()
     launch_form, launch_direct_ms, launch_graph_ms = sv.launch_form(1)
-    stepping, step2_ms, step1_ms = sv.stepping()
+    stepping, stepping_ms = sv.stepping()
     achieved = bytes_step / step_s / 1e9
     tr = traffic_from_profile()
     roof = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
@@ -535,7 +535,8 @@ def main():
                        + f" (model-row interior, two steps per sweep, {tile_rows}-row tiles) beside k_step_strip + "
                        "k_step_bottom + k_step_interior (single-step lists, twice per pass)") if tile_kernel else
                       ("one time step of all shots of a wave, run as single steps (the tuner measured them faster): "
-                       "k_step_interior beside k_step_strip + k_step_bottom"),
+                       + ("k_step_fused (interior, strips and bottom tiles in one launch)" if stepping == "single-fused"
+                          else "k_step_interior beside k_step_strip + k_step_bottom")),
             "algorithmic_bytes_per_launch": bytes_step, "avg_launch_ms": step_s * 1e3,
             "single_step_bytes": bytes_single, "single_step_equivalent_GBps": bytes_single / step_s / 1e9,
             "two_step_tile_bytes_per_pass": tile_bytes_pass,
@@ -623,10 +624,18 @@ def main():
             tt = torch.tensor([te], device="cuda")
             torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
             te = float(tt.item())
+        bsv = F.batch_survey()
+        batch_plan = None
+        if bsv is not None:
+            bk, br, _ = bsv.tiles()
+            batch_plan = {"tile_kernel": bk, "tile_rows": br, "tile_edge_rows": bsv.edge_tiles()[0],
+                          "wave_band": list(bsv.tuning()), "time_stepping": bsv.stepping()[0],
+                          "launch": list(bsv.launch_form(1))}
         e2e = {"value": world * len(spec.shots) * a.steps / te, "unit": METRIC,
                "h2d_bytes_per_step": int(h_lam.nbytes + h_obs.nbytes + h_src.nbytes + h_grad.nbytes),
                "d2h_bytes_per_step": int(h_grad.nbytes + 8 * sum(len(s.nxRec) for s in spec.shots)),
-               "call": "fwi_misfit_gradient_batch (calculate_misfit_gradient drop-in), pinned host buffers"}
+               "call": "fwi_misfit_gradient_batch (calculate_misfit_gradient drop-in), pinned host buffers",
+               "batch_plan": batch_plan}
 
     cpu = None
     if rank == 0 and world == 1 and not a.no_cpu:
@@ -649,8 +658,7 @@ def main():
                            "recompute_segment_steps": rc_plan[0], "recompute_segments": rc_plan[1],
                            "launch": {"form": launch_form, "direct_ms": launch_direct_ms,
                                       "graph_replay_ms": launch_graph_ms},
-                           "time_stepping": {"form": stepping, "tuner_two_step_ms_per_2_steps": step2_ms,
-                                             "tuner_single_ms_per_2_steps": step1_ms},
+                           "time_stepping": {"form": stepping, "tuner_ms_per_2_steps": stepping_ms},
                            "l2": "inputs larger than L2 (wavefields of all shots of a wave and their snapshots: "
                                  "tens to hundreds of GB)"},
                 "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "plain": plain, "gpu_launches": int(launches),

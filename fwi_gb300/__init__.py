@@ -15,6 +15,7 @@ from ._native import (  # noqa: F401
     SURVEY_NO_GRAPH,
     SURVEY_RECOMPUTE,
     SURVEY_SINGLE_STEP,
+    SURVEY_FUSED_STEP,
     FwiError,
     load,
 )
@@ -25,6 +26,7 @@ from .api import (  # noqa: E402,F401
     Misfit_function,
     Ricker_mcs,
     Survey,
+    batch_survey,
     calculate_misfit_gradient,
     first_step,
     init,

@@ -22,6 +22,7 @@ SNAP_F32, SNAP_BF16, SNAP_F16 = 0, 1, 2
 SURVEY_NO_GRAPH = 1
 SURVEY_RECOMPUTE = 2
 SURVEY_SINGLE_STEP = 4
+SURVEY_FUSED_STEP = 8
 GRAD_F32, GRAD_F64 = 0, 1
 
 EXPORTS = [
@@ -34,7 +35,7 @@ EXPORTS = [
     "fwi_interpolation_akima", "fwi_su_info", "fwi_su_read", "fwi_su_write", "fwi_read_nav",
     "fwi_survey_time_steps", "fwi_misfit_gradient_batch", "fwi_solver_forward_noalloc", "fwi_survey_tiles",
     "fwi_batch_plans", "fwi_batch_release", "fwi_first_step", "fwi_model_update", "fwi_was_geometry", "fwi_su_supershot", "fwi_survey_edge_tiles",
-    "fwi_survey_launch_form", "fwi_survey_stepping",
+    "fwi_survey_launch_form", "fwi_survey_stepping", "fwi_batch_survey",
 ]
 
 
@@ -113,7 +114,8 @@ def load():
     lib.fwi_survey_tiles.argtypes = [P, IP, IP, P, P, IP]
     lib.fwi_survey_edge_tiles.argtypes = [P, IP, P, P, IP]
     lib.fwi_survey_launch_form.argtypes = [P, I, IP, C.POINTER(F), C.POINTER(F)]
-    lib.fwi_survey_stepping.argtypes = [P, IP, C.POINTER(F), C.POINTER(F)]
+    lib.fwi_survey_stepping.argtypes = [P, IP, C.POINTER(F), C.POINTER(F), C.POINTER(F)]
+    lib.fwi_batch_survey.argtypes = [C.POINTER(C.c_void_p)]
     lib.fwi_survey_time_steps.argtypes = [P, I]
     lib.fwi_misfit_gradient_batch.argtypes = [C.POINTER(FwiSurveyDesc), P, I, P, P]
     lib.fwi_solver_forward_noalloc.argtypes = [I, I, P, P, P, P, P, F, F, I, I, P, I, P]

@@ -267,14 +267,15 @@ class Survey:
 
     def __init__(self, spec: SurveySpec, snap_form=N.SNAP_F32, grad_form=N.GRAD_F64, hbm_budget=0, wave_shots=0,
                  band_rows=0, graph=True, recompute=False, two_step=True, tile_kernel=0, tile_rows=0,
-                 tile_edge_rows=0):
+                 tile_edge_rows=0, fused_step=False):
         """tile_kernel: 0 = the tuner's choice, 1 = register-queue, 2 = shared-queue
         two-step kernel; tile_rows: rows per two-step tile; tile_edge_rows: rows
         of the bottom edge band, the last two-step rows (0 = the tuner's;
-        above the model's rows: the last core-height band)."""
+        above the model's rows: the last core-height band); two_step=False:
+        single steps; fused_step: single steps, one launch each."""
         self.spec = spec
         flags = ((0 if graph else N.SURVEY_NO_GRAPH) | (N.SURVEY_RECOMPUTE if recompute else 0)
-                 | (0 if two_step else N.SURVEY_SINGLE_STEP))
+                 | (0 if two_step else N.SURVEY_SINGLE_STEP) | (N.SURVEY_FUSED_STEP if fused_step else 0))
         self._h = _DescHolder(spec, snap_form, grad_form, hbm_budget, wave_shots, band_rows, flags, tile_kernel,
                               tile_rows, tile_edge_rows)
         handle = C.c_void_p()
@@ -283,6 +284,9 @@ class Survey:
         self.nt, self.dt = spec.nt, spec.dt
 
     def close(self):
+        if getattr(self, "_borrowed", False):  # the library owns it (batch_survey)
+            self.handle = C.c_void_p()
+            return
         if getattr(self, "handle", None) and self.handle.value:
             N.load().fwi_survey_destroy(self.handle)
             self.handle = C.c_void_p()
@@ -398,12 +402,14 @@ class Survey:
         return e.value, {cand[c]: float(times[c]) for c in range(n.value) if times[c] >= 0}
 
     def stepping(self):
-        """("two-step" | "single", two-step ms, single-step ms): the survey's
-        time stepping and the tuner's timings of the first wave per two time
-        steps (-1 where not measured)."""
-        t, a, b = C.c_int(0), C.c_float(0.0), C.c_float(0.0)
-        N.check(N.load().fwi_survey_stepping(self.handle, C.byref(t), C.byref(a), C.byref(b)))
-        return ("two-step" if t.value else "single"), float(a.value), float(b.value)
+        """("two-step" | "single" | "single-fused", {form: ms}): the survey's
+        time stepping ("single-fused": one launch per step) and the tuner's
+        timings of the first wave per two time steps (empty where not
+        measured: a forced or cached choice)."""
+        t, a, b, c = C.c_int(0), C.c_float(0.0), C.c_float(0.0), C.c_float(0.0)
+        N.check(N.load().fwi_survey_stepping(self.handle, C.byref(t), C.byref(a), C.byref(b), C.byref(c)))
+        times = {k: float(v.value) for k, v in (("two-step", a), ("single", b), ("single-fused", c)) if v.value >= 0}
+        return {0: "single", 1: "two-step", 2: "single-fused"}[t.value], times
 
     def launch_form(self, step=1):
         """("graph" | "direct" | "undecided", direct-launch ms, graph-replay ms)
@@ -434,3 +440,19 @@ def calculate_misfit_gradient(spec: SurveySpec, lam, step, Misfit, Grad, snap_fo
     m = C.c_float(Misfit)
     N.check(N.load().fwi_misfit_gradient_batch(C.byref(h.desc), _p(lam), step, C.byref(m), _p(Grad)))
     return np.float32(m.value)
+
+
+def batch_survey():
+    """The survey of fwi_misfit_gradient_batch's current plan (owned by the
+    library) for the query methods -- tiles(), edge_tiles(), stepping(),
+    launch_form(), tuning() -- or None before the first call.  Valid until the
+    batch call changes geometry or the plan is released."""
+    h = C.c_void_p()
+    N.check(N.load().fwi_batch_survey(C.byref(h)))
+    if not h.value:
+        return None
+    v = Survey.__new__(Survey)
+    v.handle = h
+    v.spec = None
+    v._borrowed = True
+    return v

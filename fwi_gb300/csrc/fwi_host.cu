@@ -28,6 +28,8 @@ namespace fwi {
 cudaError_t launch_step2(int acc, int mode, int var, const StepParams& pf, cudaStream_t st);
 cudaError_t launch_step(int acc, int mode, int kstrip, const StepParams& pm, const StepParams& pb, cudaStream_t sm,
                         cudaStream_t sb, cudaStream_t ss);
+cudaError_t launch_step_fused(int acc, int mode, int kstrip, const StepParams& pm, const StepParams& pb,
+                              cudaStream_t st);
 cudaError_t configure_step_kernels();
 cudaError_t launch_build_c2(float* c2, int nyt, int pitch, int off, int dn, int ny, int nx, const float* src, int ldv,
                             int x0, int from_lambda, float dt2, float d2, cudaStream_t st);
@@ -372,6 +374,7 @@ StepParams base_params(int acc, float dt, int store_snap, int snap_form, int gra
 struct StepSet {
     StepParams pm, pb;  // interior list; boundary list (pb.nstrip side strips, then bottom tiles)
     int kstrip = 1;
+    bool fused = false;  // single steps as one launch (k_step_fused) instead of three on three streams
 };
 
 // Wavefield buffers of step k.  A shot's state (p, p_1) lives in pair 0
@@ -438,6 +441,11 @@ int step_kernels(const StepSet& ps) {
 // dependencies under stream capture).
 int step_fork_join(int acc, int mode, const StepSet& ps, cudaStream_t st, cudaStream_t st2) {
     const bool has_m = ps.pm.nitems > 0, has_b = ps.pb.nitems > ps.pb.nstrip, has_s = ps.pb.nstrip > 0;
+    if (ps.fused) {
+        L().launches += (has_m || has_b || has_s) ? 1 : 0;
+        CK(launch_step_fused(acc, mode, ps.kstrip, ps.pm, ps.pb, st));
+        return FWI_OK;
+    }
     L().launches += step_kernels(ps);
     if (!has_m || (!has_s && !has_b)) {
         CK(launch_step(acc, mode, ps.kstrip, ps.pm, ps.pb, st, st, st));
@@ -1081,10 +1089,11 @@ struct fwi_survey {
     int wave = 1, band = 64;
     int tile_var = 1, tile_band = TWO_STEP_BAND;  // two-step kernel and rows per two-step tile
     int tile_eband = 0;                           // rows of the bottom edge band (0: a core-height band)
-    // single steps chosen by the tuner over the two-step passes, and the two
-    // timings it compared (ms per two time steps of the first wave)
-    bool single_step = false;
-    float tune_two_ms = -1.f, tune_single_ms = -1.f;
+    // single steps chosen by the tuner over the two-step passes (fused: each
+    // step one launch), and the timings it compared (ms per two time steps
+    // of the first wave)
+    bool single_step = false, fused = false;
+    float tune_two_ms = -1.f, tune_single_ms = -1.f, tune_fused_ms = -1.f;
     std::vector<float> tune_ms;                   // tuner: [variant][band candidate] ms per pass (-1: not run)
     std::vector<float> tune_ems;                  // tuner: [edge band candidate] ms per pass
     std::vector<std::vector<int>> waves;  // shot indices per wave
@@ -1105,11 +1114,14 @@ struct fwi_survey {
         // launch form per direction, chosen by measurement: the first run of
         // a time axis is timed as direct launches, the first replay of its
         // graph as a replay (CUDA events around the wave); a graph slower
-        // than the direct launches is dropped for good
+        // than the direct launches is dropped for good.  A graph that looks
+        // faster is kept only after a second direct run (the first one may
+        // be the first pass over freshly allocated buffers) confirms it.
         cudaEvent_t tev[2] = {nullptr, nullptr};
         int timing = 0, timing_gi = 0;            // in flight: 1 direct, 2 graph
         float t_direct[3] = {0.f, 0.f, 0.f}, t_graph[3] = {0.f, 0.f, 0.f};
         bool direct_only[3] = {false, false, false};
+        bool recheck[3] = {false, false, false}, rechecked[3] = {false, false, false};
         DBuf save_jobs, restore_jobs;  // checkpoint copies: [ckpt][shot][field]
     };
     std::vector<std::unique_ptr<WaveDev>> wdev;
@@ -1194,7 +1206,9 @@ int survey_prepare_waves(fwi_survey* s) {
             l.push_back(s->lays[sh]);
         }
         Lists lists = build_lists(g, l, s->band,
-                                  ((D.flags & FWI_SURVEY_SINGLE_STEP) || s->single_step) ? 0 : s->tile_band,
+                                  ((D.flags & (FWI_SURVEY_SINGLE_STEP | FWI_SURVEY_FUSED_STEP)) || s->single_step)
+                                      ? 0
+                                      : s->tile_band,
                                   s->tile_eband);
         std::unique_ptr<fwi_survey::WaveDev> wd(new fwi_survey::WaveDev());
         TRY(upload(wd->items_if, lists.int_fwd, st));
@@ -1348,7 +1362,7 @@ bool tune_lookup(const std::string& key, std::vector<int>& out) {
         char k[900];
         int b = 0, v = 0, r = 0, e = 0, one = 0;
         const int n = sscanf(line, "%899s %d %d %d %d %d", k, &b, &v, &r, &e, &one);
-        if (n >= 5 && key == k && b > 0 && (v == 0 || v == 1) && r > 0 && e >= 0 && (one == 0 || one == 1)) {
+        if (n >= 5 && key == k && b > 0 && (v == 0 || v == 1) && r > 0 && e >= 0 && one >= 0 && one <= 2) {
             out = {b, v, r, e, n == 6 ? one : 0};
             found = true;
         }
@@ -1373,7 +1387,8 @@ void tune_store(const std::string& key, const std::vector<int>& v) {
 
 int tune_plan(fwi_survey* s) {
     const auto& D = s->desc;
-    bool two = (D.flags & FWI_SURVEY_SINGLE_STEP) == 0;
+    if (D.flags & FWI_SURVEY_FUSED_STEP) s->fused = true;
+    bool two = (D.flags & (FWI_SURVEY_SINGLE_STEP | FWI_SURVEY_FUSED_STEP)) == 0;
     if (two) {
         two = false;
         for (int sh : s->waves[0]) two = two || two_step_ok(s->lays[sh]);
@@ -1405,6 +1420,7 @@ int tune_plan(fwi_survey* s) {
             if (two && D.tile_edge_rows <= 0) s->tile_eband = hit[3];
             if (two && D.tile_kernel <= 0 && D.tile_rows <= 0 && D.tile_edge_rows <= 0) {
                 s->single_step = hit[4] != 0;
+                s->fused = hit[4] == 2;
                 if (s->single_step && D.band_rows <= 0) s->band = hit[0];
             }
         } else {
@@ -1516,13 +1532,27 @@ int tune_plan(fwi_survey* s) {
                         b1 = bb;
                     }
                 }
+                // single steps in one launch each (the fused kernel), at that band
+                s->band = b1;
+                s->fused = true;
+                TRY(survey_prepare_waves(s));
+                float mf = 1e30f, ms = 0.f;
+                TRY(time_wave0_steps(s, 8, &ms, true));
+                for (int r = 0; r < 3; ++r) {
+                    TRY(time_wave0_steps(s, 2 * TUNE_PASSES, &ms, true));
+                    mf = std::min(mf, ms);
+                }
+                mf /= TUNE_PASSES;
                 s->tune_two_ms = m2;
                 s->tune_single_ms = m1;
+                s->tune_fused_ms = mf;
                 // single steps only where they are clearly faster (2 %)
-                s->single_step = m1 < 0.98f * m2;
+                s->single_step = std::min(m1, mf) < 0.98f * m2;
+                s->fused = s->single_step && mf < m1;
                 s->band = s->single_step ? b1 : keep_band;
             }
-            tune_store(key, {s->band, s->tile_var, s->tile_band, s->tile_eband, s->single_step ? 1 : 0});
+            tune_store(key, {s->band, s->tile_var, s->tile_band, s->tile_eband,
+                             s->single_step ? (s->fused ? 2 : 1) : 0});
         }
         if (two) {
             L().tile_var = s->tile_var;
@@ -1652,6 +1682,7 @@ int rc_adjoint(fwi_survey* s, size_t wi, StepSet ps, cudaStream_t st, cudaStream
     psf.pb.nitems = wd.n_bf;
     psf.pb.nstrip = wd.n_strip;
     psf.kstrip = wd.kstrip;
+    psf.fused = s->fused;
     ps.pm.items = wd.items_ia.as<WorkItem>();
     ps.pm.nitems = wd.n_ia;
     ps.pm.shots = wd.shots_a.as<ShotDev>();
@@ -1662,6 +1693,7 @@ int rc_adjoint(fwi_survey* s, size_t wi, StepSet ps, cudaStream_t st, cudaStream
     ps.pb.nitems = wd.n_ba;
     ps.pb.nstrip = wd.n_strip;
     ps.kstrip = wd.kstrip;
+    ps.fused = s->fused;
     const TwoStep twf = two_step_set(psf, 0, wd.items_ff, wd.n_ff, wd.n_core, wd.items_lf, wd.n_lf, s->tile_var);
     const TwoStep twa = two_step_set(ps, 1, wd.items_fa, wd.n_fa, wd.n_core, wd.items_la, wd.n_la, s->tile_var);
     const TwoStep* pf = wd.n_ff ? &twf : nullptr;
@@ -1735,6 +1767,7 @@ int issue_wave(fwi_survey* s, size_t wi, int step, cudaStream_t st, cudaStream_t
     ps.pb.nitems = wd.n_bf;
     ps.pb.nstrip = wd.n_strip;
     ps.kstrip = wd.kstrip;
+    ps.fused = s->fused;
     {
         const TwoStep tw = two_step_set(ps, 0, wd.items_ff, wd.n_ff, wd.n_core, wd.items_lf, wd.n_lf, s->tile_var);
         const TwoStep* ptw = wd.n_ff ? &tw : nullptr;
@@ -1782,6 +1815,7 @@ int issue_wave(fwi_survey* s, size_t wi, int step, cudaStream_t st, cudaStream_t
     ps.pb.nitems = wd.n_ba;
     ps.pb.nstrip = wd.n_strip;
     ps.kstrip = wd.kstrip;
+    ps.fused = s->fused;
     TwoStep tw = two_step_set(ps, 1, wd.items_fa, wd.n_fa, wd.n_core, wd.items_la, wd.n_la, s->tile_var);
     TRY(run_time_loop(D.acc, 1, D.nt, D.store_snap, s->nt_store, true, ps, st, st2, wd.n_fa ? &tw : nullptr));
     LK(launch_stack(s->d_G.as<double>(), D.ny, D.nx_model, wd.stack.p, (int)w.size(), D.grad_form, st));
@@ -1985,7 +2019,7 @@ int fwi_survey_set_time(fwi_survey* s, float dt, int nt, const float* src, const
             for (int& n : w->direct_runs) n = 0;
             for (int i = 0; i < 3; ++i) {
                 w->t_direct[i] = w->t_graph[i] = 0.f;
-                w->direct_only[i] = false;
+                w->direct_only[i] = w->recheck[i] = w->rechecked[i] = false;
             }
             w->timing = 0;
         }
@@ -2052,8 +2086,8 @@ int fwi_survey_run(fwi_survey* s, int step, double* misfit, float* grad) {
             CK(cudaEventCreate(&wd.tev[0]));
             CK(cudaEventCreate(&wd.tev[1]));
         }
-        if (no_graph || wd.direct_only[gi] || (!wd.graph[gi] && wd.direct_runs[gi] == 0)) {
-            const bool timed = !no_graph && wd.t_direct[gi] == 0.f;
+        if (no_graph || wd.direct_only[gi] || wd.recheck[gi] || (!wd.graph[gi] && wd.direct_runs[gi] == 0)) {
+            const bool timed = !no_graph && (wd.t_direct[gi] == 0.f || wd.recheck[gi]);
             if (timed) CK(cudaEventRecord(wd.tev[0], st));
             TRY(issue_wave(s, wi, step, st, L().aux));
             if (timed) {
@@ -2115,12 +2149,24 @@ int fwi_survey_run(fwi_survey* s, int step, double* misfit, float* grad) {
         const int g2 = wd.timing_gi;
         float ms = 0.f;
         CK(cudaEventElapsedTime(&ms, wd.tev[0], wd.tev[1]));
-        (wd.timing == 1 ? wd.t_direct[g2] : wd.t_graph[g2]) = ms;
+        if (wd.timing == 2) {
+            wd.t_graph[g2] = ms;
+        } else if (wd.recheck[g2]) {
+            wd.t_direct[g2] = std::min(wd.t_direct[g2], ms);
+            wd.recheck[g2] = false;
+            wd.rechecked[g2] = true;
+        } else {
+            wd.t_direct[g2] = ms;
+        }
         wd.timing = 0;
-        if (wd.t_direct[g2] > 0.f && wd.t_graph[g2] > 1.002f * wd.t_direct[g2] && wd.graph[g2]) {
-            CK(cudaGraphExecDestroy(wd.graph[g2]));
-            wd.graph[g2] = nullptr;
-            wd.direct_only[g2] = true;
+        if (wd.t_direct[g2] > 0.f && wd.t_graph[g2] > 0.f && wd.graph[g2]) {
+            if (wd.t_graph[g2] > 1.002f * wd.t_direct[g2]) {
+                CK(cudaGraphExecDestroy(wd.graph[g2]));
+                wd.graph[g2] = nullptr;
+                wd.direct_only[g2] = true;
+            } else if (!wd.rechecked[g2]) {
+                wd.recheck[g2] = true;  // the next run: direct launches once more
+            }
         }
     }
     double tot = 0.0;
@@ -2216,11 +2262,12 @@ int fwi_survey_edge_tiles(fwi_survey* s, int* edge_rows, int* cand, float* times
     return FWI_OK;
 }
 
-int fwi_survey_stepping(fwi_survey* s, int* two_step, float* two_step_ms, float* single_ms) {
+int fwi_survey_stepping(fwi_survey* s, int* form, float* two_step_ms, float* single_ms, float* fused_ms) {
     if (!s || s->wdev.empty()) return fail(FWI_ERR_STATE, "survey not prepared");
-    if (two_step) *two_step = s->wdev[0]->n_ff > 0 ? 1 : 0;
+    if (form) *form = s->wdev[0]->n_ff > 0 ? 1 : (s->fused ? 2 : 0);
     if (two_step_ms) *two_step_ms = s->tune_two_ms;
     if (single_ms) *single_ms = s->tune_single_ms;
+    if (fused_ms) *fused_ms = s->tune_fused_ms;
     return FWI_OK;
 }
 
@@ -2275,6 +2322,7 @@ int time_wave0_steps(fwi_survey* s, int steps, float* ms, bool single_only) {
     ps.pb.nitems = wd.n_bf;
     ps.pb.nstrip = wd.n_strip;
     ps.kstrip = wd.kstrip;
+    ps.fused = s->fused;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     if (ms) {
         CK(cudaEventCreate(&e0));
@@ -2377,6 +2425,13 @@ int fwi_misfit_gradient_batch(const fwi_survey_desc* desc, const float* lambda, 
 }
 
 int64_t fwi_batch_plans(void) { return batch_plan().plans; }
+
+int fwi_batch_survey(fwi_survey** s) {
+    std::lock_guard<std::recursive_mutex> g(L().mu);
+    if (!s) return fail(FWI_ERR_ARG, "null argument");
+    *s = batch_plan().s;
+    return FWI_OK;
+}
 
 int fwi_batch_release(void) {
     std::lock_guard<std::recursive_mutex> g(L().mu);

@@ -542,16 +542,16 @@ __device__ __forceinline__ void cp8(void* smem_dst, const void* gmem_src) {
     asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(d), "l"(gmem_src) : "memory");
 }
 
+// Interior item `wid` of the list P.items, run by one warp (w: the warp's
+// index in its block, smem: the block's shared memory).
 template <int R, int MODE, bool SNAP>
-__global__ void __launch_bounds__(128, (MODE == 1 && SNAP) ? 3 : 5) k_step_interior(const __grid_constant__ StepParams P) {
+__device__ __forceinline__ void interior_rows(const StepParams& P, int wid, int w, float4* smem) {
     constexpr bool IMG = (MODE == 1) && SNAP;
     constexpr int SZ = IMG ? IN_SIZE_IMG : IN_SIZE;
     constexpr int DEPTH = IMG ? IN_DEPTH_IMG : IN_DEPTH;
-    extern __shared__ float4 smem[];
     const int lane = threadIdx.x & 31;
-    const int wid = blockIdx.x * 4 + (threadIdx.x >> 5);
     if (wid >= P.nitems) return;
-    float4* ring = smem + (threadIdx.x >> 5) * (DEPTH * SZ + IN_LINE);
+    float4* ring = smem + w * (DEPTH * SZ + IN_LINE);
     float4* line = ring + DEPTH * SZ;
     const WorkItem it = P.items[wid];
     const ShotDev& S = P.shots[it.shot];
@@ -708,6 +708,13 @@ __global__ void __launch_bounds__(128, (MODE == 1 && SNAP) ? 3 : 5) k_step_inter
         slot = (slot + 1 == DEPTH) ? 0 : slot + 1;
     }
     cp_wait<0>();
+}
+
+template <int R, int MODE, bool SNAP>
+__global__ void __launch_bounds__(128, (MODE == 1 && SNAP) ? 3 : 5) k_step_interior(const __grid_constant__ StepParams P) {
+    extern __shared__ float4 smem[];
+    const int w = threadIdx.x >> 5;
+    interior_rows<R, MODE, SNAP>(P, blockIdx.x * 4 + w, w, smem);
 }
 
 // ---------------------------------------------------------------------------
@@ -1679,6 +1686,44 @@ __global__ void __launch_bounds__(128, F2S<R, MODE == 1 && SNAP>::BLOCKS)
 // k_step_interior and k_step_strip.
 constexpr int BND_SMEM = 4 * BOT_DEPTH * SB_SIZE * 16;
 
+// One single step of a small wave in one launch: blocks [0, bm) take the
+// interior list, [bm, bm + bs) the side strips, the rest the bottom tiles --
+// the work of k_step_interior, k_step_strip and k_step_bottom, which touch
+// disjoint cells and read only the step's inputs.  A small wave's step is set
+// by launch latency, which one launch instead of three on three streams
+// (forked and joined around every step) shortens.
+template <int R, int MODE, bool SNAP, int K>
+__global__ void __launch_bounds__(128, 3)
+    k_step_fused(const __grid_constant__ StepParams Pm, const __grid_constant__ StepParams Pb, int bm, int bs) {
+    extern __shared__ float4 smem[];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    int b = blockIdx.x;
+    if (b < bm) {
+        interior_rows<R, MODE, SNAP>(Pm, b * 4 + w, w, smem);
+        return;
+    }
+    b -= bm;
+    if (b < bs) {
+        const int wid = b * 4 + w;
+        if (wid >= Pb.nstrip) return;
+        float* sw = reinterpret_cast<float*>(smem) + w * StripLayout<R, K>::WARP;
+        const WorkItem it = Pb.items[wid];
+        if (it.kind == 3) strip_rows<R, MODE, K, true>(Pb, it, sw, lane);
+        else strip_rows<R, MODE, K, false>(Pb, it, sw, lane);
+        return;
+    }
+    b -= bs;
+    const int wid = Pb.nstrip + b * 4 + w;
+    if (wid >= Pb.nitems) return;
+    bottom_rows<R, MODE>(Pb, Pb.items[wid], smem + w * (BOT_DEPTH * SB_SIZE), lane);
+}
+
+template <int R, int MODE, bool SNAP, int K>
+constexpr int fused_smem() {
+    constexpr int a = (MODE == 1 && SNAP) ? IN_SMEM_IMG : IN_SMEM, b = strip_smem<R, K>(), c = BND_SMEM;
+    return a > b ? (a > c ? a : c) : (b > c ? b : c);
+}
+
 template <int R, int MODE>
 __global__ void __launch_bounds__(128, 3) k_step_bottom(const __grid_constant__ StepParams P) {
     extern __shared__ float4 smem[];
@@ -1713,6 +1758,10 @@ cudaError_t configure_variant() {
     if (e == cudaSuccess) e = kernel_smem(k_step2_interior<R, MODE, true>, F2Ring<R, MODE == 1>::SMEM);
     if (e == cudaSuccess) e = kernel_smem(k_step2s_interior<R, MODE, false>, F2S<R, false>::SMEM);
     if (e == cudaSuccess) e = kernel_smem(k_step2s_interior<R, MODE, true>, F2S<R, MODE == 1>::SMEM);
+    if (e == cudaSuccess) e = kernel_smem(k_step_fused<R, MODE, false, 1>, fused_smem<R, MODE, false, 1>());
+    if (e == cudaSuccess) e = kernel_smem(k_step_fused<R, MODE, true, 1>, fused_smem<R, MODE, true, 1>());
+    if (e == cudaSuccess) e = kernel_smem(k_step_fused<R, MODE, false, 2>, fused_smem<R, MODE, false, 2>());
+    if (e == cudaSuccess) e = kernel_smem(k_step_fused<R, MODE, true, 2>, fused_smem<R, MODE, true, 2>());
     return e;
 }
 
@@ -1753,6 +1802,36 @@ cudaError_t launch_step(int acc, int mode, int kstrip, const StepParams& pm, con
     } else if (acc == 4) {
         if (mode == 0) launch_variant<4, 0>(kstrip, pm, pb, sm, sb, ss);
         else launch_variant<4, 1>(kstrip, pm, pb, sm, sb, ss);
+    } else {
+        return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+}
+
+template <int R, int MODE>
+void launch_fused_variant(int kstrip, const StepParams& pm, const StepParams& pb, cudaStream_t st) {
+    const int bm = (pm.nitems + 3) / 4, bs = (pb.nstrip + 3) / 4, bb = (pb.nitems - pb.nstrip + 3) / 4;
+    const int nb = bm + bs + bb;
+    if (!nb) return;
+    if (kstrip == 1) {
+        if (pm.snap >= 0) k_step_fused<R, MODE, true, 1><<<nb, 128, fused_smem<R, MODE, true, 1>(), st>>>(pm, pb, bm, bs);
+        else k_step_fused<R, MODE, false, 1><<<nb, 128, fused_smem<R, MODE, false, 1>(), st>>>(pm, pb, bm, bs);
+    } else {
+        if (pm.snap >= 0) k_step_fused<R, MODE, true, 2><<<nb, 128, fused_smem<R, MODE, true, 2>(), st>>>(pm, pb, bm, bs);
+        else k_step_fused<R, MODE, false, 2><<<nb, 128, fused_smem<R, MODE, false, 2>(), st>>>(pm, pb, bm, bs);
+    }
+}
+
+// One single step in one launch (k_step_fused) on stream st.
+cudaError_t launch_step_fused(int acc, int mode, int kstrip, const StepParams& pm, const StepParams& pb,
+                              cudaStream_t st) {
+    if (kstrip != 1 && kstrip != 2) return cudaErrorInvalidValue;
+    if (acc == 3) {
+        if (mode == 0) launch_fused_variant<3, 0>(kstrip, pm, pb, st);
+        else launch_fused_variant<3, 1>(kstrip, pm, pb, st);
+    } else if (acc == 4) {
+        if (mode == 0) launch_fused_variant<4, 0>(kstrip, pm, pb, st);
+        else launch_fused_variant<4, 1>(kstrip, pm, pb, st);
     } else {
         return cudaErrorInvalidValue;
     }

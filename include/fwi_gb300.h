@@ -251,6 +251,11 @@ typedef struct fwi_survey_desc {
  * run as two-step passes (the model-row interior advanced twice per sweep
  * over the wavefields); the results are bit-identical either way. */
 #define FWI_SURVEY_SINGLE_STEP 4
+/* fwi_survey_desc.flags: single steps, each one launch of the fused kernel
+ * (interior, side strips and bottom tiles together) instead of three on
+ * three streams; implies FWI_SURVEY_SINGLE_STEP.  The tuner picks this form
+ * for a small wave where it is measured faster; results are bit-identical. */
+#define FWI_SURVEY_FUSED_STEP 8
 
 typedef struct fwi_survey fwi_survey;
 
@@ -314,19 +319,21 @@ int fwi_survey_tiles(fwi_survey* s, int* tile_kernel, int* tile_rows, int* cand,
  * of the first wave with a bottom edge band of cand[c] rows (-1 where not
  * measured; at most 8). */
 int fwi_survey_edge_tiles(fwi_survey* s, int* edge_rows, int* cand, float* times, int* ncand);
-/* Time stepping chosen for the survey: *two_step = 1 two-step passes, 0
- * single steps (FWI_SURVEY_SINGLE_STEP, no two-step tiles, or single steps
- * measured faster by the tuner -- a small wave, whose time step is set by
- * launch latency); *two_step_ms and *single_ms: the tuner's timings of the
- * first wave per two time steps (-1 where not measured: a forced or cached
- * choice). */
-int fwi_survey_stepping(fwi_survey* s, int* two_step, float* two_step_ms, float* single_ms);
+/* Time stepping chosen for the survey: *form = 1 two-step passes; 0 single
+ * steps, three launches on three streams each; 2 single steps, one launch
+ * each.  Single steps run under FWI_SURVEY_SINGLE_STEP, without two-step
+ * tiles, or where the tuner measured them faster (a small wave, whose time
+ * step is set by launch latency).  *two_step_ms, *single_ms, *fused_ms: the
+ * tuner's timings of the first wave per two time steps (-1 where not
+ * measured: a forced or cached choice). */
+int fwi_survey_stepping(fwi_survey* s, int* form, float* two_step_ms, float* single_ms, float* fused_ms);
 /* Launch form of the first wave's runs with this step (1 gradient, 2
  * forward and misfit): *form = 1 replays of a captured CUDA graph, 2 direct
  * launches, 0 not decided yet.  A time axis runs directly the first time and
  * as a graph replay the second; both runs are timed (*direct_ms, *graph_ms;
  * 0 where not measured), and a graph slower than the direct launches is
- * dropped.  FWI_SURVEY_NO_GRAPH: always 2. */
+ * dropped; one that looks faster is kept only if the third run, launched
+ * directly once more, does not beat it.  FWI_SURVEY_NO_GRAPH: always 2. */
 int fwi_survey_launch_form(fwi_survey* s, int step, int* form, float* direct_ms, float* graph_ms);
 /* Checkpointed recomputation plan: forward steps per segment and number of
  * segments (0, 0 when all snapshots are stored). */
@@ -349,6 +356,11 @@ int fwi_misfit_gradient_batch(const fwi_survey_desc* desc, const float* lambda, 
                               float* Misfit, float* Grad);
 /* Number of plans fwi_misfit_gradient_batch has built in this process. */
 int64_t fwi_batch_plans(void);
+/* The survey of fwi_misfit_gradient_batch's current plan (NULL before the
+ * first call), owned by the library: for the query entries (fwi_survey_tiles,
+ * fwi_survey_stepping, fwi_survey_launch_form ...); valid until the next
+ * call with another geometry, fwi_batch_release or fwi_finalize. */
+int fwi_batch_survey(fwi_survey** s);
 /* Free the plan fwi_misfit_gradient_batch holds (its device memory). */
 int fwi_batch_release(void);
 

@@ -2399,23 +2399,43 @@ int fwi_misfit_gradient_batch(const fwi_survey_desc* desc, const float* lambda, 
             // a new time axis: the sources and data below are uploaded at the new length
             TRY(fwi_survey_set_time(s, desc->dt, desc->nt, nullptr, nullptr));
         }
-        // this call's sources and observed data
+        // this call's sources and observed data; copies whose host and
+        // device ranges both continue the previous one are merged (callers
+        // that pack all shots' data in one array get one copy per array)
         cudaStream_t st = stream();
+        struct Run {
+            const char* h = nullptr;
+            char* d = nullptr;
+            size_t n = 0;
+        } rs, ro;
+        auto put = [&](Run& r, const void* h, void* d, size_t n) -> int {
+            if (r.n && static_cast<const char*>(h) == r.h + r.n && static_cast<char*>(d) == r.d + r.n) {
+                r.n += n;
+                return FWI_OK;
+            }
+            if (r.n) CK(cudaMemcpyAsync(r.d, r.h, r.n, cudaMemcpyHostToDevice, st));
+            r.h = static_cast<const char*>(h);
+            r.d = static_cast<char*>(d);
+            r.n = n;
+            return FWI_OK;
+        };
         size_t so = 0, to = 0;
         const size_t nt = desc->nt;
         for (int i = 0; i < desc->nshots; ++i) {
             const fwi_shot& sh = desc->shots[i];
             if (sh.num_sou && sh.src)
-                CK(cudaMemcpyAsync(s->d_src.as<float>() + so, sh.src, nt * sh.num_sou * 4, cudaMemcpyHostToDevice, st));
+                TRY(put(rs, sh.src, s->d_src.as<float>() + so, nt * sh.num_sou * 4));
             else if (sh.num_sou)
                 CK(cudaMemsetAsync(s->d_src.as<float>() + so, 0, nt * sh.num_sou * 4, st));
             if (sh.num_rec && sh.obs)
-                CK(cudaMemcpyAsync(s->d_obs.as<float>() + to, sh.obs, nt * sh.num_rec * 4, cudaMemcpyHostToDevice, st));
+                TRY(put(ro, sh.obs, s->d_obs.as<float>() + to, nt * sh.num_rec * 4));
             else if (sh.num_rec)
                 CK(cudaMemsetAsync(s->d_obs.as<float>() + to, 0, nt * sh.num_rec * 4, st));
             so += nt * sh.num_sou;
             to += nt * sh.num_rec;
         }
+        if (rs.n) CK(cudaMemcpyAsync(rs.d, rs.h, rs.n, cudaMemcpyHostToDevice, st));
+        if (ro.n) CK(cudaMemcpyAsync(ro.d, ro.h, ro.n, cudaMemcpyHostToDevice, st));
     }
     TRY(fwi_survey_set_lambda(s, lambda));
     double m = 0.0;

@@ -101,6 +101,7 @@ struct LibState {
     cudaStream_t user = nullptr;
     cudaStream_t aux = nullptr;      // bottom-row kernels run here, concurrently
     cudaStream_t aux3 = nullptr;     // side-strip kernels run here, concurrently
+    cudaStream_t copy_in = nullptr;  // the batch call's observed-data uploads, beside the forward pass
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_join2 = nullptr;
     cudaEvent_t ev2[10] = {};  // two-step pipeline (two sets of five)
     int prio_hi = 0;
@@ -702,6 +703,7 @@ int fwi_init(int device) {
         CK(cudaDeviceGetStreamPriorityRange(&lo, &hi));
         CK(cudaStreamCreateWithPriority(&L().aux3, cudaStreamNonBlocking, hi));
     }
+    if (!L().copy_in) CK(cudaStreamCreateWithFlags(&L().copy_in, cudaStreamNonBlocking));
     if (!L().ev_fork) CK(cudaEventCreateWithFlags(&L().ev_fork, cudaEventDisableTiming));
     if (!L().ev_join) CK(cudaEventCreateWithFlags(&L().ev_join, cudaEventDisableTiming));
     if (!L().ev_join2) CK(cudaEventCreateWithFlags(&L().ev_join2, cudaEventDisableTiming));
@@ -724,6 +726,7 @@ int fwi_finalize(void) {
     if (L().own) cudaStreamDestroy(L().own);
     if (L().aux) cudaStreamDestroy(L().aux);
     if (L().aux3) cudaStreamDestroy(L().aux3);
+    if (L().copy_in) cudaStreamDestroy(L().copy_in);
     if (L().ev_fork) cudaEventDestroy(L().ev_fork);
     if (L().ev_join) cudaEventDestroy(L().ev_join);
     if (L().ev_join2) cudaEventDestroy(L().ev_join2);
@@ -731,7 +734,7 @@ int fwi_finalize(void) {
         if (e) cudaEventDestroy(e);
         e = nullptr;
     }
-    L().own = L().aux = L().aux3 = nullptr;
+    L().own = L().aux = L().aux3 = L().copy_in = nullptr;
     L().ev_fork = L().ev_join = L().ev_join2 = nullptr;
     L().user = nullptr;
     L().init = false;
@@ -1093,6 +1096,10 @@ struct fwi_survey {
     // step one launch), and the timings it compared (ms per two time steps
     // of the first wave)
     bool single_step = false, fused = false;
+    // observed data uploaded on the copy stream by the batch call: the misfit
+    // (or a graph launch) waits for obs_ready while obs_pending
+    cudaEvent_t obs_ready = nullptr;
+    bool obs_pending = false;
     float tune_two_ms = -1.f, tune_single_ms = -1.f, tune_fused_ms = -1.f;
     std::vector<float> tune_ms;                   // tuner: [variant][band candidate] ms per pass (-1: not run)
     std::vector<float> tune_ems;                  // tuner: [edge band candidate] ms per pass
@@ -1132,6 +1139,7 @@ struct fwi_survey {
     int rc_C = 0, rc_J = 0, rc_slots = 0;
     std::vector<int> ev, blk_seg, blk_slot;
     ~fwi_survey() {
+        if (obs_ready) cudaEventDestroy(obs_ready);
         for (auto& w : wdev) {
             for (auto& gexec : w->graph)
                 if (gexec) cudaGraphExecDestroy(gexec);
@@ -1779,7 +1787,9 @@ int issue_wave(fwi_survey* s, size_t wi, int step, cudaStream_t st, cudaStream_t
         LK(launch_rec_last(s->d_synth.as<float>() + (size_t)s->tr_off[sh] * D.nt, D.nt, (int)s->geoms[sh].nxR.size(), st));
     }
     // misfit + adjoint source for this wave's traces (one launch per shot:
-    // the shots of a wave need not be consecutive)
+    // the shots of a wave need not be consecutive); the observed data may
+    // still be on their way (the batch call uploads them beside the forward)
+    if (s->obs_pending) CK(cudaStreamWaitEvent(st, s->obs_ready, 0));
     for (int sh : w) {
         const int t0 = s->tr_off[sh], t1 = s->tr_off[sh + 1];
         if (t1 == t0) continue;
@@ -2098,6 +2108,12 @@ int fwi_survey_run(fwi_survey* s, int step, double* misfit, float* grad) {
             ++wd.direct_runs[gi];
             continue;
         }
+        // a graph replay reads the observed data without waiting inside: they
+        // must be on the device before it starts
+        if (s->obs_pending) {
+            CK(cudaStreamWaitEvent(st, s->obs_ready, 0));
+            s->obs_pending = false;
+        }
         if (!wd.graph[gi]) {
             cudaStream_t cap, cap2;
             CK(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
@@ -2127,6 +2143,10 @@ int fwi_survey_run(fwi_survey* s, int step, double* misfit, float* grad) {
             wd.timing_gi = gi;
         }
         L().launches += wd.graph_kernels[gi];
+    }
+    if (s->obs_pending) {
+        CK(cudaStreamWaitEvent(st, s->obs_ready, 0));
+        s->obs_pending = false;
     }
     // per-shot misfits (FP64) in shot order
     std::vector<double> mis_tr(s->ntr);
@@ -2263,6 +2283,7 @@ int fwi_survey_edge_tiles(fwi_survey* s, int* edge_rows, int* cand, float* times
 }
 
 int fwi_survey_stepping(fwi_survey* s, int* form, float* two_step_ms, float* single_ms, float* fused_ms) {
+    std::lock_guard<std::recursive_mutex> g(L().mu);
     if (!s || s->wdev.empty()) return fail(FWI_ERR_STATE, "survey not prepared");
     if (form) *form = s->wdev[0]->n_ff > 0 ? 1 : (s->fused ? 2 : 0);
     if (two_step_ms) *two_step_ms = s->tune_two_ms;
@@ -2272,6 +2293,7 @@ int fwi_survey_stepping(fwi_survey* s, int* form, float* two_step_ms, float* sin
 }
 
 int fwi_survey_launch_form(fwi_survey* s, int step, int* form, float* direct_ms, float* graph_ms) {
+    std::lock_guard<std::recursive_mutex> g(L().mu);
     if (!s || s->wdev.empty()) return fail(FWI_ERR_STATE, "survey not prepared");
     if (step != 1 && step != 2) return fail(FWI_ERR_ARG, "step must be 1 or 2");
     const auto& wd = *s->wdev[0];
@@ -2435,7 +2457,18 @@ int fwi_misfit_gradient_batch(const fwi_survey_desc* desc, const float* lambda, 
             to += nt * sh.num_rec;
         }
         if (rs.n) CK(cudaMemcpyAsync(rs.d, rs.h, rs.n, cudaMemcpyHostToDevice, st));
-        if (ro.n) CK(cudaMemcpyAsync(ro.d, ro.h, ro.n, cudaMemcpyHostToDevice, st));
+        if (ro.n) {
+            // the observed data: first read by the misfit, after the forward
+            // pass, so they go on the copy stream beside it (ordered after
+            // the work already on the stream)
+            if (!s->obs_ready) CK(cudaEventCreateWithFlags(&s->obs_ready, cudaEventDisableTiming));
+            cudaStream_t sc = L().copy_in;
+            CK(cudaEventRecord(s->obs_ready, st));
+            CK(cudaStreamWaitEvent(sc, s->obs_ready, 0));
+            CK(cudaMemcpyAsync(ro.d, ro.h, ro.n, cudaMemcpyHostToDevice, sc));
+            CK(cudaEventRecord(s->obs_ready, sc));
+            s->obs_pending = true;
+        }
     }
     TRY(fwi_survey_set_lambda(s, lambda));
     double m = 0.0;

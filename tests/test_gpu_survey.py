@@ -342,3 +342,44 @@ def test_launch_form_chosen_by_timing_bit_identical():
     m, _ = plain.run(1, g)
     assert plain.launch_form(1)[0] == "direct"
     assert m == outs[0][0] and np.array_equal(g, outs[0][1])
+
+
+def test_batch_entry_packed_data_and_new_observations():
+    """The batch call with all shots' sources and observed traces as slices of
+    one array each (the copies merged, the traces uploaded on a copy stream
+    beside the forward pass) gives the bits of separate per-shot arrays, and
+    observed traces changed between calls reach that call's misfit."""
+    import fwi_gb300 as F
+    from fwi_gb300.synth import lam_from_vp
+    spec, vp = make(13, nshots=4)
+    lam = lam_from_vp(vp)
+    nt = spec.nt
+
+    def batch():
+        g = np.zeros((spec.ny, spec.nx_model), np.float32, order="F")
+        m = F.calculate_misfit_gradient(spec, lam, 1, np.float32(0.0), g)
+        return m, g
+
+    ref = batch()  # separate arrays per shot
+    nrec = [len(sh.nxRec) for sh in spec.shots]
+    nsou = [np.asarray(sh.src).reshape(nt, -1, order="F").shape[1] for sh in spec.shots]
+    obs_all = np.asfortranarray(np.concatenate([np.asarray(sh.obs, np.float32) for sh in spec.shots], axis=1))
+    src_all = np.asfortranarray(np.concatenate(
+        [np.asarray(sh.src, np.float32).reshape(nt, -1, order="F") for sh in spec.shots], axis=1))
+    ro = np.concatenate([[0], np.cumsum(nrec)])
+    so = np.concatenate([[0], np.cumsum(nsou)])
+    for i, sh in enumerate(spec.shots):
+        sh.obs = obs_all[:, ro[i]:ro[i + 1]]
+        sh.src = src_all[:, so[i]:so[i + 1]]
+        assert sh.obs.flags.f_contiguous and sh.src.flags.f_contiguous
+    packed = batch()
+    assert packed[0] == ref[0] and np.array_equal(packed[1], ref[1])
+    # new observations in place: the next call's misfit and gradient follow them
+    obs_all *= np.float32(0.5)
+    m_half, g_half = batch()
+    sv = F.Survey(spec)
+    sv.set_lambda(lam)
+    g2 = np.zeros_like(g_half)
+    m2, _ = sv.run(1, g2)
+    assert m_half == np.float32(m2) and np.array_equal(g_half, g2)
+    assert m_half != ref[0]

@@ -266,7 +266,10 @@ Lists build_lists(const std::vector<ShotGeom>& geoms, const std::vector<Layout>&
         for (int side = 0; side < 2; ++side) {
             const int c0 = l.off + (side ? l.sr : 0), c1 = l.off + (side ? l.nxt : l.sl);
             if (c1 <= c0) continue;
-            bands(l.ny, STRIP_BAND, [&](int y0, int y1) {
+            // model-row strips in bands of STRIP_BAND rows, or of the interior
+            // items' height when that is shorter (a small grid: more warps,
+            // shorter row marches)
+            bands(l.ny, std::min(STRIP_BAND, band_rows), [&](int y0, int y1) {
                 append_item(out, strip_f, out.src_fwd, cells_f, recs, (int)s, side, l.dn + y0, l.dn + y1, 2, true,
                             c0, c1);
                 append_item(out, strip_a, out.src_adj, cells_a, recs, (int)s, side, l.dn + y0, l.dn + y1, 2, false,

@@ -1198,12 +1198,18 @@ int survey_prepare_slots(fwi_survey* s) {
 int survey_prepare_waves(fwi_survey* s) {
     const auto& D = s->desc;
     cudaStream_t st = stream();
-    for (auto& w : s->wdev)
+    for (auto& w : s->wdev) {
         for (auto& gexec : w->graph)
             if (gexec) {
                 cudaGraphExecDestroy(gexec);
                 gexec = nullptr;
             }
+        for (auto& e : w->tev)
+            if (e) {
+                cudaEventDestroy(e);
+                e = nullptr;
+            }
+    }
     s->wdev.clear();
     for (size_t wi = 0; wi < s->waves.size(); ++wi) {
         const auto& w = s->waves[wi];

@@ -1689,9 +1689,10 @@ constexpr int BND_SMEM = 4 * BOT_DEPTH * SB_SIZE * 16;
 // One single step of a small wave in one launch: blocks [0, bm) take the
 // interior list, [bm, bm + bs) the side strips, the rest the bottom tiles --
 // the work of k_step_interior, k_step_strip and k_step_bottom, which touch
-// disjoint cells and read only the step's inputs.  A small wave's step is set
-// by launch latency, which one launch instead of three on three streams
-// (forked and joined around every step) shortens.
+// disjoint cells and read only the step's inputs.  A small wave's step is
+// latency-bound; one launch instead of three on three streams (forked and
+// joined around every step) takes the fork, the join and two launches out
+// of it.
 template <int R, int MODE, bool SNAP, int K>
 __global__ void __launch_bounds__(128, 3)
     k_step_fused(const __grid_constant__ StepParams Pm, const __grid_constant__ StepParams Pb, int bm, int bs) {

@@ -323,7 +323,7 @@ int fwi_survey_edge_tiles(fwi_survey* s, int* edge_rows, int* cand, float* times
  * steps, three launches on three streams each; 2 single steps, one launch
  * each.  Single steps run under FWI_SURVEY_SINGLE_STEP, without two-step
  * tiles, or where the tuner measured them faster (a small wave, whose time
- * step is set by launch latency).  *two_step_ms, *single_ms, *fused_ms: the
+ * step is latency-bound).  *two_step_ms, *single_ms, *fused_ms: the
  * tuner's timings of the first wave per two time steps (-1 where not
  * measured: a forced or cached choice). */
 int fwi_survey_stepping(fwi_survey* s, int* form, float* two_step_ms, float* single_ms, float* fused_ms);

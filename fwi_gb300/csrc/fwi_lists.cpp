@@ -254,7 +254,7 @@ Lists build_lists(const std::vector<ShotGeom>& geoms, const std::vector<Layout>&
                     for (auto& b : main_a.back()) out.lft_adj.insert(out.lft_adj.end(), b.begin(), b.end());
                 }
             }
-            bands(l.dn, BOTTOM_BAND, [&](int j0, int j1) {
+            bands(l.dn, std::min(BOTTOM_BAND, band_rows), [&](int j0, int j1) {
                 for (int t = xa / TILE; t <= (xb - 1) / TILE; ++t) {
                     const int c0 = std::max(t * TILE, xa), c1 = std::min((t + 1) * TILE, xb);
                     append_item(out, bot_f, out.src_fwd, none, recs, (int)s, t, yb0 + j0, yb0 + j1, 1, true, c0, c1);
@@ -268,14 +268,14 @@ Lists build_lists(const std::vector<ShotGeom>& geoms, const std::vector<Layout>&
             if (c1 <= c0) continue;
             // model-row strips in bands of STRIP_BAND rows, or of the interior
             // items' height when that is shorter (a small grid: more warps,
-            // shorter row marches)
+            // shorter row marches; the bottom pad's bands follow it too)
             bands(l.ny, std::min(STRIP_BAND, band_rows), [&](int y0, int y1) {
                 append_item(out, strip_f, out.src_fwd, cells_f, recs, (int)s, side, l.dn + y0, l.dn + y1, 2, true,
                             c0, c1);
                 append_item(out, strip_a, out.src_adj, cells_a, recs, (int)s, side, l.dn + y0, l.dn + y1, 2, false,
                             c0, c1);
             });
-            bands(l.dn, STRIP_BOTTOM_BAND, [&](int j0, int j1) {
+            bands(l.dn, std::min(STRIP_BOTTOM_BAND, band_rows), [&](int j0, int j1) {
                 append_item(out, sbot_f, out.src_fwd, none, recs, (int)s, side, yb0 + j0, yb0 + j1, 3, true, c0, c1);
                 append_item(out, sbot_a, out.src_adj, none, recs, (int)s, side, yb0 + j0, yb0 + j1, 3, false, c0,
                             c1);

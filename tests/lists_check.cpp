@@ -309,6 +309,11 @@ int main() {
     }
     check(37, 61, 3, 20, 3, 32, 48);
     check(12, 90, 4, 8, 3, 16, 64);
+    for (int band : {1, 2, 3, 4, 5}) {  // short bands: the strips and the bottom pad follow them
+        check(37, 61, 3, 20, 3, band, 48);
+        check(200, 400, 4, 20, 2, band, 0);
+        check(23, 150, 4, 8, 3, band, 16, 7);
+    }
     int cases = 4;
     for (int nx = 20; nx < 400 && !fails; nx += 7)
         for (int dpml : {1, 5, 10, 20, 25, 30, 40, 54})

@@ -1336,9 +1336,9 @@ int time_wave0_steps(fwi_survey* s, int steps, float* ms, bool single_only = fal
 
 constexpr int TILE_BANDS[] = {16, 32, 48, 64, 96};  // short tiles: more warps for small grids
 constexpr int NTB = 5;
-// 2-8: small grids, whose time step is the latency of the row marches (the
+// 1-8: small grids, whose time step is the latency of the row marches (the
 // strips and the bottom pad follow a band shorter than their own)
-constexpr int BANDS[] = {2, 4, 8, 16, 24, 32, 48, 64};
+constexpr int BANDS[] = {1, 2, 4, 8, 16, 24, 32, 48, 64};
 // edge-tile heights (0: the core tiles' bands): the edge tiles run on the
 // pass's critical path beside the single-step lists, so shorter edge tiles
 // can pay for their extra halo rows

@@ -385,3 +385,46 @@ def test_batch_entry_packed_data_and_new_observations():
     m2, _ = sv.run(1, g2)
     assert m_half == np.float32(m2) and np.array_equal(g_half, g2)
     assert m_half != ref[0]
+
+
+def test_tuning_cache_file_across_processes(tmp_path):
+    """The tuner's choices persist in $FWI_TUNE_CACHE: a second process with
+    the same grid reads them from the file (no candidate timed) and makes the
+    same choices; a line of the older five-value form is still read."""
+    import json
+    import os
+    import subprocess
+    import sys
+    cache = tmp_path / "tuning.txt"
+    code = r'''
+import json, sys
+sys.path.insert(0, {root!r})
+sys.path.insert(0, {tests!r})
+import fwi_gb300 as F
+from test_gpu_survey import make
+spec, vp = make(17, ny=70, nxm=400, nshots=3)
+sv = F.Survey(spec)
+k, r, meas = sv.tiles()
+form, st = sv.stepping()
+print(json.dumps({{"tiles": [k, r], "band": sv.tuning()[1], "form": form, "measured": len(meas) + len(st)}}))
+'''.format(root=os.path.dirname(os.path.dirname(os.path.abspath(__file__))),
+           tests=os.path.dirname(os.path.abspath(__file__)))
+    env = dict(os.environ, FWI_TUNE_CACHE=str(cache))
+
+    def run():
+        out = subprocess.run([sys.executable, "-c", code], env=env, capture_output=True, text=True, timeout=600)
+        assert out.returncode == 0, out.stderr[-2000:]
+        return json.loads([l for l in out.stdout.splitlines() if l.startswith("{")][-1])
+
+    first = run()
+    assert first["measured"] > 0
+    lines = cache.read_text().split("\n")
+    assert any(len(l.split()) == 6 for l in lines)
+    second = run()
+    assert second["measured"] == 0  # every choice came from the file
+    assert {k: second[k] for k in ("tiles", "band", "form")} == {k: first[k] for k in ("tiles", "band", "form")}
+    # the older five-value form: two-step passes, as the file says
+    key, band, var, rows, eb, _ = [l for l in lines if len(l.split()) == 6][-1].split()
+    cache.write_text(f"{key} {band} {var} {rows} {eb}\n")
+    third = run()
+    assert third["measured"] == 0 and third["form"] == "two-step" and third["tiles"] == [int(var) + 1, int(rows)]

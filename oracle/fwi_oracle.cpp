@@ -705,6 +705,11 @@ int oracle_gradient_batch_f32(int nshots, int ny, float d, float dt, int nt, int
                                  sou_off, nxS, nyS, S, nrec, rec_off, nxR, nyR, obs, step, kern_off, kernels,
                                  synth_all, mis32, mis64, nthreads);
 }
+/* quantize_snapshots on an array of nsnap snapshots (ny, nx) each, in place. */
+void oracle_quantize_snapshots(float* F, int ny, int nx, int nsnap, int form) {
+    quantize_snapshots(F, ny, nx, nsnap, form);
+}
+
 /* oracle_gradient_batch_f32 with the stored snapshots in the form snap_form
  * (quantize_snapshots): the precision forms' error against FP64. */
 int oracle_gradient_batch_f32_form(int nshots, int ny, float d, float dt, int nt, int store_snap, int acc, int dPML,

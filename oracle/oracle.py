@@ -51,6 +51,7 @@ def lib():
                                                   _P, _P, _P, _P, I, _P, _P, _P, _P, _P, I]
         _lib.oracle_gradient_batch_f64.argtypes = [I, I, D, D, I, I, I, I, _P, I, _P, _P, _P, _P, _P, _P, _P, _P,
                                                   _P, _P, _P, _P, I, _P, _P, _P, _P, _P, I]
+        _lib.oracle_quantize_snapshots.argtypes = [_P, I, I, I, I]
         _lib.oracle_gradient_batch_f32_form.argtypes = [I, I, F, F, I, I, I, I, _P, I, _P, _P, _P, _P, _P, _P, _P,
                                                        _P, _P, _P, _P, _P, I, _P, _P, _P, _P, _P, I, I]
     return _lib
@@ -152,6 +153,15 @@ def pml_coeffs(acc, dpml, dt, d):
 # stored-snapshot forms of gradient_batch(snap_form=...) (FP32 solver only)
 SNAP_FORMS = {"f32": 0, "f16_snapshot_scale": 1, "bf16_snapshot_scale": 2, "f16_segment_pow2": 3,
               "bf16_segment_pow2": 4}
+
+
+def quantize_snapshots(fields, form):
+    """The stored-snapshot form `form` (SNAP_FORMS) applied to a float32
+    array of snapshots (ny, nx, nsnap) in Fortran order, in place; returns it."""
+    assert fields.dtype == np.float32 and fields.flags.f_contiguous and fields.ndim == 3
+    ny, nx, ns = fields.shape
+    lib().oracle_quantize_snapshots(_ptr(fields), ny, nx, ns, int(form))
+    return fields
 
 
 def gradient_batch(survey, vp_model, step=1, fp64=False, nthreads=1, want_synth=False, snap_form=0):

@@ -94,3 +94,57 @@ def test_sixteen_bit_forms_error(forms):
     for p in ("f16", "bf16"):
         r = e[p + "_segment_pow2"] / e[p + "_snapshot_scale"]
         assert 1 / 1.5 < r < 1.5, (p, r)
+
+
+def _bf16(x):
+    """Round float32 to the nearest bfloat16 (ties to even), as float32."""
+    u = np.asarray(x, np.float32).view(np.uint32).astype(np.uint64)
+    u = (u + 0x7FFF + ((u >> 16) & 1)) & 0xFFFF0000
+    return u.astype(np.uint32).view(np.float32)
+
+
+def _f16(x):
+    return np.asarray(x, np.float32).astype(np.float16).astype(np.float32)
+
+
+def _forms_numpy(A, form):
+    """The snapshot forms restated in numpy: one max-abs scale per snapshot
+    (forms 1, 2) or a power-of-two scale per 128-column segment of a row
+    (forms 3, 4); FP16 (1, 3) or BF16 (2, 4)."""
+    rnd = _f16 if form in (1, 3) else _bf16
+    out = A.copy()
+    f32 = np.float32
+    for k in range(A.shape[2]):
+        S = out[:, :, k]
+        if form in (1, 2):
+            m = f32(np.abs(S).max())
+            if m == 0:
+                continue
+            up, down = f32(16384.0) / m, m / f32(16384.0)
+            out[:, :, k] = rnd(S * up) * down
+        else:
+            for j in range(S.shape[0]):
+                for i0 in range(0, S.shape[1], 128):
+                    seg = S[j, i0:i0 + 128]
+                    m = f32(np.abs(seg).max())
+                    ex = int(np.frexp(m)[1]) if m > 0 else 0
+                    sh = 14 - ex
+                    S[j, i0:i0 + 128] = np.ldexp(rnd(np.ldexp(seg, sh)), -sh)
+    return out
+
+
+def test_quantize_snapshots_matches_numpy():
+    """The oracle's snapshot forms (quantize_snapshots) against their numpy
+    restatement, bit for bit, on values spanning nine decades, zeros, an
+    all-zero snapshot and a ragged last segment."""
+    rng = np.random.default_rng(3)
+    ny, nx, ns = 7, 300, 4
+    A = (rng.standard_normal((ny, nx, ns)) * 10.0 ** rng.uniform(-6, 3, size=(ny, nx, ns))).astype(np.float32)
+    A[:, :5, 1] = 0.0
+    A[:, :, 3] = 0.0
+    A = np.asfortranarray(A)
+    for form in (1, 2, 3, 4):
+        got = O.quantize_snapshots(np.asfortranarray(A.copy()), form)
+        np.testing.assert_array_equal(got, _forms_numpy(A, form), err_msg=f"form {form}")
+        assert not np.array_equal(got, A)  # the form rounds
+    np.testing.assert_array_equal(O.quantize_snapshots(np.asfortranarray(A.copy()), 0), A)

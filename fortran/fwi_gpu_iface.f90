@@ -13,7 +13,7 @@ module fwi_gpu_iface
   integer(c_int), parameter :: FWI_OK = 0
   ! fwi_survey_desc%flags bits
   integer(c_int), parameter :: FWI_SURVEY_NO_GRAPH = 1, FWI_SURVEY_RECOMPUTE = 2, FWI_SURVEY_SINGLE_STEP = 4, &
-                                FWI_SURVEY_FUSED_STEP = 8
+                                FWI_SURVEY_FUSED_STEP = 8, FWI_SURVEY_GRAPH = 16
 
   type, bind(C) :: fwi_shot
      integer(c_int) :: x0, nx, num_sou, num_rec

@@ -16,6 +16,7 @@ from ._native import (  # noqa: F401
     SURVEY_RECOMPUTE,
     SURVEY_SINGLE_STEP,
     SURVEY_FUSED_STEP,
+    SURVEY_GRAPH,
     FwiError,
     load,
 )
@@ -26,6 +27,7 @@ from .api import (  # noqa: E402,F401
     Misfit_function,
     Ricker_mcs,
     Survey,
+    batch_release,
     batch_survey,
     calculate_misfit_gradient,
     first_step,

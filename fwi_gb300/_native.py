@@ -23,6 +23,7 @@ SURVEY_NO_GRAPH = 1
 SURVEY_RECOMPUTE = 2
 SURVEY_SINGLE_STEP = 4
 SURVEY_FUSED_STEP = 8
+SURVEY_GRAPH = 16
 GRAD_F32, GRAD_F64 = 0, 1
 
 EXPORTS = [

@@ -431,11 +431,12 @@ class Survey:
 
 
 def calculate_misfit_gradient(spec: SurveySpec, lam, step, Misfit, Grad, snap_form=N.SNAP_F32,
-                              grad_form=N.GRAD_F64):
+                              grad_form=N.GRAD_F64, flags=0):
     """calculate_misfit_gradient over every shot of `spec` in one call with
     host buffers.  Returns the updated Misfit (float32); Grad (ny, nx_model)
-    float32 Fortran array is updated in place (step=1)."""
-    h = _DescHolder(spec, snap_form, grad_form)
+    float32 Fortran array is updated in place (step=1).  flags: SURVEY_* bits
+    of the plan (part of its key)."""
+    h = _DescHolder(spec, snap_form, grad_form, flags=flags)
     lam = _f32(lam)
     m = C.c_float(Misfit)
     N.check(N.load().fwi_misfit_gradient_batch(C.byref(h.desc), _p(lam), step, C.byref(m), _p(Grad)))
@@ -456,3 +457,8 @@ def batch_survey():
     v.spec = None
     v._borrowed = True
     return v
+
+
+def batch_release():
+    """Release fwi_misfit_gradient_batch's plan (its survey and buffers)."""
+    N.check(N.load().fwi_batch_release())

@@ -1796,8 +1796,15 @@ int issue_wave(fwi_survey* s, size_t wi, int step, cudaStream_t st, cudaStream_t
     }
     // misfit + adjoint source for this wave's traces (one launch per shot:
     // the shots of a wave need not be consecutive); the observed data may
-    // still be on their way (the batch call uploads them beside the forward)
-    if (s->obs_pending) CK(cudaStreamWaitEvent(st, s->obs_ready, 0));
+    // still be on their way (the batch call uploads them beside the forward
+    // pass and records obs_ready before it launches a wave); a captured wave
+    // waits for that event inside its graph
+    {
+        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+        CK(cudaStreamIsCapturing(st, &cs));
+        if (cs == cudaStreamCaptureStatusActive) CK(cudaStreamWaitEvent(st, s->obs_ready, cudaEventWaitExternal));
+        else if (s->obs_pending) CK(cudaStreamWaitEvent(st, s->obs_ready, 0));
+    }
     for (int sh : w) {
         const int t0 = s->tr_off[sh], t1 = s->tr_off[sh + 1];
         if (t1 == t0) continue;
@@ -1919,6 +1926,7 @@ int fwi_survey_create(const fwi_survey_desc* desc, fwi_survey** out) {
         return fail(FWI_ERR_ARG, "bad snap_form / grad_form");
     std::unique_ptr<fwi_survey> s(new fwi_survey());
     s->desc = D;
+    CK(cudaEventCreateWithFlags(&s->obs_ready, cudaEventDisableTiming));
     s->nt_store = D.nt / D.store_snap;
     if ((int)snapshot_steps(D.nt, D.store_snap).size() > s->nt_store)
         return fail(FWI_ERR_ARG, "nt/store_snap snapshots exceed nt_Store");
@@ -2104,7 +2112,9 @@ int fwi_survey_run(fwi_survey* s, int step, double* misfit, float* grad) {
             CK(cudaEventCreate(&wd.tev[0]));
             CK(cudaEventCreate(&wd.tev[1]));
         }
-        if (no_graph || wd.direct_only[gi] || wd.recheck[gi] || (!wd.graph[gi] && wd.direct_runs[gi] == 0)) {
+        const bool graph_only = (D.flags & FWI_SURVEY_GRAPH) != 0;
+        if (no_graph ||
+            (!graph_only && (wd.direct_only[gi] || wd.recheck[gi] || (!wd.graph[gi] && wd.direct_runs[gi] == 0)))) {
             const bool timed = !no_graph && (wd.t_direct[gi] == 0.f || wd.recheck[gi]);
             if (timed) CK(cudaEventRecord(wd.tev[0], st));
             TRY(issue_wave(s, wi, step, st, L().aux));
@@ -2115,12 +2125,6 @@ int fwi_survey_run(fwi_survey* s, int step, double* misfit, float* grad) {
             }
             ++wd.direct_runs[gi];
             continue;
-        }
-        // a graph replay reads the observed data without waiting inside: they
-        // must be on the device before it starts
-        if (s->obs_pending) {
-            CK(cudaStreamWaitEvent(st, s->obs_ready, 0));
-            s->obs_pending = false;
         }
         if (!wd.graph[gi]) {
             cudaStream_t cap, cap2;
@@ -2187,7 +2191,7 @@ int fwi_survey_run(fwi_survey* s, int step, double* misfit, float* grad) {
             wd.t_direct[g2] = ms;
         }
         wd.timing = 0;
-        if (wd.t_direct[g2] > 0.f && wd.t_graph[g2] > 0.f && wd.graph[g2]) {
+        if (wd.t_direct[g2] > 0.f && wd.t_graph[g2] > 0.f && wd.graph[g2] && !(D.flags & FWI_SURVEY_GRAPH)) {
             if (wd.t_graph[g2] > 1.002f * wd.t_direct[g2]) {
                 CK(cudaGraphExecDestroy(wd.graph[g2]));
                 wd.graph[g2] = nullptr;
@@ -2469,7 +2473,6 @@ int fwi_misfit_gradient_batch(const fwi_survey_desc* desc, const float* lambda, 
             // the observed data: first read by the misfit, after the forward
             // pass, so they go on the copy stream beside it (ordered after
             // the work already on the stream)
-            if (!s->obs_ready) CK(cudaEventCreateWithFlags(&s->obs_ready, cudaEventDisableTiming));
             cudaStream_t sc = L().copy_in;
             CK(cudaEventRecord(s->obs_ready, st));
             CK(cudaStreamWaitEvent(sc, s->obs_ready, 0));

@@ -256,6 +256,10 @@ typedef struct fwi_survey_desc {
  * three streams; implies FWI_SURVEY_SINGLE_STEP.  The tuner picks this form
  * for a small wave where it is measured faster; results are bit-identical. */
 #define FWI_SURVEY_FUSED_STEP 8
+/* fwi_survey_desc.flags: replay the captured CUDA graph from the first run
+ * on, without timing it against direct launches (FWI_SURVEY_NO_GRAPH wins
+ * over it). */
+#define FWI_SURVEY_GRAPH 16
 
 typedef struct fwi_survey fwi_survey;
 

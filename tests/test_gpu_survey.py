@@ -344,20 +344,25 @@ def test_launch_form_chosen_by_timing_bit_identical():
     assert m == outs[0][0] and np.array_equal(g, outs[0][1])
 
 
-def test_batch_entry_packed_data_and_new_observations():
+@pytest.mark.parametrize("graph", [False, True])
+def test_batch_entry_packed_data_and_new_observations(graph):
     """The batch call with all shots' sources and observed traces as slices of
     one array each (the copies merged, the traces uploaded on a copy stream
     beside the forward pass) gives the bits of separate per-shot arrays, and
-    observed traces changed between calls reach that call's misfit."""
+    observed traces changed between calls reach that call's misfit -- also
+    when every call replays the captured graph (the graph waits for the
+    upload inside, before the misfit)."""
     import fwi_gb300 as F
     from fwi_gb300.synth import lam_from_vp
     spec, vp = make(13, nshots=4)
     lam = lam_from_vp(vp)
     nt = spec.nt
+    flags = F.SURVEY_GRAPH if graph else 0
+    F.batch_release()
 
     def batch():
         g = np.zeros((spec.ny, spec.nx_model), np.float32, order="F")
-        m = F.calculate_misfit_gradient(spec, lam, 1, np.float32(0.0), g)
+        m = F.calculate_misfit_gradient(spec, lam, 1, np.float32(0.0), g, flags=flags)
         return m, g
 
     ref = batch()  # separate arrays per shot
@@ -377,14 +382,18 @@ def test_batch_entry_packed_data_and_new_observations():
     # new observations in place (a time-shifted mix: the misfit normalises
     # every trace by its maximum, so a plain scale would not change it): the
     # next call's misfit and gradient follow them
-    obs_all += np.float32(0.3) * np.roll(obs_all, 7, axis=0)
-    m_half, g_half = batch()
-    sv = F.Survey(spec)
-    sv.set_lambda(lam)
-    g2 = np.zeros_like(g_half)
-    m2, _ = sv.run(1, g2)
-    assert m_half == np.float32(m2) and np.array_equal(g_half, g2)
-    assert m_half != ref[0]
+    for r in range(2):
+        obs_all += np.float32(0.3) * np.roll(obs_all, 7 + r, axis=0)
+        m_half, g_half = batch()
+        sv = F.Survey(spec)
+        sv.set_lambda(lam)
+        g2 = np.zeros_like(g_half)
+        m2, _ = sv.run(1, g2)
+        sv.close()
+        assert m_half == np.float32(m2) and np.array_equal(g_half, g2)
+        assert m_half != ref[0]
+    if graph:
+        assert F.batch_survey().launch_form(1)[0] == "graph"
 
 
 def test_tuning_cache_file_across_processes(tmp_path):
